@@ -1,0 +1,630 @@
+// fec_abi.cu -- the C ABI of libfec_gb300.so (declared in include/fec_gb300.h):
+// context, mesh/physics/DOF set-up, the symbolic phase that builds the CSC
+// pattern and the element -> nzval maps, and the assembly driver.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../../include/fec_gb300.h"
+#include "fec_launch.h"
+
+using fec::BlockInfo;
+using fec::ElemArgs;
+using fec::GatherArgs;
+
+namespace {
+
+thread_local int g_create_status = FEC_OK;
+thread_local char g_create_msg[256] = "";
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+struct Block {
+  int elem_type = 0, nnpe = 0, nq = 0;
+  int64_t ne = 0;
+  int64_t elem_start = 0, conn_off = 0, epos_off = 0;
+  int physics = 0;
+  double props[8] = {0};
+  int nprops = 0;
+};
+
+}  // namespace
+
+struct fec_ctx {
+  int device = 0;
+  int status = FEC_OK;
+  std::string msg;
+  int last_launches = 0;
+  // mesh
+  int dim = 0;
+  int64_t nn = 0, ne_total = 0;
+  std::vector<Block> blocks;
+  std::vector<int32_t> conn;  // 0-based, all blocks
+  // dofs
+  int nf = 0;
+  int64_t n_unknowns = -1;
+  std::vector<int64_t> dof_to_unknown;  // 0-based index or -1
+  std::vector<uint8_t> umask;
+  // pattern
+  bool pattern_ready = false;
+  int64_t nnz = 0;
+  std::vector<int64_t> nbr_ptr;
+  std::vector<int32_t> nbr;
+  std::vector<int64_t> col_base;
+  std::vector<int32_t> col_len;
+  int acc_stride = 0;
+  // device
+  DevBuf d_coords, d_conn, d_ref, d_nadj_ptr, d_nadj, d_epos, d_umask, d_col_base, d_col_len, d_dtu, d_unknown_dofs;
+  DevBuf d_Ke, d_Re;
+  std::vector<int64_t> ref_off;  // per block offset (doubles) into d_ref
+};
+
+namespace {
+
+int fail(fec_ctx* c, int status, const char* fmt, ...) {
+  char buf[240];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) {
+    c->status = status;
+    c->msg = buf;
+  } else {
+    g_create_status = status;
+    snprintf(g_create_msg, sizeof g_create_msg, "%s", buf);
+  }
+  return status;
+}
+
+int ok(fec_ctx* c) {
+  c->status = FEC_OK;
+  c->msg.clear();
+  return FEC_OK;
+}
+
+#define FEC_CUDA(ctx, call)                                                                             \
+  do {                                                                                                  \
+    cudaError_t _e = (call);                                                                            \
+    if (_e != cudaSuccess) return fail(ctx, FEC_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(_e));    \
+  } while (0)
+
+int upload(fec_ctx* c, DevBuf& b, const void* src, size_t bytes) {
+  b.release();
+  if (bytes == 0 || c->device < 0) return FEC_OK;
+  FEC_CUDA(c, cudaMalloc(&b.p, bytes));
+  b.bytes = bytes;
+  FEC_CUDA(c, cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice));
+  return FEC_OK;
+}
+
+int ensure(fec_ctx* c, DevBuf& b, size_t bytes) {
+  if (b.bytes >= bytes) return FEC_OK;
+  b.release();
+  FEC_CUDA(c, cudaMalloc(&b.p, bytes));
+  b.bytes = bytes;
+  return FEC_OK;
+}
+
+int num_fields_of(int physics) { return physics == FEC_PHYS_POISSON ? 1 : 3; }
+int num_states_of(int physics) { return physics == FEC_PHYS_J2 ? 7 : 0; }
+
+// U[bc_dofs[i]-1] = vals[i]
+__global__ void set_dirichlet_kernel(double* U, int64_t n, const int64_t* dofs, const double* vals) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) U[dofs[i] - 1] = vals[i];
+}
+
+// U[unknown_dofs[k]] = Uu[k]  (unknown_dofs 0-based here)
+__global__ void set_unknowns_kernel(double* U, int64_t n, const int64_t* unknown_dofs, const double* Uu) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) U[unknown_dofs[k]] = Uu[k];
+}
+
+void invalidate_pattern(fec_ctx* c) {
+  c->pattern_ready = false;
+  c->nnz = 0;
+  c->d_nadj_ptr.release();
+  c->d_nadj.release();
+  c->d_epos.release();
+  c->d_col_base.release();
+  c->d_col_len.release();
+}
+
+}  // namespace
+
+extern "C" {
+
+int fec_ctx_create(int device, fec_ctx** out) {
+  if (!out) return fail(nullptr, FEC_ERR_ARG, "fec_ctx_create: out is NULL");
+  *out = nullptr;
+  if (device == -1) {  // host-only context: mesh, dofs and the symbolic phase
+    fec_ctx* c = new fec_ctx();
+    c->device = -1;
+    *out = c;
+    g_create_status = FEC_OK;
+    g_create_msg[0] = 0;
+    return FEC_OK;
+  }
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess) return fail(nullptr, FEC_ERR_CUDA, "cudaGetDeviceCount: %s", cudaGetErrorString(e));
+  if (device < 0 || device >= count) return fail(nullptr, FEC_ERR_ARG, "device %d out of range (%d)", device, count);
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return fail(nullptr, FEC_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+  fec_ctx* c = new fec_ctx();
+  c->device = device;
+  *out = c;
+  g_create_status = FEC_OK;
+  g_create_msg[0] = 0;
+  return FEC_OK;
+}
+
+int fec_ctx_destroy(fec_ctx* c) {
+  if (!c) return FEC_OK;
+  if (c->device >= 0) cudaSetDevice(c->device);
+  for (DevBuf* b : {&c->d_coords, &c->d_conn, &c->d_ref, &c->d_nadj_ptr, &c->d_nadj, &c->d_epos, &c->d_umask,
+                    &c->d_col_base, &c->d_col_len, &c->d_dtu, &c->d_unknown_dofs, &c->d_Ke, &c->d_Re})
+    b->release();
+  delete c;
+  return FEC_OK;
+}
+
+int fec_last_error(const fec_ctx* c, char* buf, size_t len) {
+  const char* m = c ? c->msg.c_str() : g_create_msg;
+  if (buf && len) {
+    strncpy(buf, m, len - 1);
+    buf[len - 1] = 0;
+  }
+  return c ? c->status : g_create_status;
+}
+
+int fec_last_launch_count(const fec_ctx* c) { return c ? c->last_launches : 0; }
+
+int fec_sizes(const fec_ctx* c, int64_t* nn, int64_t* ne, int64_t* nu, int64_t* nnz, int64_t* state_len) {
+  if (!c) return FEC_ERR_ARG;
+  if (nn) *nn = c->nn;
+  if (ne) *ne = c->ne_total;
+  if (nu) *nu = c->n_unknowns;
+  if (nnz) *nnz = c->nnz;
+  if (state_len) {
+    int64_t s = 0;
+    for (const Block& b : c->blocks) s += int64_t(num_states_of(b.physics)) * b.nq * b.ne;
+    *state_len = s;
+  }
+  return FEC_OK;
+}
+
+int fec_mesh_set(fec_ctx* c, int dim, int64_t nn, const double* coords, int nblocks, const int32_t* elem_types,
+                 const int64_t* block_ne, const int64_t* conn) {
+  if (!c) return FEC_ERR_ARG;
+  if (dim != 2 && dim != 3) return fail(c, FEC_ERR_ARG, "dim must be 2 or 3 (got %d)", dim);
+  if (nn <= 0 || !coords) return fail(c, FEC_ERR_ARG, "need num_nodes > 0 and coords");
+  if (nblocks <= 0 || nblocks > fec::MAX_BLOCKS)
+    return fail(c, FEC_ERR_ARG, "num_blocks must be in 1..%d (got %d)", fec::MAX_BLOCKS, nblocks);
+  if (nn >= (int64_t(1) << 31)) return fail(c, FEC_ERR_ARG, "num_nodes must be < 2^31");
+  if (c->device >= 0) cudaSetDevice(c->device);
+  std::vector<Block> blocks(nblocks);
+  int64_t total_conn = 0, ne_total = 0, epos_total = 0;
+  for (int b = 0; b < nblocks; ++b) {
+    Block& B = blocks[b];
+    B.elem_type = elem_types[b];
+    B.nnpe = fec::elem_nnpe(B.elem_type);
+    B.nq = fec::elem_nq(B.elem_type);
+    if (!B.nnpe) return fail(c, FEC_ERR_UNSUPPORTED, "block %d: unsupported element type %d", b + 1, B.elem_type);
+    if (fec::elem_dim(B.elem_type) != dim)
+      return fail(c, FEC_ERR_ARG, "block %d: element type %d is not %dD", b + 1, B.elem_type, dim);
+    if (block_ne[b] < 0) return fail(c, FEC_ERR_ARG, "block %d: negative element count", b + 1);
+    B.ne = block_ne[b];
+    B.elem_start = ne_total;
+    B.conn_off = total_conn;
+    B.epos_off = epos_total;
+    ne_total += B.ne;
+    total_conn += B.ne * B.nnpe;
+    epos_total += B.ne * B.nnpe * B.nnpe;
+  }
+  if (ne_total >= (int64_t(1) << 58)) return fail(c, FEC_ERR_ARG, "too many elements");
+  std::vector<int32_t> conn0(total_conn);
+  int64_t bad = -1;
+#pragma omp parallel for schedule(static) reduction(max : bad)
+  for (int64_t i = 0; i < total_conn; ++i) {
+    const int64_t v = conn[i];
+    if (v < 1 || v > nn) bad = std::max(bad, i);
+    conn0[i] = int32_t(v - 1);
+  }
+  if (bad >= 0)
+    return fail(c, FEC_ERR_ARG, "connectivity entry %lld = %lld is outside 1..%lld", (long long)bad + 1,
+                (long long)conn[bad], (long long)nn);
+  // elements must not repeat a node (the gather relies on distinct slots)
+  for (const Block& B : blocks) {
+    int64_t dup = -1;
+#pragma omp parallel for schedule(static) reduction(max : dup)
+    for (int64_t e = 0; e < B.ne; ++e) {
+      const int32_t* ce = conn0.data() + B.conn_off + e * B.nnpe;
+      for (int a = 0; a < B.nnpe; ++a)
+        for (int b2 = a + 1; b2 < B.nnpe; ++b2)
+          if (ce[a] == ce[b2]) dup = std::max(dup, e);
+    }
+    if (dup >= 0) return fail(c, FEC_ERR_ARG, "element %lld repeats a node", (long long)(B.elem_start + dup + 1));
+  }
+  // reference tables
+  std::vector<double> ref;
+  std::vector<int64_t> ref_off(nblocks);
+  for (int b = 0; b < nblocks; ++b) {
+    double tmp[8192];
+    const int n = fec::ref_tables(blocks[b].elem_type, tmp, 8192);
+    ref_off[b] = int64_t(ref.size());
+    ref.insert(ref.end(), tmp, tmp + n);
+    while (ref.size() % 2) ref.push_back(0.0);
+  }
+  int rc;
+  if ((rc = upload(c, c->d_coords, coords, sizeof(double) * size_t(nn) * dim))) return rc;
+  if ((rc = upload(c, c->d_conn, conn0.data(), sizeof(int32_t) * conn0.size()))) return rc;
+  if ((rc = upload(c, c->d_ref, ref.data(), sizeof(double) * ref.size()))) return rc;
+  c->dim = dim;
+  c->nn = nn;
+  c->ne_total = ne_total;
+  c->blocks = std::move(blocks);
+  c->conn = std::move(conn0);
+  c->ref_off = std::move(ref_off);
+  c->n_unknowns = -1;
+  c->nf = 0;
+  invalidate_pattern(c);
+  return ok(c);
+}
+
+int fec_physics_set(fec_ctx* c, int block, int physics, const double* props, int nprops) {
+  if (!c) return FEC_ERR_ARG;
+  if (block < 1 || block > int(c->blocks.size()))
+    return fail(c, FEC_ERR_ARG, "block %d out of range 1..%d", block, int(c->blocks.size()));
+  if (physics != FEC_PHYS_POISSON && physics != FEC_PHYS_NEOHOOKEAN && physics != FEC_PHYS_J2)
+    return fail(c, FEC_ERR_UNSUPPORTED, "unknown physics %d", physics);
+  const int need = physics == FEC_PHYS_POISSON ? 1 : (physics == FEC_PHYS_NEOHOOKEAN ? 2 : 4);
+  if (nprops < need || nprops > 8 || (nprops > 0 && !props))
+    return fail(c, FEC_ERR_ARG, "physics %d needs %d properties (got %d)", physics, need, nprops);
+  Block& B = c->blocks[block - 1];
+  if (physics != FEC_PHYS_POISSON && c->dim != 3)
+    return fail(c, FEC_ERR_UNSUPPORTED, "mechanics physics needs a 3D mesh");
+  B.physics = physics;
+  B.nprops = nprops;
+  for (int i = 0; i < 8; ++i) B.props[i] = i < nprops ? props[i] : 0.0;
+  return ok(c);
+}
+
+int fec_dofs_set(fec_ctx* c, int nf, const int64_t* dtu, int64_t n_unknowns) {
+  if (!c) return FEC_ERR_ARG;
+  if (c->nn <= 0) return fail(c, FEC_ERR_STATE, "fec_dofs_set before fec_mesh_set");
+  if (nf != 1 && nf != 3) return fail(c, FEC_ERR_UNSUPPORTED, "num_fields must be 1 or 3 (got %d)", nf);
+  if (!dtu) return fail(c, FEC_ERR_ARG, "dof_to_unknown is NULL");
+  const int64_t ndofs = int64_t(nf) * c->nn;
+  std::vector<int64_t> d(ndofs);
+  std::vector<int64_t> unknown_dofs;
+  unknown_dofs.reserve(size_t(std::max<int64_t>(n_unknowns, 0)));
+  std::vector<uint8_t> um(c->nn, 0);
+  int64_t next = 1;
+  for (int64_t i = 0; i < ndofs; ++i) {
+    const int64_t v = dtu[i];
+    if (v == -1) {
+      d[i] = -1;
+      continue;
+    }
+    if (v != next)
+      return fail(c, FEC_ERR_ARG,
+                  "dof_to_unknown[%lld] = %lld: unknowns must be numbered 1..n in increasing dof order "
+                  "(expected %lld or -1)",
+                  (long long)i + 1, (long long)v, (long long)next);
+    d[i] = v - 1;
+    unknown_dofs.push_back(i);
+    um[i / nf] |= uint8_t(1u << (i % nf));
+    ++next;
+  }
+  if (next - 1 != n_unknowns)
+    return fail(c, FEC_ERR_ARG, "num_unknowns = %lld but dof_to_unknown numbers %lld unknowns", (long long)n_unknowns,
+                (long long)(next - 1));
+  int rc;
+  if ((rc = upload(c, c->d_dtu, d.data(), sizeof(int64_t) * d.size()))) return rc;
+  if ((rc = upload(c, c->d_umask, um.data(), um.size()))) return rc;
+  if ((rc = upload(c, c->d_unknown_dofs, unknown_dofs.data(), sizeof(int64_t) * unknown_dofs.size()))) return rc;
+  c->nf = nf;
+  c->n_unknowns = n_unknowns;
+  c->dof_to_unknown = std::move(d);
+  c->umask = std::move(um);
+  invalidate_pattern(c);
+  return ok(c);
+}
+
+int fec_pattern_build(fec_ctx* c, int64_t* nnz_out) {
+  if (!c) return FEC_ERR_ARG;
+  if (c->n_unknowns < 0) return fail(c, FEC_ERR_STATE, "fec_pattern_build before fec_dofs_set");
+  if (c->device >= 0) cudaSetDevice(c->device);
+  const int64_t nn = c->nn;
+  // node -> (element, local node) adjacency, elements ascending
+  std::vector<int64_t> nadj_ptr(nn + 1, 0);
+  for (const Block& B : c->blocks)
+    for (int64_t i = 0; i < B.ne * B.nnpe; ++i) nadj_ptr[c->conn[B.conn_off + i] + 1]++;
+  for (int64_t n = 0; n < nn; ++n) nadj_ptr[n + 1] += nadj_ptr[n];
+  std::vector<int64_t> nadj(nadj_ptr[nn]);
+  {
+    std::vector<int64_t> fill(nadj_ptr.begin(), nadj_ptr.end() - 1);
+    for (const Block& B : c->blocks)
+      for (int64_t e = 0; e < B.ne; ++e)
+        for (int a = 0; a < B.nnpe; ++a) {
+          const int32_t n = c->conn[B.conn_off + e * B.nnpe + a];
+          nadj[fill[n]++] = ((B.elem_start + e) << 5) | a;
+        }
+  }
+  auto elem_nodes = [&](int64_t ge, int* nnpe) -> const int32_t* {
+    size_t b = 0;
+    while (b + 1 < c->blocks.size() && ge >= c->blocks[b + 1].elem_start) ++b;
+    const Block& B = c->blocks[b];
+    *nnpe = B.nnpe;
+    return c->conn.data() + B.conn_off + (ge - B.elem_start) * B.nnpe;
+  };
+  // sorted unique neighbour lists (two passes: count, then fill)
+  std::vector<int64_t> nbr_ptr(nn + 1, 0);
+  int64_t max_nbr = 0;
+#pragma omp parallel reduction(max : max_nbr)
+  {
+    std::vector<int32_t> tmp;
+#pragma omp for schedule(dynamic, 4096)
+    for (int64_t n = 0; n < nn; ++n) {
+      tmp.clear();
+      for (int64_t p = nadj_ptr[n]; p < nadj_ptr[n + 1]; ++p) {
+        int A;
+        const int32_t* ce = elem_nodes(nadj[p] >> 5, &A);
+        tmp.insert(tmp.end(), ce, ce + A);
+      }
+      std::sort(tmp.begin(), tmp.end());
+      const int64_t u = std::unique(tmp.begin(), tmp.end()) - tmp.begin();
+      nbr_ptr[n + 1] = u;
+      max_nbr = std::max(max_nbr, u);
+    }
+  }
+  for (int64_t n = 0; n < nn; ++n) nbr_ptr[n + 1] += nbr_ptr[n];
+  std::vector<int32_t> nbr(nbr_ptr[nn]);
+  std::vector<int32_t> col_len(nn, 0);
+  std::vector<int32_t> rowoff(nbr_ptr[nn]);
+  int64_t bad_len = 0;
+#pragma omp parallel reduction(max : bad_len)
+  {
+    std::vector<int32_t> tmp;
+#pragma omp for schedule(dynamic, 4096)
+    for (int64_t n = 0; n < nn; ++n) {
+      tmp.clear();
+      for (int64_t p = nadj_ptr[n]; p < nadj_ptr[n + 1]; ++p) {
+        int A;
+        const int32_t* ce = elem_nodes(nadj[p] >> 5, &A);
+        tmp.insert(tmp.end(), ce, ce + A);
+      }
+      std::sort(tmp.begin(), tmp.end());
+      tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+      int32_t L = 0;
+      for (size_t r = 0; r < tmp.size(); ++r) {
+        nbr[nbr_ptr[n] + r] = tmp[r];
+        rowoff[nbr_ptr[n] + r] = L;
+        L += __builtin_popcount(c->umask[tmp[r]]);
+      }
+      col_len[n] = L;
+      bad_len = std::max<int64_t>(bad_len, L);
+    }
+  }
+  if (bad_len >= 65535) return fail(c, FEC_ERR_UNSUPPORTED, "a node couples to %lld dofs (limit 65534)", (long long)bad_len);
+  std::vector<int64_t> col_base(nn, 0);
+  int64_t nnz = 0;
+  int max_cols = 0;
+  for (int64_t n = 0; n < nn; ++n) {
+    col_base[n] = nnz;
+    const int nc = __builtin_popcount(c->umask[n]);
+    nnz += int64_t(nc) * col_len[n];
+    if (nc) max_cols = std::max(max_cols, nc * col_len[n]);
+  }
+  // element map: row offset of node conn[b] within node conn[a]'s columns
+  int64_t epos_total = 0;
+  for (const Block& B : c->blocks) epos_total += B.ne * B.nnpe * B.nnpe;
+  std::vector<uint16_t> epos(epos_total);
+  for (const Block& B : c->blocks) {
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < B.ne; ++e) {
+      const int32_t* ce = c->conn.data() + B.conn_off + e * B.nnpe;
+      for (int a = 0; a < B.nnpe; ++a) {
+        const int32_t n = ce[a];
+        const int32_t* lo = nbr.data() + nbr_ptr[n];
+        const int32_t* hi = nbr.data() + nbr_ptr[n + 1];
+        for (int b = 0; b < B.nnpe; ++b) {
+          const int64_t r = std::lower_bound(lo, hi, ce[b]) - lo;
+          epos[B.epos_off + (e * B.nnpe + a) * B.nnpe + b] = uint16_t(rowoff[nbr_ptr[n] + r]);
+        }
+      }
+    }
+  }
+  const int acc_stride = std::max(2, (max_cols + 1) & ~1);
+  if (size_t(acc_stride) * sizeof(double) > 200 * 1024)
+    return fail(c, FEC_ERR_UNSUPPORTED, "a node's columns hold %d entries; the gather supports %d", max_cols,
+                int(200 * 1024 / sizeof(double)));
+  int rc;
+  if ((rc = upload(c, c->d_nadj_ptr, nadj_ptr.data(), sizeof(int64_t) * nadj_ptr.size()))) return rc;
+  if ((rc = upload(c, c->d_nadj, nadj.data(), sizeof(int64_t) * nadj.size()))) return rc;
+  if ((rc = upload(c, c->d_epos, epos.data(), sizeof(uint16_t) * epos.size()))) return rc;
+  if ((rc = upload(c, c->d_col_base, col_base.data(), sizeof(int64_t) * col_base.size()))) return rc;
+  if ((rc = upload(c, c->d_col_len, col_len.data(), sizeof(int32_t) * col_len.size()))) return rc;
+  c->nbr_ptr = std::move(nbr_ptr);
+  c->nbr = std::move(nbr);
+  c->col_base = std::move(col_base);
+  c->col_len = std::move(col_len);
+  c->nnz = nnz;
+  c->acc_stride = acc_stride;
+  c->pattern_ready = true;
+  if (nnz_out) *nnz_out = nnz;
+  return ok(c);
+}
+
+int fec_pattern_get(const fec_ctx* cc, int64_t* colptr, int64_t* rowval) {
+  fec_ctx* c = const_cast<fec_ctx*>(cc);
+  if (!c) return FEC_ERR_ARG;
+  if (!c->pattern_ready) return fail(c, FEC_ERR_STATE, "fec_pattern_get before fec_pattern_build");
+  const int nf = c->nf;
+  if (colptr) {
+    colptr[0] = 1;
+    for (int64_t n = 0; n < c->nn; ++n) {
+      int kk = 0;
+      for (int k = 0; k < nf; ++k) {
+        if (!((c->umask[n] >> k) & 1)) continue;
+        const int64_t col = c->dof_to_unknown[n * nf + k];
+        colptr[col + 1] = c->col_base[n] + int64_t(kk + 1) * c->col_len[n] + 1;
+        ++kk;
+      }
+    }
+  }
+  if (rowval) {
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int64_t n = 0; n < c->nn; ++n) {
+      const int nc = __builtin_popcount(c->umask[n]);
+      int64_t w = c->col_base[n];
+      for (int kk = 0; kk < nc; ++kk)
+        for (int64_t p = c->nbr_ptr[n]; p < c->nbr_ptr[n + 1]; ++p) {
+          const int32_t m = c->nbr[p];
+          for (int i = 0; i < nf; ++i)
+            if ((c->umask[m] >> i) & 1) rowval[w++] = c->dof_to_unknown[int64_t(m) * nf + i] + 1;
+        }
+    }
+  }
+  return ok(c);
+}
+
+int fec_update_field(fec_ctx* c, double* U, const double* Uu, int64_t num_bc, const int64_t* bc_dofs,
+                     const double* bc_vals, void* stream) {
+  if (!c) return FEC_ERR_ARG;
+  if (c->n_unknowns < 0) return fail(c, FEC_ERR_STATE, "fec_update_field before fec_dofs_set");
+  if (c->device < 0) return fail(c, FEC_ERR_STATE, "host-only context (device -1) cannot run kernels");
+  if (!U) return fail(c, FEC_ERR_ARG, "U is NULL");
+  if (num_bc < 0 || (num_bc > 0 && (!bc_dofs || !bc_vals))) return fail(c, FEC_ERR_ARG, "bad Dirichlet arrays");
+  cudaSetDevice(c->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (num_bc > 0) {
+    set_dirichlet_kernel<<<unsigned((num_bc + 255) / 256), 256, 0, s>>>(U, num_bc, bc_dofs, bc_vals);
+    FEC_CUDA(c, cudaGetLastError());
+  }
+  if (c->n_unknowns > 0) {
+    if (!Uu) return fail(c, FEC_ERR_ARG, "Uu is NULL");
+    set_unknowns_kernel<<<unsigned((c->n_unknowns + 255) / 256), 256, 0, s>>>(
+        U, c->n_unknowns, static_cast<const int64_t*>(c->d_unknown_dofs.p), Uu);
+    FEC_CUDA(c, cudaGetLastError());
+  }
+  return ok(c);
+}
+
+int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const double* U, const double* U_old,
+                 const double* state_old, double* state_new, double* R_u, double* nzval, void* stream) {
+  (void)t;
+  (void)dt;
+  (void)U_old;
+  if (!c) return FEC_ERR_ARG;
+  c->last_launches = 0;
+  if (!c->pattern_ready) return fail(c, FEC_ERR_STATE, "fec_assemble before fec_pattern_build");
+  if (c->device < 0) return fail(c, FEC_ERR_STATE, "host-only context (device -1) cannot run kernels");
+  if (precision != FEC_FP64 && precision != FEC_FP32_ELEMENT)
+    return fail(c, FEC_ERR_ARG, "unknown precision %d", precision);
+  const bool want_r = (want & FEC_WANT_RESIDUAL) != 0, want_k = (want & FEC_WANT_STIFFNESS) != 0;
+  if (!want_r && !want_k) return ok(c);
+  if (!U) return fail(c, FEC_ERR_ARG, "U is NULL");
+  if (want_r && !R_u && c->n_unknowns > 0) return fail(c, FEC_ERR_ARG, "R_u is NULL");
+  if (want_k && !nzval && c->nnz > 0) return fail(c, FEC_ERR_ARG, "nzval is NULL");
+  bool any_state = false;
+  for (size_t b = 0; b < c->blocks.size(); ++b) {
+    const Block& B = c->blocks[b];
+    if (!B.physics) return fail(c, FEC_ERR_STATE, "block %d has no physics", int(b) + 1);
+    if (num_fields_of(B.physics) != c->nf)
+      return fail(c, FEC_ERR_ARG, "block %d physics has %d fields but the dofs have %d", int(b) + 1,
+                  num_fields_of(B.physics), c->nf);
+    if (num_states_of(B.physics)) any_state = true;
+  }
+  if (any_state && !state_old) return fail(c, FEC_ERR_ARG, "state_old is NULL for a physics with state");
+  cudaSetDevice(c->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t rsz = precision == FEC_FP64 ? sizeof(double) : sizeof(float);
+  int64_t ke_total = 0, re_total = 0;
+  for (const Block& B : c->blocks) {
+    const int ndof = c->nf * B.nnpe;
+    ke_total += B.ne * ndof * ndof;
+    re_total += B.ne * ndof;
+  }
+  int rc;
+  if (want_k && (rc = ensure(c, c->d_Ke, rsz * size_t(ke_total)))) return rc;
+  if (want_r && (rc = ensure(c, c->d_Re, rsz * size_t(re_total)))) return rc;
+  // element kernels, one launch per block
+  GatherArgs ga;
+  memset(&ga, 0, sizeof ga);
+  int64_t ke_off = 0, re_off = 0, st_off = 0;
+  for (size_t b = 0; b < c->blocks.size(); ++b) {
+    const Block& B = c->blocks[b];
+    const int ndof = c->nf * B.nnpe;
+    ElemArgs ea;
+    memset(&ea, 0, sizeof ea);
+    ea.conn = static_cast<const int32_t*>(c->d_conn.p) + B.conn_off;
+    ea.ne = B.ne;
+    ea.coords = static_cast<const double*>(c->d_coords.p);
+    ea.U = U;
+    ea.ref = static_cast<const double*>(c->d_ref.p) + c->ref_off[b];
+    for (int i = 0; i < 8; ++i) ea.props[i] = B.props[i];
+    const int ns = num_states_of(B.physics);
+    ea.state_old = ns ? state_old + st_off : nullptr;
+    ea.state_new = (ns && state_new) ? state_new + st_off : nullptr;
+    ea.Ke = want_k ? static_cast<char*>(c->d_Ke.p) + rsz * size_t(ke_off) : nullptr;
+    ea.Re = want_r ? static_cast<char*>(c->d_Re.p) + rsz * size_t(re_off) : nullptr;
+    cudaError_t e;
+    if (B.physics == FEC_PHYS_POISSON)
+      e = fec::launch_poisson(B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
+    else
+      e = fec::launch_mech(B.physics, B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
+    if (e == cudaErrorNotSupported)
+      return fail(c, FEC_ERR_UNSUPPORTED, "block %d: physics %d on element type %d is not built", int(b) + 1,
+                  B.physics, B.elem_type);
+    if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "element kernel launch: %s", cudaGetErrorString(e));
+    BlockInfo& bi = ga.blk[b];
+    bi.elem_start = B.elem_start;
+    bi.ke_off = ke_off;
+    bi.re_off = re_off;
+    bi.conn_off = B.conn_off;
+    bi.epos_off = B.epos_off;
+    bi.nnpe = B.nnpe;
+    bi.ndof = ndof;
+    ke_off += B.ne * ndof * ndof;
+    re_off += B.ne * ndof;
+    st_off += int64_t(ns) * B.nq * B.ne;
+  }
+  ga.nn = c->nn;
+  ga.nf = c->nf;
+  ga.nblocks = int(c->blocks.size());
+  ga.nadj_ptr = static_cast<const int64_t*>(c->d_nadj_ptr.p);
+  ga.nadj = static_cast<const int64_t*>(c->d_nadj.p);
+  ga.conn = static_cast<const int32_t*>(c->d_conn.p);
+  ga.epos = static_cast<const uint16_t*>(c->d_epos.p);
+  ga.umask = static_cast<const uint8_t*>(c->d_umask.p);
+  ga.col_base = static_cast<const int64_t*>(c->d_col_base.p);
+  ga.col_len = static_cast<const int32_t*>(c->d_col_len.p);
+  ga.dof_to_unknown = static_cast<const int64_t*>(c->d_dtu.p);
+  ga.Ke = c->d_Ke.p;
+  ga.Re = c->d_Re.p;
+  ga.nzval = want_k ? nzval : nullptr;
+  ga.R_u = want_r ? R_u : nullptr;
+  ga.acc_stride = c->acc_stride;
+  cudaError_t e = fec::launch_gather(precision, c->nf, ga, s, &c->last_launches);
+  if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "gather launch: %s", cudaGetErrorString(e));
+  return ok(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,148 @@
+// fec_gather.cu -- instantiations of the node gather and the mechanics
+// dispatcher, plus the reference-element tables.
+#include <cmath>
+#include "fec_launch.h"
+
+namespace fec {
+
+cudaError_t launch_mech_neohookean(int, int, bool, bool, const ElemArgs&, cudaStream_t, int*);
+cudaError_t launch_mech_j2(int, int, bool, bool, const ElemArgs&, cudaStream_t, int*);
+
+cudaError_t launch_mech(int physics, int elem_type, int precision, bool want_r, bool want_k, const ElemArgs& a,
+                        cudaStream_t s, int* launches) {
+  if (physics == 2) return launch_mech_neohookean(elem_type, precision, want_r, want_k, a, s, launches);
+  if (physics == 3) return launch_mech_j2(elem_type, precision, want_r, want_k, a, s, launches);
+  return cudaErrorNotSupported;
+}
+
+namespace {
+constexpr int WPB = 8;
+
+template <typename Real, int NF>
+cudaError_t go(const GatherArgs& g, cudaStream_t s, int* launches) {
+  if (g.nn <= 0) return cudaSuccess;
+  const size_t smem = sizeof(double) * size_t(WPB) * size_t(g.acc_stride);
+  auto kern = node_gather_kernel<Real, NF, WPB>;
+  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (err != cudaSuccess) return err;
+  const unsigned grid = unsigned((g.nn + WPB - 1) / WPB);
+  kern<<<grid, WPB * 32, smem, s>>>(g);
+  ++*launches;
+  return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_gather(int precision, int nf, const GatherArgs& g, cudaStream_t s, int* launches) {
+  if (precision == 0) {
+    if (nf == 1) return go<double, 1>(g, s, launches);
+    if (nf == 3) return go<double, 3>(g, s, launches);
+  } else if (precision == 1) {
+    if (nf == 1) return go<float, 1>(g, s, launches);
+    if (nf == 3) return go<float, 3>(g, s, launches);
+  }
+  return cudaErrorNotSupported;
+}
+
+int elem_nnpe(int et) {
+  switch (et) { case 1: return 8; case 2: return 4; case 6: return 4; case 7: return 10; case 8: return 27; }
+  return 0;
+}
+int elem_dim(int et) {
+  switch (et) { case 1: case 6: case 7: case 8: return 3; case 2: return 2; }
+  return 0;
+}
+int elem_nq(int et) {
+  switch (et) { case 1: return 8; case 2: return 4; case 6: return 1; case 7: return 4; case 8: return 27; }
+  return 0;
+}
+
+// Lagrange shape functions and quadrature rules of the reference elements on
+// the path (the rules ReferenceFiniteElements.jl supplies to
+// src/FunctionSpaces.jl:104-126): Q1 quad/hex with the 2-point Gauss-Legendre
+// tensor rule, P1 tet with its 1-point rule, P2 tet (exodus TETRA10 node order)
+// with the 4-point rule, Q2 hex with the 3-point Gauss-Legendre tensor rule.
+int ref_tables(int et, double* out, int cap) {
+  const int A = elem_nnpe(et), D = elem_dim(et), NQ = elem_nq(et);
+  if (!A) return 0;
+  const int size = NQ * A + NQ * A * D + NQ;
+  if (size > cap) return 0;
+  double* N = out;
+  double* dN = out + NQ * A;
+  double* w = dN + NQ * A * D;
+  const double g = 1.0 / std::sqrt(3.0);
+  if (et == 2) {
+    const double xi[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
+    for (int q = 0; q < 4; ++q) {
+      const double s = (q & 1) ? g : -g, t = (q & 2) ? g : -g;
+      w[q] = 1.0;
+      for (int a = 0; a < 4; ++a) {
+        N[q * 4 + a] = 0.25 * (1 + xi[a][0] * s) * (1 + xi[a][1] * t);
+        dN[(q * 4 + a) * 2 + 0] = 0.25 * xi[a][0] * (1 + xi[a][1] * t);
+        dN[(q * 4 + a) * 2 + 1] = 0.25 * xi[a][1] * (1 + xi[a][0] * s);
+      }
+    }
+  } else if (et == 1) {
+    const double xi[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                             {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+    for (int q = 0; q < 8; ++q) {
+      const double s = (q & 1) ? g : -g, t = (q & 2) ? g : -g, u = (q & 4) ? g : -g;
+      w[q] = 1.0;
+      for (int a = 0; a < 8; ++a) {
+        const double fs = 1 + xi[a][0] * s, ft = 1 + xi[a][1] * t, fu = 1 + xi[a][2] * u;
+        N[q * 8 + a] = 0.125 * fs * ft * fu;
+        dN[(q * 8 + a) * 3 + 0] = 0.125 * xi[a][0] * ft * fu;
+        dN[(q * 8 + a) * 3 + 1] = 0.125 * xi[a][1] * fs * fu;
+        dN[(q * 8 + a) * 3 + 2] = 0.125 * xi[a][2] * fs * ft;
+      }
+    }
+  } else if (et == 6) {
+    w[0] = 1.0 / 6.0;
+    const double dl[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int a = 0; a < 4; ++a) {
+      N[a] = 0.25;
+      for (int k = 0; k < 3; ++k) dN[a * 3 + k] = dl[a][k];
+    }
+  } else if (et == 7) {
+    const double al = (5.0 + 3.0 * std::sqrt(5.0)) / 20.0, be = (5.0 - std::sqrt(5.0)) / 20.0;
+    const double pts[4][3] = {{be, be, be}, {al, be, be}, {be, al, be}, {be, be, al}};
+    const double dl[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    const int ed[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+    for (int q = 0; q < 4; ++q) {
+      w[q] = 1.0 / 24.0;
+      const double l[4] = {1 - pts[q][0] - pts[q][1] - pts[q][2], pts[q][0], pts[q][1], pts[q][2]};
+      for (int v = 0; v < 4; ++v) {
+        N[q * 10 + v] = l[v] * (2 * l[v] - 1);
+        for (int k = 0; k < 3; ++k) dN[(q * 10 + v) * 3 + k] = (4 * l[v] - 1) * dl[v][k];
+      }
+      for (int e = 0; e < 6; ++e) {
+        const int i = ed[e][0], j = ed[e][1];
+        N[q * 10 + 4 + e] = 4 * l[i] * l[j];
+        for (int k = 0; k < 3; ++k) dN[(q * 10 + 4 + e) * 3 + k] = 4 * (dl[i][k] * l[j] + l[i] * dl[j][k]);
+      }
+    }
+  } else if (et == 8) {
+    const double p = std::sqrt(0.6);
+    const double gp[3] = {-p, 0.0, p}, gw[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+    auto lag = [](double x, double* v, double* d) {
+      v[0] = 0.5 * x * (x - 1.0); d[0] = x - 0.5;
+      v[1] = 1.0 - x * x;         d[1] = -2.0 * x;
+      v[2] = 0.5 * x * (x + 1.0); d[2] = x + 0.5;
+    };
+    for (int q = 0; q < 27; ++q) {
+      const int qx = q % 3, qy = (q / 3) % 3, qz = q / 9;
+      w[q] = gw[qx] * gw[qy] * gw[qz];
+      double vx[3], dx[3], vy[3], dy[3], vz[3], dz[3];
+      lag(gp[qx], vx, dx); lag(gp[qy], vy, dy); lag(gp[qz], vz, dz);
+      for (int a = 0; a < 27; ++a) {
+        const int i = a % 3, j = (a / 3) % 3, k = a / 9;
+        N[q * 27 + a] = vx[i] * vy[j] * vz[k];
+        dN[(q * 27 + a) * 3 + 0] = dx[i] * vy[j] * vz[k];
+        dN[(q * 27 + a) * 3 + 1] = vx[i] * dy[j] * vz[k];
+        dN[(q * 27 + a) * 3 + 2] = vx[i] * vy[j] * dz[k];
+      }
+    }
+  }
+  return size;
+}
+
+}  // namespace fec

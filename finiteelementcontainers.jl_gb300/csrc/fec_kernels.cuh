@@ -1,0 +1,615 @@
+// fec_kernels.cuh -- sm_103a kernels of the assembly path.
+//
+// Two kernel families run per fec_assemble call:
+//
+//  1. element kernels (one launch per element block, as foreach_block in
+//     src/Utils.jl:171-189 launches _assemble_block! per block): a CTA holds
+//     EPB elements; each element is served by TPE = NDOF*CSPLIT threads, one
+//     (row, column-chunk) of the element matrix each.  The connectivity and the
+//     nodal coordinates/field are gathered once per element into shared memory;
+//     the quadrature-point kinematics (isoparametric map, deformation gradient)
+//     and the constitutive update are computed once per point and shared; every
+//     thread then accumulates its row of K_e and R_e over the points in q order
+//     (src/assemblers/Assemblers.jl:418-431).  K_e is written row-major
+//     (K_e[r][c] = dR_r/du_c) and R_e next to it, into element-ordered storage:
+//     the same element-slot layout the reference fills in
+//     src/assemblers/Assemblers.jl:109-124 (there column-major, i.e. transposed).
+//
+//  2. the node gather (one warp per mesh node): walks the node's adjacent
+//     elements in increasing element order, reads the rows of K_e/R_e that
+//     belong to the node (contiguous, coalesced), and adds each value to its
+//     CSC position in a shared-memory accumulator.  Each CSC entry therefore
+//     receives its element contributions in increasing element order -- the
+//     order SparseArrays.sparse! combines the reference's element-ordered COO
+//     entries (src/assemblers/SparsityPatterns.jl:301-308) -- with no atomics,
+//     so results are bitwise reproducible.  The node's CSC columns are
+//     contiguous in nzval (unknowns are numbered node-major), so the final
+//     write is coalesced too.  The residual over unknowns is produced in the
+//     same pass (residual(asm), src/assemblers/Assemblers.jl:347-371).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fec {
+
+// ---------------------------------------------------------------------------
+// element traits
+// ---------------------------------------------------------------------------
+template <int ET> struct Elem;
+template <> struct Elem<1> { static constexpr int DIM = 3, NNPE = 8, NQ = 8; };    // HEX8
+template <> struct Elem<2> { static constexpr int DIM = 2, NNPE = 4, NQ = 4; };    // QUAD4
+template <> struct Elem<6> { static constexpr int DIM = 3, NNPE = 4, NQ = 1; };    // TET4
+template <> struct Elem<7> { static constexpr int DIM = 3, NNPE = 10, NQ = 4; };   // TET10
+template <> struct Elem<8> { static constexpr int DIM = 3, NNPE = 27, NQ = 27; };  // HEX27
+
+// Reference-element tables, packed: N[q][a], dN[q][a][k], w[q] (doubles).
+template <int ET> struct RefLayout {
+  using E = Elem<ET>;
+  static constexpr int N_OFF = 0;
+  static constexpr int DN_OFF = E::NQ * E::NNPE;
+  static constexpr int W_OFF = DN_OFF + E::NQ * E::NNPE * E::DIM;
+  static constexpr int SIZE = W_OFF + E::NQ;
+};
+
+struct ElemArgs {
+  const int32_t* conn;      // block connectivity, 0-based, conn[e*NNPE + a]
+  int64_t ne;               // elements in the block
+  const double* coords;     // coords[node*DIM + d]
+  const double* U;          // U[node*NF + f]
+  const double* ref;        // reference tables (RefLayout)
+  double props[8];
+  const double* state_old;  // block base, (NS, NQ, NE) column-major
+  double* state_new;
+  void* Ke;                 // block base, Real[ne][NDOF][NDOF]
+  void* Re;                 // block base, Real[ne][NDOF]
+};
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double det3(const double J[3][3]) {
+  return J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+         J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+}
+
+// Isoparametric map at one point, always in FP64: J = X_el dN_xi, JxW = det(J) w,
+// dN_X = dN_xi J^{-1}.  Writes dN_X (as Real) and returns JxW; Xq optional.
+template <int ET, typename Real>
+__device__ __forceinline__ double map_point(const double* __restrict__ s_ref, int q, const double* __restrict__ s_x,
+                                            Real* __restrict__ dNX, double* Xq) {
+  using E = Elem<ET>;
+  using L = RefLayout<ET>;
+  constexpr int D = E::DIM, A = E::NNPE;
+  const double* dN = s_ref + L::DN_OFF + q * A * D;
+  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+  for (int a = 0; a < A; ++a)
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+#pragma unroll
+      for (int k = 0; k < D; ++k) J[d][k] = fma(s_x[a * D + d], dN[a * D + k], J[d][k]);
+  double Ji[3][3];
+  double det;
+  if (D == 2) {
+    det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    const double r = 1.0 / det;
+    Ji[0][0] = J[1][1] * r; Ji[0][1] = -J[0][1] * r;
+    Ji[1][0] = -J[1][0] * r; Ji[1][1] = J[0][0] * r;
+  } else {
+    det = det3(J);
+    const double r = 1.0 / det;
+    Ji[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * r;
+    Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
+    Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+    Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * r;
+    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+    Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
+    Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * r;
+    Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * r;
+    Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+  }
+#pragma unroll
+  for (int a = 0; a < A; ++a)
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      double s = 0;
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fma(dN[a * D + k], Ji[k][d], s);
+      dNX[a * D + d] = Real(s);
+    }
+  if (Xq) {
+    const double* N = s_ref + L::N_OFF + q * A;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      double s = 0;
+#pragma unroll
+      for (int a = 0; a < A; ++a) s = fma(N[a], s_x[a * D + d], s);
+      Xq[d] = s;
+    }
+  }
+  return det * s_ref[L::W_OFF + q];
+}
+
+// Copy the reference tables and gather X (and U) of each element of the CTA
+// into shared memory.  Threads of element slot ty use tx = 0..TPE-1.
+template <int ET, int NF, int EPB, int TPE>
+__device__ __forceinline__ void stage_element(const ElemArgs& g, int64_t e, int tx, int ty, double* s_ref, int* s_conn,
+                                              double* s_x, double* s_u) {
+  using E = Elem<ET>;
+  constexpr int D = E::DIM, A = E::NNPE;
+  const int tid = ty * TPE + tx;
+  for (int i = tid; i < RefLayout<ET>::SIZE; i += EPB * TPE) s_ref[i] = g.ref[i];
+  const bool live = e < g.ne;
+  if (live)
+    for (int a = tx; a < A; a += TPE) s_conn[a] = g.conn[e * A + a];
+  __syncthreads();
+  if (live) {
+    for (int i = tx; i < A * D; i += TPE) s_x[i] = __ldg(&g.coords[int64_t(s_conn[i / D]) * D + (i % D)]);
+    for (int i = tx; i < A * NF; i += TPE) s_u[i] = __ldg(&g.U[int64_t(s_conn[i / NF]) * NF + (i % NF)]);
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Poisson (test/poisson/TestPoissonCommon.jl:75-107):
+//   R_q = JxW (grad u . dN_X_a - N_a f(X_q)),  K_q = JxW dN_X_a . dN_X_b
+// one thread per element row a
+// ---------------------------------------------------------------------------
+template <int ET, typename Real, int EPB, bool WANT_R, bool WANT_K>
+__global__ void __launch_bounds__(EPB * Elem<ET>::NNPE) poisson_element_kernel(ElemArgs g) {
+  using E = Elem<ET>;
+  using L = RefLayout<ET>;
+  constexpr int D = E::DIM, A = E::NNPE, NQ = E::NQ, TPE = A;
+  __shared__ double s_ref[L::SIZE];
+  __shared__ int s_conn_all[EPB][A];
+  __shared__ double s_x_all[EPB][A * D];
+  __shared__ double s_u_all[EPB][A];
+  __shared__ Real s_dNX_all[EPB][NQ][A * D];
+  __shared__ Real s_jxw_all[EPB][NQ];
+  __shared__ Real s_gu_all[EPB][NQ][D];
+  __shared__ Real s_f_all[EPB][NQ];
+
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int64_t e = int64_t(blockIdx.x) * EPB + ty;
+  stage_element<ET, 1, EPB, TPE>(g, e, tx, ty, s_ref, s_conn_all[ty], s_x_all[ty], s_u_all[ty]);
+  const bool live = e < g.ne;
+  if (live) {
+    for (int q = tx; q < NQ; q += TPE) {
+      double Xq[3];
+      Real* dNX = s_dNX_all[ty][q];
+      const double jxw = map_point<ET, Real>(s_ref, q, s_x_all[ty], dNX, Xq);
+      s_jxw_all[ty][q] = Real(jxw);
+      if (WANT_R) {
+        double f = g.props[0];
+#pragma unroll
+        for (int d = 0; d < D; ++d) f *= sin(M_PI * Xq[d]);
+        s_f_all[ty][q] = Real(jxw * f);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          Real s = 0;
+#pragma unroll
+          for (int a = 0; a < A; ++a) s = fma(Real(s_u_all[ty][a]), dNX[a * D + d], s);
+          s_gu_all[ty][q][d] = s;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (!live) return;
+  const int a = tx;
+  Real Krow[A];
+#pragma unroll
+  for (int b = 0; b < A; ++b) Krow[b] = 0;
+  Real R = 0;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    const Real* dNX = s_dNX_all[ty][q];
+    const Real w = s_jxw_all[ty][q];
+    Real ga[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) ga[d] = dNX[a * D + d];
+    if (WANT_R) {
+      Real s = 0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) s = fma(s_gu_all[ty][q][d], ga[d], s);
+      R = fma(w, s, R);
+      R = fma(-Real(s_ref[L::N_OFF + q * A + a]), s_f_all[ty][q], R);
+    }
+    if (WANT_K) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) ga[d] *= w;
+#pragma unroll
+      for (int b = 0; b < A; ++b) {
+        Real s = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) s = fma(ga[d], dNX[b * D + d], s);
+        Krow[b] += s;
+      }
+    }
+  }
+  if (WANT_K) {
+    Real* Ke = static_cast<Real*>(g.Ke) + (e * A + a) * A;
+#pragma unroll
+    for (int b = 0; b < A; ++b) Ke[b] = Krow[b];
+  }
+  if (WANT_R) static_cast<Real*>(g.Re)[e * A + a] = R;
+}
+
+// ---------------------------------------------------------------------------
+// Constitutive models for the mechanics kernel.  Per quadrature point, point()
+// receives grad u (row-major [i][J]) and writes JxW-scaled P (P9[i*3+J]) plus
+// what aentries() needs to produce JxW-scaled A_iJkL for one i.
+// ---------------------------------------------------------------------------
+
+// Compressible Neo-Hookean (test/mechanics/TestMechanicsLargeDeformation.jl:17-27)
+//   psi = K/2 (1/2 (J-1)^2 - ln J) + G/2 (J^{-2/3} F:F - 3)
+//   P = c1 H + c2 (F - I1/3 H),  H = F^{-T}, c1 = K/2 (J^2-J-1), c2 = G J^{-2/3}
+//   A_iJkL = a1 H_iJ H_kL + a2 H_iL H_kJ + c2 d_ik d_JL - 2/3 c2 (H_kL F_iJ + F_kL H_iJ)
+//   a1 = K/2 (2J-1) J + 2/9 c2 I1,  a2 = I1/3 c2 - c1
+struct NeoHookean {
+  static constexpr int NS = 0;
+  static constexpr int SCR = 21;  // F(9) H(9) a1 a2 c2
+  template <typename Real>
+  __device__ static void point(const double* props, Real gu[3][3], Real jxw, const double*, double*, Real* P9,
+                               Real* scr) {
+    const Real Kb = Real(props[0]), Gs = Real(props[1]);
+    Real F[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) F[i][j] = gu[i][j] + (i == j ? Real(1) : Real(0));
+    const Real c00 = F[1][1] * F[2][2] - F[1][2] * F[2][1];
+    const Real c01 = F[1][2] * F[2][0] - F[1][0] * F[2][2];
+    const Real c02 = F[1][0] * F[2][1] - F[1][1] * F[2][0];
+    const Real J = F[0][0] * c00 + F[0][1] * c01 + F[0][2] * c02;
+    const Real rJ = Real(1) / J;
+    Real H[3][3];
+    H[0][0] = c00 * rJ; H[0][1] = c01 * rJ; H[0][2] = c02 * rJ;
+    H[1][0] = (F[0][2] * F[2][1] - F[0][1] * F[2][2]) * rJ;
+    H[1][1] = (F[0][0] * F[2][2] - F[0][2] * F[2][0]) * rJ;
+    H[1][2] = (F[0][1] * F[2][0] - F[0][0] * F[2][1]) * rJ;
+    H[2][0] = (F[0][1] * F[1][2] - F[0][2] * F[1][1]) * rJ;
+    H[2][1] = (F[0][2] * F[1][0] - F[0][0] * F[1][2]) * rJ;
+    H[2][2] = (F[0][0] * F[1][1] - F[0][1] * F[1][0]) * rJ;
+    Real I1 = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) I1 = fma(F[i][j], F[i][j], I1);
+    const Real c1 = Real(0.5) * Kb * (J * J - J - Real(1));
+    const Real c2 = Gs * pow(J, Real(-2.0 / 3.0));
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) P9[i * 3 + j] = jxw * (c1 * H[i][j] + c2 * (F[i][j] - I1 / Real(3) * H[i][j]));
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      scr[i] = F[i / 3][i % 3];
+      scr[9 + i] = H[i / 3][i % 3];
+    }
+    scr[18] = jxw * (Real(0.5) * Kb * (Real(2) * J - Real(1)) * J + Real(2.0 / 9.0) * c2 * I1);
+    scr[19] = jxw * (I1 / Real(3) * c2 - c1);
+    scr[20] = jxw * c2;
+  }
+  // out[J*9 + k*3 + L] = JxW A_iJkL
+  template <typename Real>
+  __device__ static void aentries(const Real* scr, int i, Real* out) {
+    const Real* F = scr;
+    const Real* H = scr + 9;
+    const Real a1 = scr[18], a2 = scr[19], c2 = scr[20];
+    const Real m23 = Real(-2.0 / 3.0) * c2;
+#pragma unroll
+    for (int J = 0; J < 3; ++J)
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int L = 0; L < 3; ++L) {
+          Real v = a1 * H[i * 3 + J] * H[k * 3 + L] + a2 * H[i * 3 + L] * H[k * 3 + J] +
+                   m23 * (H[k * 3 + L] * F[i * 3 + J] + F[k * 3 + L] * H[i * 3 + J]);
+          if (i == k && J == L) v += c2;
+          out[J * 9 + k * 3 + L] = v;
+        }
+  }
+};
+
+// J2 small-strain plasticity with linear isotropic hardening: radial return and
+// the consistent tangent (Simo & Hughes 1998, Box 3.2).  props = {E, nu, sy, H};
+// state (7) = plastic strain (xx, yy, zz, yz, xz, xy) + equivalent plastic strain.
+struct J2 {
+  static constexpr int NS = 7;
+  static constexpr int SCR = 13;  // n(9) kap' 2mu th' 2mu thb' (unused)
+  template <typename Real>
+  __device__ static void point(const double* props, Real gu[3][3], Real jxw, const double* st_old, double* st_new,
+                               Real* P9, Real* scr) {
+    const double E = props[0], nu = props[1], sy = props[2], Hh = props[3];
+    const double mu = E / (2 * (1 + nu)), lam = E * nu / ((1 + nu) * (1 - 2 * nu)), kap = lam + 2.0 / 3.0 * mu;
+    double eps[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) eps[i][j] = 0.5 * (double(gu[i][j]) + double(gu[j][i]));
+    const double ep[3][3] = {{st_old[0], st_old[5], st_old[4]},
+                             {st_old[5], st_old[1], st_old[3]},
+                             {st_old[4], st_old[3], st_old[2]}};
+    const double eqps_old = st_old[6];
+    double ee[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) ee[i][j] = eps[i][j] - ep[i][j];
+    const double tr = ee[0][0] + ee[1][1] + ee[2][2];
+    double s[3][3];
+    double sn2 = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        s[i][j] = 2 * mu * (ee[i][j] - (i == j ? tr / 3.0 : 0.0));
+        sn2 += s[i][j] * s[i][j];
+      }
+    const double snorm = sqrt(sn2);
+    const double sq23 = sqrt(2.0 / 3.0);
+    const double f = snorm - sq23 * (sy + Hh * eqps_old);
+    double dgam = 0, th = 1, thb = 0;
+    double n[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    if (f > 0) {
+      dgam = f / (2 * mu + 2.0 / 3.0 * Hh);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) n[i][j] = s[i][j] / snorm;
+      th = 1.0 - 2 * mu * dgam / snorm;
+      thb = 1.0 / (1.0 + Hh / (3 * mu)) - (1.0 - th);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        P9[i * 3 + j] = Real(double(jxw) * (s[i][j] - 2 * mu * dgam * n[i][j] + (i == j ? kap * tr : 0.0)));
+    if (st_new) {
+      st_new[0] = ep[0][0] + dgam * n[0][0];
+      st_new[1] = ep[1][1] + dgam * n[1][1];
+      st_new[2] = ep[2][2] + dgam * n[2][2];
+      st_new[3] = ep[1][2] + dgam * n[1][2];
+      st_new[4] = ep[0][2] + dgam * n[0][2];
+      st_new[5] = ep[0][1] + dgam * n[0][1];
+      st_new[6] = eqps_old + sq23 * dgam;
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) scr[i] = Real(n[i / 3][i % 3]);
+    scr[9] = Real(double(jxw) * kap);
+    scr[10] = Real(double(jxw) * 2 * mu * th);
+    scr[11] = Real(double(jxw) * 2 * mu * thb);
+    scr[12] = 0;
+  }
+  // C_iJkL = kap d_iJ d_kL + 2 mu th (I_sym - 1/3 d_iJ d_kL) - 2 mu thb n_iJ n_kL
+  template <typename Real>
+  __device__ static void aentries(const Real* scr, int i, Real* out) {
+    const Real* n = scr;
+    const Real kp = scr[9], mt = scr[10], mb = scr[11];
+#pragma unroll
+    for (int J = 0; J < 3; ++J)
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int L = 0; L < 3; ++L) {
+          const Real dij = (i == J) ? Real(1) : Real(0), dkl = (k == L) ? Real(1) : Real(0);
+          const Real isym = Real(0.5) * (Real((i == k) && (J == L)) + Real((i == L) && (J == k)));
+          out[J * 9 + k * 3 + L] = kp * dij * dkl + mt * (isym - dij * dkl / Real(3)) - mb * n[i * 3 + J] * n[k * 3 + L];
+        }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Mechanics (test/mechanics/TestMechanicsCommon.jl:140-190 with
+// src/Formulations.jl:462-576): f = JxW G P, K = JxW G A G^T with
+// G[(a,i),(i,J)] = dN_X[a][J].  Thread (r = a*3+i, cs) owns row r, column
+// chunk cs:  R_r += sum_J dNX_aJ P'_iJ;  t_kL = sum_J dNX_aJ A'_iJkL;
+// K_r,(b,k) += sum_L t_kL dNX_bL.
+// ---------------------------------------------------------------------------
+template <int ET, class Model, typename Real, int EPB, int CSPLIT, bool WANT_R, bool WANT_K>
+__global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
+    mech_element_kernel(ElemArgs g) {
+  using E = Elem<ET>;
+  using L = RefLayout<ET>;
+  constexpr int D = 3, A = E::NNPE, NQ = E::NQ, NDOF = 3 * A, TPE = NDOF * CSPLIT;
+  constexpr int CW = (A + CSPLIT - 1) / CSPLIT;  // nodes b per column chunk
+  constexpr int NS = Model::NS, SCR = Model::SCR;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // carve shared memory
+  double* s_ref = reinterpret_cast<double*>(smem_raw);
+  double* s_x_all = s_ref + ((L::SIZE + 1) & ~1);
+  double* s_u_all = s_x_all + EPB * A * D;
+  Real* s_dNX_all = reinterpret_cast<Real*>(s_u_all + EPB * A * D);
+  Real* s_jxw_all = s_dNX_all + EPB * NQ * A * D;
+  Real* s_P_all = s_jxw_all + EPB * NQ;
+  Real* s_scr_all = s_P_all + EPB * NQ * 9;
+  Real* s_A_all = s_scr_all + EPB * NQ * SCR;
+  int* s_conn_all = reinterpret_cast<int*>(s_A_all + (WANT_K ? EPB * NQ * 81 : 0));
+
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int64_t e = int64_t(blockIdx.x) * EPB + ty;
+  double* s_x = s_x_all + ty * A * D;
+  double* s_u = s_u_all + ty * A * D;
+  Real* s_dNX = s_dNX_all + ty * NQ * A * D;
+  Real* s_jxw = s_jxw_all + ty * NQ;
+  Real* s_P = s_P_all + ty * NQ * 9;
+  Real* s_scr = s_scr_all + ty * NQ * SCR;
+  Real* s_A = s_A_all + ty * NQ * 81;
+  stage_element<ET, 3, EPB, TPE>(g, e, tx, ty, s_ref, s_conn_all + ty * A, s_x, s_u);
+  const bool live = e < g.ne;
+
+  // quadrature-point kinematics + constitutive update (one thread per point)
+  if (live) {
+    for (int q = tx; q < NQ; q += TPE) {
+      Real* dNX = s_dNX + q * A * D;
+      const double jxw = map_point<ET, Real>(s_ref, q, s_x, dNX, nullptr);
+      s_jxw[q] = Real(jxw);
+      Real gu[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          Real s = 0;
+#pragma unroll
+          for (int a = 0; a < A; ++a) s = fma(Real(s_u[a * 3 + i]), dNX[a * 3 + j], s);
+          gu[i][j] = s;
+        }
+      const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
+      double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
+      Model::point(g.props, gu, Real(jxw), so, sn, s_P + q * 9, s_scr + q * SCR);
+    }
+  }
+  __syncthreads();
+  // JxW-scaled tangent entries A'_iJkL, one (q, i) per thread
+  if (WANT_K && live) {
+    for (int w = tx; w < NQ * 3; w += TPE) {
+      const int q = w / 3, i = w % 3;
+      Model::aentries(s_scr + q * SCR, i, s_A + q * 81 + i * 27);
+    }
+  }
+  __syncthreads();
+  if (!live) return;
+
+  const int r = tx % NDOF, cs = tx / NDOF;
+  const int a = r / 3, i = r % 3;
+  const int b0 = cs * CW;
+  Real Krow[CW * 3];
+#pragma unroll
+  for (int c = 0; c < CW * 3; ++c) Krow[c] = 0;
+  Real R = 0;
+  for (int q = 0; q < NQ; ++q) {
+    const Real* dNX = s_dNX + q * A * D;
+    const Real g0 = dNX[a * 3 + 0], g1 = dNX[a * 3 + 1], g2 = dNX[a * 3 + 2];
+    if (WANT_R && cs == 0) {
+      const Real* P = s_P + q * 9 + i * 3;
+      R = fma(g0, P[0], fma(g1, P[1], fma(g2, P[2], R)));
+    }
+    if (WANT_K) {
+      const Real* Ai = s_A + q * 81 + i * 27;
+      Real t[9];
+#pragma unroll
+      for (int kl = 0; kl < 9; ++kl) t[kl] = fma(g0, Ai[kl], fma(g1, Ai[9 + kl], g2 * Ai[18 + kl]));
+#pragma unroll
+      for (int bb = 0; bb < CW; ++bb) {
+        const int b = b0 + bb;
+        if (b < A) {
+          const Real h0 = dNX[b * 3 + 0], h1 = dNX[b * 3 + 1], h2 = dNX[b * 3 + 2];
+#pragma unroll
+          for (int k = 0; k < 3; ++k)
+            Krow[bb * 3 + k] += fma(t[k * 3 + 0], h0, fma(t[k * 3 + 1], h1, t[k * 3 + 2] * h2));
+        }
+      }
+    }
+  }
+  if (WANT_K) {
+    Real* Ke = static_cast<Real*>(g.Ke) + (e * NDOF + r) * NDOF + b0 * 3;
+#pragma unroll
+    for (int c = 0; c < CW * 3; ++c)
+      if (b0 * 3 + c < NDOF) Ke[c] = Krow[c];
+  }
+  if (WANT_R && cs == 0) static_cast<Real*>(g.Re)[e * NDOF + r] = R;
+}
+
+template <int ET, class Model, typename Real, int EPB, bool WANT_K>
+constexpr size_t mech_smem_bytes() {
+  using E = Elem<ET>;
+  constexpr int A = E::NNPE, NQ = E::NQ;
+  return sizeof(double) * (((RefLayout<ET>::SIZE + 1) & ~1) + 2 * EPB * A * 3) +
+         sizeof(Real) * (EPB * NQ * A * 3 + EPB * NQ + EPB * NQ * 9 + EPB * NQ * Model::SCR +
+                         (WANT_K ? EPB * NQ * 81 : 0)) +
+         sizeof(int) * EPB * A + 16;
+}
+
+// ---------------------------------------------------------------------------
+// Node gather: deterministic element-ordered reduction into CSC nzval and the
+// residual over unknowns.
+// ---------------------------------------------------------------------------
+struct BlockInfo {
+  int64_t elem_start;   // first global element id of the block
+  int64_t ke_off;       // Ke offset (entries) of the block
+  int64_t re_off;       // Re offset (entries) of the block
+  int64_t conn_off;     // offset into conn (entries)
+  int64_t epos_off;     // offset into epos (entries)
+  int nnpe;
+  int ndof;
+};
+
+constexpr int MAX_BLOCKS = 16;
+
+struct GatherArgs {
+  int64_t nn;                  // nodes
+  int nf;                      // fields per node
+  int nblocks;
+  BlockInfo blk[MAX_BLOCKS];
+  const int64_t* nadj_ptr;     // [nn+1]
+  const int64_t* nadj;         // (global element << 5) | local node
+  const int32_t* conn;         // all blocks, 0-based
+  const uint16_t* epos;        // [elem][a][b] row offset of node conn[b] inside node conn[a]'s columns
+  const uint8_t* umask;        // per node: bit f set when dof (node, f) is unknown
+  const int64_t* col_base;     // per node: nzval offset of its first column
+  const int32_t* col_len;      // per node: rows per column
+  const int64_t* dof_to_unknown;  // per dof: 0-based unknown index or -1
+  const void* Ke;
+  const void* Re;
+  double* nzval;               // may be null
+  double* R_u;                 // may be null
+  int acc_stride;              // doubles of accumulator per warp
+};
+
+template <typename Real, int NF, int WPB>
+__global__ void __launch_bounds__(WPB * 32) node_gather_kernel(GatherArgs g) {
+  extern __shared__ __align__(16) double s_acc[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t n = int64_t(blockIdx.x) * WPB + warp;
+  if (n >= g.nn) return;
+  const unsigned um = g.umask[n];
+  if (um == 0) return;
+  const int Ln = g.col_len[n];
+  const int ncols = __popc(um);
+  double* acc = s_acc + warp * g.acc_stride;
+  const bool wantK = g.nzval != nullptr;
+  const bool wantR = g.R_u != nullptr;
+  if (wantK)
+    for (int j = lane; j < ncols * Ln; j += 32) acc[j] = 0.0;
+  double racc = 0.0;
+  __syncwarp();
+  const int64_t p0 = g.nadj_ptr[n], p1 = g.nadj_ptr[n + 1];
+  for (int64_t p = p0; p < p1; ++p) {
+    const int64_t packed = g.nadj[p];
+    const int64_t ge = packed >> 5;
+    const int a = int(packed & 31);
+    int bi = 0;
+    while (bi + 1 < g.nblocks && ge >= g.blk[bi + 1].elem_start) ++bi;
+    const BlockInfo& B = g.blk[bi];
+    const int64_t le = ge - B.elem_start;
+    const int A = B.nnpe, NDOF = B.ndof;
+    if (wantR && lane < NF && ((um >> lane) & 1u))
+      racc += double(static_cast<const Real*>(g.Re)[B.re_off + le * NDOF + a * NF + lane]);
+    if (wantK) {
+      const Real* Krows = static_cast<const Real*>(g.Ke) + B.ke_off + (le * NDOF + int64_t(a) * NF) * NDOF;
+      const int32_t* cn = g.conn + B.conn_off + le * A;
+      const uint16_t* ep = g.epos + B.epos_off + (le * A + a) * A;
+      const int total = NF * NDOF;
+      for (int t = lane; t < total; t += 32) {
+        const int k = t / NDOF, rem = t - k * NDOF;
+        const int b = rem / NF, i = rem - b * NF;
+        if (!((um >> k) & 1u)) continue;
+        const int m = cn[b];
+        const unsigned umm = g.umask[m];
+        if (!((umm >> i) & 1u)) continue;
+        const int kk = __popc(um & ((1u << k) - 1u));
+        const int ii = __popc(umm & ((1u << i) - 1u));
+        acc[kk * Ln + ep[b] + ii] += double(Krows[t]);
+      }
+      __syncwarp();
+    }
+  }
+  if (wantK) {
+    double* out = g.nzval + g.col_base[n];
+    for (int j = lane; j < ncols * Ln; j += 32) out[j] = acc[j];
+  }
+  if (wantR && lane < NF && ((um >> lane) & 1u)) g.R_u[g.dof_to_unknown[n * NF + lane]] = racc;
+}
+
+}  // namespace fec

@@ -1,0 +1,25 @@
+// fec_launch.h -- host-side launchers of the kernels in fec_kernels.cuh.
+// Each physics family is instantiated in its own translation unit so the
+// library builds in parallel.
+#pragma once
+#include <cuda_runtime.h>
+#include "fec_kernels.cuh"
+
+namespace fec {
+
+// Return cudaSuccess, or cudaErrorNotSupported for a combination that is not
+// built.  *launches is incremented by the kernels launched.
+cudaError_t launch_poisson(int elem_type, int precision, bool want_r, bool want_k, const ElemArgs& args,
+                           cudaStream_t stream, int* launches);
+cudaError_t launch_mech(int physics, int elem_type, int precision, bool want_r, bool want_k, const ElemArgs& args,
+                        cudaStream_t stream, int* launches);
+cudaError_t launch_gather(int precision, int nf, const GatherArgs& args, cudaStream_t stream, int* launches);
+
+// Reference-element tables (RefLayout order) for an element type, in double.
+// Returns the number of doubles written (0 for an unknown type).
+int ref_tables(int elem_type, double* out, int cap);
+int elem_nnpe(int elem_type);
+int elem_dim(int elem_type);
+int elem_nq(int elem_type);
+
+}  // namespace fec

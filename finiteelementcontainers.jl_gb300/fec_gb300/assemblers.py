@@ -1,0 +1,298 @@
+"""SparseMatrixAssembler and the assembly entry points, over libfec_gb300.so.
+
+Mirrors src/assemblers/SparseMatrixAssembler.jl, Vector.jl, Matrix.jl and the
+residual/stiffness accessors of Assemblers.jl for the default configuration
+(CSC, non-condensed, return-value physics methods).  Julia's in-place `!`
+names lose the bang: assemble_vector!(asm, residual, Uu, p) becomes
+assemble_vector(asm, residual, Uu, p).
+
+Device memory, streams and the host<->device copies use torch; every
+assembly FLOP runs in the library's sm_103a kernels.  There is no CPU
+fallback: without the library (or without a GPU) these calls raise."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .bcs import dirichlet_dofs
+from .dofs import DofManager, update_dofs
+from .meshes import ELEMENT_IDS
+from .physics import AbstractPhysics
+from .spaces import FunctionSpace
+
+PRECISIONS = {"fp64": _lib.FEC_FP64, "fp32_element": _lib.FEC_FP32_ELEMENT}
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class CSCMatrix:
+    """Sparse CSC matrix over unknowns: 1-based int64 colptr/rowval on the host
+    (SparseMatrixCSC layout) and the values on the device (CuSparseMatrixCSC's nzval)."""
+
+    def __init__(self, n: int, colptr: np.ndarray, rowval: np.ndarray, nzval):
+        self.shape = (n, n)
+        self.colptr = colptr
+        self.rowval = rowval
+        self.nzval = nzval
+
+    @property
+    def nnz(self) -> int:
+        return int(self.rowval.size)
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        vals = self.nzval.detach().cpu().numpy() if hasattr(self.nzval, "detach") else np.asarray(self.nzval)
+        return sp.csc_matrix((vals, self.rowval - 1, self.colptr - 1), shape=self.shape)
+
+
+class SparseMatrixAssembler:
+    """SparseMatrixAssembler(var; sparse_matrix_type=:csc, use_condensed=false)
+    (src/assemblers/SparseMatrixAssembler.jl:64-133).
+
+    device: CUDA device index, or -1 for a host-only assembler that can build
+    the pattern (colptr/rowval) but not assemble values."""
+
+    def __init__(self, var_or_dof, *, sparse_matrix_type: str = "csc", use_condensed: bool = False,
+                 use_inplace_methods: bool = False, device: int = 0, precision: str = "fp64"):
+        if sparse_matrix_type != "csc":
+            raise NotImplementedError(f"sparse_matrix_type={sparse_matrix_type!r}: the accelerated path builds CSC")
+        if use_condensed:
+            raise NotImplementedError("use_condensed=true is not on the accelerated path")
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
+        self.dof = var_or_dof if isinstance(var_or_dof, DofManager) else DofManager(var_or_dof)
+        self.fspace: FunctionSpace = self.dof.var.fspace
+        self.use_inplace_methods = use_inplace_methods
+        self.precision = precision
+        self.device = device
+        self._lib = _lib.load()
+        h = C.c_void_p()
+        st = self._lib.fec_ctx_create(device, C.byref(h))
+        if st != _lib.FEC_OK:
+            raise _lib.FECError(st, _lib.last_error(self._lib, None))
+        self._ctx = h
+        fs = self.fspace
+        coords = np.ascontiguousarray(fs.coords, dtype=np.float64)
+        types = fs.element_type_ids()
+        self._call("fec_mesh_set", fs.num_dimensions, fs.num_nodes, _lib.ptr(coords), len(types), _lib.ptr(types),
+                   _lib.ptr(fs.block_num_elems), _lib.ptr(fs.conn_data))
+        self._physics_key = None
+        self._push_dofs()
+
+    # -- plumbing ---------------------------------------------------------------
+    def _call(self, name, *args):
+        _lib.check(self._lib, self._ctx, getattr(self._lib, name)(self._ctx, *args))
+
+    def __del__(self):
+        ctx = getattr(self, "_ctx", None)
+        if ctx is not None and ctx.value:
+            self._lib.fec_ctx_destroy(ctx)
+            self._ctx = None
+
+    def _push_dofs(self):
+        dtu = np.ascontiguousarray(self.dof.dof_to_unknown, dtype=np.int64)
+        self._call("fec_dofs_set", self.dof.nf, _lib.ptr(dtu), int(self.dof.unknown_dofs.size))
+        self._pattern_dirty = True
+        self._csc_host = None
+        self.residual_unknowns = None
+        self.stiffness_nzval = None
+
+    def _ensure_pattern(self):
+        if self._pattern_dirty:
+            nnz = C.c_int64()
+            self._call("fec_pattern_build", C.byref(nnz))
+            self.nnz = int(nnz.value)
+            self._pattern_dirty = False
+        return self.nnz
+
+    def _torch_device(self):
+        return f"cuda:{self.device}"
+
+    # -- reference API -------------------------------------------------------------
+    def pattern(self) -> tuple[np.ndarray, np.ndarray]:
+        """1-based (colptr, rowval) of the CSC stiffness over unknowns."""
+        self._ensure_pattern()
+        if self._csc_host is None:
+            n = int(self.dof.unknown_dofs.size)
+            colptr = np.empty(n + 1, dtype=np.int64)
+            rowval = np.empty(self.nnz, dtype=np.int64)
+            self._call("fec_pattern_get", _lib.ptr(colptr), _lib.ptr(rowval))
+            self._csc_host = (colptr, rowval)
+        return self._csc_host
+
+    def create_field(self):
+        return _torch().zeros(len(self.dof), dtype=_torch().float64, device=self._torch_device())
+
+    def create_unknowns(self):
+        return _torch().zeros(self.dof.unknown_dofs.size, dtype=_torch().float64, device=self._torch_device())
+
+    def last_launch_count(self) -> int:
+        return int(self._lib.fec_last_launch_count(self._ctx))
+
+
+def update_dofs_bcs(asm: SparseMatrixAssembler, dirichlet_bcs) -> None:
+    """update_dofs!(asm, dirichlet_bcs, periodic_bcs) (SparseMatrixAssembler.jl:228-274)."""
+    ddofs = dirichlet_dofs(dirichlet_bcs, asm.fspace.mesh, asm.dof)
+    update_dofs(asm.dof, ddofs)
+    asm._push_dofs()
+
+
+class Parameters:
+    """The parts of Parameters (src/Parameters.jl) the assembly reads: time,
+    nodal field U (device), per-block physics/properties, state old/new
+    ((NS, NQ, NE) per block, concatenated) and Dirichlet values."""
+
+    def __init__(self, mesh, asm: SparseMatrixAssembler, physics, props=None, *, dirichlet_bcs=(), t: float = 0.0,
+                 dt: float = 0.0):
+        torch = _torch()
+        nb = asm.fspace.num_blocks()
+        if isinstance(physics, AbstractPhysics):
+            physics = {name: physics for name in asm.fspace.block_names}
+        self.physics = [physics[name] for name in asm.fspace.block_names]
+        if props is None:
+            props = {name: ph.create_properties() for name, ph in zip(asm.fspace.block_names, self.physics)}
+        elif not isinstance(props, dict):
+            props = {name: props for name in asm.fspace.block_names}
+        self.props = [np.ascontiguousarray(props[name], dtype=np.float64) for name in asm.fspace.block_names]
+        for ph in self.physics:
+            if ph.NF != asm.dof.nf:
+                raise ValueError(f"physics {type(ph).__name__} has {ph.NF} fields but the function has {asm.dof.nf}")
+        dev = asm._torch_device()
+        self.t, self.dt = float(t), float(dt)
+        self.dirichlet_bcs = list(dirichlet_bcs)
+        update_dofs_bcs(asm, self.dirichlet_bcs)
+        self.field = torch.zeros(len(asm.dof), dtype=torch.float64, device=dev)
+        self.field_old = torch.zeros_like(self.field)
+        sizes = []
+        for b, (ph, (nq, ne)) in enumerate(zip(self.physics, asm.fspace.block_quadrature_sizes())):
+            s0 = ph.create_initial_state()
+            sizes.append(np.tile(s0, nq * ne))
+        init = np.concatenate(sizes) if sizes else np.zeros(0)
+        self.state_old = torch.as_tensor(init, dtype=torch.float64).to(dev)
+        self.state_new = self.state_old.clone()
+        self._mesh = mesh
+        self._asm = asm
+        self.update_bc_values()
+        assert nb == len(self.physics)
+
+    def update_bc_values(self):
+        """update_bc_values!(dirichlet_bcs, X, t): evaluate each BC at its nodes."""
+        torch = _torch()
+        dofs, vals = [], []
+        X = self._asm.fspace.coords
+        for bc in self.dirichlet_bcs:
+            d, nodes = bc.dofs_and_nodes(self._mesh, self._asm.dof)
+            dofs.append(d)
+            vals.append(np.array([bc.func(X[n - 1], self.t) for n in nodes], dtype=np.float64))
+        dev = self._asm._torch_device()
+        if dofs:
+            d = np.concatenate(dofs)
+            v = np.concatenate(vals)
+            self.bc_dofs = torch.as_tensor(d, dtype=torch.int64).to(dev)
+            self.bc_vals = torch.as_tensor(v, dtype=torch.float64).to(dev)
+        else:
+            self.bc_dofs = torch.zeros(0, dtype=torch.int64, device=dev)
+            self.bc_vals = torch.zeros(0, dtype=torch.float64, device=dev)
+
+    def swap_states(self):
+        """state_old <- state_new after a converged step (the reference leaves
+        this to downstream applications)."""
+        self.state_old, self.state_new = self.state_new, self.state_old
+
+
+def create_parameters(mesh, asm, physics, props=None, *, dirichlet_bcs=(), t: float = 0.0, dt: float = 0.0):
+    """create_parameters(mesh, asm, physics, props; dirichlet_bcs) (src/Parameters.jl:288-302)."""
+    return Parameters(mesh, asm, physics, props, dirichlet_bcs=dirichlet_bcs, t=t, dt=dt)
+
+
+# -- physics-method markers (the Julia generic functions residual/stiffness) ---------------------
+
+def residual(obj, *args):
+    """residual(asm): the assembled residual over unknowns (Assemblers.jl:347-371).
+    Passed as the function argument of assemble_vector it selects the physics'
+    residual, which runs on the device."""
+    if isinstance(obj, SparseMatrixAssembler):
+        if obj.residual_unknowns is None:
+            obj.residual_unknowns = obj.create_unknowns()
+        return obj.residual_unknowns
+    raise TypeError("physics residuals run inside the device kernels; pass `residual` to assemble_vector")
+
+
+def stiffness(obj, *args):
+    """stiffness(asm): the assembled CSC tangent over unknowns (Assemblers.jl:376-388)."""
+    if isinstance(obj, SparseMatrixAssembler):
+        colptr, rowval = obj.pattern()
+        if obj.stiffness_nzval is None:
+            obj.stiffness_nzval = _torch().zeros(obj.nnz, dtype=_torch().float64, device=obj._torch_device())
+        return CSCMatrix(int(obj.dof.unknown_dofs.size), colptr, rowval, obj.stiffness_nzval)
+    raise TypeError("physics tangents run inside the device kernels; pass `stiffness` to assemble_stiffness")
+
+
+def _as_device_unknowns(asm, Uu):
+    torch = _torch()
+    dev = asm._torch_device()
+    if isinstance(Uu, np.ndarray):
+        return torch.from_numpy(np.ascontiguousarray(Uu, dtype=np.float64)).to(dev, non_blocking=True)
+    if Uu.device.type != "cuda":
+        return Uu.to(dev, dtype=torch.float64, non_blocking=True)
+    if Uu.dtype != torch.float64 or not Uu.is_contiguous():
+        raise TypeError("Uu must be a contiguous float64 tensor")
+    return Uu
+
+
+def _assemble(asm: SparseMatrixAssembler, want: int, Uu, p: Parameters, precision: str | None):
+    torch = _torch()
+    asm._ensure_pattern()
+    key = tuple((ph.ID, pr.tobytes()) for ph, pr in zip(p.physics, p.props))
+    if key != asm._physics_key:
+        for b, (ph, pr) in enumerate(zip(p.physics, p.props), start=1):
+            asm._call("fec_physics_set", b, ph.ID, _lib.ptr(pr), int(pr.size))
+        asm._physics_key = key
+    n_u = int(asm.dof.unknown_dofs.size)
+    Uu_d = _as_device_unknowns(asm, Uu)
+    if Uu_d.numel() != n_u:
+        raise ValueError(f"Uu has {Uu_d.numel()} entries, expected {n_u}")
+    stream = C.c_void_p(torch.cuda.current_stream(asm.device).cuda_stream)
+    asm._call("fec_update_field", _lib.ptr(p.field), _lib.ptr(Uu_d), int(p.bc_dofs.numel()),
+              _lib.ptr(p.bc_dofs) if p.bc_dofs.numel() else None,
+              _lib.ptr(p.bc_vals) if p.bc_vals.numel() else None, stream)
+    R = residual(asm) if want & _lib.FEC_WANT_RESIDUAL else None
+    K = stiffness(asm) if want & _lib.FEC_WANT_STIFFNESS else None
+    has_state = any(ph.NS for ph in p.physics)
+    asm._call("fec_assemble", want, PRECISIONS[precision or asm.precision], p.t, p.dt, _lib.ptr(p.field),
+              _lib.ptr(p.field_old), _lib.ptr(p.state_old) if has_state else None,
+              _lib.ptr(p.state_new) if has_state else None, _lib.ptr(R), _lib.ptr(K.nzval) if K else None, stream)
+    return R, K
+
+
+def assemble_vector(asm: SparseMatrixAssembler, func, Uu, p: Parameters, *, precision: str | None = None):
+    """assemble_vector!(asm, residual, Uu, p) (src/assemblers/Vector.jl:4-20)."""
+    if func is not residual:
+        raise NotImplementedError("assemble_vector supports the physics `residual` method")
+    _assemble(asm, _lib.FEC_WANT_RESIDUAL, Uu, p, precision)
+
+
+def assemble_stiffness(asm: SparseMatrixAssembler, func, Uu, p: Parameters, *, precision: str | None = None):
+    """assemble_stiffness!(asm, stiffness, Uu, p) (src/assemblers/Matrix.jl:12-21)."""
+    if func is not stiffness:
+        raise NotImplementedError("assemble_stiffness supports the physics `stiffness` method")
+    _assemble(asm, _lib.FEC_WANT_STIFFNESS, Uu, p, precision)
+
+
+assemble_matrix = assemble_stiffness
+
+
+def assemble_residual_and_stiffness(asm: SparseMatrixAssembler, Uu, p: Parameters, *, precision: str | None = None):
+    """One fused pass producing both residual(asm) and stiffness(asm), the pair a
+    Newton iteration assembles (src/Solvers.jl:128-153)."""
+    return _assemble(asm, _lib.FEC_WANT_RESIDUAL | _lib.FEC_WANT_STIFFNESS, Uu, p, precision)
+
+
+__all__ = ["SparseMatrixAssembler", "CSCMatrix", "Parameters", "create_parameters", "update_dofs_bcs",
+           "assemble_vector", "assemble_stiffness", "assemble_matrix", "assemble_residual_and_stiffness",
+           "residual", "stiffness", "ELEMENT_IDS"]

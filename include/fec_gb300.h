@@ -1,0 +1,151 @@
+/*
+ * fec_gb300.h -- C ABI of the GB300 (sm_103a) assembly library libfec_gb300.so.
+ *
+ * The library replaces the KernelAbstractions/Atomix device path of
+ * FiniteElementContainers.jl's SparseMatrixAssembler: per-element quadrature of
+ * the physics residual and tangent, the DOF/coordinate gather through the
+ * DofManager and FunctionSpace connectivity, and the deterministic scatter into
+ * the global residual over unknowns and the CSC nzval.
+ *
+ * Conventions (all follow the reference so that its arrays pass unchanged):
+ *   - integer inputs are 1-based int64 (Julia Int), as the reference stores them;
+ *   - coordinates and nodal fields are interleaved, field[(node-1)*NF + d]
+ *     (H1Field, src/Fields.jl:36-40, 237-254);
+ *   - connectivity is the flat concatenation of per-block NNPE x NE
+ *     column-major matrices (Connectivity, src/Fields.jl:129-160);
+ *   - colptr/rowval come back 1-based int64, ready for SparseMatrixCSC;
+ *   - pointers named *_dev are device pointers owned by the caller (a CuArray's
+ *     pointer(x) in Julia, a torch tensor's data_ptr() in Python); everything
+ *     else is host memory.  The library owns connectivity, maps and workspaces
+ *     inside the context and frees them in fec_ctx_destroy.
+ *   - every call returns FEC_OK (0) or a negative fec_status; fec_last_error
+ *     gives the message.  Nothing aborts or traps.
+ *   - device work is ordered on the caller's stream (cudaStream_t passed as
+ *     void*; NULL = legacy default stream).  One context per host thread.
+ */
+#ifndef FEC_GB300_H
+#define FEC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fec_ctx fec_ctx;
+
+/* status codes */
+enum {
+  FEC_OK = 0,
+  FEC_ERR_ARG = -1,       /* bad argument (null, size, range) */
+  FEC_ERR_STATE = -2,     /* call out of order (e.g. assemble before pattern) */
+  FEC_ERR_CUDA = -3,      /* a CUDA runtime call failed */
+  FEC_ERR_UNSUPPORTED = -4,/* element/physics combination not built */
+  FEC_ERR_NONFINITE = -5, /* NaN/Inf found in an assembled output */
+  FEC_ERR_DEVICE = -6     /* a kernel reported an error status */
+};
+
+/* element types: the reference's juliac-safe ids where it has one
+ * (src/FunctionSpaces.jl:48-62); HEX27 is this library's own */
+enum { FEC_HEX8 = 1, FEC_QUAD4 = 2, FEC_TET4 = 6, FEC_TET10 = 7, FEC_HEX27 = 8 };
+
+/* physics plugins; the reference selects them by Julia dispatch on
+ * AbstractPhysics{NF,NP,NS} (src/Physics.jl:1-57), which cannot cross a C ABI,
+ * so here they are an enum plus a property block */
+enum {
+  FEC_PHYS_POISSON = 1,    /* NF=1; props[0] = source amplitude a, f(X) = a prod_d sin(pi X_d) */
+  FEC_PHYS_NEOHOOKEAN = 2, /* NF=3; props = {bulk K, shear G} */
+  FEC_PHYS_J2 = 3          /* NF=3, NS=7; props = {E, nu, sigma_y, H} */
+};
+
+/* arithmetic of the element kernels */
+enum {
+  FEC_FP64 = 0,         /* FP64 throughout */
+  FEC_FP32_ELEMENT = 1  /* per-element kinematics/stress/tangent in FP32, Jacobian
+                           det/inverse and the global accumulation in FP64 */
+};
+
+/* what fec_assemble writes */
+enum { FEC_WANT_RESIDUAL = 1, FEC_WANT_STIFFNESS = 2 };
+
+/* Context ------------------------------------------------------------------ */
+
+/* Replaces: the device move of an assembler, asm |> cuda
+ * (ext/CUDAExt.jl:8-10, src/Utils.jl:286-291).  device = -1 makes a host-only
+ * context: mesh, DOF and pattern calls work, kernel calls return FEC_ERR_STATE. */
+int fec_ctx_create(int device, fec_ctx** out);
+int fec_ctx_destroy(fec_ctx* ctx);
+/* Copies the last error message of ctx (or of the last failed create when
+ * ctx is NULL) into buf; returns the last status. */
+int fec_last_error(const fec_ctx* ctx, char* buf, size_t len);
+
+/* Mesh / FunctionSpace ------------------------------------------------------ */
+
+/* Replaces: FunctionSpace(mesh, H1Field, Lagrange) connectivity + coordinates
+ * (src/FunctionSpaces.jl:104-126, src/Fields.jl:129-188).
+ * coords: dim x num_nodes interleaved; conn: flat 1-based, block b holding
+ * nnpe(elem_types[b]) * block_num_elems[b] entries. */
+int fec_mesh_set(fec_ctx* ctx, int dim, int64_t num_nodes, const double* coords, int num_blocks,
+                 const int32_t* elem_types, const int64_t* block_num_elems, const int64_t* conn);
+
+/* Per-block physics and properties (the (physics, props) pair that
+ * foreach_block hands to _assemble_block!, src/Utils.jl:171-189). */
+int fec_physics_set(fec_ctx* ctx, int block, int physics, const double* props, int num_props);
+
+/* DofManager ---------------------------------------------------------------- */
+
+/* Replaces: update_dofs!(dof, dirichlet_dofs, ...) (src/DofManagers.jl:227-298)
+ * as consumed by the assembler.  dof_to_unknown has num_fields * num_nodes
+ * entries: the 1-based unknown index of each dof, or -1 for a Dirichlet dof;
+ * unknowns must be numbered in increasing dof order, as the reference does. */
+int fec_dofs_set(fec_ctx* ctx, int num_fields, const int64_t* dof_to_unknown, int64_t num_unknowns);
+
+/* Sparsity pattern ---------------------------------------------------------- */
+
+/* Replaces: SparseMatrixPattern + _update_dofs! (src/assemblers/SparsityPatterns.jl:53-117,
+ * 160-231) together with the colptr/rowval half of SparseArrays.sparse!
+ * (:301-308).  Builds the CSC pattern over unknowns and the element -> nzval
+ * maps; returns the number of stored entries. */
+int fec_pattern_build(fec_ctx* ctx, int64_t* nnz_out);
+/* Copies the 1-based colptr (num_unknowns + 1) and rowval (nnz) to host. */
+int fec_pattern_get(const fec_ctx* ctx, int64_t* colptr, int64_t* rowval);
+
+/* Field update -------------------------------------------------------------- */
+
+/* Replaces: update_field_dirichlet_bcs! + update_field_unknowns!
+ * (src/bcs/DirichletBCs.jl:411-418, src/DofManagers.jl:349-411).
+ * U_dev[bc_dofs[i]-1] = bc_vals[i];  U_dev[unknown_dofs[k]-1] = Uu_dev[k].
+ * bc_dofs_dev/bc_vals_dev may be NULL when num_bc == 0. */
+int fec_update_field(fec_ctx* ctx, double* U_dev, const double* Uu_dev, int64_t num_bc, const int64_t* bc_dofs_dev,
+                     const double* bc_vals_dev, void* stream);
+
+/* Assembly ------------------------------------------------------------------ */
+
+/* Replaces: assemble_vector! + residual(asm) and assemble_stiffness!/
+ * assemble_matrix! + stiffness(asm) (src/assemblers/Vector.jl:4-74,
+ * src/assemblers/Matrix.jl:12-75, src/assemblers/Assemblers.jl:347-388, 402-432),
+ * non-condensed, CSC.
+ *   U_dev        full nodal field (NF * num_nodes), already updated
+ *   U_old_dev    previous field (may be NULL; no physics here reads it)
+ *   state_*_dev  per block (NS, NQ, NE) column-major, blocks concatenated; NULL when NS = 0
+ *   R_u_dev      residual over unknowns (num_unknowns), written when want & FEC_WANT_RESIDUAL
+ *   nzval_dev    CSC values (nnz), written when want & FEC_WANT_STIFFNESS
+ * Contributions to one output entry are summed in increasing element order,
+ * the order SparseArrays.sparse! combines the reference's element-ordered COO
+ * entries, so repeated calls give bitwise-identical results. */
+int fec_assemble(fec_ctx* ctx, int want, int precision, double t, double dt, const double* U_dev,
+                 const double* U_old_dev, const double* state_old_dev, double* state_new_dev, double* R_u_dev,
+                 double* nzval_dev, void* stream);
+
+/* Number of kernels fec_assemble launched in the last call (for accounting). */
+int fec_last_launch_count(const fec_ctx* ctx);
+
+/* Sizes the context knows (any pointer may be NULL). */
+int fec_sizes(const fec_ctx* ctx, int64_t* num_nodes, int64_t* num_elems, int64_t* num_unknowns, int64_t* nnz,
+              int64_t* state_len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FEC_GB300_H */

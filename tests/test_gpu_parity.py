@@ -1,0 +1,199 @@
+"""GPU parity: libfec_gb300.so through its C ABI (via the fec_gb300 host mirror)
+against the CPU oracle on the same seeded inputs.
+
+Bar: colptr/rowval and DOF numbering bit-exact; FP64 residual and nzval within
+1e-12 relative (max-abs over max-abs, and 2-norm); the FP32-element variant
+within 1e-5 relative of the FP64 oracle."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spl
+
+from helpers import blocks_of, rel_err, stretch_field
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+TOL64 = 1e-12
+TOL32 = 1e-5
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _setup(fec, mesh, var_kind, physics, bcs=(), precision="fp64"):
+    V = fec.FunctionSpace(mesh)
+    var = fec.ScalarFunction(V, "u") if var_kind == "scalar" else fec.VectorFunction(V, "u")
+    asm = fec.SparseMatrixAssembler(var, device=0, precision=precision)
+    p = fec.create_parameters(mesh, asm, physics, dirichlet_bcs=bcs)
+    return asm, p
+
+
+def _run(fec, asm, p, Ufull, precision=None):
+    torch = _torch()
+    Uu = torch.from_numpy(Ufull[asm.dof.unknown_dofs - 1].copy()).cuda()
+    R, K = fec.assemble_residual_and_stiffness(asm, Uu, p, precision=precision)
+    torch.cuda.synchronize()
+    return R.cpu().numpy().copy(), K.nzval.cpu().numpy().copy(), K
+
+
+def _oracle(orc, mesh, phys_name, props, Ufull, asm, st_old=None, st_new=None):
+    return orc.assembled_system(blocks_of(mesh), mesh.nodal_coords, phys_name, props, Ufull,
+                                asm.dof.dof_to_unknown, asm.dof.unknown_dofs, st_old, st_new)
+
+
+def test_poisson_hex8_32cubed_all_faces_dirichlet(fec, orc):
+    """Plain Poisson workload: unit cube, 32^3 hex8, u = 0 on all faces, u ~ U[-1,1] (seed 0),
+    f = sin(pi x) sin(pi y) sin(pi z)."""
+    n = 33
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n, n, n))
+    bcs = [fec.DirichletBC("u", lambda X, t: 0.0, nodeset_name=f) for f in orc.HEX8_FACES]
+    asm, p = _setup(fec, mesh, "scalar", fec.Poisson(1.0), bcs)
+    assert asm.dof.unknown_dofs.size == 29791
+    rng = np.random.default_rng(0)
+    U = rng.uniform(-1.0, 1.0, n ** 3)
+    U[asm.dof.dirichlet_dofs - 1] = 0.0
+    R, nz, K = _run(fec, asm, p, U)
+    Ro, colptr, rowval, nzo = _oracle(orc, mesh, "poisson", [1.0], U, asm)
+    assert np.array_equal(K.colptr, colptr) and np.array_equal(K.rowval, rowval)
+    assert K.nnz == 753571
+    assert max(rel_err(R, Ro)) <= TOL64
+    assert max(rel_err(nz, nzo)) <= TOL64
+    # determinism: bitwise-identical on a second call
+    R2, nz2, _ = _run(fec, asm, p, U)
+    assert np.array_equal(R, R2) and np.array_equal(nz, nz2)
+
+
+def test_poisson_vector_and_matrix_entry_points_agree(fec, orc):
+    """assemble_vector / assemble_stiffness separately equal the fused pass."""
+    torch = _torch()
+    n = 9
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n, n, n))
+    bcs = [fec.DirichletBC("u", lambda X, t: 0.0, nodeset_name="left")]
+    asm, p = _setup(fec, mesh, "scalar", fec.Poisson(2.0), bcs)
+    U = np.random.default_rng(3).uniform(-1, 1, n ** 3)
+    R, nz, _ = _run(fec, asm, p, U)
+    Uu = torch.from_numpy(U[asm.dof.unknown_dofs - 1].copy()).cuda()
+    fec.assemble_vector(asm, fec.residual, Uu, p)
+    fec.assemble_stiffness(asm, fec.stiffness, Uu, p)
+    torch.cuda.synchronize()
+    assert np.array_equal(fec.residual(asm).cpu().numpy(), R)
+    assert np.array_equal(fec.stiffness(asm).nzval.cpu().numpy(), nz)
+    # host input (end-to-end path) gives the same bits
+    fec.assemble_vector(asm, fec.residual, U[asm.dof.unknown_dofs - 1].copy(), p)
+    torch.cuda.synchronize()
+    assert np.array_equal(fec.residual(asm).cpu().numpy(), R)
+
+
+def test_poisson_quad4_gold_through_gpu(fec):
+    """test/poisson/TestPoisson.jl:54-100: GPU-assembled residual and CSC stiffness
+    on poisson.g, one linear solve, compared with poisson.gold."""
+    g = np.load(GOLD / "poisson_quad4.npz")
+    mesh = fec.UnstructuredMesh(g["coords"], {"block_1": ("QUAD4", g["conn"])},
+                                nodesets={f"nset_{i}": g[f"nset_{i}"] for i in range(1, 5)})
+    bcs = [fec.DirichletBC("u", lambda X, t: 0.0, nodeset_name=f"nset_{i}") for i in range(1, 5)]
+    asm, p = _setup(fec, mesh, "scalar", fec.Poisson(2 * np.pi ** 2), bcs)
+    R, nz, K = _run(fec, asm, p, np.zeros(mesh.num_nodes))
+    Ks = K.to_scipy()
+    u = np.zeros(mesh.num_nodes)
+    u[asm.dof.unknown_dofs - 1] = spl.spsolve(Ks.tocsc(), -R)
+    assert np.abs(u - g["u_gold"]).max() <= 1e-10 * np.abs(g["u_gold"]).max()
+
+
+@pytest.mark.parametrize("n", [5, 9])
+def test_neohookean_hex8_fp64(fec, orc, n):
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n, n, n))
+    phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+    asm, p = _setup(fec, mesh, "vector", phys)
+    U = stretch_field(mesh.nodal_coords, seed=1).ravel()
+    R, nz, K = _run(fec, asm, p, U)
+    Ro, colptr, rowval, nzo = _oracle(orc, mesh, "neohookean", phys.create_properties(), U, asm)
+    assert np.array_equal(K.colptr, colptr) and np.array_equal(K.rowval, rowval)
+    assert max(rel_err(R, Ro)) <= TOL64, rel_err(R, Ro)
+    assert max(rel_err(nz, nzo)) <= TOL64, rel_err(nz, nzo)
+
+
+def test_neohookean_hex8_fp32_element(fec, orc):
+    n = 9
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n, n, n))
+    phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+    asm, p = _setup(fec, mesh, "vector", phys, precision="fp32_element")
+    U = stretch_field(mesh.nodal_coords, seed=1).ravel()
+    R, nz, _ = _run(fec, asm, p, U)
+    Ro, _, _, nzo = _oracle(orc, mesh, "neohookean", phys.create_properties(), U, asm)
+    er, ek = rel_err(R, Ro), rel_err(nz, nzo)
+    print(f"fp32-element error vs FP64 oracle: residual {er}, stiffness {ek}")
+    assert max(ek) <= TOL32 and er[1] <= TOL32
+
+
+def test_neohookean_with_dirichlet_and_two_blocks(fec, orc):
+    """Two element blocks with different properties and partial Dirichlet elimination."""
+    a = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (5, 5, 5))
+    b = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (4, 5, 6))
+    mesh = fec.meshes.merge_meshes([a, b])
+    mesh.nodeset_nodes["fix"] = np.arange(1, 30, dtype=np.int64)
+    V = fec.FunctionSpace(mesh)
+    asm = fec.SparseMatrixAssembler(fec.VectorFunction(V, "u"), device=0)
+    p1, p2 = fec.NeoHookean(0.8, 0.4), fec.NeoHookean(2.0, 0.1)
+    bcs = [fec.DirichletBC("u_x", lambda X, t: 0.0, nodeset_name="fix"),
+           fec.DirichletBC("u_z", lambda X, t: 0.0, nodeset_name="fix")]
+    p = fec.create_parameters(mesh, asm, {"block_1": p1, "block_2": p2}, dirichlet_bcs=bcs)
+    U = stretch_field(mesh.nodal_coords, seed=5).ravel()
+    U[asm.dof.dirichlet_dofs - 1] = 0.0
+    R, nz, K = _run(fec, asm, p, U)
+    # oracle per block, merged the reference way (single COO over both blocks)
+    Rf = np.zeros(U.size)
+    Ks = []
+    for name, ph in (("block_1", p1), ("block_2", p2)):
+        r, k = orc.assemble([("HEX8", mesh.element_conns[name])], mesh.nodal_coords, "neohookean",
+                            ph.create_properties(), U)
+        Rf += r
+        Ks.append(k)
+    Is, Js, slots = orc.pattern(blocks_of(mesh), 3, asm.dof.dof_to_unknown)
+    n_u = asm.dof.unknown_dofs.size
+    colptr, rowval, nzo = orc.sparse_csc(n_u, n_u, Is, Js, np.concatenate(Ks)[slots - 1])
+    assert np.array_equal(K.colptr, colptr) and np.array_equal(K.rowval, rowval)
+    assert max(rel_err(nz, nzo)) <= TOL64
+    assert max(rel_err(R, Rf[asm.dof.unknown_dofs - 1])) <= 1e-11
+
+
+@pytest.mark.parametrize("kind", ["tet4", "tet10", "hex27"])
+def test_higher_order_and_simplex_elements(fec, orc, kind):
+    gen = {"tet4": fec.meshes.box_tet4, "tet10": fec.meshes.box_tet10, "hex27": fec.meshes.box_hex27}[kind]
+    mesh = gen((4, 4, 4))
+    phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+    asm, p = _setup(fec, mesh, "vector", phys)
+    U = stretch_field(mesh.nodal_coords, seed=2).ravel()
+    R, nz, K = _run(fec, asm, p, U)
+    Ro, colptr, rowval, nzo = _oracle(orc, mesh, "neohookean", phys.create_properties(), U, asm)
+    assert np.array_equal(K.colptr, colptr) and np.array_equal(K.rowval, rowval)
+    assert max(rel_err(R, Ro)) <= TOL64
+    assert max(rel_err(nz, nzo)) <= TOL64
+
+
+def test_j2_one_load_step_with_state(fec, orc):
+    torch = _torch()
+    n = 6
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n, n, n))
+    phys = fec.J2Plasticity(200.0, 0.3, 0.25, 2.0)
+    asm, p = _setup(fec, mesh, "vector", phys)
+    rng = np.random.default_rng(3)
+    X = mesh.nodal_coords
+    U = np.zeros_like(X)
+    U[:, 0] = 0.01 * X[:, 0]
+    U[:, 1] = -0.003 * X[:, 1]
+    U = (U + 1e-5 * rng.standard_normal(U.shape)).ravel()
+    so = rng.uniform(0, 1e-4, p.state_old.numel())
+    p.state_old.copy_(torch.from_numpy(so))
+    R, nz, _ = _run(fec, asm, p, U)
+    sn = np.zeros_like(so)
+    Ro, _, _, nzo = _oracle(orc, mesh, "j2", phys.create_properties(), U, asm, so, sn)
+    assert max(rel_err(R, Ro)) <= TOL64
+    assert max(rel_err(nz, nzo)) <= TOL64
+    assert max(rel_err(p.state_new.cpu().numpy(), sn)) <= TOL64
+    assert sn[6::7].max() > 0  # some points yielded
