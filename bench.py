@@ -1,0 +1,385 @@
+#!/usr/bin/env python
+"""R+K assembly throughput on GB300 (Melem/s) with the HBM roofline of the
+dominant kernel, for the 3D compressible Neo-Hookean workload: vector hex8 on a
+128^3 structured box (2,097,152 elements, 6,440,067 dofs, 513,599,625 CSC
+entries), 2x2x2 Gauss points, E = 1, nu = 0.3, displacement = affine stretch
+diag(1.05, 0.98, 0.98) - I plus N(0, 1e-3^2) nodal noise (seed 1).
+
+A step is one fused residual + tangent assembly (field update, element kernel,
+deterministic node gather into the residual over unknowns and the CSC nzval).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload neohookean|poisson] [--precision fp64|fp32_element]
+
+Under torchrun (N > 1) each rank assembles its own copy of the workload on its
+own GPU (weak scaling, no collective on the data path); value = all ranks'
+elements / max-over-ranks time.  --impl reference times the reference
+algorithm's CPU implementation (element loop -> element-ordered COO ->
+sparse!-style COO->CSC, OpenMP over the host cores) on a bounded sample of the
+same workload; only rank 0 runs it.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for _p in (str(ROOT / "finiteelementcontainers.jl_gb300"), str(ROOT)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "R+K assembly Melem/s & % HBM roofline; MLP closure vs exact at 1e-3 stress err"
+UNIT = "Melem/s"
+# compulsory HBM bytes per element of one R+K pass (int32 connectivity, X and U
+# gathers, residual and nzval written once), see the design doc
+WORKLOADS = {
+    "neohookean": dict(n=128, kind="vector", name="neohookean_hex8_128cubed", flop_per_elem=48e3),
+    "poisson": dict(n=32, kind="scalar", name="poisson_hex8_32cubed", flop_per_elem=8e3),
+}
+CPU_SAMPLE_N = {"neohookean": 40, "poisson": 32}
+
+
+def algorithmic_bytes(ne: int, nn: int, nf: int, n_unknowns: int, nnz: int, nnpe: int = 8) -> int:
+    return 4 * nnpe * ne + 8 * 3 * nn + 8 * nf * nn + 8 * n_unknowns + 8 * nnz
+
+
+def build_workload(fec, wl: str, n: int, device: int, precision: str):
+    import torch
+    from fec_gb300.workloads import stretch_field
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n + 1,) * 3)
+    V = fec.FunctionSpace(mesh)
+    if wl == "neohookean":
+        var = fec.VectorFunction(V, "u")
+        asm = fec.SparseMatrixAssembler(var, device=device, precision=precision)
+        phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+        p = fec.create_parameters(mesh, asm, phys)
+        U = stretch_field(mesh.nodal_coords, seed=1).ravel()
+    else:
+        var = fec.ScalarFunction(V, "u")
+        asm = fec.SparseMatrixAssembler(var, device=device, precision=precision)
+        bcs = [fec.DirichletBC("u", lambda X, t: 0.0, nodeset_name=f)
+               for f in ("bottom", "right", "front", "top", "left", "back")]
+        p = fec.create_parameters(mesh, asm, fec.Poisson(1.0), dirichlet_bcs=bcs)
+        U = np.random.default_rng(0).uniform(-1.0, 1.0, mesh.num_nodes)
+    Uu = np.ascontiguousarray(U[asm.dof.unknown_dofs - 1])
+    asm._ensure_pattern()
+    return mesh, asm, p, Uu
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        try:
+            for line in Path(self.path).read_text().splitlines():
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                    rows.append(parts)
+        finally:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows]
+        mx = max(float(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        loaded = [s for s in sm if s > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())
+                if any(r[3].replace(".", "").isdigit() for r in rows) else None}
+
+
+def measured_peaks() -> dict:
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profiled_traffic(workload: str) -> dict | None:
+    """DRAM bytes per element of each kernel, from the committed ncu summary."""
+    f = ROOT / "profiles" / f"traffic_{workload}.json"
+    if f.exists():
+        return json.loads(f.read_text())
+    return None
+
+
+def cpu_reference_run(wl: str, n: int, threads: int) -> tuple[float, int, str]:
+    """One call of the reference algorithm on the host cores (oracle port):
+    element loop (OpenMP, atomic residual scatter) + slot gather + sparse!.
+    Returns (seconds, elements, description).  Pattern set-up is excluded, as
+    the reference builds it once in update_dofs!."""
+    from oracle import oracle
+    from fec_gb300.workloads import stretch_field
+    coords, conns = oracle.structured_hex8((n + 1,) * 3)
+    nn = coords.shape[0]
+    if wl == "neohookean":
+        nf, phys, props = 3, "neohookean", [1.0 / (3 * 0.4), 1.0 / 2.6]
+        U = stretch_field(coords, seed=1).ravel()
+        dd = np.zeros(0, dtype=np.int64)
+    else:
+        nf, phys, props = 1, "poisson", [1.0]
+        U = np.random.default_rng(0).uniform(-1, 1, nn)
+        dd = np.unique(np.concatenate([oracle.hex8_nodeset((n + 1,) * 3, f) for f in oracle.HEX8_FACES]))
+    unknown, dtu = oracle.update_dofs(nf * nn, dd)
+    blocks = [("HEX8", conns)]
+    Is, Js, slots = oracle.pattern(blocks, nf, dtu)
+    t0 = time.perf_counter()
+    R, K = oracle.assemble(blocks, coords, phys, props, U, threads=threads)
+    Ru = R[unknown - 1]
+    oracle.sparse_csc(unknown.size, unknown.size, Is, Js, K[slots - 1])
+    dt = time.perf_counter() - t0
+    assert np.isfinite(Ru).all()
+    return dt, conns.shape[0], f"{n}^3 hex8 {wl} (element loop on {threads} threads + serial sparse!)"
+
+
+def cpu_baseline(wl: str, target_s: float = 10.0) -> dict:
+    from oracle import oracle
+    threads = oracle.max_threads()
+    n = CPU_SAMPLE_N[wl]
+    total, elems, reps = 0.0, 0, 0
+    desc = ""
+    while (total < target_s and reps < 5) or reps == 0:
+        dt, ne, desc = cpu_reference_run(wl, n, threads)
+        total += dt
+        elems += ne
+        reps += 1
+    return {"value": elems / total / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{reps} x {desc}, {total:.1f} s"}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle
+    threads = oracle.max_threads()
+    n = CPU_SAMPLE_N[args.workload]
+    for _ in range(args.warmup):
+        cpu_reference_run(args.workload, n, threads)
+    times, desc, ne = [], "", 0
+    for _ in range(args.steps):
+        dt, ne, desc = cpu_reference_run(args.workload, n, threads)
+        times.append(dt)
+    total = sum(times)
+    value = ne * args.steps / total / 1e6
+    wl = WORKLOADS[args.workload]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": wl["name"], "precision": "fp64", "cpu_sample": f"{n}^3 elements per step"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} x {desc}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import torch
+    import torch.distributed as dist
+    import __graft_entry__ as ge
+    fec = ge.load_package()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    torch.cuda.set_device(local)
+    wl = WORKLOADS[args.workload]
+    mesh, asm, p, Uu_np = build_workload(fec, args.workload, wl["n"], local, args.precision)
+    ne, nn, nf = mesh.num_elements(), mesh.num_nodes, asm.dof.nf
+    n_u = int(asm.dof.unknown_dofs.size)
+    stream = torch.cuda.current_stream()
+    Uu_d = torch.from_numpy(Uu_np).cuda()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def step(Uu):
+        return fec.assemble_residual_and_stiffness(asm, Uu, p)
+
+    # ---- device-resident timing -------------------------------------------------
+    for _ in range(args.warmup):
+        step(Uu_d)
+    asm.set_profiling(True)
+    per_kernel: dict[str, list[float]] = {}
+    launches = 0
+    barrier()
+    with ClockSampler(local) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step(Uu_d)
+            for name, ms in asm.kernel_times():
+                per_kernel.setdefault(name, []).append(ms)
+                launches += 1
+        e1.record(stream)
+        barrier()
+    asm.set_profiling(False)
+    t_ms = e0.elapsed_time(e1)
+    if world > 1:
+        tt = torch.tensor([t_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    clocks = clk.summary()
+    value = world * ne * args.steps / (t_ms * 1e-3) / 1e6
+
+    # ---- end to end through the public API with host buffers --------------------
+    R0, K0 = step(Uu_d)
+    nnz = K0.nnz
+    Uu_h = torch.from_numpy(Uu_np).pin_memory()
+    R_h = torch.empty(n_u, dtype=torch.float64).pin_memory()
+    nz_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        R, K = fec.assemble_residual_and_stiffness(asm, Uu_h, p)
+        R_h.copy_(R, non_blocking=True)
+        nz_h.copy_(K.nzval, non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    f1.record(stream)
+    barrier()
+    t_e2e = f0.elapsed_time(f1)
+    if world > 1:
+        tt = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e_value = world * ne * args.steps / (t_e2e * 1e-3) / 1e6
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant kernel ------------------------------------------
+    peaks = measured_peaks()
+    totals = {k: sum(v) for k, v in per_kernel.items()}
+    dom = max(totals, key=totals.get)
+    avg_ms = totals[dom] / len(per_kernel[dom])
+    alg_bytes = algorithmic_bytes(ne, nn, nf, n_u, nnz)
+    achieved = alg_bytes / (avg_ms * 1e-3) / 1e9
+    traffic = None
+    prof = profiled_traffic(wl["name"] + "_" + args.precision)
+    if prof and dom in prof.get("bytes_per_elem", {}):
+        traffic = prof["bytes_per_elem"][dom] * ne
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"] + " (burst copy)",
+                "traffic": traffic, "algorithmic_bytes_per_elem": alg_bytes / ne,
+                "kernels_ms": {k: sum(v) / len(v) for k, v in per_kernel.items()},
+                "kernel_share": {k: v / sum(totals.values()) for k, v in totals.items()}}
+    fp = {}
+    lib = fec.load_library()
+    import ctypes as C
+    for prec, code in (("fp64", 0), ("fp32", 1)):
+        tf = C.c_double()
+        if lib.fec_probe_fma_rate(local, code, C.byref(tf)) == 0:
+            fp[prec] = tf.value
+    elem_ms = sum(v for k, v in roofline["kernels_ms"].items() if k.startswith("element"))
+    pipe = "fp64" if args.precision == "fp64" else "fp32"
+    compute = {"pipe": pipe, "flop_per_elem": wl["flop_per_elem"],
+               "achieved_tflops": wl["flop_per_elem"] * ne / (elem_ms * 1e-3) / 1e12,
+               "peak_tflops": fp.get(pipe), "peak_source": "measured FMA probe (fec_probe_fma_rate)"}
+    if compute["peak_tflops"]:
+        compute["frac"] = compute["achieved_tflops"] / compute["peak_tflops"]
+
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.workload)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32-element/f64-accumulate",
+        "data": "synthetic",
+        "config": {"workload": wl["name"], "elements": ne, "dofs": nf * nn, "nnz": nnz, "precision": args.precision,
+                   "quadrature": "2x2x2 Gauss", "l2": "inputs larger than L2 (element scratch %.1f GB, nzval %.1f GB)"
+                   % ((ne * (nf * 8) ** 2 * (8 if args.precision == "fp64" else 4)) / 1e9, nnz * 8 / 1e9),
+                   "parallelism": f"{world} independent replicas" if world > 1 else "single GPU"},
+        "roofline": roofline,
+        "compute_roofline": compute,
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n_u,
+                "d2h_bytes_per_step": 8 * (n_u + nnz)},
+        "gpu_launches": launches,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="neohookean")
+    ap.add_argument("--precision", choices=["fp64", "fp32_element"], default="fp64")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

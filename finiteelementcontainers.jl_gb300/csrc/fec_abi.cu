@@ -71,6 +71,11 @@ struct fec_ctx {
   DevBuf d_coords, d_conn, d_ref, d_nadj_ptr, d_nadj, d_epos, d_umask, d_col_base, d_col_len, d_dtu, d_unknown_dofs;
   DevBuf d_Ke, d_Re;
   std::vector<int64_t> ref_off;  // per block offset (doubles) into d_ref
+  // optional per-launch timing (CUDA events on the caller's stream)
+  bool profiling = false;
+  std::vector<cudaEvent_t> events;  // 2 per timed launch
+  std::vector<std::string> ev_names;
+  int n_timed = 0;
 };
 
 namespace {
@@ -135,6 +140,32 @@ __global__ void set_unknowns_kernel(double* U, int64_t n, const int64_t* unknown
   if (k < n) U[unknown_dofs[k]] = Uu[k];
 }
 
+// Records an event pair around launch `name` when profiling is on.
+struct LaunchTimer {
+  fec_ctx* c;
+  cudaStream_t s;
+  int slot = -1;
+  LaunchTimer(fec_ctx* c_, cudaStream_t s_, const char* name) : c(c_), s(s_) {
+    if (!c->profiling) return;
+    slot = c->n_timed;
+    if (int(c->events.size()) < 2 * (slot + 1)) {
+      cudaEvent_t a, b;
+      if (cudaEventCreate(&a) != cudaSuccess) { slot = -1; return; }
+      if (cudaEventCreate(&b) != cudaSuccess) { cudaEventDestroy(a); slot = -1; return; }
+      c->events.push_back(a);
+      c->events.push_back(b);
+    }
+    if (int(c->ev_names.size()) <= slot) c->ev_names.resize(slot + 1);
+    c->ev_names[slot] = name;
+    cudaEventRecord(c->events[2 * slot], s);
+  }
+  ~LaunchTimer() {
+    if (slot < 0) return;
+    cudaEventRecord(c->events[2 * slot + 1], s);
+    c->n_timed = slot + 1;
+  }
+};
+
 void invalidate_pattern(fec_ctx* c) {
   c->pattern_ready = false;
   c->nnz = 0;
@@ -177,6 +208,7 @@ int fec_ctx_create(int device, fec_ctx** out) {
 int fec_ctx_destroy(fec_ctx* c) {
   if (!c) return FEC_OK;
   if (c->device >= 0) cudaSetDevice(c->device);
+  for (cudaEvent_t e : c->events) cudaEventDestroy(e);
   for (DevBuf* b : {&c->d_coords, &c->d_conn, &c->d_ref, &c->d_nadj_ptr, &c->d_nadj, &c->d_epos, &c->d_umask,
                     &c->d_col_base, &c->d_col_len, &c->d_dtu, &c->d_unknown_dofs, &c->d_Ke, &c->d_Re})
     b->release();
@@ -514,6 +546,8 @@ int fec_update_field(fec_ctx* c, double* U, const double* Uu, int64_t num_bc, co
   if (num_bc < 0 || (num_bc > 0 && (!bc_dofs || !bc_vals))) return fail(c, FEC_ERR_ARG, "bad Dirichlet arrays");
   cudaSetDevice(c->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  c->n_timed = 0;
+  LaunchTimer timer(c, s, "update_field");
   if (num_bc > 0) {
     set_dirichlet_kernel<<<unsigned((num_bc + 255) / 256), 256, 0, s>>>(U, num_bc, bc_dofs, bc_vals);
     FEC_CUDA(c, cudaGetLastError());
@@ -555,6 +589,7 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
   if (any_state && !state_old) return fail(c, FEC_ERR_ARG, "state_old is NULL for a physics with state");
   cudaSetDevice(c->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (c->n_timed > 1) c->n_timed = 0;  // keep a preceding fec_update_field timing
   const size_t rsz = precision == FEC_FP64 ? sizeof(double) : sizeof(float);
   int64_t ke_total = 0, re_total = 0;
   for (const Block& B : c->blocks) {
@@ -586,10 +621,14 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     ea.Ke = want_k ? static_cast<char*>(c->d_Ke.p) + rsz * size_t(ke_off) : nullptr;
     ea.Re = want_r ? static_cast<char*>(c->d_Re.p) + rsz * size_t(re_off) : nullptr;
     cudaError_t e;
-    if (B.physics == FEC_PHYS_POISSON)
-      e = fec::launch_poisson(B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
-    else
-      e = fec::launch_mech(B.physics, B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
+    {
+      LaunchTimer timer(c, s, B.physics == FEC_PHYS_POISSON ? "element_poisson"
+                              : B.physics == FEC_PHYS_NEOHOOKEAN ? "element_neohookean" : "element_j2");
+      if (B.physics == FEC_PHYS_POISSON)
+        e = fec::launch_poisson(B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
+      else
+        e = fec::launch_mech(B.physics, B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
+    }
     if (e == cudaErrorNotSupported)
       return fail(c, FEC_ERR_UNSUPPORTED, "block %d: physics %d on element type %d is not built", int(b) + 1,
                   B.physics, B.elem_type);
@@ -622,9 +661,96 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
   ga.nzval = want_k ? nzval : nullptr;
   ga.R_u = want_r ? R_u : nullptr;
   ga.acc_stride = c->acc_stride;
-  cudaError_t e = fec::launch_gather(precision, c->nf, ga, s, &c->last_launches);
+  cudaError_t e;
+  {
+    LaunchTimer timer(c, s, "node_gather");
+    e = fec::launch_gather(precision, c->nf, ga, s, &c->last_launches);
+  }
   if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "gather launch: %s", cudaGetErrorString(e));
   return ok(c);
+}
+
+int fec_set_profiling(fec_ctx* c, int on) {
+  if (!c) return FEC_ERR_ARG;
+  c->profiling = on != 0;
+  c->n_timed = 0;
+  return ok(c);
+}
+
+int fec_kernel_times(fec_ctx* c, float* ms, int cap, char* names, size_t len) {
+  if (!c) return FEC_ERR_ARG;
+  if (c->device < 0) return fail(c, FEC_ERR_STATE, "host-only context");
+  std::string all;
+  const int n = c->n_timed;
+  for (int i = 0; i < n; ++i) {
+    cudaError_t e = cudaEventSynchronize(c->events[2 * i + 1]);
+    if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "cudaEventSynchronize: %s", cudaGetErrorString(e));
+    float t = 0.f;
+    e = cudaEventElapsedTime(&t, c->events[2 * i], c->events[2 * i + 1]);
+    if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "cudaEventElapsedTime: %s", cudaGetErrorString(e));
+    if (ms && i < cap) ms[i] = t;
+    if (i) all += ",";
+    all += c->ev_names[i];
+  }
+  if (names && len) {
+    strncpy(names, all.c_str(), len - 1);
+    names[len - 1] = 0;
+  }
+  ok(c);
+  return n;
+}
+
+}  // extern "C"
+
+namespace {
+template <typename T>
+__global__ void fma_probe_kernel(T* out, int iters, T a, T b) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  T x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = T(tid) * T(1e-9) + T(k);
+  for (int i = 0; i < iters; ++i)
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+  T s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  out[tid] = s;
+}
+template <typename T>
+int probe(int device, int iters, double* tflops) {
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return FEC_ERR_CUDA;
+  const int blocks = sms * 8, threads = 256;
+  T* out = nullptr;
+  if (cudaMalloc(&out, sizeof(T) * blocks * threads) != cudaSuccess) return FEC_ERR_CUDA;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  fma_probe_kernel<T><<<blocks, threads>>>(out, 16, T(0.999), T(1e-3));
+  cudaEventRecord(e0);
+  fma_probe_kernel<T><<<blocks, threads>>>(out, iters, T(0.999), T(1e-3));
+  cudaEventRecord(e1);
+  cudaError_t st = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (st != cudaSuccess || ms <= 0.f) return FEC_ERR_CUDA;
+  *tflops = 2.0 * double(blocks) * threads * iters * 8 / (double(ms) * 1e-3) / 1e12;
+  return FEC_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int fec_probe_fma_rate(int device, int precision, double* tflops) {
+  if (!tflops) return FEC_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return FEC_ERR_CUDA;
+  if (precision == FEC_FP64) return probe<double>(device, 4000, tflops);
+  if (precision == FEC_FP32_ELEMENT) return probe<float>(device, 40000, tflops);
+  return FEC_ERR_ARG;
 }
 
 }  // extern "C"

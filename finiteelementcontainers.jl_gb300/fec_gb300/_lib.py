@@ -44,6 +44,9 @@ SIGNATURES = {
     "fec_assemble": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_double, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fec_last_launch_count": (C.c_int, [_vp]),
     "fec_sizes": (C.c_int, [_vp, _i64p, _i64p, _i64p, _i64p, _i64p]),
+    "fec_set_profiling": (C.c_int, [_vp, C.c_int]),
+    "fec_kernel_times": (C.c_int, [_vp, C.POINTER(C.c_float), C.c_int, C.c_char_p, C.c_size_t]),
+    "fec_probe_fma_rate": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
 }
 
 

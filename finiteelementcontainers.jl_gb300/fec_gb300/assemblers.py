@@ -134,6 +134,19 @@ class SparseMatrixAssembler:
     def last_launch_count(self) -> int:
         return int(self._lib.fec_last_launch_count(self._ctx))
 
+    def set_profiling(self, on: bool) -> None:
+        self._call("fec_set_profiling", int(bool(on)))
+
+    def kernel_times(self) -> list[tuple[str, float]]:
+        """(name, ms) of each launch of the last update+assemble pair (profiling on)."""
+        ms = (C.c_float * 64)()
+        names = C.create_string_buffer(1024)
+        n = self._lib.fec_kernel_times(self._ctx, ms, 64, names, 1024)
+        if n < 0:
+            _lib.check(self._lib, self._ctx, n)
+        labels = names.value.decode().split(",") if n else []
+        return [(labels[i], float(ms[i])) for i in range(n)]
+
 
 def update_dofs_bcs(asm: SparseMatrixAssembler, dirichlet_bcs) -> None:
     """update_dofs!(asm, dirichlet_bcs, periodic_bcs) (SparseMatrixAssembler.jl:228-274)."""

@@ -141,6 +141,21 @@ int fec_assemble(fec_ctx* ctx, int want, int precision, double t, double dt, con
 /* Number of kernels fec_assemble launched in the last call (for accounting). */
 int fec_last_launch_count(const fec_ctx* ctx);
 
+/* Measurement helpers (no counterpart in the reference, which only times whole
+ * sections with TimerOutputs, src/Solvers.jl:133-151). ------------------------ */
+
+/* When on, fec_update_field/fec_assemble bracket each kernel launch with a CUDA
+ * event pair on the caller's stream.  Off by default. */
+int fec_set_profiling(fec_ctx* ctx, int on);
+/* Durations (ms) of the launches timed by the last fec_update_field +
+ * fec_assemble pair, in launch order; names gets a comma-separated list.
+ * Waits for those events.  Returns the number of timed launches (>= 0). */
+int fec_kernel_times(fec_ctx* ctx, float* ms, int cap, char* names, size_t len);
+/* FMA throughput probe on `device` (TFLOP/s, 2 flops per FMA) in FP64
+ * (precision FEC_FP64) or FP32 (FEC_FP32_ELEMENT): the denominator of the
+ * FP64-bound roofline of the element kernels. */
+int fec_probe_fma_rate(int device, int precision, double* tflops);
+
 /* Sizes the context knows (any pointer may be NULL). */
 int fec_sizes(const fec_ctx* ctx, int64_t* num_nodes, int64_t* num_elems, int64_t* num_unknowns, int64_t* nnz,
               int64_t* state_len);

@@ -134,7 +134,7 @@ def test_neohookean_hex8_fp32_element(fec, orc):
 def test_neohookean_with_dirichlet_and_two_blocks(fec, orc):
     """Two element blocks with different properties and partial Dirichlet elimination."""
     a = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (5, 5, 5))
-    b = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (4, 5, 6))
+    b = fec.StructuredMesh("hex", (1.5, 0.0, 0.0), (2.5, 1.0, 1.2), (4, 4, 4))
     mesh = fec.meshes.merge_meshes([a, b])
     mesh.nodeset_nodes["fix"] = np.arange(1, 30, dtype=np.int64)
     V = fec.FunctionSpace(mesh)
