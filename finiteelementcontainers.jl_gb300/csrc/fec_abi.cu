@@ -5,6 +5,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 #ifdef _OPENMP
@@ -751,6 +752,160 @@ int fec_probe_fma_rate(int device, int precision, double* tflops) {
   if (precision == FEC_FP64) return probe<double>(device, 4000, tflops);
   if (precision == FEC_FP32_ELEMENT) return probe<float>(device, 40000, tflops);
   return FEC_ERR_ARG;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Assembly without device allocation.
+//
+// fec_assemble keeps its element-matrix workspace in context memory that it
+// cudaMallocs on first use (and grows).  Some callers cannot let a library do
+// that: applications that route every device allocation through their own pool
+// (CUDA.jl's memory pool, PyTorch's caching allocator) and must not see memory
+// appear outside the pool's accounting or a cudaFree synchronize the device in
+// the middle of their step, and callers that fix their device-memory budget up
+// front.  fec_assemble_noalloc does the same work with its workspace in the
+// statically sized device array below, which the CUDA module reserves when the
+// library is loaded on a device and keeps until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[FEC_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[kMaxDevices] = {nullptr};
+
+// Device address of g_noalloc_scratch on the current device `dev`, looked up
+// once per device (host code cannot use the symbol itself as a pointer).
+int noalloc_scratch_address(fec_ctx* c, int dev, void** out) {
+  if (dev < 0 || dev >= kMaxDevices) return fail(c, FEC_ERR_ARG, "device %d out of range for the static scratch", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(c, FEC_ERR_CUDA, "cudaGetSymbolAddress(static scratch): %s", cudaGetErrorString(e));
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return FEC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double dt, const double* U,
+                         const double* U_old, const double* state_old, double* state_new, double* R_u, double* nzval,
+                         void* stream) {
+  (void)t;
+  (void)dt;
+  (void)U_old;
+  if (!c) return FEC_ERR_ARG;
+  c->last_launches = 0;
+  if (!c->pattern_ready) return fail(c, FEC_ERR_STATE, "fec_assemble_noalloc before fec_pattern_build");
+  if (c->device < 0) return fail(c, FEC_ERR_STATE, "host-only context (device -1) cannot run kernels");
+  if (precision != FEC_FP64 && precision != FEC_FP32_ELEMENT)
+    return fail(c, FEC_ERR_ARG, "unknown precision %d", precision);
+  const bool want_r = (want & FEC_WANT_RESIDUAL) != 0, want_k = (want & FEC_WANT_STIFFNESS) != 0;
+  if (!want_r && !want_k) return ok(c);
+  if (!U) return fail(c, FEC_ERR_ARG, "U is NULL");
+  if (want_r && !R_u && c->n_unknowns > 0) return fail(c, FEC_ERR_ARG, "R_u is NULL");
+  if (want_k && !nzval && c->nnz > 0) return fail(c, FEC_ERR_ARG, "nzval is NULL");
+  bool any_state = false;
+  for (size_t b = 0; b < c->blocks.size(); ++b) {
+    const Block& B = c->blocks[b];
+    if (!B.physics) return fail(c, FEC_ERR_STATE, "block %d has no physics", int(b) + 1);
+    if (num_fields_of(B.physics) != c->nf)
+      return fail(c, FEC_ERR_ARG, "block %d physics has %d fields but the dofs have %d", int(b) + 1,
+                  num_fields_of(B.physics), c->nf);
+    if (num_states_of(B.physics)) any_state = true;
+  }
+  if (any_state && !state_old) return fail(c, FEC_ERR_ARG, "state_old is NULL for a physics with state");
+  // workspace: element matrices, then (256-byte aligned) element residuals
+  const size_t rsz = precision == FEC_FP64 ? sizeof(double) : sizeof(float);
+  int64_t ke_total = 0, re_total = 0;
+  for (const Block& B : c->blocks) {
+    const int ndof = c->nf * B.nnpe;
+    ke_total += B.ne * ndof * ndof;
+    re_total += B.ne * ndof;
+  }
+  const size_t ke_bytes = want_k ? rsz * size_t(ke_total) : 0;
+  const size_t re_off_bytes = (ke_bytes + 255) & ~size_t(255);
+  const size_t need = re_off_bytes + (want_r ? rsz * size_t(re_total) : 0);
+  if (need > FEC_NOALLOC_SCRATCH_BYTES)
+    return fail(c, FEC_ERR_ARG,
+                "fec_assemble_noalloc needs %zu bytes of element workspace but the static scratch holds %zu "
+                "(FEC_NOALLOC_SCRATCH_BYTES); use fec_assemble for this mesh",
+                need, size_t(FEC_NOALLOC_SCRATCH_BYTES));
+  if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, FEC_ERR_CUDA, "cudaSetDevice(%d) failed", c->device);
+  void* scratch = nullptr;
+  int rc = noalloc_scratch_address(c, c->device, &scratch);
+  if (rc) return rc;
+  void* Ke = want_k ? scratch : nullptr;
+  void* Re = want_r ? static_cast<char*>(scratch) + re_off_bytes : nullptr;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  GatherArgs ga;
+  memset(&ga, 0, sizeof ga);
+  int64_t ke_off = 0, re_off = 0, st_off = 0;
+  for (size_t b = 0; b < c->blocks.size(); ++b) {
+    const Block& B = c->blocks[b];
+    const int ndof = c->nf * B.nnpe;
+    ElemArgs ea;
+    memset(&ea, 0, sizeof ea);
+    ea.conn = static_cast<const int32_t*>(c->d_conn.p) + B.conn_off;
+    ea.ne = B.ne;
+    ea.coords = static_cast<const double*>(c->d_coords.p);
+    ea.U = U;
+    ea.ref = static_cast<const double*>(c->d_ref.p) + c->ref_off[b];
+    for (int i = 0; i < 8; ++i) ea.props[i] = B.props[i];
+    const int ns = num_states_of(B.physics);
+    ea.state_old = ns ? state_old + st_off : nullptr;
+    ea.state_new = (ns && state_new) ? state_new + st_off : nullptr;
+    ea.Ke = want_k ? static_cast<char*>(Ke) + rsz * size_t(ke_off) : nullptr;
+    ea.Re = want_r ? static_cast<char*>(Re) + rsz * size_t(re_off) : nullptr;
+    cudaError_t e;
+    if (B.physics == FEC_PHYS_POISSON)
+      e = fec::launch_poisson(B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
+    else
+      e = fec::launch_mech(B.physics, B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
+    if (e == cudaErrorNotSupported)
+      return fail(c, FEC_ERR_UNSUPPORTED, "block %d: physics %d on element type %d is not built", int(b) + 1,
+                  B.physics, B.elem_type);
+    if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "element kernel launch: %s", cudaGetErrorString(e));
+    BlockInfo& bi = ga.blk[b];
+    bi.elem_start = B.elem_start;
+    bi.ke_off = ke_off;
+    bi.re_off = re_off;
+    bi.conn_off = B.conn_off;
+    bi.epos_off = B.epos_off;
+    bi.nnpe = B.nnpe;
+    bi.ndof = ndof;
+    ke_off += B.ne * ndof * ndof;
+    re_off += B.ne * ndof;
+    st_off += int64_t(ns) * B.nq * B.ne;
+  }
+  ga.nn = c->nn;
+  ga.nf = c->nf;
+  ga.nblocks = int(c->blocks.size());
+  ga.nadj_ptr = static_cast<const int64_t*>(c->d_nadj_ptr.p);
+  ga.nadj = static_cast<const int64_t*>(c->d_nadj.p);
+  ga.conn = static_cast<const int32_t*>(c->d_conn.p);
+  ga.epos = static_cast<const uint16_t*>(c->d_epos.p);
+  ga.umask = static_cast<const uint8_t*>(c->d_umask.p);
+  ga.col_base = static_cast<const int64_t*>(c->d_col_base.p);
+  ga.col_len = static_cast<const int32_t*>(c->d_col_len.p);
+  ga.dof_to_unknown = static_cast<const int64_t*>(c->d_dtu.p);
+  ga.Ke = Ke;
+  ga.Re = Re;
+  ga.nzval = want_k ? nzval : nullptr;
+  ga.R_u = want_r ? R_u : nullptr;
+  ga.acc_stride = c->acc_stride;
+  cudaError_t e = fec::launch_gather(precision, c->nf, ga, s, &c->last_launches);
+  if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "gather launch: %s", cudaGetErrorString(e));
+  return ok(c);
 }
 
 }  // extern "C"

@@ -42,6 +42,8 @@ SIGNATURES = {
     "fec_pattern_get": (C.c_int, [_vp, _vp, _vp]),
     "fec_update_field": (C.c_int, [_vp, _vp, _vp, C.c_int64, _vp, _vp, _vp]),
     "fec_assemble": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_double, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "fec_assemble_noalloc": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_double, _vp, _vp, _vp, _vp, _vp, _vp,
+                                       _vp]),
     "fec_last_launch_count": (C.c_int, [_vp]),
     "fec_sizes": (C.c_int, [_vp, _i64p, _i64p, _i64p, _i64p, _i64p]),
     "fec_set_profiling": (C.c_int, [_vp, C.c_int]),

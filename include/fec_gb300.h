@@ -138,6 +138,31 @@ int fec_assemble(fec_ctx* ctx, int want, int precision, double t, double dt, con
                  const double* U_old_dev, const double* state_old_dev, double* state_new_dev, double* R_u_dev,
                  double* nzval_dev, void* stream);
 
+/* Assembly that allocates no device memory.  No counterpart in the reference.
+ *
+ * fec_assemble keeps its element-matrix workspace in memory it cudaMallocs on
+ * first use.  Callers that cannot let a library allocate -- applications whose
+ * device memory all goes through their own pool (CUDA.jl's pool, PyTorch's
+ * caching allocator), where a private cudaMalloc escapes the pool's accounting
+ * and a cudaFree synchronizes the device mid-step, or callers with a device
+ * memory budget fixed up front -- call this instead.  Same arguments, same
+ * results as fec_assemble; the context still has to be set up (mesh, dofs,
+ * pattern) beforehand, and the inputs and outputs are the caller's.
+ *
+ * Its workspace is one static device array of FEC_NOALLOC_SCRATCH_BYTES that
+ * every GPU which loads the library holds until the process exits.  Meshes
+ * whose element workspace (NE * NDOF^2 element-matrix entries plus NE * NDOF
+ * element-residual entries, 8 bytes each in FP64, 4 in FP32) exceeds it are
+ * rejected with FEC_ERR_ARG.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls share the array: calls whose work overlaps on the
+ * GPU (different streams, different contexts) race on it.  Nothing in it needs
+ * clearing, as every element rewrites its entries before they are read. */
+#define FEC_NOALLOC_SCRATCH_BYTES (64u << 20)
+int fec_assemble_noalloc(fec_ctx* ctx, int want, int precision, double t, double dt, const double* U_dev,
+                         const double* U_old_dev, const double* state_old_dev, double* state_new_dev,
+                         double* R_u_dev, double* nzval_dev, void* stream);
+
 /* Number of kernels fec_assemble launched in the last call (for accounting). */
 int fec_last_launch_count(const fec_ctx* ctx);
 
