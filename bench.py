@@ -232,7 +232,10 @@ def run_ours(args) -> None:
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
     torch.cuda.set_device(local)
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    if args.n:
+        wl["n"] = args.n
+        wl["name"] = wl["name"].split("_")[0] + f"_hex8_{args.n}cubed"
     mesh, asm, p, Uu_np = build_workload(fec, args.workload, wl["n"], local, args.precision)
     ne, nn, nf = mesh.num_elements(), mesh.num_nodes, asm.dof.nf
     n_u = int(asm.dof.unknown_dofs.size)
@@ -277,6 +280,9 @@ def run_ours(args) -> None:
     # ---- end to end through the public API with host buffers --------------------
     R0, K0 = step(Uu_d)
     nnz = K0.nnz
+    if args.no_e2e:
+        return finish(args, fec, world, rank, local, wl, mesh, asm, ne, nn, nf, n_u, nnz, t_ms, value, clocks,
+                      per_kernel, launches, None)
     Uu_h = torch.from_numpy(Uu_np).pin_memory()
     R_h = torch.empty(n_u, dtype=torch.float64).pin_memory()
     nz_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
@@ -302,7 +308,14 @@ def run_ours(args) -> None:
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_e2e = float(tt.item())
     e2e_value = world * ne * args.steps / (t_e2e * 1e-3) / 1e6
+    e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n_u, "d2h_bytes_per_step": 8 * (n_u + nnz)}
+    finish(args, fec, world, rank, local, wl, mesh, asm, ne, nn, nf, n_u, nnz, t_ms, value, clocks, per_kernel,
+           launches, e2e)
 
+
+def finish(args, fec, world, rank, local, wl, mesh, asm, ne, nn, nf, n_u, nnz, t_ms, value, clocks, per_kernel,
+           launches, e2e):
+    import torch.distributed as dist
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -355,8 +368,7 @@ def run_ours(args) -> None:
         "roofline": roofline,
         "compute_roofline": compute,
         "clocks": clocks,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n_u,
-                "d2h_bytes_per_step": 8 * (n_u + nnz)},
+        "e2e": e2e,
         "gpu_launches": launches,
         "cpu_baseline": cpu,
     }
@@ -374,6 +386,8 @@ def main() -> None:
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="neohookean")
     ap.add_argument("--precision", choices=["fp64", "fp32_element"], default="fp64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) measurement")
+    ap.add_argument("--n", type=int, default=None, help="elements per box side (default: the workload's size)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
