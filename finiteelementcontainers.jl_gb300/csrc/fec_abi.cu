@@ -126,6 +126,9 @@ int ensure(fec_ctx* c, DevBuf& b, size_t bytes) {
   return FEC_OK;
 }
 
+// element-matrix blocks start on 16-byte boundaries (vectorised copy-out)
+inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3); }
+
 int num_fields_of(int physics) { return physics == FEC_PHYS_POISSON ? 1 : 3; }
 int num_states_of(int physics) { return physics == FEC_PHYS_J2 ? 7 : 0; }
 
@@ -268,7 +271,7 @@ int fec_mesh_set(fec_ctx* c, int dim, int64_t nn, const double* coords, int nblo
     B.epos_off = epos_total;
     ne_total += B.ne;
     total_conn += B.ne * B.nnpe;
-    epos_total += B.ne * B.nnpe * B.nnpe;
+    epos_total += (B.ne * B.nnpe * B.nnpe + 3) & ~int64_t(3);  // 8-byte aligned blocks
   }
   if (ne_total >= (int64_t(1) << 58)) return fail(c, FEC_ERR_ARG, "too many elements");
   std::vector<int32_t> conn0(total_conn);
@@ -456,6 +459,17 @@ int fec_pattern_build(fec_ctx* c, int64_t* nnz_out) {
     }
   }
   if (bad_len >= 65535) return fail(c, FEC_ERR_UNSUPPORTED, "a node couples to %lld dofs (limit 65534)", (long long)bad_len);
+  std::vector<uint8_t> fullnbr(nn, 0);
+  // fast-path flag: the node and all the nodes it couples to are fully unknown
+  {
+    const uint8_t full = uint8_t((1u << c->nf) - 1u);
+#pragma omp parallel for schedule(static)
+    for (int64_t n = 0; n < nn; ++n) {
+      bool all = (c->umask[n] & 0x7f) == full;
+      for (int64_t p = nbr_ptr[n]; all && p < nbr_ptr[n + 1]; ++p) all = (c->umask[nbr[p]] & 0x7f) == full;
+      fullnbr[n] = all ? 1 : 0;
+    }
+  }
   std::vector<int64_t> col_base(nn, 0);
   int64_t nnz = 0;
   int max_cols = 0;
@@ -467,7 +481,7 @@ int fec_pattern_build(fec_ctx* c, int64_t* nnz_out) {
   }
   // element map: row offset of node conn[b] within node conn[a]'s columns
   int64_t epos_total = 0;
-  for (const Block& B : c->blocks) epos_total += B.ne * B.nnpe * B.nnpe;
+  for (const Block& B : c->blocks) epos_total += (B.ne * B.nnpe * B.nnpe + 3) & ~int64_t(3);
   std::vector<uint16_t> epos(epos_total);
   for (const Block& B : c->blocks) {
 #pragma omp parallel for schedule(static)
@@ -494,6 +508,12 @@ int fec_pattern_build(fec_ctx* c, int64_t* nnz_out) {
   if ((rc = upload(c, c->d_epos, epos.data(), sizeof(uint16_t) * epos.size()))) return rc;
   if ((rc = upload(c, c->d_col_base, col_base.data(), sizeof(int64_t) * col_base.size()))) return rc;
   if ((rc = upload(c, c->d_col_len, col_len.data(), sizeof(int32_t) * col_len.size()))) return rc;
+  {
+    std::vector<uint8_t> um2(c->umask);
+    for (int64_t n = 0; n < nn; ++n)
+      if (fullnbr[n]) um2[n] |= uint8_t(fec::UMASK_FULL_NBR);
+    if ((rc = upload(c, c->d_umask, um2.data(), um2.size()))) return rc;
+  }
   c->nbr_ptr = std::move(nbr_ptr);
   c->nbr = std::move(nbr);
   c->col_base = std::move(col_base);
@@ -595,7 +615,7 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
   int64_t ke_total = 0, re_total = 0;
   for (const Block& B : c->blocks) {
     const int ndof = c->nf * B.nnpe;
-    ke_total += B.ne * ndof * ndof;
+    ke_total += pad4(B.ne * ndof * ndof);
     re_total += B.ne * ndof;
   }
   int rc;
@@ -642,7 +662,9 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     bi.epos_off = B.epos_off;
     bi.nnpe = B.nnpe;
     bi.ndof = ndof;
-    ke_off += B.ne * ndof * ndof;
+    // the hex8 mechanics kernels write the node-rows layout
+    bi.layout = (B.elem_type == FEC_HEX8 && c->nf == 3) ? fec::KE_NODE_ROWS : fec::KE_ROW_MAJOR;
+    ke_off += pad4(B.ne * ndof * ndof);
     re_off += B.ne * ndof;
     st_off += int64_t(ns) * B.nq * B.ne;
   }
@@ -829,7 +851,7 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
   int64_t ke_total = 0, re_total = 0;
   for (const Block& B : c->blocks) {
     const int ndof = c->nf * B.nnpe;
-    ke_total += B.ne * ndof * ndof;
+    ke_total += pad4(B.ne * ndof * ndof);
     re_total += B.ne * ndof;
   }
   const size_t ke_bytes = want_k ? rsz * size_t(ke_total) : 0;
@@ -883,7 +905,9 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
     bi.epos_off = B.epos_off;
     bi.nnpe = B.nnpe;
     bi.ndof = ndof;
-    ke_off += B.ne * ndof * ndof;
+    // the hex8 mechanics kernels write the node-rows layout
+    bi.layout = (B.elem_type == FEC_HEX8 && c->nf == 3) ? fec::KE_NODE_ROWS : fec::KE_ROW_MAJOR;
+    ke_off += pad4(B.ne * ndof * ndof);
     re_off += B.ne * ndof;
     st_off += int64_t(ns) * B.nq * B.ne;
   }

@@ -1,6 +1,7 @@
 // fec_gather.cu -- instantiations of the node gather and the mechanics
 // dispatcher, plus the reference-element tables.
 #include <cmath>
+#include <cstdlib>
 #include "fec_launch.h"
 
 namespace fec {
@@ -18,11 +19,20 @@ cudaError_t launch_mech(int physics, int elem_type, int precision, bool want_r, 
 namespace {
 constexpr int WPB = 8;
 
-template <typename Real, int NF>
-cudaError_t go(const GatherArgs& g, cudaStream_t s, int* launches) {
-  if (g.nn <= 0) return cudaSuccess;
-  const size_t smem = sizeof(double) * size_t(WPB) * size_t(g.acc_stride);
-  auto kern = node_gather_kernel<Real, NF, WPB>;
+// Gather variants: (min blocks per SM, values in flight per lane).  Variant 0
+// favours occupancy, variant 1 favours loads in flight per warp.
+int gather_variant() {
+  static int v = [] {
+    const char* e = getenv("FEC_GATHER_VARIANT");
+    return e ? atoi(e) : 0;
+  }();
+  return v;
+}
+
+template <typename Real, int NF, int A, int MINB, int BUDGET>
+cudaError_t go1(const GatherArgs& g, cudaStream_t s, int* launches) {
+  const size_t smem = sizeof(float) * GatherAcc<Real>::WORDS * size_t(WPB) * size_t(g.acc_stride);
+  auto kern = node_gather_kernel<Real, NF, A, WPB, MINB, BUDGET>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (err != cudaSuccess) return err;
   const unsigned grid = unsigned((g.nn + WPB - 1) / WPB);
@@ -30,15 +40,36 @@ cudaError_t go(const GatherArgs& g, cudaStream_t s, int* launches) {
   ++*launches;
   return cudaGetLastError();
 }
+
+template <typename Real, int NF, int A>
+cudaError_t go(const GatherArgs& g, cudaStream_t s, int* launches) {
+  if (g.nn <= 0) return cudaSuccess;
+  if (gather_variant() == 1) return go1<Real, NF, A, 2, sizeof(Real) == 8 ? 12 : 18>(g, s, launches);
+  return go1<Real, NF, A, 3, sizeof(Real) == 8 ? 6 : 12>(g, s, launches);
+}
+
+template <typename Real, int NF>
+cudaError_t by_size(const GatherArgs& g, cudaStream_t s, int* launches) {
+  int A = g.blk[0].nnpe;
+  for (int b = 1; b < g.nblocks; ++b)
+    if (g.blk[b].nnpe != A) A = 0;
+  switch (A) {
+    case 8: return go<Real, NF, 8>(g, s, launches);
+    case 4: return go<Real, NF, 4>(g, s, launches);
+    case 10: return go<Real, NF, 10>(g, s, launches);
+    case 27: return go<Real, NF, 27>(g, s, launches);
+    default: return go<Real, NF, 0>(g, s, launches);
+  }
+}
 }  // namespace
 
 cudaError_t launch_gather(int precision, int nf, const GatherArgs& g, cudaStream_t s, int* launches) {
   if (precision == 0) {
-    if (nf == 1) return go<double, 1>(g, s, launches);
-    if (nf == 3) return go<double, 3>(g, s, launches);
+    if (nf == 1) return by_size<double, 1>(g, s, launches);
+    if (nf == 3) return by_size<double, 3>(g, s, launches);
   } else if (precision == 1) {
-    if (nf == 1) return go<float, 1>(g, s, launches);
-    if (nf == 3) return go<float, 3>(g, s, launches);
+    if (nf == 1) return by_size<float, 1>(g, s, launches);
+    if (nf == 3) return by_size<float, 3>(g, s, launches);
   }
   return cudaErrorNotSupported;
 }

@@ -29,6 +29,8 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <type_traits>
+#include "fec_df64.cuh"
 
 namespace fec {
 
@@ -277,7 +279,8 @@ struct NeoHookean {
 #pragma unroll
       for (int j = 0; j < 3; ++j) I1 = fma(F[i][j], F[i][j], I1);
     const Real c1 = Real(0.5) * Kb * (J * J - J - Real(1));
-    const Real c2 = Gs * pow(J, Real(-2.0 / 3.0));
+    const Real r3 = rcbrt(J);  // J^{-1/3}
+    const Real c2 = Gs * r3 * r3;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -290,6 +293,34 @@ struct NeoHookean {
     scr[18] = jxw * (Real(0.5) * Kb * (Real(2) * J - Real(1)) * J + Real(2.0 / 9.0) * c2 * I1);
     scr[19] = jxw * (I1 / Real(3) * c2 - c1);
     scr[20] = jxw * c2;
+  }
+  // JxW A_iJkL
+  template <typename Real>
+  __device__ static Real aentry(const Real* scr, int i, int J, int k, int L) {
+    const Real* F = scr;
+    const Real* H = scr + 9;
+    Real v = scr[18] * H[i * 3 + J] * H[k * 3 + L] + scr[19] * H[i * 3 + L] * H[k * 3 + J] +
+             Real(-2.0 / 3.0) * scr[20] * (H[k * 3 + L] * F[i * 3 + J] + F[k * 3 + L] * H[i * 3 + J]);
+    if (i == k && J == L) v += scr[20];
+    return v;
+  }
+  // df64 form of the scratch: F(9), H(9), a1, a2, c2, -2/3 c2 (all JxW-scaled where scr is)
+  static constexpr int SCR2 = 22;
+  __device__ static void split_scratch(const double* scr, float2* out) {
+#pragma unroll
+    for (int m = 0; m < 21; ++m) out[m] = df64_split(scr[m]);
+    out[21] = df64_split(-2.0 / 3.0 * scr[20]);
+  }
+  // JxW A_iJkL in df64
+  __device__ static float2 aentry_df64(const float2* s, int i, int J, int k, int L) {
+    const float2* F = s;
+    const float2* H = s + 9;
+    float2 v = df64_mul(s[18], df64_mul(H[i * 3 + J], H[k * 3 + L]));
+    v = df64_fma(s[19], df64_mul(H[i * 3 + L], H[k * 3 + J]), v);
+    const float2 t = df64_fma(H[k * 3 + L], F[i * 3 + J], df64_mul(F[k * 3 + L], H[i * 3 + J]));
+    v = df64_fma(s[21], t, v);
+    if (i == k && J == L) v = df64_add(v, s[20]);
+    return v;
   }
   // out[J*9 + k*3 + L] = JxW A_iJkL
   template <typename Real>
@@ -381,6 +412,28 @@ struct J2 {
     scr[10] = Real(double(jxw) * 2 * mu * th);
     scr[11] = Real(double(jxw) * 2 * mu * thb);
     scr[12] = 0;
+  }
+  template <typename Real>
+  __device__ static Real aentry(const Real* scr, int i, int J, int k, int L) {
+    const Real dij = (i == J) ? Real(1) : Real(0), dkl = (k == L) ? Real(1) : Real(0);
+    const Real isym = Real(0.5) * (Real((i == k) && (J == L)) + Real((i == L) && (J == k)));
+    return scr[9] * dij * dkl + scr[10] * (isym - dij * dkl / Real(3)) - scr[11] * scr[i * 3 + J] * scr[k * 3 + L];
+  }
+  // df64 form: n(9), c_a = kap' - mt'/3 (d_iJ d_kL), c_b = mt'/2 (each I_sym term), mb'
+  static constexpr int SCR2 = 12;
+  __device__ static void split_scratch(const double* scr, float2* out) {
+#pragma unroll
+    for (int m = 0; m < 9; ++m) out[m] = df64_split(scr[m]);
+    out[9] = df64_split(scr[9] - scr[10] / 3.0);
+    out[10] = df64_split(0.5 * scr[10]);
+    out[11] = df64_split(scr[11]);
+  }
+  __device__ static float2 aentry_df64(const float2* s, int i, int J, int k, int L) {
+    float2 v = df64_neg(df64_mul(s[11], df64_mul(s[i * 3 + J], s[k * 3 + L])));
+    if (i == J && k == L) v = df64_add(v, s[9]);
+    if (i == k && J == L) v = df64_add(v, s[10]);
+    if (i == L && J == k) v = df64_add(v, s[10]);
+    return v;
   }
   // C_iJkL = kap d_iJ d_kL + 2 mu th (I_sym - 1/3 d_iJ d_kL) - 2 mu thb n_iJ n_kL
   template <typename Real>
@@ -533,9 +586,19 @@ struct BlockInfo {
   int64_t epos_off;     // offset into epos (entries)
   int nnpe;
   int ndof;
+  int layout;           // element-matrix layout, see ke_index
 };
 
 constexpr int MAX_BLOCKS = 16;
+
+// Element-matrix workspace layouts.  Entry (row (a,k), column (b,i)) of one
+// element, NF fields, A nodes:
+//   KE_ROW_MAJOR:   (a*NF + k)*NF*A + b*NF + i        (K_e row-major)
+//   KE_NODE_ROWS:   ((a*NF + k)*NF + i)*A + b         (column node fastest; used by
+//                   the hex8 mechanics kernels so that the gather reads, per row
+//                   component and column component, the 8 column nodes as two
+//                   16-byte vectors)
+enum { KE_ROW_MAJOR = 0, KE_NODE_ROWS = 1 };
 
 struct GatherArgs {
   int64_t nn;                  // nodes
@@ -557,59 +620,273 @@ struct GatherArgs {
   int acc_stride;              // doubles of accumulator per warp
 };
 
-template <typename Real, int NF, int WPB>
-__global__ void __launch_bounds__(WPB * 32) node_gather_kernel(GatherArgs g) {
-  extern __shared__ __align__(16) double s_acc[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t n = int64_t(blockIdx.x) * WPB + warp;
-  if (n >= g.nn) return;
-  const unsigned um = g.umask[n];
-  if (um == 0) return;
-  const int Ln = g.col_len[n];
-  const int ncols = __popc(um);
-  double* acc = s_acc + warp * g.acc_stride;
-  const bool wantK = g.nzval != nullptr;
-  const bool wantR = g.R_u != nullptr;
-  if (wantK)
-    for (int j = lane; j < ncols * Ln; j += 32) acc[j] = 0.0;
-  double racc = 0.0;
-  __syncwarp();
-  const int64_t p0 = g.nadj_ptr[n], p1 = g.nadj_ptr[n + 1];
-  for (int64_t p = p0; p < p1; ++p) {
+// Bit 7 of umask[n]: node n and every node it couples to have all NF components
+// unknown, so CSC positions need no per-neighbour lookups.
+constexpr unsigned UMASK_FULL_NBR = 0x80u;
+
+// Exact float -> double widening with integer operations only (the hardware
+// conversion issues on the FP64 pipe, 1/64 of the FP32 rate on this part).
+// Handles zero, subnormal, inf and nan without branches.
+__device__ __forceinline__ double widen_exact(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint64_t sign = uint64_t(u & 0x80000000u) << 32;
+  const uint32_t ex = (u >> 23) & 0xffu;
+  const uint32_t m = u & 0x7fffffu;
+  // normal: rebias the exponent
+  uint64_t bits = sign | (uint64_t(ex + (1023u - 127u)) << 52) | (uint64_t(m) << 29);
+  // subnormal: normalise the mantissa (m != 0, ex == 0)
+  const int lz = __clz(m) - 8;  // leading zeros inside the 23-bit field, plus one
+  const uint64_t sub = sign | (uint64_t(1023 - 126 - lz) << 52) | (uint64_t((m << lz) & 0x7fffffu) << 29);
+  bits = (ex == 0u) ? (m == 0u ? sign : sub) : bits;
+  bits = (ex == 0xffu) ? (sign | (uint64_t(0x7ffu) << 52) | (uint64_t(m) << 29)) : bits;
+  return __longlong_as_double(int64_t(bits));
+}
+
+// Accumulator of the node gather.  FP64 inputs are added in FP64.  FP32 inputs
+// (the FP32-element variant) are added in compensated FP32: (hi, lo) with the
+// rounding error of every addition recovered exactly by TwoSum (Knuth) into
+// lo, which keeps the sum to about 2^-48 relative -- FP64-class accumulation
+// carried by the FP32 pipes -- and only the final hi + lo is formed in FP64.
+template <typename Real> struct GatherAcc;
+template <> struct GatherAcc<double> {
+  static constexpr int WORDS = 2;  // 4-byte words per entry
+  __device__ static void zero(float* base, int j) { reinterpret_cast<double*>(base)[j] = 0.0; }
+  __device__ static void add(float* base, int j, double v) { reinterpret_cast<double*>(base)[j] += v; }
+  __device__ static double value(const float* base, int j) { return reinterpret_cast<const double*>(base)[j]; }
+};
+template <> struct GatherAcc<float> {
+  static constexpr int WORDS = 2;
+  __device__ static void zero(float* base, int j) { reinterpret_cast<float2*>(base)[j] = make_float2(0.f, 0.f); }
+  __device__ static void add(float* base, int j, float v) {
+    float2 a = reinterpret_cast<float2*>(base)[j];
+    const float s = a.x + v;
+    const float bp = s - a.x;
+    const float err = (a.x - (s - bp)) + (v - bp);
+    a.x = s;
+    a.y += err;
+    reinterpret_cast<float2*>(base)[j] = a;
+  }
+  __device__ static double value(const float* base, int j) {
+    const float2 a = reinterpret_cast<const float2*>(base)[j];
+    return widen_exact(a.x) + widen_exact(a.y);
+  }
+};
+
+// Adds the contributions of adjacency entries [p, pend) -- all from one element
+// block with A nodes per element -- to the node's accumulator, in entry
+// (= increasing element) order.  Each lane fetches one adjacency entry, the
+// entries are broadcast by shuffles, and the row loads of up to CH elements
+// are all issued before their additions, so a warp keeps CH*VPL loads in
+// flight per lane instead of a dependent load chain per element.
+template <typename Real, int NF, int A, int BUDGET>
+__device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo& B, int64_t p, int64_t pend, unsigned um,
+                                           bool fast, int Ln, float* acc, double& racc, int lane, bool wantK,
+                                           bool wantR) {
+  constexpr int NDOF = NF * A;
+  constexpr int TOTAL = NF * NDOF;                         // values of one element's rows for this node
+  constexpr int VPL = (TOTAL + 31) / 32;                   // values per lane per element
+  constexpr int CH = VPL >= BUDGET ? 1 : (BUDGET / VPL > 8 ? 8 : BUDGET / VPL);
+  const Real* Ke = static_cast<const Real*>(g.Ke) + B.ke_off;
+  const Real* Re = static_cast<const Real*>(g.Re) + B.re_off;
+  for (; p < pend; p += 32) {
+    const int64_t left32 = pend - p;
+    const int n32 = left32 < 32 ? int(left32) : 32;
+    const int64_t mine = lane < n32 ? g.nadj[p + lane] : 0;
+    for (int c0 = 0; c0 < n32; c0 += CH) {
+      const int nh = (n32 - c0) < CH ? (n32 - c0) : CH;
+      Real v[CH][VPL];
+      int pos[CH][VPL];
+      Real rv[CH];
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        const int64_t packed = __shfl_sync(0xffffffffu, mine, (c0 + c) & 31);
+        rv[c] = Real(0);
+#pragma unroll
+        for (int j = 0; j < VPL; ++j) pos[c][j] = -1;
+        if (c < nh) {
+          const int64_t le = (packed >> 5) - B.elem_start;
+          const int a = int(packed & 31);
+          if (wantR) rv[c] = Re[le * NDOF + a * NF + lane];
+          if (wantK) {
+            const Real* Krows = Ke + (le * NDOF + int64_t(a) * NF) * NDOF;
+            const uint16_t* ep = g.epos + B.epos_off + (le * A + a) * A;
+#pragma unroll
+            for (int j = 0; j < VPL; ++j) {
+              const int t = lane + 32 * j;
+              if (t < TOTAL) {
+                const int k = t / NDOF, rem = t % NDOF;
+                const int b = rem / NF, i = rem % NF;
+                v[c][j] = Krows[t];
+                if (fast) {
+                  pos[c][j] = k * Ln + ep[b] + i;
+                } else if ((um >> k) & 1u) {
+                  const unsigned umm = g.umask[g.conn[B.conn_off + le * A + b]] & ~UMASK_FULL_NBR;
+                  if ((umm >> i) & 1u)
+                    pos[c][j] = __popc(um & ((1u << k) - 1u)) * Ln + ep[b] + __popc(umm & ((1u << i) - 1u));
+                }
+              }
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        if (c < nh) {
+          racc += double(rv[c]);
+          if (wantK) {
+#pragma unroll
+            for (int j = 0; j < VPL; ++j)
+              if (pos[c][j] >= 0) GatherAcc<Real>::add(acc, pos[c][j], v[c][j]);
+            __syncwarp();
+          }
+        }
+      }
+    }
+  }
+}
+
+// Same for a run whose element size is only known at run time (meshes whose
+// blocks have different element sizes).
+template <typename Real, int NF>
+__device__ __forceinline__ void gather_run_generic(const GatherArgs& g, const BlockInfo& B, int64_t p, int64_t pend,
+                                                   unsigned um, int Ln, float* acc, double& racc, int lane,
+                                                   bool wantK, bool wantR) {
+  const int A = B.nnpe, NDOF = B.ndof, TOTAL = NF * B.ndof;
+  const bool node_rows = B.layout == KE_NODE_ROWS;
+  const Real* Ke = static_cast<const Real*>(g.Ke) + B.ke_off;
+  const Real* Re = static_cast<const Real*>(g.Re) + B.re_off;
+  for (; p < pend; ++p) {
     const int64_t packed = g.nadj[p];
-    const int64_t ge = packed >> 5;
+    const int64_t le = (packed >> 5) - B.elem_start;
     const int a = int(packed & 31);
-    int bi = 0;
-    while (bi + 1 < g.nblocks && ge >= g.blk[bi + 1].elem_start) ++bi;
-    const BlockInfo& B = g.blk[bi];
-    const int64_t le = ge - B.elem_start;
-    const int A = B.nnpe, NDOF = B.ndof;
-    if (wantR && lane < NF && ((um >> lane) & 1u))
-      racc += double(static_cast<const Real*>(g.Re)[B.re_off + le * NDOF + a * NF + lane]);
+    if (wantR) racc += double(Re[le * NDOF + a * NF + lane]);
     if (wantK) {
-      const Real* Krows = static_cast<const Real*>(g.Ke) + B.ke_off + (le * NDOF + int64_t(a) * NF) * NDOF;
-      const int32_t* cn = g.conn + B.conn_off + le * A;
+      const Real* Krows = Ke + (le * NDOF + int64_t(a) * NF) * NDOF;
       const uint16_t* ep = g.epos + B.epos_off + (le * A + a) * A;
-      const int total = NF * NDOF;
-      for (int t = lane; t < total; t += 32) {
+      for (int t = lane; t < TOTAL; t += 32) {
         const int k = t / NDOF, rem = t - k * NDOF;
         const int b = rem / NF, i = rem - b * NF;
         if (!((um >> k) & 1u)) continue;
-        const int m = cn[b];
-        const unsigned umm = g.umask[m];
+        const unsigned umm = g.umask[g.conn[B.conn_off + le * A + b]] & ~UMASK_FULL_NBR;
         if (!((umm >> i) & 1u)) continue;
-        const int kk = __popc(um & ((1u << k) - 1u));
-        const int ii = __popc(umm & ((1u << i) - 1u));
-        acc[kk * Ln + ep[b] + ii] += double(Krows[t]);
+        const int off = node_rows ? (k * NF + i) * A + b : t;
+        GatherAcc<Real>::add(acc, __popc(um & ((1u << k) - 1u)) * Ln + ep[b] + __popc(umm & ((1u << i) - 1u)),
+                             Krows[off]);
       }
       __syncwarp();
     }
   }
+}
+
+// Vector hex8 in the KE_NODE_ROWS layout, for nodes whose whole neighbourhood
+// is unknown: lane l < 18 owns (row component k, column component i) = (l/2)
+// and the column nodes b = 4(l%2) .. 4(l%2)+3, read as one 16-byte (FP32) or
+// two 16-byte (FP64) vectors, with their CSC row offsets from one 8-byte load
+// of the element map.  Positions are k*Ln + i + epos[b]: two integer ops per
+// value.
+template <typename Real>
+__device__ __forceinline__ void gather_run_hex8v(const GatherArgs& g, const BlockInfo& B, int64_t p, int64_t pend,
+                                                 int Ln, float* acc, double& racc, int lane, bool wantK, bool wantR) {
+  constexpr int CH = sizeof(Real) == 8 ? 4 : 6;
+  using V4 = typename std::conditional<sizeof(Real) == 4, float4, double4_32a>::type;
+  const Real* Ke = static_cast<const Real*>(g.Ke) + B.ke_off;
+  const Real* Re = static_cast<const Real*>(g.Re) + B.re_off;
+  const bool kl = lane < 18;
+  const int ki = lane >> 1, bh = lane & 1;
+  const int base = (ki / 3) * Ln + (ki % 3);
+  for (; p < pend; p += 32) {
+    const int64_t left32 = pend - p;
+    const int n32 = left32 < 32 ? int(left32) : 32;
+    const int64_t mine = lane < n32 ? g.nadj[p + lane] : 0;
+    for (int c0 = 0; c0 < n32; c0 += CH) {
+      const int nh = (n32 - c0) < CH ? (n32 - c0) : CH;
+      V4 v[CH];
+      uint2 ep[CH];
+      Real rv[CH];
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        const int64_t packed = __shfl_sync(0xffffffffu, mine, (c0 + c) & 31);
+        rv[c] = Real(0);
+        if (c < nh) {
+          const int64_t le = (packed >> 5) - B.elem_start;
+          const int a = int(packed & 31);
+          if (wantR) rv[c] = Re[le * 24 + a * 3 + lane];
+          if (wantK && kl) {
+            v[c] = *reinterpret_cast<const V4*>(Ke + le * 576 + a * 72 + ki * 8 + bh * 4);
+            ep[c] = *reinterpret_cast<const uint2*>(g.epos + B.epos_off + (le * 8 + a) * 8 + bh * 4);
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        if (c < nh) {
+          racc += double(rv[c]);
+          if (wantK) {
+            if (kl) {
+              GatherAcc<Real>::add(acc, base + int(ep[c].x & 0xffffu), v[c].x);
+              GatherAcc<Real>::add(acc, base + int(ep[c].x >> 16), v[c].y);
+              GatherAcc<Real>::add(acc, base + int(ep[c].y & 0xffffu), v[c].z);
+              GatherAcc<Real>::add(acc, base + int(ep[c].y >> 16), v[c].w);
+            }
+            __syncwarp();
+          }
+        }
+      }
+    }
+  }
+}
+
+// One warp per node.  A > 0: every block has A nodes per element; A == 0: mixed.
+template <typename Real, int NF, int A, int WPB, int MINB, int BUDGET>
+__global__ void __launch_bounds__(WPB * 32, MINB) node_gather_kernel(GatherArgs g) {
+  extern __shared__ __align__(16) float s_acc[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t n = int64_t(blockIdx.x) * WPB + warp;
+  if (n >= g.nn) return;
+  const unsigned um_raw = g.umask[n];
+  const bool fast = (um_raw & UMASK_FULL_NBR) != 0;
+  const unsigned um = um_raw & ~UMASK_FULL_NBR;
+  if (um == 0) return;
+  const int Ln = g.col_len[n];
+  const int ncols = __popc(um);
+  float* acc = s_acc + warp * g.acc_stride * GatherAcc<Real>::WORDS;
+  const bool wantK = g.nzval != nullptr;
+  const bool wantR = g.R_u != nullptr && lane < NF && ((um >> lane) & 1u);
+  if (wantK)
+    for (int j = lane; j < ncols * Ln; j += 32) GatherAcc<Real>::zero(acc, j);
+  double racc = 0.0;
+  __syncwarp();
+  int64_t p = g.nadj_ptr[n];
+  const int64_t p1 = g.nadj_ptr[n + 1];
+  while (p < p1) {
+    // the run of entries from one element block
+    const int64_t ge = g.nadj[p] >> 5;
+    int bi = 0;
+    while (bi + 1 < g.nblocks && ge >= g.blk[bi + 1].elem_start) ++bi;
+    const BlockInfo& B = g.blk[bi];
+    int64_t q = p1;
+    if (bi + 1 < g.nblocks) {
+      const int64_t bend = g.blk[bi + 1].elem_start;
+      q = p + 1;
+      while (q < p1 && (g.nadj[q] >> 5) < bend) ++q;
+    }
+    if constexpr (A == 8 && NF == 3) {
+      if (fast && B.layout == KE_NODE_ROWS)
+        gather_run_hex8v<Real>(g, B, p, q, Ln, acc, racc, lane, wantK, wantR);
+      else
+        gather_run_generic<Real, NF>(g, B, p, q, um, Ln, acc, racc, lane, wantK, wantR);
+    } else if constexpr (A > 0) {
+      gather_run<Real, NF, A, BUDGET>(g, B, p, q, um, fast, Ln, acc, racc, lane, wantK, wantR);
+    } else {
+      gather_run_generic<Real, NF>(g, B, p, q, um, Ln, acc, racc, lane, wantK, wantR);
+    }
+    p = q;
+  }
   if (wantK) {
     double* out = g.nzval + g.col_base[n];
-    for (int j = lane; j < ncols * Ln; j += 32) out[j] = acc[j];
+    for (int j = lane; j < ncols * Ln; j += 32) out[j] = GatherAcc<Real>::value(acc, j);
   }
-  if (wantR && lane < NF && ((um >> lane) & 1u)) g.R_u[g.dof_to_unknown[n * NF + lane]] = racc;
+  if (wantR) g.R_u[g.dof_to_unknown[n * NF + lane]] = racc;
 }
 
 }  // namespace fec

@@ -1,0 +1,603 @@
+// fec_mech_hex8.cuh -- the hex8 mechanics element kernel used for the
+// benchmark workloads (vector hex8, 2x2x2 points, symmetric tangent).
+//
+// Compared with the generic mech_element_kernel (one thread per element row):
+//  * the tangent is symmetric for the hyperelastic and associative-plastic
+//    models here (A_iJkL = A_kLiJ), so each element is served by 12 threads,
+//    thread (p, i) owning rows (p, i) and (7-p, i) and only the column blocks
+//    b >= row node: 9 node blocks per thread, 36 of the 64 node pairs in all,
+//    which removes 32% of the contraction FMAs -- the work that binds the FP64
+//    variant to the GB300's FP64 pipe;
+//  * the tangent tensor is evaluated from its 45 unique entries;
+//  * K_e is staged in shared memory (the mirrored half written there) in the
+//    KE_NODE_ROWS layout the node gather reads, and leaves the CTA as one
+//    contiguous, 16-byte vectorised stream;
+//  * in the FP32-element variant the isoparametric map runs in FP32 on
+//    coordinate differences taken in FP64 (x_a - x_0), with the FP64 map kept
+//    for distorted elements (Hadamard ratio |det J| / prod |J col| < 0.25), so
+//    the FP64 pipe no longer carries the per-point kinematics.
+#pragma once
+#include <type_traits>
+#include "fec_kernels.cuh"
+
+namespace fec {
+
+// (r1, r2), r1 <= r2, of the m-th unique entry of a symmetric 9x9 matrix
+__device__ __forceinline__ void sym_pair(int m, int& r1, int& r2) {
+  int r = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const int cnt = 9 - r;
+    if (m >= cnt) {
+      m -= cnt;
+      ++r;
+    }
+  }
+  r1 = r;
+  r2 = r + m;
+}
+
+// FP32 map of a hex8 point from FP64-differenced coordinates; falls back to the
+// FP64 map for distorted elements.  Returns JxW.
+__device__ __forceinline__ float map_hex8_mixed(const double* __restrict__ s_ref, const float* __restrict__ s_reff,
+                                                int q, const double* __restrict__ x, const float* __restrict__ xd,
+                                                float* __restrict__ dNX) {
+  using L = RefLayout<1>;
+  const float* dN = s_reff + L::DN_OFF + q * 24;
+  float J[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+#pragma unroll
+  for (int a = 1; a < 8; ++a)  // xd[0] = 0
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) J[d][k] = fmaf(xd[a * 3 + d], dN[a * 3 + k], J[d][k]);
+  const float c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+  const float c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  const float c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  const float det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+  float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    n0 = fmaf(J[d][0], J[d][0], n0);
+    n1 = fmaf(J[d][1], J[d][1], n1);
+    n2 = fmaf(J[d][2], J[d][2], n2);
+  }
+  if (!(fabsf(det) >= 0.25f * sqrtf(n0 * n1 * n2))) return float(map_point<1, float>(s_ref, q, x, dNX, nullptr));
+  const float r = 1.0f / det;
+  float Ji[3][3];
+  Ji[0][0] = c00 * r;
+  Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
+  Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+  Ji[1][0] = c01 * r;
+  Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+  Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
+  Ji[2][0] = c02 * r;
+  Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * r;
+  Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      dNX[a * 3 + d] = fmaf(dN[a * 3 + 0], Ji[0][d], fmaf(dN[a * 3 + 1], Ji[1][d], dN[a * 3 + 2] * Ji[2][d]));
+  return det * float(s_ref[L::W_OFF + q]);
+}
+
+template <class Model, typename Real, int EPB>
+struct Hex8Smem {
+  static constexpr int NQ = 8, SCR = Model::SCR;
+  static constexpr int REF = RefLayout<1>::SIZE;                   // 264
+  static constexpr int D_REF = 0, D_X = D_REF + REF;                // doubles
+  static constexpr int N_DOUBLE = D_X + EPB * 24;
+  static constexpr int R_REFF = 0;                                  // Reals, after the doubles
+  static constexpr int R_XD = R_REFF + REF;
+  static constexpr int R_U = R_XD + EPB * 24;
+  static constexpr int R_DNX = R_U + EPB * 24;
+  static constexpr int R_JXW = R_DNX + EPB * NQ * 24;
+  static constexpr int R_P = R_JXW + EPB * NQ;
+  static constexpr int R_SCR = R_P + EPB * NQ * 9;
+  static constexpr int R_A = (R_SCR + EPB * NQ * SCR + 3) & ~3;     // 16-byte aligned for the vector copy-out
+  static constexpr int A_STRIDE = NQ * 81;                          // per element; >= 576 for the K staging
+  static constexpr int N_REAL = R_A + EPB * A_STRIDE;
+  static constexpr size_t BYTES = sizeof(double) * N_DOUBLE + sizeof(Real) * N_REAL + sizeof(int) * EPB * 8;
+};
+
+template <class Model, typename Real, int EPB, bool WANT_R, bool WANT_K>
+__global__ void __launch_bounds__(EPB * 12) mech_hex8_sym_kernel(ElemArgs g) {
+  constexpr int NQ = 8, TPE = 12, NS = Model::NS, SCR = Model::SCR;
+  constexpr bool F64 = std::is_same<Real, double>::value;
+  using S = Hex8Smem<Model, Real, EPB>;
+  using L = RefLayout<1>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* s_ref = reinterpret_cast<double*>(smem_raw) + S::D_REF;
+  double* s_x_all = reinterpret_cast<double*>(smem_raw) + S::D_X;
+  Real* rb = reinterpret_cast<Real*>(reinterpret_cast<double*>(smem_raw) + S::N_DOUBLE);
+  Real* s_reff = rb + S::R_REFF;
+  int* s_conn_all = reinterpret_cast<int*>(rb + S::N_REAL);
+
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int tid = ty * TPE + tx, nthr = EPB * TPE;
+  const int64_t e0 = int64_t(blockIdx.x) * EPB;
+  const int64_t e = e0 + ty;
+  const bool live = e < g.ne;
+  double* s_x = s_x_all + ty * 24;
+  Real* s_xd = rb + S::R_XD + ty * 24;
+  Real* s_u = rb + S::R_U + ty * 24;
+  Real* s_dNX = rb + S::R_DNX + ty * NQ * 24;
+  Real* s_jxw = rb + S::R_JXW + ty * NQ;
+  Real* s_P = rb + S::R_P + ty * NQ * 9;
+  Real* s_scr = rb + S::R_SCR + ty * NQ * SCR;
+  Real* s_A = rb + S::R_A + ty * S::A_STRIDE;
+  int* s_conn = s_conn_all + ty * 8;
+
+  for (int i = tid; i < L::SIZE; i += nthr) {
+    const double v = g.ref[i];
+    s_ref[i] = v;
+    if (!F64) s_reff[i] = Real(v);
+  }
+  if (live && tx < 8) s_conn[tx] = g.conn[e * 8 + tx];
+  __syncthreads();
+  if (live) {
+    for (int i = tx; i < 24; i += TPE) {
+      const int a = i / 3, d = i % 3;
+      const double xv = __ldg(&g.coords[int64_t(s_conn[a]) * 3 + d]);
+      s_x[i] = xv;
+      if (!F64) s_xd[i] = Real(xv - __ldg(&g.coords[int64_t(s_conn[0]) * 3 + d]));
+      s_u[i] = Real(__ldg(&g.U[int64_t(s_conn[a]) * 3 + d]));
+    }
+  }
+  __syncthreads();
+
+  // per-point kinematics and constitutive update
+  if (live && tx < NQ) {
+    const int q = tx;
+    Real* dNX = s_dNX + q * 24;
+    Real jxw;
+    if constexpr (F64)
+      jxw = Real(map_point<1, double>(s_ref, q, s_x, dNX, nullptr));
+    else
+      jxw = map_hex8_mixed(s_ref, s_reff, q, s_x, s_xd, dNX);
+    s_jxw[q] = jxw;
+    Real gu[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        Real s = 0;
+#pragma unroll
+        for (int a = 0; a < 8; ++a) s = fma(s_u[a * 3 + i], dNX[a * 3 + j], s);
+        gu[i][j] = s;
+      }
+    const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
+    double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
+    Model::point(g.props, gu, jxw, so, sn, s_P + q * 9, s_scr + q * SCR);
+  }
+  __syncthreads();
+  // JxW-scaled tangent from its 45 unique entries
+  if (WANT_K && live) {
+    for (int w = tx; w < NQ * 45; w += TPE) {
+      const int q = w / 45;
+      int r1, r2;
+      sym_pair(w - q * 45, r1, r2);
+      const Real v = Model::aentry(s_scr + q * SCR, r1 / 3, r1 % 3, r2 / 3, r2 % 3);
+      Real* Aq = s_A + q * 81;
+      Aq[r1 * 9 + r2] = v;
+      Aq[r2 * 9 + r1] = v;
+    }
+  }
+  __syncthreads();
+
+  const int pp = tx / 3, i = tx % 3;
+  const int a1 = pp, a2 = 7 - pp;
+  const int split = 8 - pp;  // blocks j < split belong to row node a1
+  Real K[27];
+#pragma unroll
+  for (int c = 0; c < 27; ++c) K[c] = 0;
+  Real R1 = 0, R2 = 0;
+  if (live) {
+    for (int q = 0; q < NQ; ++q) {
+      const Real* dNX = s_dNX + q * 24;
+      const Real g10 = dNX[a1 * 3], g11 = dNX[a1 * 3 + 1], g12 = dNX[a1 * 3 + 2];
+      const Real g20 = dNX[a2 * 3], g21 = dNX[a2 * 3 + 1], g22 = dNX[a2 * 3 + 2];
+      if (WANT_R) {
+        const Real* P = s_P + q * 9 + i * 3;
+        R1 = fma(g10, P[0], fma(g11, P[1], fma(g12, P[2], R1)));
+        R2 = fma(g20, P[0], fma(g21, P[1], fma(g22, P[2], R2)));
+      }
+      if (WANT_K) {
+        const Real* Ai = s_A + q * 81 + i * 27;
+        Real t1[9], t2[9];
+#pragma unroll
+        for (int kl = 0; kl < 9; ++kl) {
+          const Real x0 = Ai[kl], x1 = Ai[9 + kl], x2 = Ai[18 + kl];
+          t1[kl] = fma(g10, x0, fma(g11, x1, g12 * x2));
+          t2[kl] = fma(g20, x0, fma(g21, x1, g22 * x2));
+        }
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+          const bool first = j < split;
+          const int b = first ? pp + j : j - 1;
+          const Real h0 = dNX[b * 3], h1 = dNX[b * 3 + 1], h2 = dNX[b * 3 + 2];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const Real u0 = first ? t1[k * 3] : t2[k * 3];
+            const Real u1 = first ? t1[k * 3 + 1] : t2[k * 3 + 1];
+            const Real u2 = first ? t1[k * 3 + 2] : t2[k * 3 + 2];
+            K[j * 3 + k] += fma(u0, h0, fma(u1, h1, u2 * h2));
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();  // s_A is reused for the K staging below
+  if (WANT_K && live) {
+    Real* Ks = s_A;  // 576 entries, KE_NODE_ROWS layout ((a*3 + k)*3 + i)*8 + b
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+      const bool first = j < split;
+      const int an = first ? a1 : a2;
+      const int b = first ? pp + j : j - 1;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        Ks[((an * 3 + i) * 3 + k) * 8 + b] = K[j * 3 + k];
+        if (b != an) Ks[((b * 3 + k) * 3 + i) * 8 + an] = K[j * 3 + k];
+      }
+    }
+  }
+  if (WANT_R && live) {
+    Real* Re = static_cast<Real*>(g.Re) + e * 24;
+    Re[a1 * 3 + i] = R1;
+    Re[a2 * 3 + i] = R2;
+  }
+  if (WANT_K) {
+    __syncthreads();
+    using V = typename std::conditional<sizeof(Real) == 4, float4, double2>::type;
+    constexpr int VW = 16 / sizeof(Real);
+    constexpr int PER = 576 / VW;
+    const int64_t left = g.ne - e0;
+    const int nlive = left < EPB ? int(left) : EPB;
+    V* dst = reinterpret_cast<V*>(static_cast<Real*>(g.Ke) + e0 * 576);
+    const Real* src = rb + S::R_A;
+    for (int idx = tid; idx < nlive * PER; idx += nthr) {
+      const int el = idx / PER, off = idx - el * PER;
+      dst[idx] = *reinterpret_cast<const V*>(src + el * S::A_STRIDE + off * VW);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP32-element variant.  On the FP32 pipes the contraction FMAs are cheap and
+// integer/select work is what limits the symmetric kernel, so here each of the
+// 12 threads of an element owns two full rows (p, i) and (p+4, i) over all 8
+// column blocks: 57 shared-memory loads per 198 FMAs per point, every index a
+// compile-time constant, no selects.  The tangent slice A_i... of a point is
+// produced by one thread with i fixed at compile time.
+// ---------------------------------------------------------------------------
+template <class Model, typename Real, int I>
+__device__ __forceinline__ void tangent_slice(const Real* scr, Real* out) {
+#pragma unroll
+  for (int J = 0; J < 3; ++J)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int L = 0; L < 3; ++L) out[J * 9 + k * 3 + L] = Model::aentry(scr, I, J, k, L);
+}
+
+template <class Model, int EPB, bool WANT_R, bool WANT_K>
+__global__ void __launch_bounds__(EPB * 12) mech_hex8_rows2_kernel(ElemArgs g) {
+  using Real = float;
+  constexpr int NQ = 8, TPE = 12, NS = Model::NS, SCR = Model::SCR;
+  using S = Hex8Smem<Model, Real, EPB>;
+  using L = RefLayout<1>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* s_ref = reinterpret_cast<double*>(smem_raw) + S::D_REF;
+  double* s_x_all = reinterpret_cast<double*>(smem_raw) + S::D_X;
+  Real* rb = reinterpret_cast<Real*>(reinterpret_cast<double*>(smem_raw) + S::N_DOUBLE);
+  Real* s_reff = rb + S::R_REFF;
+  int* s_conn_all = reinterpret_cast<int*>(rb + S::N_REAL);
+
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int tid = ty * TPE + tx, nthr = EPB * TPE;
+  const int64_t e0 = int64_t(blockIdx.x) * EPB;
+  const int64_t e = e0 + ty;
+  const bool live = e < g.ne;
+  double* s_x = s_x_all + ty * 24;
+  Real* s_xd = rb + S::R_XD + ty * 24;
+  Real* s_u = rb + S::R_U + ty * 24;
+  Real* s_dNX = rb + S::R_DNX + ty * NQ * 24;
+  Real* s_P = rb + S::R_P + ty * NQ * 9;
+  Real* s_scr = rb + S::R_SCR + ty * NQ * SCR;
+  Real* s_A = rb + S::R_A + ty * S::A_STRIDE;
+  int* s_conn = s_conn_all + ty * 8;
+
+  for (int i = tid; i < L::SIZE; i += nthr) {
+    const double v = g.ref[i];
+    s_ref[i] = v;
+    s_reff[i] = Real(v);
+  }
+  if (live && tx < 8) s_conn[tx] = g.conn[e * 8 + tx];
+  __syncthreads();
+  if (live) {
+    for (int i = tx; i < 24; i += TPE) {
+      const int a = i / 3, d = i % 3;
+      const double xv = __ldg(&g.coords[int64_t(s_conn[a]) * 3 + d]);
+      s_x[i] = xv;
+      s_xd[i] = Real(xv - __ldg(&g.coords[int64_t(s_conn[0]) * 3 + d]));
+      s_u[i] = Real(__ldg(&g.U[int64_t(s_conn[a]) * 3 + d]));
+    }
+  }
+  __syncthreads();
+  if (live && tx < NQ) {
+    const int q = tx;
+    Real* dNX = s_dNX + q * 24;
+    const Real jxw = map_hex8_mixed(s_ref, s_reff, q, s_x, s_xd, dNX);
+    Real gu[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        Real s = 0;
+#pragma unroll
+        for (int a = 0; a < 8; ++a) s = fmaf(s_u[a * 3 + i], dNX[a * 3 + j], s);
+        gu[i][j] = s;
+      }
+    const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
+    double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
+    Model::point(g.props, gu, jxw, so, sn, s_P + q * 9, s_scr + q * SCR);
+  }
+  __syncthreads();
+  const int pp = tx / 3, i = tx % 3;
+  if (WANT_K && live) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int q = pp + 4 * h;
+      const Real* scr = s_scr + q * SCR;
+      Real* out = s_A + q * 81 + i * 27;
+      if (i == 0) tangent_slice<Model, Real, 0>(scr, out);
+      else if (i == 1) tangent_slice<Model, Real, 1>(scr, out);
+      else tangent_slice<Model, Real, 2>(scr, out);
+    }
+  }
+  __syncthreads();
+  const int a1 = pp, a2 = pp + 4;
+  Real K1[24], K2[24];
+#pragma unroll
+  for (int c = 0; c < 24; ++c) K1[c] = K2[c] = 0.f;
+  Real R1 = 0.f, R2 = 0.f;
+  if (live) {
+    for (int q = 0; q < NQ; ++q) {
+      const Real* dNX = s_dNX + q * 24;
+      const Real g10 = dNX[a1 * 3], g11 = dNX[a1 * 3 + 1], g12 = dNX[a1 * 3 + 2];
+      const Real g20 = dNX[a2 * 3], g21 = dNX[a2 * 3 + 1], g22 = dNX[a2 * 3 + 2];
+      if (WANT_R) {
+        const Real* P = s_P + q * 9 + i * 3;
+        R1 = fmaf(g10, P[0], fmaf(g11, P[1], fmaf(g12, P[2], R1)));
+        R2 = fmaf(g20, P[0], fmaf(g21, P[1], fmaf(g22, P[2], R2)));
+      }
+      if (WANT_K) {
+        const Real* Ai = s_A + q * 81 + i * 27;
+        Real t1[9], t2[9];
+#pragma unroll
+        for (int kl = 0; kl < 9; ++kl) {
+          const Real x0 = Ai[kl], x1 = Ai[9 + kl], x2 = Ai[18 + kl];
+          t1[kl] = fmaf(g10, x0, fmaf(g11, x1, g12 * x2));
+          t2[kl] = fmaf(g20, x0, fmaf(g21, x1, g22 * x2));
+        }
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+          const Real h0 = dNX[b * 3], h1 = dNX[b * 3 + 1], h2 = dNX[b * 3 + 2];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            K1[b * 3 + k] += fmaf(t1[k * 3], h0, fmaf(t1[k * 3 + 1], h1, t1[k * 3 + 2] * h2));
+            K2[b * 3 + k] += fmaf(t2[k * 3], h0, fmaf(t2[k * 3 + 1], h1, t2[k * 3 + 2] * h2));
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();  // s_A is reused for the K staging below
+  if (WANT_K && live) {
+    // KE_NODE_ROWS layout: ((a*3 + k)*3 + i)*8 + b, column node b fastest
+    float4* r1 = reinterpret_cast<float4*>(s_A + (a1 * 3 + i) * 24);
+    float4* r2 = reinterpret_cast<float4*>(s_A + (a2 * 3 + i) * 24);
+#pragma unroll
+    for (int kc = 0; kc < 3; ++kc) {
+      r1[2 * kc] = make_float4(K1[kc], K1[3 + kc], K1[6 + kc], K1[9 + kc]);
+      r1[2 * kc + 1] = make_float4(K1[12 + kc], K1[15 + kc], K1[18 + kc], K1[21 + kc]);
+      r2[2 * kc] = make_float4(K2[kc], K2[3 + kc], K2[6 + kc], K2[9 + kc]);
+      r2[2 * kc + 1] = make_float4(K2[12 + kc], K2[15 + kc], K2[18 + kc], K2[21 + kc]);
+    }
+  }
+  if (WANT_R && live) {
+    Real* Re = static_cast<Real*>(g.Re) + e * 24;
+    Re[a1 * 3 + i] = R1;
+    Re[a2 * 3 + i] = R2;
+  }
+  if (WANT_K) {
+    __syncthreads();
+    constexpr int PER = 576 / 4;
+    const int64_t left = g.ne - e0;
+    const int nlive = left < EPB ? int(left) : EPB;
+    float4* dst = reinterpret_cast<float4*>(static_cast<Real*>(g.Ke) + e0 * 576);
+    const Real* src = rb + S::R_A;
+    for (int idx = tid; idx < nlive * PER; idx += nthr) {
+      const int el = idx / PER, off = idx - el * PER;
+      dst[idx] = *reinterpret_cast<const float4*>(src + el * S::A_STRIDE + off * 4);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 variant with the contraction on the FP32 pipes.  Kinematics and the
+// constitutive update stay in FP64; the shape-function gradients, the stress and
+// the tangent scratch are split into double-float (hi + lo) once per point, the
+// tangent entries and the whole K_e / R_e contraction run in df64, and the
+// results are widened back to FP64 for the workspace.  Same thread mapping and
+// symmetry as mech_hex8_sym_kernel.
+// ---------------------------------------------------------------------------
+template <class Model, int EPB>
+struct Hex8Df64Smem {
+  static constexpr int NQ = 8, SCR2 = Model::SCR2;
+  static constexpr int REF = RefLayout<1>::SIZE;
+  static constexpr int D_REF = 0, D_X = REF, D_U = D_X + EPB * 24;
+  static constexpr int N_DOUBLE = D_U + EPB * 24;
+  static constexpr int F_DNX = 0;                       // float2 entries, after the doubles
+  static constexpr int F_P = F_DNX + EPB * NQ * 24;
+  static constexpr int F_SCR = F_P + EPB * NQ * 9;
+  static constexpr int F_A = (F_SCR + EPB * NQ * SCR2 + 1) & ~1;  // 16-byte aligned
+  static constexpr int A_STRIDE = NQ * 81;              // >= 576 doubles of K staging
+  static constexpr int N_F2 = F_A + EPB * A_STRIDE;
+  static constexpr size_t BYTES = sizeof(double) * N_DOUBLE + sizeof(float2) * N_F2 + sizeof(int) * EPB * 8;
+};
+
+template <class Model, int EPB, bool WANT_R, bool WANT_K>
+__global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
+  constexpr int NQ = 8, TPE = 12, NS = Model::NS, SCR = Model::SCR, SCR2 = Model::SCR2;
+  using S = Hex8Df64Smem<Model, EPB>;
+  using L = RefLayout<1>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* dbase = reinterpret_cast<double*>(smem_raw);
+  double* s_ref = dbase + S::D_REF;
+  float2* fb = reinterpret_cast<float2*>(dbase + S::N_DOUBLE);
+  int* s_conn_all = reinterpret_cast<int*>(fb + S::N_F2);
+
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int tid = ty * TPE + tx, nthr = EPB * TPE;
+  const int64_t e0 = int64_t(blockIdx.x) * EPB;
+  const int64_t e = e0 + ty;
+  const bool live = e < g.ne;
+  double* s_x = dbase + S::D_X + ty * 24;
+  double* s_u = dbase + S::D_U + ty * 24;
+  float2* s_dNX = fb + S::F_DNX + ty * NQ * 24;
+  float2* s_P = fb + S::F_P + ty * NQ * 9;
+  float2* s_scr = fb + S::F_SCR + ty * NQ * SCR2;
+  float2* s_A = fb + S::F_A + ty * S::A_STRIDE;
+  int* s_conn = s_conn_all + ty * 8;
+
+  for (int i = tid; i < L::SIZE; i += nthr) s_ref[i] = g.ref[i];
+  if (live && tx < 8) s_conn[tx] = g.conn[e * 8 + tx];
+  __syncthreads();
+  if (live) {
+    for (int i = tx; i < 24; i += TPE) {
+      const int a = i / 3, d = i % 3;
+      s_x[i] = __ldg(&g.coords[int64_t(s_conn[a]) * 3 + d]);
+      s_u[i] = __ldg(&g.U[int64_t(s_conn[a]) * 3 + d]);
+    }
+  }
+  __syncthreads();
+  if (live && tx < NQ) {
+    const int q = tx;
+    double dNX[24];
+    const double jxw = map_point<1, double>(s_ref, q, s_x, dNX, nullptr);
+    double gu[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        double s = 0;
+#pragma unroll
+        for (int a = 0; a < 8; ++a) s = fma(s_u[a * 3 + i], dNX[a * 3 + j], s);
+        gu[i][j] = s;
+      }
+    const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
+    double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
+    double P9[9], scr[SCR];
+    Model::point(g.props, gu, jxw, so, sn, P9, scr);
+#pragma unroll
+    for (int m = 0; m < 24; ++m) s_dNX[q * 24 + m] = df64_split(dNX[m]);
+#pragma unroll
+    for (int m = 0; m < 9; ++m) s_P[q * 9 + m] = df64_split(P9[m]);
+    Model::split_scratch(scr, s_scr + q * SCR2);
+  }
+  __syncthreads();
+  if (WANT_K && live) {
+    for (int w = tx; w < NQ * 45; w += TPE) {
+      const int q = w / 45;
+      int r1, r2;
+      sym_pair(w - q * 45, r1, r2);
+      const float2 v = Model::aentry_df64(s_scr + q * SCR2, r1 / 3, r1 % 3, r2 / 3, r2 % 3);
+      float2* Aq = s_A + q * 81;
+      Aq[r1 * 9 + r2] = v;
+      Aq[r2 * 9 + r1] = v;
+    }
+  }
+  __syncthreads();
+
+  const int pp = tx / 3, i = tx % 3;
+  const int a1 = pp, a2 = 7 - pp;
+  const int split = 8 - pp;
+  const float2 z = make_float2(0.f, 0.f);
+  float2 K[27];
+#pragma unroll
+  for (int c = 0; c < 27; ++c) K[c] = z;
+  float2 R1 = z, R2 = z;
+  if (live) {
+    for (int q = 0; q < NQ; ++q) {
+      const float2* dNX = s_dNX + q * 24;
+      const float2 g10 = dNX[a1 * 3], g11 = dNX[a1 * 3 + 1], g12 = dNX[a1 * 3 + 2];
+      const float2 g20 = dNX[a2 * 3], g21 = dNX[a2 * 3 + 1], g22 = dNX[a2 * 3 + 2];
+      if (WANT_R) {
+        const float2* P = s_P + q * 9 + i * 3;
+        R1 = df64_fma(g10, P[0], df64_fma(g11, P[1], df64_fma(g12, P[2], R1)));
+        R2 = df64_fma(g20, P[0], df64_fma(g21, P[1], df64_fma(g22, P[2], R2)));
+      }
+      if (WANT_K) {
+        const float2* Ai = s_A + q * 81 + i * 27;
+        float2 t1[9], t2[9];
+#pragma unroll
+        for (int kl = 0; kl < 9; ++kl) {
+          const float2 x0 = Ai[kl], x1 = Ai[9 + kl], x2 = Ai[18 + kl];
+          t1[kl] = df64_fma(g10, x0, df64_fma(g11, x1, df64_mul(g12, x2)));
+          t2[kl] = df64_fma(g20, x0, df64_fma(g21, x1, df64_mul(g22, x2)));
+        }
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+          const bool first = j < split;
+          const int b = first ? pp + j : j - 1;
+          const float2 h0 = dNX[b * 3], h1 = dNX[b * 3 + 1], h2 = dNX[b * 3 + 2];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const float2 u0 = first ? t1[k * 3] : t2[k * 3];
+            const float2 u1 = first ? t1[k * 3 + 1] : t2[k * 3 + 1];
+            const float2 u2 = first ? t1[k * 3 + 2] : t2[k * 3 + 2];
+            K[j * 3 + k] = df64_fma(u0, h0, df64_fma(u1, h1, df64_fma(u2, h2, K[j * 3 + k])));
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();  // s_A is reused for the K staging below (as doubles)
+  if (WANT_K && live) {
+    double* Ks = reinterpret_cast<double*>(s_A);  // 576 entries, KE_NODE_ROWS layout
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+      const bool first = j < split;
+      const int an = first ? a1 : a2;
+      const int b = first ? pp + j : j - 1;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const double v = widen_exact(K[j * 3 + k].x) + widen_exact(K[j * 3 + k].y);
+        Ks[((an * 3 + i) * 3 + k) * 8 + b] = v;
+        if (b != an) Ks[((b * 3 + k) * 3 + i) * 8 + an] = v;
+      }
+    }
+  }
+  if (WANT_R && live) {
+    double* Re = static_cast<double*>(g.Re) + e * 24;
+    Re[a1 * 3 + i] = widen_exact(R1.x) + widen_exact(R1.y);
+    Re[a2 * 3 + i] = widen_exact(R2.x) + widen_exact(R2.y);
+  }
+  if (WANT_K) {
+    __syncthreads();
+    constexpr int PER = 576 / 2;
+    const int64_t left = g.ne - e0;
+    const int nlive = left < EPB ? int(left) : EPB;
+    double2* dst = reinterpret_cast<double2*>(static_cast<double*>(g.Ke) + e0 * 576);
+    const double* src = reinterpret_cast<const double*>(fb + S::F_A);
+    for (int idx = tid; idx < nlive * PER; idx += nthr) {
+      const int el = idx / PER, off = idx - el * PER;
+      dst[idx] = *reinterpret_cast<const double2*>(src + el * S::A_STRIDE + off * 2);
+    }
+  }
+}
+
+}  // namespace fec
