@@ -393,14 +393,16 @@ int fec_pattern_build(fec_ctx* c, int64_t* nnz_out) {
   for (const Block& B : c->blocks)
     for (int64_t i = 0; i < B.ne * B.nnpe; ++i) nadj_ptr[c->conn[B.conn_off + i] + 1]++;
   for (int64_t n = 0; n < nn; ++n) nadj_ptr[n + 1] += nadj_ptr[n];
-  std::vector<int64_t> nadj(nadj_ptr[nn]);
+  if (c->ne_total >= (int64_t(1) << 27))
+    return fail(c, FEC_ERR_UNSUPPORTED, "more than 2^27 elements (%lld)", (long long)c->ne_total);
+  std::vector<uint32_t> nadj(nadj_ptr[nn]);
   {
     std::vector<int64_t> fill(nadj_ptr.begin(), nadj_ptr.end() - 1);
     for (const Block& B : c->blocks)
       for (int64_t e = 0; e < B.ne; ++e)
         for (int a = 0; a < B.nnpe; ++a) {
           const int32_t n = c->conn[B.conn_off + e * B.nnpe + a];
-          nadj[fill[n]++] = ((B.elem_start + e) << 5) | a;
+          nadj[fill[n]++] = uint32_t(((B.elem_start + e) << 5) | a);
         }
   }
   auto elem_nodes = [&](int64_t ge, int* nnpe) -> const int32_t* {
@@ -504,7 +506,7 @@ int fec_pattern_build(fec_ctx* c, int64_t* nnz_out) {
                 int(200 * 1024 / sizeof(double)));
   int rc;
   if ((rc = upload(c, c->d_nadj_ptr, nadj_ptr.data(), sizeof(int64_t) * nadj_ptr.size()))) return rc;
-  if ((rc = upload(c, c->d_nadj, nadj.data(), sizeof(int64_t) * nadj.size()))) return rc;
+  if ((rc = upload(c, c->d_nadj, nadj.data(), sizeof(uint32_t) * nadj.size()))) return rc;
   if ((rc = upload(c, c->d_epos, epos.data(), sizeof(uint16_t) * epos.size()))) return rc;
   if ((rc = upload(c, c->d_col_base, col_base.data(), sizeof(int64_t) * col_base.size()))) return rc;
   if ((rc = upload(c, c->d_col_len, col_len.data(), sizeof(int32_t) * col_len.size()))) return rc;
@@ -672,7 +674,7 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
   ga.nf = c->nf;
   ga.nblocks = int(c->blocks.size());
   ga.nadj_ptr = static_cast<const int64_t*>(c->d_nadj_ptr.p);
-  ga.nadj = static_cast<const int64_t*>(c->d_nadj.p);
+  ga.nadj = static_cast<const uint32_t*>(c->d_nadj.p);
   ga.conn = static_cast<const int32_t*>(c->d_conn.p);
   ga.epos = static_cast<const uint16_t*>(c->d_epos.p);
   ga.umask = static_cast<const uint8_t*>(c->d_umask.p);
@@ -915,7 +917,7 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
   ga.nf = c->nf;
   ga.nblocks = int(c->blocks.size());
   ga.nadj_ptr = static_cast<const int64_t*>(c->d_nadj_ptr.p);
-  ga.nadj = static_cast<const int64_t*>(c->d_nadj.p);
+  ga.nadj = static_cast<const uint32_t*>(c->d_nadj.p);
   ga.conn = static_cast<const int32_t*>(c->d_conn.p);
   ga.epos = static_cast<const uint16_t*>(c->d_epos.p);
   ga.umask = static_cast<const uint8_t*>(c->d_umask.p);

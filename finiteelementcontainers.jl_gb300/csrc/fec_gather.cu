@@ -31,7 +31,7 @@ int gather_variant() {
 
 template <typename Real, int NF, int A, int MINB, int BUDGET>
 cudaError_t go1(const GatherArgs& g, cudaStream_t s, int* launches) {
-  const size_t smem = sizeof(float) * GatherAcc<Real>::WORDS * size_t(WPB) * size_t(g.acc_stride);
+  const size_t smem = sizeof(float) * GatherAcc::WORDS * size_t(WPB) * size_t(g.acc_stride);
   auto kern = node_gather_kernel<Real, NF, A, WPB, MINB, BUDGET>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (err != cudaSuccess) return err;
@@ -64,9 +64,9 @@ cudaError_t by_size(const GatherArgs& g, cudaStream_t s, int* launches) {
 }  // namespace
 
 cudaError_t launch_gather(int precision, int nf, const GatherArgs& g, cudaStream_t s, int* launches) {
-  if (precision == 0) {
-    if (nf == 1) return by_size<double, 1>(g, s, launches);
-    if (nf == 3) return by_size<double, 3>(g, s, launches);
+  if (precision == 0) {  // FP64 kernels leave double-float workspace entries
+    if (nf == 1) return by_size<float2, 1>(g, s, launches);
+    if (nf == 3) return by_size<float2, 3>(g, s, launches);
   } else if (precision == 1) {
     if (nf == 1) return by_size<float, 1>(g, s, launches);
     if (nf == 3) return by_size<float, 3>(g, s, launches);

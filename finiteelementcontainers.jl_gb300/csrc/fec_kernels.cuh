@@ -67,6 +67,24 @@ struct ElemArgs {
 };
 
 // ---------------------------------------------------------------------------
+// Element workspace entries.  FP32-element kernels store floats.  FP64 kernels
+// store double-float pairs (hi, lo), 8 bytes like a double: the df64 kernel
+// produces them directly, the others split their FP64 results.  The node gather
+// then accumulates in compensated FP32 on the FP32 pipes and touches the FP64
+// pipe once per assembled entry (the GB300's FP64 pipe is 1/64 of its FP32
+// rate and occupies a whole warp-instruction slot however few lanes are active).
+// ---------------------------------------------------------------------------
+template <typename Real> struct WS;
+template <> struct WS<double> {
+  using T = float2;
+  __device__ static T from(double v) { return df64_split(v); }
+};
+template <> struct WS<float> {
+  using T = float;
+  __device__ static T from(float v) { return v; }
+};
+
+// ---------------------------------------------------------------------------
 // small helpers
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double det3(const double J[3][3]) {
@@ -230,11 +248,11 @@ __global__ void __launch_bounds__(EPB * Elem<ET>::NNPE) poisson_element_kernel(E
     }
   }
   if (WANT_K) {
-    Real* Ke = static_cast<Real*>(g.Ke) + (e * A + a) * A;
+    typename WS<Real>::T* Ke = static_cast<typename WS<Real>::T*>(g.Ke) + (e * A + a) * A;
 #pragma unroll
-    for (int b = 0; b < A; ++b) Ke[b] = Krow[b];
+    for (int b = 0; b < A; ++b) Ke[b] = WS<Real>::from(Krow[b]);
   }
-  if (WANT_R) static_cast<Real*>(g.Re)[e * A + a] = R;
+  if (WANT_R) static_cast<typename WS<Real>::T*>(g.Re)[e * A + a] = WS<Real>::from(R);
 }
 
 // ---------------------------------------------------------------------------
@@ -556,12 +574,12 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
     }
   }
   if (WANT_K) {
-    Real* Ke = static_cast<Real*>(g.Ke) + (e * NDOF + r) * NDOF + b0 * 3;
+    typename WS<Real>::T* Ke = static_cast<typename WS<Real>::T*>(g.Ke) + (e * NDOF + r) * NDOF + b0 * 3;
 #pragma unroll
     for (int c = 0; c < CW * 3; ++c)
-      if (b0 * 3 + c < NDOF) Ke[c] = Krow[c];
+      if (b0 * 3 + c < NDOF) Ke[c] = WS<Real>::from(Krow[c]);
   }
-  if (WANT_R && cs == 0) static_cast<Real*>(g.Re)[e * NDOF + r] = R;
+  if (WANT_R && cs == 0) static_cast<typename WS<Real>::T*>(g.Re)[e * NDOF + r] = WS<Real>::from(R);
 }
 
 template <int ET, class Model, typename Real, int EPB, bool WANT_K>
@@ -606,7 +624,7 @@ struct GatherArgs {
   int nblocks;
   BlockInfo blk[MAX_BLOCKS];
   const int64_t* nadj_ptr;     // [nn+1]
-  const int64_t* nadj;         // (global element << 5) | local node
+  const uint32_t* nadj;        // global element * 32 + local node (fewer than 2^27 elements)
   const int32_t* conn;         // all blocks, 0-based
   const uint16_t* epos;        // [elem][a][b] row offset of node conn[b] inside node conn[a]'s columns
   const uint8_t* umask;        // per node: bit f set when dof (node, f) is unknown
@@ -642,34 +660,28 @@ __device__ __forceinline__ double widen_exact(float f) {
   return __longlong_as_double(int64_t(bits));
 }
 
-// Accumulator of the node gather.  FP64 inputs are added in FP64.  FP32 inputs
-// (the FP32-element variant) are added in compensated FP32: (hi, lo) with the
-// rounding error of every addition recovered exactly by TwoSum (Knuth) into
-// lo, which keeps the sum to about 2^-48 relative -- FP64-class accumulation
-// carried by the FP32 pipes -- and only the final hi + lo is formed in FP64.
-template <typename Real> struct GatherAcc;
-template <> struct GatherAcc<double> {
+// Accumulator of the node gather: a compensated FP32 pair (hi, lo).  Adding a
+// float recovers its rounding error exactly with TwoSum (Knuth); adding a
+// double-float pair is a df64 addition.  Either keeps the sum to about 2^-48
+// relative -- FP64-class accumulation carried by the FP32 pipes -- and only the
+// final hi + lo is formed in FP64.
+struct GatherAcc {
   static constexpr int WORDS = 2;  // 4-byte words per entry
-  __device__ static void zero(float* base, int j) { reinterpret_cast<double*>(base)[j] = 0.0; }
-  __device__ static void add(float* base, int j, double v) { reinterpret_cast<double*>(base)[j] += v; }
-  __device__ static double value(const float* base, int j) { return reinterpret_cast<const double*>(base)[j]; }
-};
-template <> struct GatherAcc<float> {
-  static constexpr int WORDS = 2;
   __device__ static void zero(float* base, int j) { reinterpret_cast<float2*>(base)[j] = make_float2(0.f, 0.f); }
-  __device__ static void add(float* base, int j, float v) {
-    float2 a = reinterpret_cast<float2*>(base)[j];
-    const float s = a.x + v;
-    const float bp = s - a.x;
-    const float err = (a.x - (s - bp)) + (v - bp);
-    a.x = s;
-    a.y += err;
-    reinterpret_cast<float2*>(base)[j] = a;
+  __device__ static float2 plus(float2 a, float v) {
+    const float s = __fadd_rn(a.x, v);
+    const float bp = __fsub_rn(s, a.x);
+    const float err = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bp)), __fsub_rn(v, bp));
+    return make_float2(s, __fadd_rn(a.y, err));
   }
-  __device__ static double value(const float* base, int j) {
-    const float2 a = reinterpret_cast<const float2*>(base)[j];
-    return widen_exact(a.x) + widen_exact(a.y);
+  __device__ static float2 plus(float2 a, float2 v) { return df64_add(a, v); }
+  template <typename W>
+  __device__ static void add(float* base, int j, W v) {
+    float2* p = reinterpret_cast<float2*>(base) + j;
+    *p = plus(*p, v);
   }
+  __device__ static double value(float2 a) { return widen_exact(a.x) + widen_exact(a.y); }
+  __device__ static double value(const float* base, int j) { return value(reinterpret_cast<const float2*>(base)[j]); }
 };
 
 // Adds the contributions of adjacency entries [p, pend) -- all from one element
@@ -680,7 +692,7 @@ template <> struct GatherAcc<float> {
 // flight per lane instead of a dependent load chain per element.
 template <typename Real, int NF, int A, int BUDGET>
 __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo& B, int64_t p, int64_t pend, unsigned um,
-                                           bool fast, int Ln, float* acc, double& racc, int lane, bool wantK,
+                                           bool fast, int Ln, float* acc, float2& racc, int lane, bool wantK,
                                            bool wantR) {
   constexpr int NDOF = NF * A;
   constexpr int TOTAL = NF * NDOF;                         // values of one element's rows for this node
@@ -691,7 +703,7 @@ __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo&
   for (; p < pend; p += 32) {
     const int64_t left32 = pend - p;
     const int n32 = left32 < 32 ? int(left32) : 32;
-    const int64_t mine = lane < n32 ? g.nadj[p + lane] : 0;
+    const uint32_t mine = lane < n32 ? g.nadj[p + lane] : 0u;
     for (int c0 = 0; c0 < n32; c0 += CH) {
       const int nh = (n32 - c0) < CH ? (n32 - c0) : CH;
       Real v[CH][VPL];
@@ -699,17 +711,18 @@ __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo&
       Real rv[CH];
 #pragma unroll
       for (int c = 0; c < CH; ++c) {
-        const int64_t packed = __shfl_sync(0xffffffffu, mine, (c0 + c) & 31);
-        rv[c] = Real(0);
+        const uint32_t packed = __shfl_sync(0xffffffffu, mine, (c0 + c) & 31);
+        rv[c] = Real{};
 #pragma unroll
         for (int j = 0; j < VPL; ++j) pos[c][j] = -1;
         if (c < nh) {
-          const int64_t le = (packed >> 5) - B.elem_start;
-          const int a = int(packed & 31);
-          if (wantR) rv[c] = Re[le * NDOF + a * NF + lane];
+          const int le = int(packed >> 5) - int(B.elem_start);
+          const int a = int(packed & 31u);
+          const uint64_t row0 = uint64_t(uint32_t(le)) * NDOF + uint32_t(a * NF);  // first row of node a
+          if (wantR) rv[c] = Re[row0 + lane];
           if (wantK) {
-            const Real* Krows = Ke + (le * NDOF + int64_t(a) * NF) * NDOF;
-            const uint16_t* ep = g.epos + B.epos_off + (le * A + a) * A;
+            const Real* Krows = Ke + row0 * NDOF;
+            const uint16_t* ep = g.epos + B.epos_off + (uint64_t(uint32_t(le)) * A + a) * A;
 #pragma unroll
             for (int j = 0; j < VPL; ++j) {
               const int t = lane + 32 * j;
@@ -720,7 +733,7 @@ __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo&
                 if (fast) {
                   pos[c][j] = k * Ln + ep[b] + i;
                 } else if ((um >> k) & 1u) {
-                  const unsigned umm = g.umask[g.conn[B.conn_off + le * A + b]] & ~UMASK_FULL_NBR;
+                  const unsigned umm = g.umask[g.conn[B.conn_off + int64_t(le) * A + b]] & ~UMASK_FULL_NBR;
                   if ((umm >> i) & 1u)
                     pos[c][j] = __popc(um & ((1u << k) - 1u)) * Ln + ep[b] + __popc(umm & ((1u << i) - 1u));
                 }
@@ -732,11 +745,11 @@ __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo&
 #pragma unroll
       for (int c = 0; c < CH; ++c) {
         if (c < nh) {
-          racc += double(rv[c]);
+          racc = GatherAcc::plus(racc, rv[c]);
           if (wantK) {
 #pragma unroll
             for (int j = 0; j < VPL; ++j)
-              if (pos[c][j] >= 0) GatherAcc<Real>::add(acc, pos[c][j], v[c][j]);
+              if (pos[c][j] >= 0) GatherAcc::add(acc, pos[c][j], v[c][j]);
             __syncwarp();
           }
         }
@@ -749,17 +762,17 @@ __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo&
 // blocks have different element sizes).
 template <typename Real, int NF>
 __device__ __forceinline__ void gather_run_generic(const GatherArgs& g, const BlockInfo& B, int64_t p, int64_t pend,
-                                                   unsigned um, int Ln, float* acc, double& racc, int lane,
+                                                   unsigned um, int Ln, float* acc, float2& racc, int lane,
                                                    bool wantK, bool wantR) {
   const int A = B.nnpe, NDOF = B.ndof, TOTAL = NF * B.ndof;
   const bool node_rows = B.layout == KE_NODE_ROWS;
   const Real* Ke = static_cast<const Real*>(g.Ke) + B.ke_off;
   const Real* Re = static_cast<const Real*>(g.Re) + B.re_off;
   for (; p < pend; ++p) {
-    const int64_t packed = g.nadj[p];
-    const int64_t le = (packed >> 5) - B.elem_start;
-    const int a = int(packed & 31);
-    if (wantR) racc += double(Re[le * NDOF + a * NF + lane]);
+    const uint32_t packed = g.nadj[p];
+    const int64_t le = int64_t(packed >> 5) - B.elem_start;
+    const int a = int(packed & 31u);
+    if (wantR) racc = GatherAcc::plus(racc, Re[le * NDOF + a * NF + lane]);
     if (wantK) {
       const Real* Krows = Ke + (le * NDOF + int64_t(a) * NF) * NDOF;
       const uint16_t* ep = g.epos + B.epos_off + (le * A + a) * A;
@@ -770,13 +783,18 @@ __device__ __forceinline__ void gather_run_generic(const GatherArgs& g, const Bl
         const unsigned umm = g.umask[g.conn[B.conn_off + le * A + b]] & ~UMASK_FULL_NBR;
         if (!((umm >> i) & 1u)) continue;
         const int off = node_rows ? (k * NF + i) * A + b : t;
-        GatherAcc<Real>::add(acc, __popc(um & ((1u << k) - 1u)) * Ln + ep[b] + __popc(umm & ((1u << i) - 1u)),
+        GatherAcc::add(acc, __popc(um & ((1u << k) - 1u)) * Ln + ep[b] + __popc(umm & ((1u << i) - 1u)),
                              Krows[off]);
       }
       __syncwarp();
     }
   }
 }
+
+// four double-float workspace entries (one 32-byte vector)
+struct alignas(32) F2x4 {
+  float2 x, y, z, w;
+};
 
 // Vector hex8 in the KE_NODE_ROWS layout, for nodes whose whole neighbourhood
 // is unknown: lane l < 18 owns (row component k, column component i) = (l/2)
@@ -786,9 +804,9 @@ __device__ __forceinline__ void gather_run_generic(const GatherArgs& g, const Bl
 // value.
 template <typename Real>
 __device__ __forceinline__ void gather_run_hex8v(const GatherArgs& g, const BlockInfo& B, int64_t p, int64_t pend,
-                                                 int Ln, float* acc, double& racc, int lane, bool wantK, bool wantR) {
+                                                 int Ln, float* acc, float2& racc, int lane, bool wantK, bool wantR) {
   constexpr int CH = sizeof(Real) == 8 ? 4 : 6;
-  using V4 = typename std::conditional<sizeof(Real) == 4, float4, double4_32a>::type;
+  using V4 = typename std::conditional<sizeof(Real) == 4, float4, F2x4>::type;
   const Real* Ke = static_cast<const Real*>(g.Ke) + B.ke_off;
   const Real* Re = static_cast<const Real*>(g.Re) + B.re_off;
   const bool kl = lane < 18;
@@ -797,7 +815,7 @@ __device__ __forceinline__ void gather_run_hex8v(const GatherArgs& g, const Bloc
   for (; p < pend; p += 32) {
     const int64_t left32 = pend - p;
     const int n32 = left32 < 32 ? int(left32) : 32;
-    const int64_t mine = lane < n32 ? g.nadj[p + lane] : 0;
+    const uint32_t mine = lane < n32 ? g.nadj[p + lane] : 0u;
     for (int c0 = 0; c0 < n32; c0 += CH) {
       const int nh = (n32 - c0) < CH ? (n32 - c0) : CH;
       V4 v[CH];
@@ -805,28 +823,30 @@ __device__ __forceinline__ void gather_run_hex8v(const GatherArgs& g, const Bloc
       Real rv[CH];
 #pragma unroll
       for (int c = 0; c < CH; ++c) {
-        const int64_t packed = __shfl_sync(0xffffffffu, mine, (c0 + c) & 31);
-        rv[c] = Real(0);
+        const uint32_t packed = __shfl_sync(0xffffffffu, mine, (c0 + c) & 31);
+        rv[c] = Real{};
         if (c < nh) {
-          const int64_t le = (packed >> 5) - B.elem_start;
-          const int a = int(packed & 31);
-          if (wantR) rv[c] = Re[le * 24 + a * 3 + lane];
+          const uint32_t le = (packed >> 5) - uint32_t(B.elem_start);
+          const uint32_t a = packed & 31u;
+          // 32-bit offsets: element rows (le*576 < 2^32 for < 2^22 elements per block is not
+          // assumed; the 576-entry row block index is widened once)
+          if (wantR) rv[c] = Re[uint64_t(le * 24u + a * 3u) + lane];
           if (wantK && kl) {
-            v[c] = *reinterpret_cast<const V4*>(Ke + le * 576 + a * 72 + ki * 8 + bh * 4);
-            ep[c] = *reinterpret_cast<const uint2*>(g.epos + B.epos_off + (le * 8 + a) * 8 + bh * 4);
+            v[c] = *reinterpret_cast<const V4*>(Ke + uint64_t(le) * 576u + (a * 72u + ki * 8u + bh * 4u));
+            ep[c] = *reinterpret_cast<const uint2*>(g.epos + B.epos_off + uint64_t(le) * 64u + (a * 8u + bh * 4u));
           }
         }
       }
 #pragma unroll
       for (int c = 0; c < CH; ++c) {
         if (c < nh) {
-          racc += double(rv[c]);
+          racc = GatherAcc::plus(racc, rv[c]);
           if (wantK) {
             if (kl) {
-              GatherAcc<Real>::add(acc, base + int(ep[c].x & 0xffffu), v[c].x);
-              GatherAcc<Real>::add(acc, base + int(ep[c].x >> 16), v[c].y);
-              GatherAcc<Real>::add(acc, base + int(ep[c].y & 0xffffu), v[c].z);
-              GatherAcc<Real>::add(acc, base + int(ep[c].y >> 16), v[c].w);
+              GatherAcc::add(acc, base + int(ep[c].x & 0xffffu), v[c].x);
+              GatherAcc::add(acc, base + int(ep[c].x >> 16), v[c].y);
+              GatherAcc::add(acc, base + int(ep[c].y & 0xffffu), v[c].z);
+              GatherAcc::add(acc, base + int(ep[c].y >> 16), v[c].w);
             }
             __syncwarp();
           }
@@ -849,18 +869,18 @@ __global__ void __launch_bounds__(WPB * 32, MINB) node_gather_kernel(GatherArgs 
   if (um == 0) return;
   const int Ln = g.col_len[n];
   const int ncols = __popc(um);
-  float* acc = s_acc + warp * g.acc_stride * GatherAcc<Real>::WORDS;
+  float* acc = s_acc + warp * g.acc_stride * GatherAcc::WORDS;
   const bool wantK = g.nzval != nullptr;
   const bool wantR = g.R_u != nullptr && lane < NF && ((um >> lane) & 1u);
   if (wantK)
-    for (int j = lane; j < ncols * Ln; j += 32) GatherAcc<Real>::zero(acc, j);
-  double racc = 0.0;
+    for (int j = lane; j < ncols * Ln; j += 32) GatherAcc::zero(acc, j);
+  float2 racc = make_float2(0.f, 0.f);
   __syncwarp();
   int64_t p = g.nadj_ptr[n];
   const int64_t p1 = g.nadj_ptr[n + 1];
   while (p < p1) {
     // the run of entries from one element block
-    const int64_t ge = g.nadj[p] >> 5;
+    const int64_t ge = int64_t(g.nadj[p] >> 5);
     int bi = 0;
     while (bi + 1 < g.nblocks && ge >= g.blk[bi + 1].elem_start) ++bi;
     const BlockInfo& B = g.blk[bi];
@@ -868,7 +888,7 @@ __global__ void __launch_bounds__(WPB * 32, MINB) node_gather_kernel(GatherArgs 
     if (bi + 1 < g.nblocks) {
       const int64_t bend = g.blk[bi + 1].elem_start;
       q = p + 1;
-      while (q < p1 && (g.nadj[q] >> 5) < bend) ++q;
+      while (q < p1 && int64_t(g.nadj[q] >> 5) < bend) ++q;
     }
     if constexpr (A == 8 && NF == 3) {
       if (fast && B.layout == KE_NODE_ROWS)
@@ -884,9 +904,9 @@ __global__ void __launch_bounds__(WPB * 32, MINB) node_gather_kernel(GatherArgs 
   }
   if (wantK) {
     double* out = g.nzval + g.col_base[n];
-    for (int j = lane; j < ncols * Ln; j += 32) out[j] = GatherAcc<Real>::value(acc, j);
+    for (int j = lane; j < ncols * Ln; j += 32) out[j] = GatherAcc::value(acc, j);
   }
-  if (wantR) g.R_u[g.dof_to_unknown[n * NF + lane]] = racc;
+  if (wantR) g.R_u[g.dof_to_unknown[n * NF + lane]] = GatherAcc::value(racc);
 }
 
 }  // namespace fec

@@ -230,7 +230,8 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_sym_kernel(ElemArgs g) {
   }
   __syncthreads();  // s_A is reused for the K staging below
   if (WANT_K && live) {
-    Real* Ks = s_A;  // 576 entries, KE_NODE_ROWS layout ((a*3 + k)*3 + i)*8 + b
+    using W = typename WS<Real>::T;
+    W* Ks = reinterpret_cast<W*>(s_A);  // 576 entries, KE_NODE_ROWS layout ((a*3 + k)*3 + i)*8 + b
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
       const bool first = j < split;
@@ -238,15 +239,16 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_sym_kernel(ElemArgs g) {
       const int b = first ? pp + j : j - 1;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        Ks[((an * 3 + i) * 3 + k) * 8 + b] = K[j * 3 + k];
-        if (b != an) Ks[((b * 3 + k) * 3 + i) * 8 + an] = K[j * 3 + k];
+        const W w = WS<Real>::from(K[j * 3 + k]);
+        Ks[((an * 3 + i) * 3 + k) * 8 + b] = w;
+        if (b != an) Ks[((b * 3 + k) * 3 + i) * 8 + an] = w;
       }
     }
   }
   if (WANT_R && live) {
-    Real* Re = static_cast<Real*>(g.Re) + e * 24;
-    Re[a1 * 3 + i] = R1;
-    Re[a2 * 3 + i] = R2;
+    typename WS<Real>::T* Re = static_cast<typename WS<Real>::T*>(g.Re) + e * 24;
+    Re[a1 * 3 + i] = WS<Real>::from(R1);
+    Re[a2 * 3 + i] = WS<Real>::from(R2);
   }
   if (WANT_K) {
     __syncthreads();
@@ -431,7 +433,7 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_rows2_kernel(ElemArgs g) {
 // constitutive update stay in FP64; the shape-function gradients, the stress and
 // the tangent scratch are split into double-float (hi + lo) once per point, the
 // tangent entries and the whole K_e / R_e contraction run in df64, and the
-// results are widened back to FP64 for the workspace.  Same thread mapping and
+// double-float results go to the workspace as they are.  Same thread mapping and
 // symmetry as mech_hex8_sym_kernel.
 // ---------------------------------------------------------------------------
 template <class Model, int EPB>
@@ -567,7 +569,7 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
   }
   __syncthreads();  // s_A is reused for the K staging below (as doubles)
   if (WANT_K && live) {
-    double* Ks = reinterpret_cast<double*>(s_A);  // 576 entries, KE_NODE_ROWS layout
+    float2* Ks = s_A;  // 576 double-float entries, KE_NODE_ROWS layout
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
       const bool first = j < split;
@@ -575,16 +577,15 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
       const int b = first ? pp + j : j - 1;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        const double v = widen_exact(K[j * 3 + k].x) + widen_exact(K[j * 3 + k].y);
-        Ks[((an * 3 + i) * 3 + k) * 8 + b] = v;
-        if (b != an) Ks[((b * 3 + k) * 3 + i) * 8 + an] = v;
+        Ks[((an * 3 + i) * 3 + k) * 8 + b] = K[j * 3 + k];
+        if (b != an) Ks[((b * 3 + k) * 3 + i) * 8 + an] = K[j * 3 + k];
       }
     }
   }
   if (WANT_R && live) {
-    double* Re = static_cast<double*>(g.Re) + e * 24;
-    Re[a1 * 3 + i] = widen_exact(R1.x) + widen_exact(R1.y);
-    Re[a2 * 3 + i] = widen_exact(R2.x) + widen_exact(R2.y);
+    float2* Re = static_cast<float2*>(g.Re) + e * 24;
+    Re[a1 * 3 + i] = R1;
+    Re[a2 * 3 + i] = R2;
   }
   if (WANT_K) {
     __syncthreads();
