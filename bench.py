@@ -42,19 +42,23 @@ UNIT = "Melem/s"
 # compulsory HBM bytes per element of one R+K pass (int32 connectivity, X and U
 # gathers, residual and nzval written once), see the design doc
 WORKLOADS = {
-    "neohookean": dict(n=128, kind="vector", name="neohookean_hex8_128cubed", flop_per_elem=48e3),
-    "poisson": dict(n=32, kind="scalar", name="poisson_hex8_32cubed", flop_per_elem=8e3),
+    "neohookean": dict(n=128, kind="vector", name="neohookean_hex8_128cubed", flop_per_elem=48e3, state=0),
+    "poisson": dict(n=32, kind="scalar", name="poisson_hex8_32cubed", flop_per_elem=8e3, state=0),
+    # J2 plasticity: 8 points x 7 state values read (old) and written (new) per element
+    "j2": dict(n=96, kind="vector", name="j2_hex8_96cubed", flop_per_elem=48e3, state=2 * 8 * 7 * 8),
 }
-CPU_SAMPLE_N = {"neohookean": 40, "poisson": 32}
+CPU_SAMPLE_N = {"neohookean": 40, "poisson": 32, "j2": 40}
+J2_STEPS = 20
 
 
-def algorithmic_bytes(ne: int, nn: int, nf: int, n_unknowns: int, nnz: int, nnpe: int = 8) -> int:
-    return 4 * nnpe * ne + 8 * 3 * nn + 8 * nf * nn + 8 * n_unknowns + 8 * nnz
+def algorithmic_bytes(ne: int, nn: int, nf: int, n_unknowns: int, nnz: int, nnpe: int = 8,
+                      state_per_elem: int = 0) -> int:
+    return 4 * nnpe * ne + 8 * 3 * nn + 8 * nf * nn + 8 * n_unknowns + 8 * nnz + state_per_elem * ne
 
 
 def build_workload(fec, wl: str, n: int, device: int, precision: str):
-    import torch
-    from fec_gb300.workloads import stretch_field
+    """Mesh, assembler, parameters and the per-step inputs [(Uu, Dirichlet values or None)]."""
+    from fec_gb300.workloads import stretch_field, uniaxial_path
     mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n + 1,) * 3)
     V = fec.FunctionSpace(mesh)
     if wl == "neohookean":
@@ -63,6 +67,22 @@ def build_workload(fec, wl: str, n: int, device: int, precision: str):
         phys = fec.NeoHookean.from_youngs(1.0, 0.3)
         p = fec.create_parameters(mesh, asm, phys)
         U = stretch_field(mesh.nodal_coords, seed=1).ravel()
+        inputs = [(np.ascontiguousarray(U[asm.dof.unknown_dofs - 1]), None)]
+    elif wl == "j2":
+        # symmetry on the x-, y-, z- faces, prescribed stretch on the x+ face; 20 load steps to 1% strain
+        var = fec.VectorFunction(V, "u")
+        asm = fec.SparseMatrixAssembler(var, device=device, precision=precision)
+        phys = fec.J2Plasticity(200.0, 0.3, 0.25, 2.0)
+        bcs = [fec.DirichletBC("u_x", lambda X, t: 0.0, nodeset_name="left"),
+               fec.DirichletBC("u_y", lambda X, t: 0.0, nodeset_name="bottom"),
+               fec.DirichletBC("u_z", lambda X, t: 0.0, nodeset_name="back"),
+               fec.DirichletBC("u_x", lambda X, t: 0.0, nodeset_name="right")]
+        p = fec.create_parameters(mesh, asm, phys, dirichlet_bcs=bcs)
+        bc_dofs = p.bc_dofs.cpu().numpy()
+        inputs = []
+        for s in range(1, J2_STEPS + 1):
+            U = uniaxial_path(mesh.nodal_coords, s, nsteps=J2_STEPS, final_strain=0.01).ravel()
+            inputs.append((np.ascontiguousarray(U[asm.dof.unknown_dofs - 1]), np.ascontiguousarray(U[bc_dofs - 1])))
     else:
         var = fec.ScalarFunction(V, "u")
         asm = fec.SparseMatrixAssembler(var, device=device, precision=precision)
@@ -70,9 +90,9 @@ def build_workload(fec, wl: str, n: int, device: int, precision: str):
                for f in ("bottom", "right", "front", "top", "left", "back")]
         p = fec.create_parameters(mesh, asm, fec.Poisson(1.0), dirichlet_bcs=bcs)
         U = np.random.default_rng(0).uniform(-1.0, 1.0, mesh.num_nodes)
-    Uu = np.ascontiguousarray(U[asm.dof.unknown_dofs - 1])
+        inputs = [(np.ascontiguousarray(U[asm.dof.unknown_dofs - 1]), None)]
     asm._ensure_pattern()
-    return mesh, asm, p, Uu
+    return mesh, asm, p, inputs
 
 
 class ClockSampler:
@@ -155,10 +175,18 @@ def cpu_reference_run(wl: str, n: int, threads: int) -> tuple[float, int, str]:
     from fec_gb300.workloads import stretch_field
     coords, conns = oracle.structured_hex8((n + 1,) * 3)
     nn = coords.shape[0]
+    st_old = st_new = None
     if wl == "neohookean":
         nf, phys, props = 3, "neohookean", [1.0 / (3 * 0.4), 1.0 / 2.6]
         U = stretch_field(coords, seed=1).ravel()
         dd = np.zeros(0, dtype=np.int64)
+    elif wl == "j2":
+        from fec_gb300.workloads import uniaxial_path
+        nf, phys, props = 3, "j2", [200.0, 0.3, 0.25, 2.0]
+        U = uniaxial_path(coords, J2_STEPS, nsteps=J2_STEPS, final_strain=0.01).ravel()
+        dd = np.zeros(0, dtype=np.int64)
+        st_old = np.zeros(7 * 8 * conns.shape[0])
+        st_new = np.zeros_like(st_old)
     else:
         nf, phys, props = 1, "poisson", [1.0]
         U = np.random.default_rng(0).uniform(-1, 1, nn)
@@ -167,7 +195,7 @@ def cpu_reference_run(wl: str, n: int, threads: int) -> tuple[float, int, str]:
     blocks = [("HEX8", conns)]
     Is, Js, slots = oracle.pattern(blocks, nf, dtu)
     t0 = time.perf_counter()
-    R, K = oracle.assemble(blocks, coords, phys, props, U, threads=threads)
+    R, K = oracle.assemble(blocks, coords, phys, props, U, st_old, st_new, threads=threads)
     Ru = R[unknown - 1]
     oracle.sparse_csc(unknown.size, unknown.size, Is, Js, K[slots - 1])
     dt = time.perf_counter() - t0
@@ -236,23 +264,34 @@ def run_ours(args) -> None:
     if args.n:
         wl["n"] = args.n
         wl["name"] = wl["name"].split("_")[0] + f"_hex8_{args.n}cubed"
-    mesh, asm, p, Uu_np = build_workload(fec, args.workload, wl["n"], local, args.precision)
+    mesh, asm, p, inputs = build_workload(fec, args.workload, wl["n"], local, args.precision)
     ne, nn, nf = mesh.num_elements(), mesh.num_nodes, asm.dof.nf
     n_u = int(asm.dof.unknown_dofs.size)
     stream = torch.cuda.current_stream()
-    Uu_d = torch.from_numpy(Uu_np).cuda()
+    dev_inputs = [(torch.from_numpy(u).cuda(), None if b is None else torch.from_numpy(b).cuda()) for u, b in inputs]
+    stateful = any(ph.NS for ph in p.physics)
+    counter = [0]
 
     def barrier():
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
 
-    def step(Uu):
-        return fec.assemble_residual_and_stiffness(asm, Uu, p)
+    def step(precision=None, feed=None):
+        """One load step: Dirichlet values and unknowns of step i, fused R+K, state swap."""
+        i = counter[0] % len(inputs)
+        counter[0] += 1
+        Uu, bc = (feed or dev_inputs)[i]
+        if bc is not None:
+            p.bc_vals = bc if bc.is_cuda else bc.to(asm._torch_device(), non_blocking=True)
+        R, K = fec.assemble_residual_and_stiffness(asm, Uu, p, precision=precision)
+        if stateful:
+            p.swap_states()
+        return R, K
 
     # ---- device-resident timing -------------------------------------------------
     for _ in range(args.warmup):
-        step(Uu_d)
+        step()
     asm.set_profiling(True)
     per_kernel: dict[str, list[float]] = {}
     launches = 0
@@ -262,7 +301,7 @@ def run_ours(args) -> None:
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
-            step(Uu_d)
+            step()
             for name, ms in asm.kernel_times():
                 per_kernel.setdefault(name, []).append(ms)
                 launches += 1
@@ -279,13 +318,14 @@ def run_ours(args) -> None:
 
     # ---- the other precision variant, same inputs --------------------------------
     variants = {}
-    R0, K0 = step(Uu_d)
+    R0, K0 = step()
     nnz = K0.nnz
     if not args.no_variants:
         other = "fp32_element" if args.precision == "fp64" else "fp64"
-        ref_R, ref_nz = R0.clone(), K0.nzval.clone()
+        if not stateful:  # compare the two variants on identical inputs
+            ref_R, ref_nz = R0.clone(), K0.nzval.clone()
         for _ in range(args.warmup):
-            fec.assemble_residual_and_stiffness(asm, Uu_d, p, precision=other)
+            step(other)
         asm.set_profiling(True)
         vk: dict[str, list[float]] = {}
         barrier()
@@ -293,7 +333,7 @@ def run_ours(args) -> None:
         g1 = torch.cuda.Event(enable_timing=True)
         g0.record(stream)
         for _ in range(args.steps):
-            Rv, Kv = fec.assemble_residual_and_stiffness(asm, Uu_d, p, precision=other)
+            Rv, Kv = step(other)
             for name, ms in asm.kernel_times():
                 vk.setdefault(name, []).append(ms)
         g1.record(stream)
@@ -302,21 +342,24 @@ def run_ours(args) -> None:
         tv = g0.elapsed_time(g1)
         variants[other] = {
             "value": world * ne * args.steps / (tv * 1e-3) / 1e6, "ms_per_step": tv / args.steps,
-            "kernels_ms": {k: sum(v) / len(v) for k, v in vk.items()},
-            "rel_err_vs_" + args.precision: {
+            "kernels_ms": {k: sum(v) / len(v) for k, v in vk.items()}}
+        if not stateful:
+            variants[other]["rel_err_vs_" + args.precision] = {
                 "nzval": float((Kv.nzval - ref_nz).norm() / ref_nz.norm()),
-                "residual": float((Rv - ref_R).norm() / ref_R.norm())}}
-        del ref_R, ref_nz
-        R0, K0 = step(Uu_d)
+                "residual": float((Rv - ref_R).norm() / ref_R.norm())}
+            del ref_R, ref_nz
+        R0, K0 = step()
     if args.no_e2e:
         return finish(args, fec, world, rank, local, wl, mesh, asm, ne, nn, nf, n_u, nnz, t_ms, value, clocks,
                       per_kernel, launches, None, variants)
-    Uu_h = torch.from_numpy(Uu_np).pin_memory()
+    host_inputs = [(torch.from_numpy(u).pin_memory(), None if b is None else torch.from_numpy(b).pin_memory())
+                   for u, b in inputs]
+    n_bc = 0 if inputs[0][1] is None else int(inputs[0][1].size)
     R_h = torch.empty(n_u, dtype=torch.float64).pin_memory()
     nz_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
 
     def e2e_step():
-        R, K = fec.assemble_residual_and_stiffness(asm, Uu_h, p)
+        R, K = step(feed=host_inputs)
         R_h.copy_(R, non_blocking=True)
         nz_h.copy_(K.nzval, non_blocking=True)
 
@@ -336,7 +379,8 @@ def run_ours(args) -> None:
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_e2e = float(tt.item())
     e2e_value = world * ne * args.steps / (t_e2e * 1e-3) / 1e6
-    e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n_u, "d2h_bytes_per_step": 8 * (n_u + nnz)}
+    e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * (n_u + n_bc),
+           "d2h_bytes_per_step": 8 * (n_u + nnz)}
     finish(args, fec, world, rank, local, wl, mesh, asm, ne, nn, nf, n_u, nnz, t_ms, value, clocks, per_kernel,
            launches, e2e, variants)
 
@@ -354,7 +398,7 @@ def finish(args, fec, world, rank, local, wl, mesh, asm, ne, nn, nf, n_u, nnz, t
     totals = {k: sum(v) for k, v in per_kernel.items()}
     dom = max(totals, key=totals.get)
     avg_ms = totals[dom] / len(per_kernel[dom])
-    alg_bytes = algorithmic_bytes(ne, nn, nf, n_u, nnz)
+    alg_bytes = algorithmic_bytes(ne, nn, nf, n_u, nnz, state_per_elem=wl["state"])
     achieved = alg_bytes / (avg_ms * 1e-3) / 1e9
     traffic = None
     prof = profiled_traffic(wl["name"] + "_" + args.precision)
@@ -394,6 +438,7 @@ def finish(args, fec, world, rank, local, wl, mesh, asm, ne, nn, nf, n_u, nnz, t
         "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32-element/f64-accumulate",
         "data": "synthetic",
         "config": {"workload": wl["name"], "elements": ne, "dofs": nf * nn, "nnz": nnz, "precision": args.precision,
+                   **({"load_path": f"{J2_STEPS} uniaxial steps to 1% strain, state carried"} if wl["state"] else {}),
                    "quadrature": "2x2x2 Gauss", "l2": "inputs larger than L2 (element scratch %.1f GB, nzval %.1f GB)"
                    % ((ne * (nf * 8) ** 2 * (8 if args.precision == "fp64" else 4)) / 1e9, nnz * 8 / 1e9),
                    "parallelism": f"{world} independent replicas" if world > 1 else "single GPU"},

@@ -8,3 +8,14 @@ def stretch_field(X: np.ndarray, seed: int, noise: float = 1e-3, diag=(1.05, 0.9
     """Displacement (diag(...) - I) X plus i.i.d. N(0, noise^2) nodal noise, shape of X."""
     rng = np.random.default_rng(seed)
     return ((np.diag(diag) - np.eye(3)) @ X.T).T + noise * rng.standard_normal(X.shape)
+
+
+def uniaxial_path(X: np.ndarray, step: int, nsteps: int = 20, final_strain: float = 0.01, nu: float = 0.3,
+                  noise: float = 1e-5, seed: int = 3) -> np.ndarray:
+    """Displacement of load step `step` (1-based) of a monotone uniaxial stretch to
+    `final_strain` in `nsteps` steps: (e x, -nu e y, -nu e z) with e = final_strain *
+    step / nsteps, plus i.i.d. N(0, noise^2) nodal noise drawn per step."""
+    e = final_strain * min(step, nsteps) / nsteps
+    rng = np.random.default_rng(seed * 1000 + step)
+    U = np.stack([e * X[:, 0], -nu * e * X[:, 1], -nu * e * X[:, 2]], axis=1)
+    return U + noise * rng.standard_normal(X.shape)

@@ -197,3 +197,33 @@ def test_j2_one_load_step_with_state(fec, orc):
     assert max(rel_err(nz, nzo)) <= TOL64
     assert max(rel_err(p.state_new.cpu().numpy(), sn)) <= TOL64
     assert sn[6::7].max() > 0  # some points yielded
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_element"])
+def test_j2_load_path_with_state(fec, orc, precision):
+    """J2 plasticity over a 6-step uniaxial load path: state carried step to step
+    (state_new of step s becomes state_old of step s+1), compared with the oracle
+    doing the same at every step."""
+    torch = _torch()
+    from fec_gb300.workloads import uniaxial_path
+    n = 6
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n, n, n))
+    phys = fec.J2Plasticity(200.0, 0.3, 0.25, 2.0)
+    asm, p = _setup(fec, mesh, "vector", phys)
+    so = np.zeros(p.state_old.numel())
+    tol = TOL64 if precision == "fp64" else TOL32
+    yielded = 0
+    for step in range(1, 7):
+        U = uniaxial_path(mesh.nodal_coords, step, nsteps=6, final_strain=0.01).ravel()
+        R, nz, _ = _run(fec, asm, p, U, precision=precision)
+        sn = np.zeros_like(so)
+        Ro, _, _, nzo = _oracle(orc, mesh, "j2", phys.create_properties(), U, asm, so, sn)
+        assert max(rel_err(R, Ro)) <= tol, (step, rel_err(R, Ro))
+        assert max(rel_err(nz, nzo)) <= tol, (step, rel_err(nz, nzo))
+        assert max(rel_err(p.state_new.cpu().numpy(), sn)) <= (1e-12 if precision == "fp64" else 1e-4)
+        yielded = max(yielded, int((sn[6::7] > 0).sum()))
+        p.swap_states()
+        so = sn
+        # the library reads state_old from the parameters; keep it equal to the oracle's
+        p.state_old.copy_(torch.from_numpy(so))
+    assert yielded > 0
