@@ -46,8 +46,12 @@ WORKLOADS = {
     "poisson": dict(n=32, kind="scalar", name="poisson_hex8_32cubed", flop_per_elem=8e3, state=0),
     # J2 plasticity: 8 points x 7 state values read (old) and written (new) per element
     "j2": dict(n=96, kind="vector", name="j2_hex8_96cubed", flop_per_elem=48e3, state=2 * 8 * 7 * 8),
+    # 64 uneven hex8 meshes (8^3..48^3, log-uniform, seed 2) in one block + a tet4/tet10/hex27 mesh,
+    # a 5-iteration Newton-type loop replayed as one CUDA graph per step
+    "batched": dict(n=0, kind="vector", name="batched_64_hex8_plus_tet4_tet10_hex27_newton5_graph",
+                    flop_per_elem=48e3, state=0),
 }
-CPU_SAMPLE_N = {"neohookean": 40, "poisson": 32, "j2": 40}
+CPU_SAMPLE_N = {"neohookean": 40, "poisson": 32, "j2": 40, "batched": 40}
 J2_STEPS = 20
 
 
@@ -176,7 +180,7 @@ def cpu_reference_run(wl: str, n: int, threads: int) -> tuple[float, int, str]:
     coords, conns = oracle.structured_hex8((n + 1,) * 3)
     nn = coords.shape[0]
     st_old = st_new = None
-    if wl == "neohookean":
+    if wl in ("neohookean", "batched"):
         nf, phys, props = 3, "neohookean", [1.0 / (3 * 0.4), 1.0 / 2.6]
         U = stretch_field(coords, seed=1).ravel()
         dd = np.zeros(0, dtype=np.int64)
@@ -243,6 +247,89 @@ def run_reference(args) -> None:
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} x {desc}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_batched(args) -> None:
+    """The batched workload: both systems assembled 5 times per step inside one CUDA graph."""
+    import torch
+    import __graft_entry__ as ge
+    fec = ge.load_package()
+    from fec_gb300 import batching
+    from fec_gb300.workloads import stretch_field
+    torch.cuda.set_device(0)
+    meshes = {"batch64": batching.box_batch(batching.lognormal_cube_sides()).mesh,
+              "tet4_tet10_hex27": batching.mixed_mesh(32, 32, 46)}
+    phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+    systems, info = [], {}
+    total_ne, alg = 0, 0
+    for name, mesh in meshes.items():
+        asm = fec.SparseMatrixAssembler(fec.VectorFunction(fec.FunctionSpace(mesh), "u"), device=0,
+                                        precision=args.precision)
+        p = fec.create_parameters(mesh, asm, phys)
+        U = stretch_field(mesh.nodal_coords, seed=2).ravel()
+        Uu = torch.from_numpy(U[asm.dof.unknown_dofs - 1].copy()).cuda()
+        asm._ensure_pattern()
+        systems.append((asm, p, Uu))
+        ne = mesh.num_elements()
+        nnpe = sum(mesh.element_conns[b].size for b in mesh.element_block_names) / ne
+        total_ne += ne
+        alg += algorithmic_bytes(ne, mesh.num_nodes, 3, int(asm.dof.unknown_dofs.size), asm.nnz, nnpe=nnpe)
+        info[name] = {"elements": ne, "blocks": {b: (mesh.element_types[b], int(mesh.element_conns[b].shape[0]))
+                                                 for b in mesh.element_block_names}, "nnz": asm.nnz}
+    iters = 5
+    loop = batching.NewtonLoop(systems, iterations=iters).capture()
+    # eager reference timing of the same loop and per-kernel times (CUDA events on the launching stream)
+    eager = batching.NewtonLoop(systems, iterations=iters)
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        eager.run_eager()
+        loop.replay()
+    torch.cuda.synchronize()
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0.record(stream)
+    for _ in range(args.steps):
+        eager.run_eager()
+    a1.record(stream)
+    torch.cuda.synchronize()
+    t_eager = a0.elapsed_time(a1)
+    per_kernel: dict[str, list[float]] = {}
+    for asm, p, Uu in systems:
+        asm.set_profiling(True)
+        fec.assemble_residual_and_stiffness(asm, Uu, p)
+        for k, ms in asm.kernel_times():
+            per_kernel.setdefault(k, []).append(ms)
+        asm.set_profiling(False)
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            loop.replay()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    t_ms = e0.elapsed_time(e1)
+    value = iters * total_ne * args.steps / (t_ms * 1e-3) / 1e6
+    kern_ms = {k: sum(v) for k, v in per_kernel.items()}
+    dom = max(kern_ms, key=kern_ms.get)
+    peaks = measured_peaks()
+    step_ms = sum(kern_ms.values())
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32-element/f64-accumulate", "data": "synthetic",
+        "config": {"workload": WORKLOADS["batched"]["name"], "elements": total_ne, "systems": info,
+                   "newton_iterations": iters, "execution": "one CUDA graph replay per step",
+                   "precision": args.precision, "l2": "inputs larger than L2"},
+        "eager_ms_per_step": t_eager / args.steps,
+        "roofline": {"bound": "hbm", "kernel": "all kernels of one R+K pass of both systems",
+                     "achieved": alg / (step_ms * 1e-3) / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": alg / (step_ms * 1e-3) / 1e9 / peaks["hbm_gbs"], "traffic": None,
+                     "kernels_ms_one_pass": kern_ms, "dominant": dom},
+        "clocks": clk.summary(), "e2e": None,
+        "gpu_launches": int(iters * sum(2 + len(a.fspace.block_names) for a, _, _ in systems) * args.steps),
+        "cpu_baseline": None,
     }
     print(json.dumps(line), flush=True)
 
@@ -470,6 +557,8 @@ def main() -> None:
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
     else:
         run_ours(args)
 

@@ -645,8 +645,14 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     ea.Re = want_r ? static_cast<char*>(c->d_Re.p) + rsz * size_t(re_off) : nullptr;
     cudaError_t e;
     {
-      LaunchTimer timer(c, s, B.physics == FEC_PHYS_POISSON ? "element_poisson"
-                              : B.physics == FEC_PHYS_NEOHOOKEAN ? "element_neohookean" : "element_j2");
+      static const char* kNames[4][9] = {
+          {"", "", "", "", "", "", "", "", ""},
+          {"", "element_poisson", "element_poisson_quad4", "", "", "", "element_poisson_tet4",
+           "element_poisson_tet10", "element_poisson_hex27"},
+          {"", "element_neohookean", "", "", "", "", "element_neohookean_tet4", "element_neohookean_tet10",
+           "element_neohookean_hex27"},
+          {"", "element_j2", "", "", "", "", "element_j2_tet4", "element_j2_tet10", "element_j2_hex27"}};
+      LaunchTimer timer(c, s, kNames[B.physics][B.elem_type]);
       if (B.physics == FEC_PHYS_POISSON)
         e = fec::launch_poisson(B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
       else

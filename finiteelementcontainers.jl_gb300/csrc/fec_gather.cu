@@ -33,7 +33,7 @@ template <typename Real, int NF, int A, int MINB, int BUDGET>
 cudaError_t go1(const GatherArgs& g, cudaStream_t s, int* launches) {
   const size_t smem = sizeof(float) * GatherAcc::WORDS * size_t(WPB) * size_t(g.acc_stride);
   auto kern = node_gather_kernel<Real, NF, A, WPB, MINB, BUDGET>;
-  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaError_t err = ensure_smem<node_gather_kernel<Real, NF, A, WPB, MINB, BUDGET>>(smem);
   if (err != cudaSuccess) return err;
   const unsigned grid = unsigned((g.nn + WPB - 1) / WPB);
   kern<<<grid, WPB * 32, smem, s>>>(g);

@@ -7,6 +7,21 @@
 
 namespace fec {
 
+// Raises a kernel's dynamic shared-memory limit once per device (and again only
+// when a larger size is asked for), so that launches recorded during CUDA graph
+// capture issue no attribute calls.  One instance per kernel.
+template <auto Kern>
+inline cudaError_t ensure_smem(size_t bytes) {
+  static int set_bytes[64] = {0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < 64 && int(bytes) <= set_bytes[dev]) return cudaSuccess;
+  e = cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+  if (e == cudaSuccess && dev >= 0 && dev < 64) set_bytes[dev] = int(bytes);
+  return e;
+}
+
 // Return cudaSuccess, or cudaErrorNotSupported for a combination that is not
 // built.  *launches is incremented by the kernels launched.
 cudaError_t launch_poisson(int elem_type, int precision, bool want_r, bool want_k, const ElemArgs& args,

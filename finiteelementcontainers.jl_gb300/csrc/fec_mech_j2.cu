@@ -12,7 +12,7 @@ cudaError_t go1(const ElemArgs& a, cudaStream_t s) {
   constexpr int TPE = 3 * Elem<ET>::NNPE * CSPLIT;
   constexpr size_t smem = mech_smem_bytes<ET, J2, Real, EPB, K>();
   auto kern = mech_element_kernel<ET, J2, Real, EPB, CSPLIT, R, K>;
-  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaError_t err = ensure_smem<mech_element_kernel<ET, J2, Real, EPB, CSPLIT, R, K>>(smem);
   if (err != cudaSuccess) return err;
   const dim3 block(TPE, EPB);
   const dim3 grid(unsigned((a.ne + EPB - 1) / EPB));
@@ -40,7 +40,7 @@ template <typename Real, int EPB, bool R, bool K>
 cudaError_t hex8_1(const ElemArgs& a, cudaStream_t s) {
   constexpr size_t smem = Hex8Smem<J2, Real, EPB>::BYTES;
   auto kern = mech_hex8_sym_kernel<J2, Real, EPB, R, K>;
-  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaError_t err = ensure_smem<mech_hex8_sym_kernel<J2, Real, EPB, R, K>>(smem);
   if (err != cudaSuccess) return err;
   const dim3 block(12, EPB);
   const dim3 grid(unsigned((a.ne + EPB - 1) / EPB));
@@ -52,7 +52,7 @@ template <int EPB, bool R, bool K>
 cudaError_t hex8_df64_1(const ElemArgs& a, cudaStream_t s) {
   constexpr size_t smem = Hex8Df64Smem<J2, EPB>::BYTES;
   auto kern = mech_hex8_df64_kernel<J2, EPB, R, K>;
-  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaError_t err = ensure_smem<mech_hex8_df64_kernel<J2, EPB, R, K>>(smem);
   if (err != cudaSuccess) return err;
   const dim3 block(12, EPB);
   const dim3 grid(unsigned((a.ne + EPB - 1) / EPB));
@@ -83,7 +83,7 @@ template <int EPB, bool R, bool K>
 cudaError_t hex8_f32_1(const ElemArgs& a, cudaStream_t s) {
   constexpr size_t smem = Hex8Smem<J2, float, EPB>::BYTES;
   auto kern = mech_hex8_rows2_kernel<J2, EPB, R, K>;
-  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaError_t err = ensure_smem<mech_hex8_rows2_kernel<J2, EPB, R, K>>(smem);
   if (err != cudaSuccess) return err;
   const dim3 block(12, EPB);
   const dim3 grid(unsigned((a.ne + EPB - 1) / EPB));

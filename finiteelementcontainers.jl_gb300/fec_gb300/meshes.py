@@ -218,8 +218,23 @@ def box_hex27(counts, mins=(0.0, 0.0, 0.0), maxs=(1.0, 1.0, 1.0)) -> Mesh:
     return Mesh(coords, ["block_1"], {"block_1": "HEX27"}, {"block_1": conn}, {}, {})
 
 
-def merge_meshes(meshes: list[Mesh], names: list[str] | None = None) -> Mesh:
-    """Disjoint union of meshes as one multi-block mesh (node ids renumbered)."""
+def merge_meshes(meshes: list[Mesh], names: list[str] | None = None, single_block: bool = False) -> Mesh:
+    """Disjoint union of meshes (node ids renumbered, mesh i's nodes and elements
+    after those of meshes 0..i-1).  One block per mesh, or, with single_block
+    and a common element type, one block holding every element -- so one kernel
+    launch covers the whole batch."""
+    if single_block:
+        types_ = {m.element_types[m.element_block_names[0]] for m in meshes}
+        if len(types_) != 1 or any(len(m.element_block_names) != 1 for m in meshes):
+            raise ValueError("single_block needs single-block meshes of one element type")
+        coords, conns, off = [], [], 0
+        for m in meshes:
+            b = m.element_block_names[0]
+            coords.append(m.nodal_coords)
+            conns.append(m.element_conns[b] + off)
+            off += m.nodal_coords.shape[0]
+        name = (names or ["block_1"])[0]
+        return Mesh(np.concatenate(coords), [name], {name: types_.pop()}, {name: np.concatenate(conns)}, {}, {})
     coords, types, conns, off = [], {}, {}, 0
     names = names or [f"block_{i + 1}" for i in range(len(meshes))]
     for name, m in zip(names, meshes):

@@ -1,0 +1,85 @@
+"""Batched uneven meshes in one launch, the mixed tet4/tet10/hex27 mesh, and the
+CUDA-graph Newton loop (GPU, against the oracle and against eager execution)."""
+import numpy as np
+import pytest
+
+from helpers import blocks_of, rel_err, stretch_field
+
+pytestmark = pytest.mark.gpu
+TOL64 = 1e-12
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _system(fec, mesh, precision="fp64"):
+    torch = _torch()
+    asm = fec.SparseMatrixAssembler(fec.VectorFunction(fec.FunctionSpace(mesh), "u"), device=0, precision=precision)
+    phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+    p = fec.create_parameters(mesh, asm, phys)
+    U = stretch_field(mesh.nodal_coords, seed=2).ravel()
+    Uu = torch.from_numpy(U[asm.dof.unknown_dofs - 1].copy()).cuda()
+    return asm, p, U, Uu, phys
+
+
+def test_batch_of_uneven_meshes_matches_per_mesh_oracle(fec, orc):
+    torch = _torch()
+    from fec_gb300 import batching
+    sides = [2, 5, 1, 3, 4]
+    batch = batching.box_batch(sides)
+    assert batch.mesh.element_block_names == ["block_1"]           # one block -> one launch per kernel
+    asm, p, U, Uu, phys = _system(fec, batch.mesh)
+    fec.assemble_residual_and_stiffness(asm, Uu, p)
+    torch.cuda.synchronize()
+    assert asm.last_launch_count() == 2                             # element kernel + gather for all meshes
+    for i, n in enumerate(sides):
+        m = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n + 1,) * 3)
+        n0, n1 = batch.node_offsets[i], batch.node_offsets[i + 1]
+        Ui = U.reshape(-1, 3)[n0:n1].ravel()
+        unknown, dtu = orc.update_dofs(3 * m.num_nodes, [])
+        Ro, colptr, rowval, nzo = orc.assembled_system(blocks_of(m), m.nodal_coords, "neohookean",
+                                                       phys.create_properties(), Ui, dtu, unknown)
+        Ri, Ki = batching.mesh_system(asm, batch, i)
+        assert np.array_equal(Ki.colptr, colptr) and np.array_equal(Ki.rowval, rowval)
+        assert max(rel_err(Ri.cpu().numpy(), Ro)) <= TOL64
+        assert max(rel_err(Ki.nzval.cpu().numpy(), nzo)) <= TOL64
+
+
+def test_mixed_tet4_tet10_hex27_mesh(fec, orc):
+    from fec_gb300 import batching
+    mesh = batching.mixed_mesh(2, 2, 2)
+    asm, p, U, Uu, phys = _system(fec, mesh)
+    R, K = fec.assemble_residual_and_stiffness(asm, Uu, p)
+    Ro, colptr, rowval, nzo = orc.assembled_system(blocks_of(mesh), mesh.nodal_coords, "neohookean",
+                                                   phys.create_properties(), U, asm.dof.dof_to_unknown,
+                                                   asm.dof.unknown_dofs)
+    assert np.array_equal(K.colptr, colptr) and np.array_equal(K.rowval, rowval)
+    assert max(rel_err(R.cpu().numpy(), Ro)) <= TOL64
+    assert max(rel_err(K.nzval.cpu().numpy(), nzo)) <= TOL64
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_element"])
+def test_newton_loop_graph_replays_eager_bits(fec, precision):
+    torch = _torch()
+    from fec_gb300 import batching
+    s1 = _system(fec, batching.box_batch([3, 6, 2]).mesh, precision)
+    s2 = _system(fec, batching.mixed_mesh(2, 1, 1), precision)
+    systems = [(s1[0], s1[1], s1[3]), (s2[0], s2[1], s2[3])]
+    eager = batching.NewtonLoop(systems, iterations=5)
+    eager.run_eager()
+    torch.cuda.synchronize()
+    graph = batching.NewtonLoop(systems, iterations=5).capture()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(eager.norms, graph.norms)
+    for s in range(2):
+        assert torch.equal(eager.unknowns(s), graph.unknowns(s))
+    assert bool(torch.isfinite(graph.norms).all())
+    # replaying again restarts from the captured inputs' current values: the loop advances
+    graph.replay()
+    torch.cuda.synchronize()
+    assert not torch.equal(eager.unknowns(0), graph.unknowns(0))

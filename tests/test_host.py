@@ -173,3 +173,19 @@ def test_product_fails_loudly_without_library(fec, tmp_path):
     from fec_gb300 import _lib
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         _lib.load(tmp_path / "missing.so")
+
+
+def test_batch_numbering(fec):
+    from fec_gb300 import batching
+    sides = batching.lognormal_cube_sides()
+    assert len(sides) == 64 and min(sides) >= 8 and max(sides) <= 48
+    batch = batching.box_batch([2, 3, 1])
+    m = batch.mesh
+    assert m.element_block_names == ["block_1"]
+    assert batch.node_offsets.tolist() == [0, 27, 91, 99]
+    assert batch.elem_offsets.tolist() == [0, 8, 35, 36]
+    conn = m.element_conns["block_1"]
+    # every element's nodes stay inside its own mesh's node range
+    for i in range(3):
+        c = conn[batch.elem_offsets[i]:batch.elem_offsets[i + 1]]
+        assert c.min() > batch.node_offsets[i] and c.max() <= batch.node_offsets[i + 1]
