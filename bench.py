@@ -46,13 +46,17 @@ WORKLOADS = {
     "poisson": dict(n=32, kind="scalar", name="poisson_hex8_32cubed", flop_per_elem=8e3, state=0),
     # J2 plasticity: 8 points x 7 state values read (old) and written (new) per element
     "j2": dict(n=96, kind="vector", name="j2_hex8_96cubed", flop_per_elem=48e3, state=2 * 8 * 7 * 8),
+    # J2 with the learned closure at plastic points, trained on 5M return-map samples (seed 4)
+    "j2mlp": dict(n=96, kind="vector", name="j2_mlp_closure_hex8_96cubed", flop_per_elem=48e3,
+                  state=2 * 8 * 7 * 8),
     # 64 uneven hex8 meshes (8^3..48^3, log-uniform, seed 2) in one block + a tet4/tet10/hex27 mesh,
     # a 5-iteration Newton-type loop replayed as one CUDA graph per step
     "batched": dict(n=0, kind="vector", name="batched_64_hex8_plus_tet4_tet10_hex27_newton5_graph",
                     flop_per_elem=48e3, state=0),
 }
-CPU_SAMPLE_N = {"neohookean": 40, "poisson": 32, "j2": 40, "batched": 40}
+CPU_SAMPLE_N = {"neohookean": 40, "poisson": 32, "j2": 40, "batched": 40, "j2mlp": 40}
 J2_STEPS = 20
+J2_PROPS = (200.0, 0.3, 0.25, 2.0)   # E, nu, yield stress, linear hardening
 
 
 def algorithmic_bytes(ne: int, nn: int, nf: int, n_unknowns: int, nnz: int, nnpe: int = 8,
@@ -60,9 +64,9 @@ def algorithmic_bytes(ne: int, nn: int, nf: int, n_unknowns: int, nnz: int, nnpe
     return 4 * nnpe * ne + 8 * 3 * nn + 8 * nf * nn + 8 * n_unknowns + 8 * nnz + state_per_elem * ne
 
 
-def build_workload(fec, wl: str, n: int, device: int, precision: str):
+def build_workload(fec, wl: str, n: int, device: int, precision: str, physics=None):
     """Mesh, assembler, parameters and the per-step inputs [(Uu, Dirichlet values or None)]."""
-    from fec_gb300.workloads import stretch_field, uniaxial_path
+    from fec_gb300.workloads import stretch_field, uniaxial_bcs, uniaxial_inputs
     mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n + 1,) * 3)
     V = fec.FunctionSpace(mesh)
     if wl == "neohookean":
@@ -76,17 +80,9 @@ def build_workload(fec, wl: str, n: int, device: int, precision: str):
         # symmetry on the x-, y-, z- faces, prescribed stretch on the x+ face; 20 load steps to 1% strain
         var = fec.VectorFunction(V, "u")
         asm = fec.SparseMatrixAssembler(var, device=device, precision=precision)
-        phys = fec.J2Plasticity(200.0, 0.3, 0.25, 2.0)
-        bcs = [fec.DirichletBC("u_x", lambda X, t: 0.0, nodeset_name="left"),
-               fec.DirichletBC("u_y", lambda X, t: 0.0, nodeset_name="bottom"),
-               fec.DirichletBC("u_z", lambda X, t: 0.0, nodeset_name="back"),
-               fec.DirichletBC("u_x", lambda X, t: 0.0, nodeset_name="right")]
-        p = fec.create_parameters(mesh, asm, phys, dirichlet_bcs=bcs)
-        bc_dofs = p.bc_dofs.cpu().numpy()
-        inputs = []
-        for s in range(1, J2_STEPS + 1):
-            U = uniaxial_path(mesh.nodal_coords, s, nsteps=J2_STEPS, final_strain=0.01).ravel()
-            inputs.append((np.ascontiguousarray(U[asm.dof.unknown_dofs - 1]), np.ascontiguousarray(U[bc_dofs - 1])))
+        phys = physics or fec.J2Plasticity(*J2_PROPS)
+        p = fec.create_parameters(mesh, asm, phys, dirichlet_bcs=uniaxial_bcs())
+        inputs = uniaxial_inputs(mesh.nodal_coords, asm.dof.unknown_dofs, p.bc_dofs.cpu().numpy(), J2_STEPS)
     else:
         var = fec.ScalarFunction(V, "u")
         asm = fec.SparseMatrixAssembler(var, device=device, precision=precision)
@@ -184,7 +180,7 @@ def cpu_reference_run(wl: str, n: int, threads: int) -> tuple[float, int, str]:
         nf, phys, props = 3, "neohookean", [1.0 / (3 * 0.4), 1.0 / 2.6]
         U = stretch_field(coords, seed=1).ravel()
         dd = np.zeros(0, dtype=np.int64)
-    elif wl == "j2":
+    elif wl in ("j2", "j2mlp"):
         from fec_gb300.workloads import uniaxial_path
         nf, phys, props = 3, "j2", [200.0, 0.3, 0.25, 2.0]
         U = uniaxial_path(coords, J2_STEPS, nsteps=J2_STEPS, final_strain=0.01).ravel()
@@ -247,6 +243,127 @@ def run_reference(args) -> None:
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} x {desc}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_closure(args) -> None:
+    """Learned closure vs exact return mapping on the 96^3 J2 load path (20 steps,
+    state carried), each path timed whole; errors per step against exact FP64."""
+    import torch
+    import __graft_entry__ as ge
+    fec = ge.load_package()
+    from fec_gb300 import closure
+    torch.cuda.set_device(0)
+    props = list(J2_PROPS)
+    t0 = time.perf_counter()
+    X, Y, plastic = closure.generate_samples(props, n_paths=250_000, steps=20, seed=4)
+    n_samples = int(X.shape[0])
+    X, Y = X[plastic], Y[plastic]
+    ntr = int(0.95 * X.shape[0])
+    trained = closure.train(X[:ntr], Y[:ntr], epochs=args.epochs, batch=4096, lr=5e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    val = closure.validation_errors(trained, props, X[ntr:], Y[ntr:])
+    n = WORKLOADS["j2mlp"]["n"] if not args.n else args.n
+    stream = torch.cuda.current_stream()
+
+    def system(physics, precision):
+        mesh, asm, p, inputs = build_workload(fec, "j2", n, 0, precision, physics=physics)
+        dev = [(torch.from_numpy(u).cuda(), torch.from_numpy(b).cuda()) for u, b in inputs]
+        return mesh, asm, p, dev
+
+    launches = [0]
+
+    def path(asm, p, dev, each=None):
+        p.state_old.zero_()
+        p.state_new.zero_()
+        for i, (Uu, bc) in enumerate(dev):
+            p.bc_vals = bc
+            R, K = fec.assemble_residual_and_stiffness(asm, Uu, p)
+            launches[0] += 2 + asm.last_launch_count()   # field update (Dirichlet + unknowns), elements, gather
+            if each is not None:
+                each(i, R, K, p)
+            p.swap_states()
+
+    def timed(asm, p, dev, stats=False):
+        for _ in range(args.warmup):
+            path(asm, p, dev)
+        torch.cuda.synchronize()
+        if stats:
+            closure.J2Closure.stats(asm, reset=True)
+        launches[0] = 0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            path(asm, p, dev)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        per_step_launches[0] = launches[0] / (args.steps * J2_STEPS)
+        return e0.elapsed_time(e1) / (args.steps * J2_STEPS)
+
+    per_step_launches = [0]
+    tols = (1e-4, 1e-3, 1e-2)
+    mesh, a64, p64, d64 = system(None, "fp64")
+    ne = mesh.num_elements()
+    _, a32, p32, d32 = system(None, "fp32_element")
+    cl = {}
+    for tol in tols:
+        phys = closure.J2Closure(*props, closure.TrainedClosure(trained.params, trained.normalisation, [], tol))
+        cl[tol] = system(phys, "fp32_element")[1:]
+    with ClockSampler(0) as clk:
+        t_cl = {}
+        for tol in tols:
+            a, p, d = cl[tol]
+            t_cl[tol] = timed(a, p, d, stats=True)
+            if tol == tols[0]:
+                main_launches = per_step_launches[0] * args.steps * J2_STEPS
+        t_x32 = timed(a32, p32, d32)
+        t_x64 = timed(a64, p64, d64)
+    # per-step errors against exact FP64 (the paths run in lockstep)
+    ref = []
+    path(a64, p64, d64, lambda i, R, K, p: ref.append((R.clone(), K.nzval.clone(), p.state_new.clone())))
+
+    def errors(asm, p, d):
+        worst = {"residual": 0.0, "nzval": 0.0, "state": 0.0}
+
+        def each(i, R, K, pp):
+            Rr, Kr, Sr = ref[i]
+            for k, a, b in (("residual", R, Rr), ("nzval", K.nzval, Kr), ("state", pp.state_new, Sr)):
+                worst[k] = max(worst[k], float((a - b).norm() / b.norm()) if float(b.norm()) > 0 else 0.0)
+        path(asm, p, d, each)
+        return worst
+
+    out = {}
+    for tol in tols:
+        a, p, d = cl[tol]
+        plast, fb = closure.J2Closure.stats(a, reset=True)   # over the timed repetitions
+        calls = args.steps * J2_STEPS
+        err = errors(a, p, d)
+        out[f"tol_{tol:g}"] = {
+            "ms_per_load_step": t_cl[tol], "Melem_per_s": ne / (t_cl[tol] * 1e-3) / 1e6,
+            "plastic_points_per_path": plast * J2_STEPS // calls, "fallback_rate": fb / max(plast, 1),
+            "max_rel_err_vs_exact_fp64_over_path": err}
+    x32_err = errors(a32, p32, d32)
+    main_t = t_cl[1e-4]
+    line = {
+        "metric": METRIC, "value": ne / (main_t * 1e-3) / 1e6, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps * J2_STEPS, "warmup": args.warmup * J2_STEPS, "ms_per_step": main_t,
+        "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-element (bf16 closure weights)", "data": "synthetic",
+        "config": {"workload": WORKLOADS["j2mlp"]["name"], "elements": ne,
+                   "step": f"one load step of the {J2_STEPS}-step uniaxial path (R+K, state carried); "
+                           f"the timed region runs the whole path {args.steps} times",
+                   "network": "14-64-64-64-64-13 SiLU, BF16 weights, FP32 accumulation",
+                   "training": {"samples_generated": n_samples, "plastic_samples_used": int(ntr),
+                                "epochs": args.epochs, "seconds": round(t_train, 1),
+                                "final_loss": trained.history[-1]},
+                   "l2": "inputs larger than L2"},
+        "closure": {"validation_rel_err": val, **out},
+        "exact": {"fp32_element_ms_per_load_step": t_x32, "fp64_ms_per_load_step": t_x64,
+                  "fp32_element_max_rel_err_vs_fp64": x32_err,
+                  "speedup_closure_vs_exact_fp64": t_x64 / main_t, "speedup_closure_vs_exact_fp32": t_x32 / main_t},
+        "clocks": clk.summary(), "e2e": None, "gpu_launches": int(main_launches), "cpu_baseline": None,
     }
     print(json.dumps(line), flush=True)
 
@@ -554,11 +671,14 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) measurement")
     ap.add_argument("--n", type=int, default=None, help="elements per box side (default: the workload's size)")
     ap.add_argument("--no-variants", action="store_true", help="skip timing the other precision variant")
+    ap.add_argument("--epochs", type=int, default=30, help="closure training epochs (j2mlp workload)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":
         run_batched(args)
+    elif args.workload == "j2mlp":
+        run_closure(args)
     else:
         run_ours(args)
 

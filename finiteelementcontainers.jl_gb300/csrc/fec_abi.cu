@@ -13,7 +13,9 @@
 #endif
 
 #include "../../include/fec_gb300.h"
+#include "fec_closure.cuh"
 #include "fec_launch.h"
+#include <cuda_bf16.h>
 
 using fec::BlockInfo;
 using fec::ElemArgs;
@@ -72,6 +74,9 @@ struct fec_ctx {
   DevBuf d_coords, d_conn, d_ref, d_nadj_ptr, d_nadj, d_epos, d_umask, d_col_base, d_col_len, d_dtu, d_unknown_dofs;
   DevBuf d_Ke, d_Re;
   std::vector<int64_t> ref_off;  // per block offset (doubles) into d_ref
+  // learned closure (FEC_PHYS_J2_MLP): BF16 parameters, normalisation, counters, and the
+  // ClosureArgs struct the kernels read
+  DevBuf d_cl_w, d_cl_norm, d_cl_cnt, d_cl_args;
   // optional per-launch timing (CUDA events on the caller's stream)
   bool profiling = false;
   std::vector<cudaEvent_t> events;  // 2 per timed launch
@@ -130,7 +135,7 @@ int ensure(fec_ctx* c, DevBuf& b, size_t bytes) {
 inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3); }
 
 int num_fields_of(int physics) { return physics == FEC_PHYS_POISSON ? 1 : 3; }
-int num_states_of(int physics) { return physics == FEC_PHYS_J2 ? 7 : 0; }
+int num_states_of(int physics) { return (physics == FEC_PHYS_J2 || physics == FEC_PHYS_J2_MLP) ? 7 : 0; }
 
 // U[bc_dofs[i]-1] = vals[i]
 __global__ void set_dirichlet_kernel(double* U, int64_t n, const int64_t* dofs, const double* vals) {
@@ -214,7 +219,8 @@ int fec_ctx_destroy(fec_ctx* c) {
   if (c->device >= 0) cudaSetDevice(c->device);
   for (cudaEvent_t e : c->events) cudaEventDestroy(e);
   for (DevBuf* b : {&c->d_coords, &c->d_conn, &c->d_ref, &c->d_nadj_ptr, &c->d_nadj, &c->d_epos, &c->d_umask,
-                    &c->d_col_base, &c->d_col_len, &c->d_dtu, &c->d_unknown_dofs, &c->d_Ke, &c->d_Re})
+                    &c->d_col_base, &c->d_col_len, &c->d_dtu, &c->d_unknown_dofs, &c->d_Ke, &c->d_Re, &c->d_cl_w,
+                    &c->d_cl_norm, &c->d_cl_cnt, &c->d_cl_args})
     b->release();
   delete c;
   return FEC_OK;
@@ -327,7 +333,8 @@ int fec_physics_set(fec_ctx* c, int block, int physics, const double* props, int
   if (!c) return FEC_ERR_ARG;
   if (block < 1 || block > int(c->blocks.size()))
     return fail(c, FEC_ERR_ARG, "block %d out of range 1..%d", block, int(c->blocks.size()));
-  if (physics != FEC_PHYS_POISSON && physics != FEC_PHYS_NEOHOOKEAN && physics != FEC_PHYS_J2)
+  if (physics != FEC_PHYS_POISSON && physics != FEC_PHYS_NEOHOOKEAN && physics != FEC_PHYS_J2 &&
+      physics != FEC_PHYS_J2_MLP)
     return fail(c, FEC_ERR_UNSUPPORTED, "unknown physics %d", physics);
   const int need = physics == FEC_PHYS_POISSON ? 1 : (physics == FEC_PHYS_NEOHOOKEAN ? 2 : 4);
   if (nprops < need || nprops > 8 || (nprops > 0 && !props))
@@ -643,15 +650,19 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     ea.state_new = (ns && state_new) ? state_new + st_off : nullptr;
     ea.Ke = want_k ? static_cast<char*>(c->d_Ke.p) + rsz * size_t(ke_off) : nullptr;
     ea.Re = want_r ? static_cast<char*>(c->d_Re.p) + rsz * size_t(re_off) : nullptr;
+    ea.closure = c->d_cl_args.p;
+    if (B.physics == FEC_PHYS_J2_MLP && !ea.closure)
+      return fail(c, FEC_ERR_STATE, "block %d uses the learned closure but fec_closure_set was not called", int(b) + 1);
     cudaError_t e;
     {
-      static const char* kNames[4][9] = {
+      static const char* kNames[5][9] = {
           {"", "", "", "", "", "", "", "", ""},
           {"", "element_poisson", "element_poisson_quad4", "", "", "", "element_poisson_tet4",
            "element_poisson_tet10", "element_poisson_hex27"},
           {"", "element_neohookean", "", "", "", "", "element_neohookean_tet4", "element_neohookean_tet10",
            "element_neohookean_hex27"},
-          {"", "element_j2", "", "", "", "", "element_j2_tet4", "element_j2_tet10", "element_j2_hex27"}};
+          {"", "element_j2", "", "", "", "", "element_j2_tet4", "element_j2_tet10", "element_j2_hex27"},
+          {"", "element_j2_mlp", "", "", "", "", "", "", ""}};
       LaunchTimer timer(c, s, kNames[B.physics][B.elem_type]);
       if (B.physics == FEC_PHYS_POISSON)
         e = fec::launch_poisson(B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
@@ -671,7 +682,9 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     bi.nnpe = B.nnpe;
     bi.ndof = ndof;
     // the hex8 mechanics kernels write the node-rows layout
-    bi.layout = (B.elem_type == FEC_HEX8 && c->nf == 3) ? fec::KE_NODE_ROWS : fec::KE_ROW_MAJOR;
+    bi.layout = (B.elem_type == FEC_HEX8 && (B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2))
+                    ? fec::KE_NODE_ROWS
+                    : fec::KE_ROW_MAJOR;
     ke_off += pad4(B.ne * ndof * ndof);
     re_off += B.ne * ndof;
     st_off += int64_t(ns) * B.nq * B.ne;
@@ -698,6 +711,44 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     e = fec::launch_gather(precision, c->nf, ga, s, &c->last_launches);
   }
   if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "gather launch: %s", cudaGetErrorString(e));
+  return ok(c);
+}
+
+int fec_closure_set(fec_ctx* c, const float* params, const float* norm, float tol) {
+  if (!c) return FEC_ERR_ARG;
+  if (!params || !norm || !(tol > 0.f)) return fail(c, FEC_ERR_ARG, "closure parameters, normalisation and tol > 0");
+  if (c->device < 0) return fail(c, FEC_ERR_STATE, "host-only context (device -1) cannot hold a closure");
+  cudaSetDevice(c->device);
+  std::vector<__nv_bfloat16> w(fec::MLP_PARAMS);
+  for (int i = 0; i < fec::MLP_PARAMS; ++i) w[i] = __float2bfloat16_rn(params[i]);
+  int rc;
+  if ((rc = upload(c, c->d_cl_w, w.data(), sizeof(__nv_bfloat16) * w.size()))) return rc;
+  const int nn = 2 * fec::MLP_IN + 2 * fec::MLP_OUT;
+  if ((rc = upload(c, c->d_cl_norm, norm, sizeof(float) * nn))) return rc;
+  const unsigned long long zero[2] = {0, 0};
+  if ((rc = upload(c, c->d_cl_cnt, zero, sizeof zero))) return rc;
+  fec::ClosureArgs a;
+  a.W = static_cast<const __nv_bfloat16*>(c->d_cl_w.p);
+  const float* nd = static_cast<const float*>(c->d_cl_norm.p);
+  a.in_mean = nd;
+  a.in_std = nd + fec::MLP_IN;
+  a.out_mean = nd + 2 * fec::MLP_IN;
+  a.out_std = nd + 2 * fec::MLP_IN + fec::MLP_OUT;
+  a.counters = static_cast<unsigned long long*>(c->d_cl_cnt.p);
+  a.tol = tol;
+  if ((rc = upload(c, c->d_cl_args, &a, sizeof a))) return rc;
+  return ok(c);
+}
+
+int fec_closure_stats(fec_ctx* c, int64_t* plastic, int64_t* fallbacks, int reset) {
+  if (!c) return FEC_ERR_ARG;
+  if (!c->d_cl_cnt.p) return fail(c, FEC_ERR_STATE, "no closure installed");
+  cudaSetDevice(c->device);
+  unsigned long long h[2];
+  FEC_CUDA(c, cudaMemcpy(h, c->d_cl_cnt.p, sizeof h, cudaMemcpyDeviceToHost));
+  if (plastic) *plastic = int64_t(h[0]);
+  if (fallbacks) *fallbacks = int64_t(h[1]);
+  if (reset) FEC_CUDA(c, cudaMemset(c->d_cl_cnt.p, 0, sizeof h));
   return ok(c);
 }
 
@@ -896,6 +947,9 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
     ea.state_new = (ns && state_new) ? state_new + st_off : nullptr;
     ea.Ke = want_k ? static_cast<char*>(Ke) + rsz * size_t(ke_off) : nullptr;
     ea.Re = want_r ? static_cast<char*>(Re) + rsz * size_t(re_off) : nullptr;
+    ea.closure = c->d_cl_args.p;
+    if (B.physics == FEC_PHYS_J2_MLP && !ea.closure)
+      return fail(c, FEC_ERR_STATE, "block %d uses the learned closure but fec_closure_set was not called", int(b) + 1);
     cudaError_t e;
     if (B.physics == FEC_PHYS_POISSON)
       e = fec::launch_poisson(B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
@@ -914,7 +968,9 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
     bi.nnpe = B.nnpe;
     bi.ndof = ndof;
     // the hex8 mechanics kernels write the node-rows layout
-    bi.layout = (B.elem_type == FEC_HEX8 && c->nf == 3) ? fec::KE_NODE_ROWS : fec::KE_ROW_MAJOR;
+    bi.layout = (B.elem_type == FEC_HEX8 && (B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2))
+                    ? fec::KE_NODE_ROWS
+                    : fec::KE_ROW_MAJOR;
     ke_off += pad4(B.ne * ndof * ndof);
     re_off += B.ne * ndof;
     st_off += int64_t(ns) * B.nq * B.ne;

@@ -8,11 +8,13 @@ namespace fec {
 
 cudaError_t launch_mech_neohookean(int, int, bool, bool, const ElemArgs&, cudaStream_t, int*);
 cudaError_t launch_mech_j2(int, int, bool, bool, const ElemArgs&, cudaStream_t, int*);
+cudaError_t launch_mech_j2mlp(int, int, bool, bool, const ElemArgs&, cudaStream_t, int*);
 
 cudaError_t launch_mech(int physics, int elem_type, int precision, bool want_r, bool want_k, const ElemArgs& a,
                         cudaStream_t s, int* launches) {
   if (physics == 2) return launch_mech_neohookean(elem_type, precision, want_r, want_k, a, s, launches);
   if (physics == 3) return launch_mech_j2(elem_type, precision, want_r, want_k, a, s, launches);
+  if (physics == 4) return launch_mech_j2mlp(elem_type, precision, want_r, want_k, a, s, launches);
   return cudaErrorNotSupported;
 }
 

@@ -64,6 +64,7 @@ struct ElemArgs {
   double* state_new;
   void* Ke;                 // block base, Real[ne][NDOF][NDOF]
   void* Re;                 // block base, Real[ne][NDOF]
+  const void* closure;      // learned-closure data (ClosureArgs) for the physics that uses one
 };
 
 // ---------------------------------------------------------------------------
@@ -267,6 +268,7 @@ __global__ void __launch_bounds__(EPB * Elem<ET>::NNPE) poisson_element_kernel(E
 //   A_iJkL = a1 H_iJ H_kL + a2 H_iL H_kJ + c2 d_ik d_JL - 2/3 c2 (H_kL F_iJ + F_kL H_iJ)
 //   a1 = K/2 (2J-1) J + 2/9 c2 I1,  a2 = I1/3 c2 - c1
 struct NeoHookean {
+  static constexpr bool USES_CLOSURE = false;
   static constexpr int NS = 0;
   static constexpr int SCR = 21;  // F(9) H(9) a1 a2 c2
   template <typename Real>
@@ -365,6 +367,7 @@ struct NeoHookean {
 // the consistent tangent (Simo & Hughes 1998, Box 3.2).  props = {E, nu, sy, H};
 // state (7) = plastic strain (xx, yy, zz, yz, xz, xy) + equivalent plastic strain.
 struct J2 {
+  static constexpr bool USES_CLOSURE = false;
   static constexpr int NS = 7;
   static constexpr int SCR = 13;  // n(9) kap' 2mu th' 2mu thb' (unused)
   template <typename Real>
@@ -528,7 +531,10 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
         }
       const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
       double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
-      Model::point(g.props, gu, Real(jxw), so, sn, s_P + q * 9, s_scr + q * SCR);
+      if constexpr (Model::USES_CLOSURE)
+        Model::point_closure(g.closure, g.props, gu, Real(jxw), so, sn, s_P + q * 9, s_scr + q * SCR);
+      else
+        Model::point(g.props, gu, Real(jxw), so, sn, s_P + q * 9, s_scr + q * SCR);
     }
   }
   __syncthreads();

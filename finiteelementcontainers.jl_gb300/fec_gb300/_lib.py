@@ -21,7 +21,7 @@ FEC_ERR_NONFINITE = -5
 FEC_ERR_DEVICE = -6
 
 FEC_HEX8, FEC_QUAD4, FEC_TET4, FEC_TET10, FEC_HEX27 = 1, 2, 6, 7, 8
-FEC_PHYS_POISSON, FEC_PHYS_NEOHOOKEAN, FEC_PHYS_J2 = 1, 2, 3
+FEC_PHYS_POISSON, FEC_PHYS_NEOHOOKEAN, FEC_PHYS_J2, FEC_PHYS_J2_MLP = 1, 2, 3, 4
 FEC_FP64, FEC_FP32_ELEMENT = 0, 1
 FEC_WANT_RESIDUAL, FEC_WANT_STIFFNESS = 1, 2
 
@@ -47,6 +47,14 @@ SIGNATURES = {
     "fec_last_launch_count": (C.c_int, [_vp]),
     "fec_sizes": (C.c_int, [_vp, _i64p, _i64p, _i64p, _i64p, _i64p]),
     "fec_set_profiling": (C.c_int, [_vp, C.c_int]),
+    "fec_mlp_param_count": (C.c_int, []),
+    "fec_j2_points": (C.c_int, [_vp, C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "fec_mlp_forward": (C.c_int, [_vp, _vp, C.c_int64, _vp, _vp]),
+    "fec_mlp_gradient": (C.c_int, [_vp, _vp, _vp, C.c_int64, _vp, C.c_int64, _vp, _vp, _vp]),
+    "fec_mlp_adam_step": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int64, C.c_int64, C.c_float, _vp, C.c_int64, _vp,
+                                    _vp]),
+    "fec_closure_set": (C.c_int, [_vp, _vp, _vp, C.c_float]),
+    "fec_closure_stats": (C.c_int, [_vp, _i64p, _i64p, C.c_int]),
     "fec_kernel_times": (C.c_int, [_vp, C.POINTER(C.c_float), C.c_int, C.c_char_p, C.c_size_t]),
     "fec_probe_fma_rate": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
 }

@@ -261,10 +261,12 @@ def _as_device_unknowns(asm, Uu):
 def _assemble(asm: SparseMatrixAssembler, want: int, Uu, p: Parameters, precision: str | None):
     torch = _torch()
     asm._ensure_pattern()
-    key = tuple((ph.ID, pr.tobytes()) for ph, pr in zip(p.physics, p.props))
+    key = tuple((ph.ID, pr.tobytes(), id(getattr(ph, "closure", None))) for ph, pr in zip(p.physics, p.props))
     if key != asm._physics_key:
         for b, (ph, pr) in enumerate(zip(p.physics, p.props), start=1):
             asm._call("fec_physics_set", b, ph.ID, _lib.ptr(pr), int(pr.size))
+            if hasattr(ph, "install"):   # physics that carry device data (the learned closure)
+                ph.install(asm)
         asm._physics_key = key
     n_u = int(asm.dof.unknown_dofs.size)
     Uu_d = _as_device_unknowns(asm, Uu)

@@ -56,7 +56,9 @@ enum { FEC_HEX8 = 1, FEC_QUAD4 = 2, FEC_TET4 = 6, FEC_TET10 = 7, FEC_HEX27 = 8 }
 enum {
   FEC_PHYS_POISSON = 1,    /* NF=1; props[0] = source amplitude a, f(X) = a prod_d sin(pi X_d) */
   FEC_PHYS_NEOHOOKEAN = 2, /* NF=3; props = {bulk K, shear G} */
-  FEC_PHYS_J2 = 3          /* NF=3, NS=7; props = {E, nu, sigma_y, H} */
+  FEC_PHYS_J2 = 3,         /* NF=3, NS=7; props = {E, nu, sigma_y, H} */
+  FEC_PHYS_J2_MLP = 4      /* J2 with the learned closure at plastic points (hex8, FEC_FP32_ELEMENT);
+                              props as FEC_PHYS_J2; needs fec_closure_set */
 };
 
 /* arithmetic of the element kernels */
@@ -162,6 +164,37 @@ int fec_assemble(fec_ctx* ctx, int want, int precision, double t, double dt, con
 int fec_assemble_noalloc(fec_ctx* ctx, int want, int precision, double t, double dt, const double* U_dev,
                          const double* U_old_dev, const double* state_old_dev, double* state_new_dev,
                          double* R_u_dev, double* nzval_dev, void* stream);
+
+/* Learned closure (no counterpart in the reference, whose physics are Julia
+ * functions; the J2 return map it replaces is the project's own).  ------------ */
+
+/* Number of MLP parameters (14-64-64-64-64-13, SiLU; per layer W [out][in]
+ * row-major then b). */
+int fec_mlp_param_count(void);
+/* Exact J2 radial return of n points (FP64, device arrays): strain (6 tensor
+ * components xx yy zz yz xz xy per point), state (7) -> stress (6), new state
+ * (7), and optionally the 6x6 consistent tangent d sigma / d eps.  props as
+ * FEC_PHYS_J2.  Used to generate training data and to judge the closure. */
+int fec_j2_points(const double* props, int64_t n, const double* strain_dev, const double* state_old_dev,
+                  double* stress_dev, double* state_new_dev, double* tangent_dev, void* stream);
+/* MLP forward pass on n normalised samples X (n x 14) -> Y (n x 13), FP32. */
+int fec_mlp_forward(const float* params_dev, const float* X_dev, int64_t n, float* Y_dev, void* stream);
+/* Gradient of the mean squared error against targets Y, summed in a fixed
+ * order; scratch needs ceil(n/64) * (params + 1) floats. */
+int fec_mlp_gradient(const float* params_dev, const float* X_dev, const float* Y_dev, int64_t n, float* scratch_dev,
+                     int64_t scratch_len, float* grad_dev, float* loss_dev, void* stream);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) on the batch (X, Y); step >= 1. */
+int fec_mlp_adam_step(float* params_dev, float* m_dev, float* v_dev, const float* X_dev, const float* Y_dev,
+                      int64_t n, int64_t step, float lr, float* scratch_dev, int64_t scratch_len, float* loss_dev,
+                      void* stream);
+/* Installs a trained closure for FEC_PHYS_J2_MLP blocks: FP32 parameters (host,
+ * stored on the device as BF16), the feature normalisation (host; 14 + 14 + 13
+ * + 13 floats: input mean, input std, output mean, output std) and the
+ * consistency threshold (relative to sigma_y) above which a point falls back
+ * to the exact update. */
+int fec_closure_set(fec_ctx* ctx, const float* params, const float* normalisation, float tol);
+/* Plastic points that used the closure path and fallbacks since the last reset. */
+int fec_closure_stats(fec_ctx* ctx, int64_t* plastic_points, int64_t* fallbacks, int reset);
 
 /* Number of kernels fec_assemble launched in the last call (for accounting). */
 int fec_last_launch_count(const fec_ctx* ctx);

@@ -1,0 +1,129 @@
+"""The learned J2 closure: the exact return-map batch against the oracle, the
+hand-written MLP kernels' forward pass and gradients against the numpy
+reference, and what training gains over the untrained network inside assembly."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+PROPS = [200.0, 0.3, 0.25, 2.0]
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def test_exact_points_match_oracle(fec, orc):
+    torch = _torch()
+    from fec_gb300 import closure
+    rng = np.random.default_rng(0)
+    n = 200
+    eps = rng.normal(0, 0.004, (n, 6))
+    st = np.concatenate([rng.normal(0, 5e-4, (n, 6)), rng.uniform(0, 2e-3, (n, 1))], 1)
+    sig, new, tan = closure.exact_points(PROPS, torch.from_numpy(eps).cuda(), torch.from_numpy(st).cuda(), True)
+    ii, jj = [0, 1, 2, 1, 0, 0], [0, 1, 2, 2, 2, 1]
+    for k in range(n):
+        gu = np.zeros((3, 3))
+        for m in range(6):
+            gu[ii[m], jj[m]] = gu[jj[m], ii[m]] = eps[k, m]
+        P, A, sn = orc.j2_update(gu, PROPS, st[k])
+        assert np.allclose(sig[k].cpu().numpy(), [P[ii[m] + 3 * jj[m]] for m in range(6)], rtol=0, atol=1e-13)
+        assert np.allclose(new[k].cpu().numpy(), sn, rtol=0, atol=1e-15)
+        C6 = np.array([[A[(ii[m] + 3 * jj[m]) + 9 * (ii[q] + 3 * jj[q])] * (2 if q >= 3 else 1) for q in range(6)]
+                       for m in range(6)])
+        assert np.allclose(tan[k].cpu().numpy(), C6, rtol=1e-13, atol=1e-10)
+
+
+def test_mlp_kernels_match_numpy_reference(fec):
+    torch = _torch()
+    from fec_gb300 import closure, _lib
+    from oracle import mlp_reference as ref
+    lib = fec.load_library()
+    rng = np.random.default_rng(1)
+    n = 300
+    X = rng.standard_normal((n, 14)).astype(np.float32)
+    Y = rng.standard_normal((n, 13)).astype(np.float32)
+    P = closure.init_params(3)
+    Pd, Xd, Yd = (torch.from_numpy(a).cuda() for a in (P, X, Y))
+    nb = (n + 63) // 64
+    scratch = torch.empty(nb * (P.size + 1), dtype=torch.float32, device="cuda")
+    grad = torch.empty(P.size, dtype=torch.float32, device="cuda")
+    loss = torch.empty(1, dtype=torch.float32, device="cuda")
+    Yo = torch.empty(n, 13, dtype=torch.float32, device="cuda")
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.fec_mlp_forward(_lib.ptr(Pd), _lib.ptr(Xd), n, _lib.ptr(Yo), s) == 0
+    assert lib.fec_mlp_gradient(_lib.ptr(Pd), _lib.ptr(Xd), _lib.ptr(Yd), n, _lib.ptr(scratch), scratch.numel(),
+                                _lib.ptr(grad), _lib.ptr(loss), s) == 0
+    torch.cuda.synchronize()
+    P64, X64, Y64 = P.astype(np.float64), X.astype(np.float64), Y.astype(np.float64)
+    assert rel_err(Yo.cpu().numpy(), ref.forward(P64, X64))[1] <= 1e-5
+    l_ref, g_ref = ref.loss_and_grad(P64, X64, Y64)
+    assert abs(float(loss) - l_ref) <= 1e-5 * l_ref
+    assert rel_err(grad.cpu().numpy(), g_ref)[1] <= 1e-4
+
+
+def _j2_path(fec, physics, n=6, nsteps=10):
+    """A 6^3 uniaxial J2 load path with state carried: per step (R, nzval), and the
+    closure statistics when the physics has a closure."""
+    torch = _torch()
+    from fec_gb300 import closure
+    from fec_gb300.workloads import uniaxial_bcs, uniaxial_inputs
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n + 1,) * 3)
+    asm = fec.SparseMatrixAssembler(fec.VectorFunction(fec.FunctionSpace(mesh), "u"), device=0,
+                                    precision="fp32_element")
+    p = fec.create_parameters(mesh, asm, physics, dirichlet_bcs=uniaxial_bcs())
+    steps = []
+    for Uu, bc in uniaxial_inputs(mesh.nodal_coords, asm.dof.unknown_dofs, p.bc_dofs.cpu().numpy(), nsteps,
+                                  final_strain=0.005):
+        p.bc_vals = torch.from_numpy(bc).cuda()
+        R, K = fec.assemble_residual_and_stiffness(asm, torch.from_numpy(Uu).cuda(), p)
+        steps.append((R.cpu().numpy().copy(), K.nzval.cpu().numpy().copy()))
+        p.swap_states()
+    torch.cuda.synchronize()
+    stats = closure.J2Closure.stats(asm) if isinstance(physics, closure.J2Closure) else None
+    return steps, stats
+
+
+def test_training_gains_over_untrained_network(fec):
+    torch = _torch()
+    from fec_gb300 import closure
+    X, Y, plastic = closure.generate_samples(PROPS, n_paths=40000, steps=10, seed=4)
+    X, Y = X[plastic], Y[plastic]
+    ntr = int(0.9 * X.shape[0])
+    trained = closure.train(X[:ntr], Y[:ntr], epochs=20, batch=2048, lr=5e-3)
+    untrained = closure.TrainedClosure(closure.init_params(0), trained.normalisation, [], 1e-4)
+    val = closure.validation_errors(trained, PROPS, X[ntr:], Y[ntr:])
+    val_un = closure.validation_errors(untrained, PROPS, X[ntr:], Y[ntr:])
+    print("validation, trained:", val, "untrained:", val_un, "losses", trained.history)
+    # the network predicts the deviatoric stress; training cuts its error by more than 10x
+    assert val["fp32_params"]["deviatoric_stress"] < 0.1 * val_un["fp32_params"]["deviatoric_stress"]
+    assert val["fp32_params"]["stress"] < 1e-2
+    # inside assembly, along a 10-step load path with state carried (the closure serves the
+    # plastic points; the exact return map judges it)
+    exact, _ = _j2_path(fec, fec.J2Plasticity(*PROPS))
+    runs = {}
+    for name, cl in (("untrained", untrained),
+                     ("trained_loose", closure.TrainedClosure(trained.params, trained.normalisation, [], 5e-2))):
+        runs[name] = _j2_path(fec, closure.J2Closure(*PROPS, cl))
+    for name, (steps, (plast, fb)) in runs.items():
+        errs = [(rel_err(R, Rx)[1], rel_err(K, Kx)[1]) for (R, K), (Rx, Kx) in zip(steps, exact)]
+        print(name, "plastic points", plast, "fallbacks", fb, "worst (R, K) error over the path",
+              tuple(max(e) for e in zip(*errs)))
+        runs[name] = (errs, plast, fb)
+    # the untrained network never passes the consistency check: every plastic point falls back,
+    # so the path equals the exact one
+    errs, plast, fb = runs["untrained"]
+    assert plast > 0 and fb == plast
+    assert max(e for pair in errs for e in pair) <= 1e-5
+    # the trained network serves most plastic points at the loose tolerance; residual and
+    # tangent stay within 5% of exact over the path (the residual of this near-equilibrium
+    # field is small against the element forces, so its relative error is the larger one)
+    errs, plast, fb = runs["trained_loose"]
+    assert plast > 0 and fb < 0.5 * plast
+    assert max(e[0] for e in errs) <= 5e-2 and max(e[1] for e in errs) <= 5e-2

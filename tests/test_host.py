@@ -189,3 +189,32 @@ def test_batch_numbering(fec):
     for i in range(3):
         c = conn[batch.elem_offsets[i]:batch.elem_offsets[i + 1]]
         assert c.min() > batch.node_offsets[i] and c.max() <= batch.node_offsets[i + 1]
+
+
+def test_closure_rows_of_exact_return_map_are_consistent(orc):
+    """The closure's training rows rebuilt from the oracle's return map: the exact
+    targets lie on the updated yield surface and give back the oracle's stress."""
+    import torch
+    from fec_gb300 import closure
+    props = [200.0, 0.3, 0.25, 2.0]
+    rng = np.random.default_rng(5)
+    n = 64
+    eps = rng.normal(0, 0.001, (n, 6)) * rng.uniform(0.2, 1.5, (n, 1))   # both sides of the yield surface
+    st = np.concatenate([rng.normal(0, 5e-5, (n, 6)), rng.uniform(0, 2e-4, (n, 1))], 1)
+    ii, jj = [0, 1, 2, 1, 0, 0], [0, 1, 2, 2, 2, 1]
+    sig, new = np.zeros((n, 6)), np.zeros((n, 7))
+    for k in range(n):
+        gu = np.zeros((3, 3))
+        for m in range(6):
+            gu[ii[m], jj[m]] = gu[jj[m], ii[m]] = eps[k, m]
+        P, _, sn = orc.j2_update(gu, props, st[k])
+        sig[k] = [P[ii[m] + 3 * jj[m]] for m in range(6)]
+        new[k] = sn
+    X, Y = closure.sample_rows(props, *(torch.from_numpy(a) for a in (eps, st, sig, new)))
+    plastic = X[:, 13] > 0
+    assert 0 < int(plastic.sum()) < n
+    res = closure.consistency_residual(props, X[plastic], Y[plastic])
+    assert float(res.max()) <= 1e-12
+    s = closure.deviatoric_stress(props, X, Y) + closure.pressure(props, X[:, :6]) * torch.tensor(
+        [1.0, 1, 1, 0, 0, 0], dtype=torch.float64)
+    assert np.allclose(s.numpy(), sig, rtol=0, atol=1e-14)
