@@ -257,7 +257,7 @@ def run_closure(args) -> None:
     torch.cuda.set_device(0)
     props = list(J2_PROPS)
     t0 = time.perf_counter()
-    X, Y, plastic = closure.generate_samples(props, n_paths=250_000, steps=20, seed=4)
+    X, Y, plastic = closure.generate_samples(props, n_paths=args.paths, steps=20, seed=4)
     n_samples = int(X.shape[0])
     X, Y = X[plastic], Y[plastic]
     ntr = int(0.95 * X.shape[0])
@@ -334,6 +334,18 @@ def run_closure(args) -> None:
         path(asm, p, d, each)
         return worst
 
+    def kernels(asm, p, d):
+        """Per-kernel milliseconds averaged over one path (CUDA events around each launch)."""
+        acc: dict[str, list[float]] = {}
+        asm.set_profiling(True)
+
+        def each(i, R, K, pp):
+            for name, ms in asm.kernel_times():
+                acc.setdefault(name, []).append(ms)
+        path(asm, p, d, each)
+        asm.set_profiling(False)
+        return {k: sum(v) / len(v) for k, v in acc.items()}
+
     out = {}
     for tol in tols:
         a, p, d = cl[tol]
@@ -343,8 +355,9 @@ def run_closure(args) -> None:
         out[f"tol_{tol:g}"] = {
             "ms_per_load_step": t_cl[tol], "Melem_per_s": ne / (t_cl[tol] * 1e-3) / 1e6,
             "plastic_points_per_path": plast * J2_STEPS // calls, "fallback_rate": fb / max(plast, 1),
-            "max_rel_err_vs_exact_fp64_over_path": err}
+            "max_rel_err_vs_exact_fp64_over_path": err, "kernels_ms": kernels(a, p, d)}
     x32_err = errors(a32, p32, d32)
+    x_kernels = {"fp32_element": kernels(a32, p32, d32), "fp64": kernels(a64, p64, d64)}
     main_t = t_cl[1e-4]
     line = {
         "metric": METRIC, "value": ne / (main_t * 1e-3) / 1e6, "unit": UNIT, "n_gpus": 1,
@@ -361,7 +374,7 @@ def run_closure(args) -> None:
                    "l2": "inputs larger than L2"},
         "closure": {"validation_rel_err": val, **out},
         "exact": {"fp32_element_ms_per_load_step": t_x32, "fp64_ms_per_load_step": t_x64,
-                  "fp32_element_max_rel_err_vs_fp64": x32_err,
+                  "fp32_element_max_rel_err_vs_fp64": x32_err, "kernels_ms": x_kernels,
                   "speedup_closure_vs_exact_fp64": t_x64 / main_t, "speedup_closure_vs_exact_fp32": t_x32 / main_t},
         "clocks": clk.summary(), "e2e": None, "gpu_launches": int(main_launches), "cpu_baseline": None,
     }
@@ -671,7 +684,9 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) measurement")
     ap.add_argument("--n", type=int, default=None, help="elements per box side (default: the workload's size)")
     ap.add_argument("--no-variants", action="store_true", help="skip timing the other precision variant")
-    ap.add_argument("--epochs", type=int, default=30, help="closure training epochs (j2mlp workload)")
+    ap.add_argument("--epochs", type=int, default=60, help="closure training epochs (j2mlp workload)")
+    ap.add_argument("--paths", type=int, default=250_000,
+                    help="random strain paths of 20 steps for the closure's training data (j2mlp workload)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

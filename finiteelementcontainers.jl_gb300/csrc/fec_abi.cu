@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -14,6 +15,7 @@
 
 #include "../../include/fec_gb300.h"
 #include "fec_closure.cuh"
+#include "fec_closure_tc.h"
 #include "fec_launch.h"
 #include <cuda_bf16.h>
 
@@ -77,6 +79,8 @@ struct fec_ctx {
   // learned closure (FEC_PHYS_J2_MLP): BF16 parameters, normalisation, counters, and the
   // ClosureArgs struct the kernels read
   DevBuf d_cl_w, d_cl_norm, d_cl_cnt, d_cl_args;
+  DevBuf d_cl_img, d_cl_table;  // tensor-core closure: packed parameters, per-point table
+  float cl_tol = 0.f;
   // optional per-launch timing (CUDA events on the caller's stream)
   bool profiling = false;
   std::vector<cudaEvent_t> events;  // 2 per timed launch
@@ -133,6 +137,20 @@ int ensure(fec_ctx* c, DevBuf& b, size_t bytes) {
 
 // element-matrix blocks start on 16-byte boundaries (vectorised copy-out)
 inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3); }
+
+// FEC_CLOSURE_ON_CUDA_CORES=1 selects the per-thread network evaluation (the
+// generic element kernel) instead of the tensor-core closure kernel.
+bool closure_on_cuda_cores() {
+  const char* v = std::getenv("FEC_CLOSURE_ON_CUDA_CORES");
+  return v && v[0] == '1';
+}
+
+// Learned-closure hex8 blocks in FP32 element arithmetic run the tensor-core
+// closure kernel and the FP32 hex8 element kernel (node-rows layout).
+bool tc_closure(const Block& B, int precision) {
+  return B.physics == FEC_PHYS_J2_MLP && B.elem_type == FEC_HEX8 && precision == FEC_FP32_ELEMENT &&
+         !closure_on_cuda_cores();
+}
 
 int num_fields_of(int physics) { return physics == FEC_PHYS_POISSON ? 1 : 3; }
 int num_states_of(int physics) { return (physics == FEC_PHYS_J2 || physics == FEC_PHYS_J2_MLP) ? 7 : 0; }
@@ -220,7 +238,7 @@ int fec_ctx_destroy(fec_ctx* c) {
   for (cudaEvent_t e : c->events) cudaEventDestroy(e);
   for (DevBuf* b : {&c->d_coords, &c->d_conn, &c->d_ref, &c->d_nadj_ptr, &c->d_nadj, &c->d_epos, &c->d_umask,
                     &c->d_col_base, &c->d_col_len, &c->d_dtu, &c->d_unknown_dofs, &c->d_Ke, &c->d_Re, &c->d_cl_w,
-                    &c->d_cl_norm, &c->d_cl_cnt, &c->d_cl_args})
+                    &c->d_cl_norm, &c->d_cl_cnt, &c->d_cl_args, &c->d_cl_img, &c->d_cl_table})
     b->release();
   delete c;
   return FEC_OK;
@@ -663,11 +681,30 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
            "element_neohookean_hex27"},
           {"", "element_j2", "", "", "", "", "element_j2_tet4", "element_j2_tet10", "element_j2_hex27"},
           {"", "element_j2_mlp", "", "", "", "", "", "", ""}};
-      LaunchTimer timer(c, s, kNames[B.physics][B.elem_type]);
-      if (B.physics == FEC_PHYS_POISSON)
-        e = fec::launch_poisson(B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
-      else
-        e = fec::launch_mech(B.physics, B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
+      if (tc_closure(B, precision)) {
+        // tensor-core closure: point table and state, then the FP32 hex8 element kernel on it
+        const size_t tbytes = sizeof(float) * fec::POINT_TABLE_STRIDE * size_t(B.ne) * 8;
+        if (int rc = ensure(c, c->d_cl_table, tbytes)) return rc;
+        fec::TcClosure tcl;
+        tcl.image = static_cast<const unsigned char*>(c->d_cl_img.p);
+        tcl.counters = static_cast<unsigned long long*>(c->d_cl_cnt.p);
+        tcl.table = static_cast<float*>(c->d_cl_table.p);
+        tcl.tol = c->cl_tol;
+        {
+          LaunchTimer timer(c, s, "closure_j2_mlp_tc");
+          e = fec::launch_j2mlp_points_tc(ea, tcl, s, &c->last_launches);
+        }
+        if (e == cudaSuccess) {
+          LaunchTimer timer(c, s, "element_j2_mlp");
+          e = fec::launch_point_table_hex8(want_r, want_k, ea, tcl.table, s, &c->last_launches);
+        }
+      } else {
+        LaunchTimer timer(c, s, kNames[B.physics][B.elem_type]);
+        if (B.physics == FEC_PHYS_POISSON)
+          e = fec::launch_poisson(B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
+        else
+          e = fec::launch_mech(B.physics, B.elem_type, precision, want_r, want_k, ea, s, &c->last_launches);
+      }
     }
     if (e == cudaErrorNotSupported)
       return fail(c, FEC_ERR_UNSUPPORTED, "block %d: physics %d on element type %d is not built", int(b) + 1,
@@ -682,7 +719,8 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     bi.nnpe = B.nnpe;
     bi.ndof = ndof;
     // the hex8 mechanics kernels write the node-rows layout
-    bi.layout = (B.elem_type == FEC_HEX8 && (B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2))
+    bi.layout = (B.elem_type == FEC_HEX8 && (B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2 ||
+                                             tc_closure(B, precision)))
                     ? fec::KE_NODE_ROWS
                     : fec::KE_ROW_MAJOR;
     ke_off += pad4(B.ne * ndof * ndof);
@@ -725,8 +763,11 @@ int fec_closure_set(fec_ctx* c, const float* params, const float* norm, float to
   if ((rc = upload(c, c->d_cl_w, w.data(), sizeof(__nv_bfloat16) * w.size()))) return rc;
   const int nn = 2 * fec::MLP_IN + 2 * fec::MLP_OUT;
   if ((rc = upload(c, c->d_cl_norm, norm, sizeof(float) * nn))) return rc;
-  const unsigned long long zero[2] = {0, 0};
+  const unsigned long long zero[4] = {0, 0, 0, 0};
   if ((rc = upload(c, c->d_cl_cnt, zero, sizeof zero))) return rc;
+  const std::vector<unsigned char> img = fec::pack_mlp_image(params, norm);
+  if ((rc = upload(c, c->d_cl_img, img.data(), img.size()))) return rc;
+  c->cl_tol = tol;
   fec::ClosureArgs a;
   a.W = static_cast<const __nv_bfloat16*>(c->d_cl_w.p);
   const float* nd = static_cast<const float*>(c->d_cl_norm.p);
@@ -744,11 +785,12 @@ int fec_closure_stats(fec_ctx* c, int64_t* plastic, int64_t* fallbacks, int rese
   if (!c) return FEC_ERR_ARG;
   if (!c->d_cl_cnt.p) return fail(c, FEC_ERR_STATE, "no closure installed");
   cudaSetDevice(c->device);
-  unsigned long long h[2];
+  unsigned long long h[3];
   FEC_CUDA(c, cudaMemcpy(h, c->d_cl_cnt.p, sizeof h, cudaMemcpyDeviceToHost));
   if (plastic) *plastic = int64_t(h[0]);
   if (fallbacks) *fallbacks = int64_t(h[1]);
-  if (reset) FEC_CUDA(c, cudaMemset(c->d_cl_cnt.p, 0, sizeof h));
+  if (h[2]) return fail(c, FEC_ERR_DEVICE, "closure kernel: a wait on the tensor cores gave up (results invalid)");
+  if (reset) FEC_CUDA(c, cudaMemset(c->d_cl_cnt.p, 0, 2 * sizeof(unsigned long long)));
   return ok(c);
 }
 

@@ -4,134 +4,10 @@
 #include <cmath>
 #include "../../include/fec_gb300.h"
 #include "fec_closure.cuh"
+#include "fec_closure_physics.cuh"
 #include "fec_launch.h"
 
 namespace fec {
-
-// Voigt index of tensor component (i, J): xx yy zz yz xz xy
-__host__ __device__ constexpr int voigt(int i, int j) {
-  return i == j ? i : (i + j == 3 ? 3 : (i + j == 2 ? 4 : 5));
-}
-
-// 6x6 tangent C6[m][n] = d sigma_m / d eps_n (tensor strain components) from a
-// 9x9 A_iJkL accessor with minor symmetry: shear columns count both (k,L), (L,k).
-template <class F>
-__device__ void tangent6_from(F aentry, float* C6) {
-  const int ii[6] = {0, 1, 2, 1, 0, 0}, jj[6] = {0, 1, 2, 2, 2, 1};
-  for (int m = 0; m < 6; ++m)
-    for (int n = 0; n < 6; ++n) C6[m * 6 + n] = aentry(ii[m], jj[m], ii[n], jj[n]) * (n >= 3 ? 2.f : 1.f);
-}
-
-// J2 with its radial return replaced at plastic points by the MLP closure;
-// elastic points and points failing the consistency check use the exact update.
-struct J2MLP {
-  static constexpr bool USES_CLOSURE = true;
-  static constexpr int NS = 7;
-  static constexpr int SCR = 36;  // JxW-scaled 6x6 tangent d sigma / d eps
-
-  template <typename Real>
-  __device__ static void exact(const double* props, Real gu[3][3], Real jxw, const double* st_old, double* st_new,
-                               Real* P9, Real* scr) {
-    Real s13[J2::SCR];
-    J2::point(props, gu, jxw, st_old, st_new, P9, s13);
-    float C6[36];
-    tangent6_from([&](int i, int J, int k, int L) { return float(J2::aentry(s13, i, J, k, L)); }, C6);
-#pragma unroll
-    for (int m = 0; m < 36; ++m) scr[m] = Real(C6[m]);
-  }
-
-  template <typename Real>
-  __device__ static void point_closure(const void* closure, const double* props, Real gu[3][3], Real jxw,
-                                       const double* st_old, double* st_new, Real* P9, Real* scr) {
-    const ClosureArgs& c = *static_cast<const ClosureArgs*>(closure);
-    const double E = props[0], nu = props[1], sy = props[2], Hh = props[3];
-    const double mu = E / (2 * (1 + nu));
-    // trial state
-    double etr[6];
-    const int ii[6] = {0, 1, 2, 1, 0, 0}, jj[6] = {0, 1, 2, 2, 2, 1};
-#pragma unroll
-    for (int m = 0; m < 6; ++m) etr[m] = 0.5 * (double(gu[ii[m]][jj[m]]) + double(gu[jj[m]][ii[m]])) - st_old[m];
-    const double tr = etr[0] + etr[1] + etr[2];
-    double sn2 = 0;
-#pragma unroll
-    for (int m = 0; m < 6; ++m) {
-      const double dev = 2 * mu * (etr[m] - (m < 3 ? tr / 3.0 : 0.0));
-      sn2 += (m < 3 ? 1.0 : 2.0) * dev * dev;
-    }
-    const double f_trial = sqrt(sn2) - sqrt(2.0 / 3.0) * (sy + Hh * st_old[6]);
-    if (f_trial <= 0) {  // elastic: exact and cheap
-      exact(props, gu, jxw, st_old, st_new, P9, scr);
-      return;
-    }
-    atomicAdd(&c.counters[0], 1ull);
-    float x[MLP_IN], y[MLP_OUT], Js[6][6];
-#pragma unroll
-    for (int m = 0; m < 6; ++m) {
-      x[m] = float(etr[m]);
-      x[6 + m] = float(st_old[m]);
-    }
-    x[12] = float(st_old[6]);
-    x[13] = 1.0f;
-    mlp_eval_with_jacobian(c, x, y, Js);
-    // the network predicts the plastic correction of the deviatoric stress; the elastic
-    // trial deviator 2 mu dev(e_tr) and the pressure kappa tr(e_tr) are exact (J2 plastic
-    // flow is deviatoric, so tr(eps_e) = tr(e_tr))
-    const float mu2 = float(2 * mu);
-#pragma unroll
-    for (int m = 0; m < 6; ++m) {
-      y[m] += float(2 * mu * (etr[m] - (m < 3 ? tr / 3.0 : 0.0)));
-#pragma unroll
-      for (int n = 0; n < 6; ++n) Js[m][n] += mu2 * ((m == n ? 1.f : 0.f) - (m < 3 && n < 3 ? 1.f / 3.f : 0.f));
-    }
-    const double kap = E / (3 * (1 - 2 * nu));
-    const float p = float(kap * tr);
-    // consistency: the predicted stress must lie on the updated yield surface
-    const double eqps_new = st_old[6] + double(y[12]);
-    const double trs = double(y[0]) + y[1] + y[2];
-    double d2 = 0;
-#pragma unroll
-    for (int m = 0; m < 6; ++m) {
-      const double dev = double(y[m]) - (m < 3 ? trs / 3.0 : 0.0);
-      d2 += (m < 3 ? 1.0 : 2.0) * dev * dev;
-    }
-    const double f = sqrt(d2) - sqrt(2.0 / 3.0) * (sy + Hh * eqps_new);
-    if (!(fabs(f) <= double(c.tol) * sy)) {
-      atomicAdd(&c.counters[1], 1ull);
-      exact(props, gu, jxw, st_old, st_new, P9, scr);
-      return;
-    }
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) P9[i * 3 + j] = jxw * Real(y[voigt(i, j)] + (i == j ? p : 0.f));
-    if (st_new) {
-#pragma unroll
-      for (int m = 0; m < 7; ++m) st_new[m] = st_old[m] + double(y[6 + m]);
-    }
-    const float kf = float(kap);
-#pragma unroll
-    for (int m = 0; m < 6; ++m)
-#pragma unroll
-      for (int n = 0; n < 6; ++n) scr[m * 6 + n] = jxw * Real(Js[m][n] + (m < 3 && n < 3 ? kf : 0.f));
-  }
-
-  template <typename Real>
-  __device__ static Real aentry(const Real* scr, int i, int J, int k, int L) {
-    return scr[voigt(i, J) * 6 + voigt(k, L)] * (k == L ? Real(1) : Real(0.5));
-  }
-  template <typename Real>
-  __device__ static void aentries(const Real* scr, int i, Real* out) {
-#pragma unroll
-    for (int J = 0; J < 3; ++J)
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int L = 0; L < 3; ++L) out[J * 9 + k * 3 + L] = aentry(scr, i, J, k, L);
-  }
-  // unused: the closure needs ElemArgs::closure
-  template <typename Real>
-  __device__ static void point(const double*, Real (*)[3], Real, const double*, double*, Real*, Real*) {}
-};
 
 cudaError_t launch_mech_j2mlp(int elem_type, int precision, bool want_r, bool want_k, const ElemArgs& a,
                               cudaStream_t s, int* launches) {

@@ -269,6 +269,7 @@ __global__ void __launch_bounds__(EPB * Elem<ET>::NNPE) poisson_element_kernel(E
 //   a1 = K/2 (2J-1) J + 2/9 c2 I1,  a2 = I1/3 c2 - c1
 struct NeoHookean {
   static constexpr bool USES_CLOSURE = false;
+  static constexpr bool USES_TABLE = false;
   static constexpr int NS = 0;
   static constexpr int SCR = 21;  // F(9) H(9) a1 a2 c2
   template <typename Real>
@@ -368,70 +369,74 @@ struct NeoHookean {
 // state (7) = plastic strain (xx, yy, zz, yz, xz, xy) + equivalent plastic strain.
 struct J2 {
   static constexpr bool USES_CLOSURE = false;
+  static constexpr bool USES_TABLE = false;
   static constexpr int NS = 7;
   static constexpr int SCR = 13;  // n(9) kap' 2mu th' 2mu thb' (unused)
+  // Arithmetic in Real: double for the FP64 variant, float for the FP32-element
+  // variant; the state is accumulated in double either way.
   template <typename Real>
   __device__ static void point(const double* props, Real gu[3][3], Real jxw, const double* st_old, double* st_new,
                                Real* P9, Real* scr) {
-    const double E = props[0], nu = props[1], sy = props[2], Hh = props[3];
-    const double mu = E / (2 * (1 + nu)), lam = E * nu / ((1 + nu) * (1 - 2 * nu)), kap = lam + 2.0 / 3.0 * mu;
-    double eps[3][3];
+    using C = Real;
+    const C E = C(props[0]), nu = C(props[1]), sy = C(props[2]), Hh = C(props[3]);
+    const C mu = E / (2 * (1 + nu)), lam = E * nu / ((1 + nu) * (1 - 2 * nu)), kap = lam + C(2.0 / 3.0) * mu;
+    C eps[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int j = 0; j < 3; ++j) eps[i][j] = 0.5 * (double(gu[i][j]) + double(gu[j][i]));
-    const double ep[3][3] = {{st_old[0], st_old[5], st_old[4]},
-                             {st_old[5], st_old[1], st_old[3]},
-                             {st_old[4], st_old[3], st_old[2]}};
-    const double eqps_old = st_old[6];
-    double ee[3][3];
+      for (int j = 0; j < 3; ++j) eps[i][j] = C(0.5) * (C(gu[i][j]) + C(gu[j][i]));
+    const C ep[3][3] = {{C(st_old[0]), C(st_old[5]), C(st_old[4])},
+                        {C(st_old[5]), C(st_old[1]), C(st_old[3])},
+                        {C(st_old[4]), C(st_old[3]), C(st_old[2])}};
+    const C eqps_old = C(st_old[6]);
+    C ee[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) ee[i][j] = eps[i][j] - ep[i][j];
-    const double tr = ee[0][0] + ee[1][1] + ee[2][2];
-    double s[3][3];
-    double sn2 = 0;
+    const C tr = ee[0][0] + ee[1][1] + ee[2][2];
+    C s[3][3];
+    C sn2 = 0;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        s[i][j] = 2 * mu * (ee[i][j] - (i == j ? tr / 3.0 : 0.0));
+        s[i][j] = 2 * mu * (ee[i][j] - (i == j ? tr / C(3.0) : C(0.0)));
         sn2 += s[i][j] * s[i][j];
       }
-    const double snorm = sqrt(sn2);
-    const double sq23 = sqrt(2.0 / 3.0);
-    const double f = snorm - sq23 * (sy + Hh * eqps_old);
-    double dgam = 0, th = 1, thb = 0;
-    double n[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    const C snorm = sqrt(sn2);
+    const C sq23 = C(sqrt(2.0 / 3.0));
+    const C f = snorm - sq23 * (sy + Hh * eqps_old);
+    C dgam = 0, th = 1, thb = 0;
+    C n[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     if (f > 0) {
-      dgam = f / (2 * mu + 2.0 / 3.0 * Hh);
+      dgam = f / (2 * mu + C(2.0 / 3.0) * Hh);
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) n[i][j] = s[i][j] / snorm;
-      th = 1.0 - 2 * mu * dgam / snorm;
-      thb = 1.0 / (1.0 + Hh / (3 * mu)) - (1.0 - th);
+      th = C(1.0) - 2 * mu * dgam / snorm;
+      thb = C(1.0) / (C(1.0) + Hh / (3 * mu)) - (C(1.0) - th);
     }
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j)
-        P9[i * 3 + j] = Real(double(jxw) * (s[i][j] - 2 * mu * dgam * n[i][j] + (i == j ? kap * tr : 0.0)));
+        P9[i * 3 + j] = Real(C(jxw) * (s[i][j] - 2 * mu * dgam * n[i][j] + (i == j ? kap * tr : C(0.0))));
     if (st_new) {
-      st_new[0] = ep[0][0] + dgam * n[0][0];
-      st_new[1] = ep[1][1] + dgam * n[1][1];
-      st_new[2] = ep[2][2] + dgam * n[2][2];
-      st_new[3] = ep[1][2] + dgam * n[1][2];
-      st_new[4] = ep[0][2] + dgam * n[0][2];
-      st_new[5] = ep[0][1] + dgam * n[0][1];
-      st_new[6] = eqps_old + sq23 * dgam;
+      st_new[0] = st_old[0] + double(dgam * n[0][0]);
+      st_new[1] = st_old[1] + double(dgam * n[1][1]);
+      st_new[2] = st_old[2] + double(dgam * n[2][2]);
+      st_new[3] = st_old[3] + double(dgam * n[1][2]);
+      st_new[4] = st_old[4] + double(dgam * n[0][2]);
+      st_new[5] = st_old[5] + double(dgam * n[0][1]);
+      st_new[6] = st_old[6] + double(sq23 * dgam);
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) scr[i] = Real(n[i / 3][i % 3]);
-    scr[9] = Real(double(jxw) * kap);
-    scr[10] = Real(double(jxw) * 2 * mu * th);
-    scr[11] = Real(double(jxw) * 2 * mu * thb);
+    scr[9] = Real(C(jxw) * kap);
+    scr[10] = Real(C(jxw) * 2 * mu * th);
+    scr[11] = Real(C(jxw) * 2 * mu * thb);
     scr[12] = 0;
   }
   template <typename Real>

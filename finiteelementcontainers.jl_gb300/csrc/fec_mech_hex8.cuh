@@ -342,9 +342,14 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_rows2_kernel(ElemArgs g) {
         for (int a = 0; a < 8; ++a) s = fmaf(s_u[a * 3 + i], dNX[a * 3 + j], s);
         gu[i][j] = s;
       }
-    const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
-    double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
-    Model::point(g.props, gu, jxw, so, sn, s_P + q * 9, s_scr + q * SCR);
+    if constexpr (Model::USES_TABLE) {
+      // constitutive response precomputed per point (by the closure kernel)
+      Model::point_table(g.closure, e * NQ + q, jxw, s_P + q * 9, s_scr + q * SCR);
+    } else {
+      const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
+      double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
+      Model::point(g.props, gu, jxw, so, sn, s_P + q * 9, s_scr + q * SCR);
+    }
   }
   __syncthreads();
   const int pp = tx / 3, i = tx % 3;

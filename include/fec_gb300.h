@@ -187,11 +187,20 @@ int fec_mlp_gradient(const float* params_dev, const float* X_dev, const float* Y
 int fec_mlp_adam_step(float* params_dev, float* m_dev, float* v_dev, const float* X_dev, const float* Y_dev,
                       int64_t n, int64_t step, float lr, float* scratch_dev, int64_t scratch_len, float* loss_dev,
                       void* stream);
-/* Installs a trained closure for FEC_PHYS_J2_MLP blocks: FP32 parameters (host,
- * stored on the device as BF16), the feature normalisation (host; 14 + 14 + 13
- * + 13 floats: input mean, input std, output mean, output std) and the
- * consistency threshold (relative to sigma_y) above which a point falls back
- * to the exact update. */
+/* The network on the tensor cores, as the assembly runs it: n rows of X (device,
+ * n x 14, physical units) -> outputs Y (n x 13, physical units) and the Jacobian
+ * of the six stress outputs with respect to the six strain inputs (n x 36,
+ * row-major 6 x 6).  Parameters and normalisation on the host, as for
+ * fec_closure_set.  Synchronises the stream.  No counterpart in the reference. */
+int fec_mlp_eval_tc(const float* params, const float* normalisation, const float* X_dev, int64_t n, float* Y_dev,
+                    float* jac_dev, void* stream);
+/* Installs a trained closure for FEC_PHYS_J2_MLP blocks: FP32 parameters (host;
+ * the device keeps a BF16 copy and the two-term BF16 split the tensor-core
+ * kernel uses), the feature normalisation (host; 14 + 14 + 13 + 13 floats:
+ * input mean, input std, output mean, output std) and the consistency threshold
+ * (relative to sigma_y) above which a point falls back to the exact update.
+ * Hex8 blocks assembled with FEC_FP32_ELEMENT run the network on the tensor
+ * cores; other combinations evaluate it per point on the CUDA cores. */
 int fec_closure_set(fec_ctx* ctx, const float* params, const float* normalisation, float tol);
 /* Plastic points that used the closure path and fallbacks since the last reset. */
 int fec_closure_stats(fec_ctx* ctx, int64_t* plastic_points, int64_t* fallbacks, int reset);

@@ -68,3 +68,27 @@ def loss_and_grad(params, X, Y):
             delta = (delta @ W) * dsilu(zs[li - 1])
     grads.reverse()
     return loss, np.concatenate([np.concatenate([gW.ravel(), gb]) for gW, gb in grads])
+
+
+def forward_physical(params, norm, X):
+    """Network in physical units: inputs normalised by (mean, std), outputs
+    de-normalised; `norm` = input mean (14), input std (14), output mean (13),
+    output std (13).  Returns (Y, Jacobian of the first six outputs with respect
+    to the first six inputs, n x 6 x 6)."""
+    nin, nout = DIMS[0], DIMS[-1]
+    im, is_ = norm[:nin], norm[nin:2 * nin]
+    om, os_ = norm[2 * nin:2 * nin + nout], norm[2 * nin + nout:]
+    a = (X - im) / is_
+    layers = unpack(params)
+    # forward-mode tangents of the six strain inputs
+    t = np.zeros((X.shape[0], 6, nin))
+    for j in range(6):
+        t[:, j, j] = 1.0 / is_[j]
+    for W, b in layers[:-1]:
+        z = a @ W.T + b
+        t = dsilu(z)[:, None, :] * (t @ W.T)
+        a = silu(z)
+    W, b = layers[-1]
+    y = (a @ W.T + b) * os_ + om
+    J = (t @ W.T)[:, :, :6] * os_[:6]          # [n, j, o]
+    return y, np.transpose(J, (0, 2, 1))       # [n, o, j]

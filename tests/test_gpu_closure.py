@@ -2,6 +2,7 @@
 hand-written MLP kernels' forward pass and gradients against the numpy
 reference, and what training gains over the untrained network inside assembly."""
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -68,6 +69,34 @@ def test_mlp_kernels_match_numpy_reference(fec):
     assert rel_err(grad.cpu().numpy(), g_ref)[1] <= 1e-4
 
 
+def test_tensor_core_network_matches_numpy_reference(fec):
+    """The network as the assembly runs it on the tensor cores (tcgen05, BF16
+    operands, FP32 accumulation in tensor memory) against the FP64 numpy
+    reference: outputs and the Jacobian of the stress outputs."""
+    torch = _torch()
+    from fec_gb300 import closure, _lib
+    from oracle import mlp_reference as ref
+    lib = fec.load_library()
+    rng = np.random.default_rng(7)
+    n = 1000  # 8 tiles of 128 rows, the last one partial
+    P = closure.init_params(5)
+    norm = np.concatenate([rng.normal(0, 1e-3, 14), rng.uniform(1e-3, 3e-3, 14), rng.normal(0, 0.1, 13),
+                           rng.uniform(0.05, 0.2, 13)]).astype(np.float32)
+    X = (norm[:14] + norm[14:28] * rng.standard_normal((n, 14))).astype(np.float32)
+    Xd = torch.from_numpy(X).cuda()
+    Y = torch.full((n, 13), float("nan"), dtype=torch.float32, device="cuda")
+    J = torch.full((n, 36), float("nan"), dtype=torch.float32, device="cuda")
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.fec_mlp_eval_tc(_lib.ptr(P), _lib.ptr(norm), _lib.ptr(Xd), n, _lib.ptr(Y), _lib.ptr(J), s) == 0
+    y_ref, J_ref = ref.forward_physical(P.astype(np.float64), norm.astype(np.float64), X.astype(np.float64))
+    y, Jg = Y.cpu().numpy(), J.cpu().numpy().reshape(n, 6, 6)
+    ey, eJ = rel_err(y, y_ref), rel_err(Jg, J_ref)
+    print("tensor-core network: output error", ey, "Jacobian error", eJ)
+    assert np.isfinite(y).all() and np.isfinite(Jg).all()
+    assert ey[1] <= 1e-4      # activation rows: two-term BF16 split of activations and weights
+    assert eJ[1] <= 3e-2      # tangent rows: one BF16 term
+
+
 def _j2_path(fec, physics, n=6, nsteps=10):
     """A 6^3 uniaxial J2 load path with state carried: per step (R, nzval), and the
     closure statistics when the physics has a closure."""
@@ -108,9 +137,15 @@ def test_training_gains_over_untrained_network(fec):
     # plastic points; the exact return map judges it)
     exact, _ = _j2_path(fec, fec.J2Plasticity(*PROPS))
     runs = {}
-    for name, cl in (("untrained", untrained),
-                     ("trained_loose", closure.TrainedClosure(trained.params, trained.normalisation, [], 5e-2))):
+    loose = closure.TrainedClosure(trained.params, trained.normalisation, [], 5e-2)
+    for name, cl in (("untrained", untrained), ("trained_loose", loose)):
         runs[name] = _j2_path(fec, closure.J2Closure(*PROPS, cl))
+    # the same network evaluated per point on the CUDA cores (BF16 weights, no split)
+    os.environ["FEC_CLOSURE_ON_CUDA_CORES"] = "1"
+    try:
+        runs["trained_loose_cuda_cores"] = _j2_path(fec, closure.J2Closure(*PROPS, loose))
+    finally:
+        del os.environ["FEC_CLOSURE_ON_CUDA_CORES"]
     for name, (steps, (plast, fb)) in runs.items():
         errs = [(rel_err(R, Rx)[1], rel_err(K, Kx)[1]) for (R, K), (Rx, Kx) in zip(steps, exact)]
         print(name, "plastic points", plast, "fallbacks", fb, "worst (R, K) error over the path",
@@ -127,3 +162,7 @@ def test_training_gains_over_untrained_network(fec):
     errs, plast, fb = runs["trained_loose"]
     assert plast > 0 and fb < 0.5 * plast
     assert max(e[0] for e in errs) <= 5e-2 and max(e[1] for e in errs) <= 5e-2
+    # the tensor-core closure is at least as accurate as the per-point CUDA-core evaluation
+    errs_cc, plast_cc, fb_cc = runs["trained_loose_cuda_cores"]
+    assert plast_cc == plast
+    assert max(e[0] for e in errs) <= 1.5 * max(e[0] for e in errs_cc) + 1e-4
