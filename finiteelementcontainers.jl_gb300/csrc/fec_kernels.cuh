@@ -506,6 +506,11 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
   Real* s_A_all = s_scr_all + EPB * NQ * SCR;
   int* s_conn_all = reinterpret_cast<int*>(s_A_all + (WANT_K ? EPB * NQ * 81 : 0));
 
+  // FP64: the tangent contraction runs in double-float on the FP32 pipes, from
+  // (hi, lo) splits of the shape gradients and of A (written over A in place)
+  constexpr bool DF = std::is_same<Real, double>::value;
+  float2* s_dNXf_all = reinterpret_cast<float2*>(s_conn_all + ((EPB * A + 3) & ~3));
+
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int64_t e = int64_t(blockIdx.x) * EPB + ty;
   double* s_x = s_x_all + ty * A * D;
@@ -515,6 +520,7 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
   Real* s_P = s_P_all + ty * NQ * 9;
   Real* s_scr = s_scr_all + ty * NQ * SCR;
   Real* s_A = s_A_all + ty * NQ * 81;
+  float2* s_dNXf = s_dNXf_all + ty * NQ * A * D;
   stage_element<ET, 3, EPB, TPE>(g, e, tx, ty, s_ref, s_conn_all + ty * A, s_x, s_u);
   const bool live = e < g.ne;
 
@@ -547,7 +553,15 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
   if (WANT_K && live) {
     for (int w = tx; w < NQ * 3; w += TPE) {
       const int q = w / 3, i = w % 3;
-      Model::aentries(s_scr + q * SCR, i, s_A + q * 81 + i * 27);
+      Real* Aq = s_A + q * 81 + i * 27;
+      Model::aentries(s_scr + q * SCR, i, Aq);
+      if constexpr (DF) {
+        float2* Af = reinterpret_cast<float2*>(Aq);
+        for (int m = 0; m < 27; ++m) Af[m] = df64_split(double(Aq[m]));
+      }
+    }
+    if constexpr (DF) {
+      for (int w = tx; w < NQ * A * D; w += TPE) s_dNXf[w] = df64_split(double(s_dNX[w]));
     }
   }
   __syncthreads();
@@ -556,6 +570,45 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
   const int r = tx % NDOF, cs = tx / NDOF;
   const int a = r / 3, i = r % 3;
   const int b0 = cs * CW;
+  if constexpr (DF) {
+    if (WANT_K) {
+      float2 Kf[CW * 3];
+#pragma unroll
+      for (int c = 0; c < CW * 3; ++c) Kf[c] = make_float2(0.f, 0.f);
+      for (int q = 0; q < NQ; ++q) {
+        const float2* dNf = s_dNXf + q * A * D;
+        const float2 g0 = dNf[a * 3 + 0], g1 = dNf[a * 3 + 1], g2 = dNf[a * 3 + 2];
+        const float2* Ai = reinterpret_cast<const float2*>(s_A + q * 81 + i * 27);
+        float2 t[9];
+#pragma unroll
+        for (int kl = 0; kl < 9; ++kl) t[kl] = df64_fma(g0, Ai[kl], df64_fma(g1, Ai[9 + kl], df64_mul(g2, Ai[18 + kl])));
+#pragma unroll
+        for (int bb = 0; bb < CW; ++bb) {
+          const int b = b0 + bb;
+          if (b < A) {
+            const float2 h0 = dNf[b * 3 + 0], h1 = dNf[b * 3 + 1], h2 = dNf[b * 3 + 2];
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+              Kf[bb * 3 + k] = df64_add(Kf[bb * 3 + k],
+                                        df64_fma(t[k * 3 + 0], h0, df64_fma(t[k * 3 + 1], h1, df64_mul(t[k * 3 + 2], h2))));
+          }
+        }
+      }
+      float2* Ke = static_cast<float2*>(g.Ke) + (e * NDOF + r) * NDOF + b0 * 3;
+#pragma unroll
+      for (int c = 0; c < CW * 3; ++c)
+        if (b0 * 3 + c < NDOF) Ke[c] = Kf[c];
+    }
+    if (WANT_R && cs == 0) {
+      double R = 0;
+      for (int q = 0; q < NQ; ++q) {
+        const double* dNX = s_dNX + q * A * D;
+        const double* P = s_P + q * 9 + i * 3;
+        R = fma(dNX[a * 3], P[0], fma(dNX[a * 3 + 1], P[1], fma(dNX[a * 3 + 2], P[2], R)));
+      }
+      static_cast<float2*>(g.Re)[e * NDOF + r] = df64_split(R);
+    }
+  } else {
   Real Krow[CW * 3];
 #pragma unroll
   for (int c = 0; c < CW * 3; ++c) Krow[c] = 0;
@@ -591,16 +644,18 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
       if (b0 * 3 + c < NDOF) Ke[c] = WS<Real>::from(Krow[c]);
   }
   if (WANT_R && cs == 0) static_cast<typename WS<Real>::T*>(g.Re)[e * NDOF + r] = WS<Real>::from(R);
+  }
 }
 
 template <int ET, class Model, typename Real, int EPB, bool WANT_K>
 constexpr size_t mech_smem_bytes() {
   using E = Elem<ET>;
   constexpr int A = E::NNPE, NQ = E::NQ;
+  constexpr bool DF = std::is_same<Real, double>::value;
   return sizeof(double) * (((RefLayout<ET>::SIZE + 1) & ~1) + 2 * EPB * A * 3) +
          sizeof(Real) * (EPB * NQ * A * 3 + EPB * NQ + EPB * NQ * 9 + EPB * NQ * Model::SCR +
                          (WANT_K ? EPB * NQ * 81 : 0)) +
-         sizeof(int) * EPB * A + 16;
+         sizeof(int) * ((EPB * A + 3) & ~3) + (DF && WANT_K ? sizeof(float2) * EPB * NQ * A * 3 : 0) + 16;
 }
 
 // ---------------------------------------------------------------------------
