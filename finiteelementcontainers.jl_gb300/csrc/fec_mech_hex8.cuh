@@ -491,29 +491,40 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
     }
   }
   __syncthreads();
-  if (live && tx < NQ) {
-    const int q = tx;
-    double dNX[24];
-    const double jxw = map_point<1, double>(s_ref, q, s_x, dNX, nullptr);
-    double gu[3][3];
+  // Per-point map and constitutive update in native FP64: the CTA's EPB * 8 points
+  // go to its first EPB * 8 threads, so every warp that issues this FP64 work has
+  // all 32 lanes busy (the FP64 pipe is the scarce one).
+  if (tid < EPB * NQ) {
+    const int el = tid / NQ, q = tid % NQ;
+    const int64_t ep = e0 + el;
+    if (ep < g.ne) {
+      const double* px = dbase + S::D_X + el * 24;
+      const double* pu = dbase + S::D_U + el * 24;
+      double dNX[24];
+      const double jxw = map_point<1, double>(s_ref, q, px, dNX, nullptr);
+      double gu[3][3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+      for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        double s = 0;
+        for (int j = 0; j < 3; ++j) {
+          double s = 0;
 #pragma unroll
-        for (int a = 0; a < 8; ++a) s = fma(s_u[a * 3 + i], dNX[a * 3 + j], s);
-        gu[i][j] = s;
-      }
-    const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
-    double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
-    double P9[9], scr[SCR];
-    Model::point(g.props, gu, jxw, so, sn, P9, scr);
+          for (int a = 0; a < 8; ++a) s = fma(pu[a * 3 + i], dNX[a * 3 + j], s);
+          gu[i][j] = s;
+        }
+      const double* so = NS ? g.state_old + (ep * NQ + q) * NS : nullptr;
+      double* sn = (NS && g.state_new) ? g.state_new + (ep * NQ + q) * NS : nullptr;
+      double P9[9], scr[SCR];
+      Model::point(g.props, gu, jxw, so, sn, P9, scr);
+      float2* pdNX = fb + S::F_DNX + el * NQ * 24;
+      float2* pP = fb + S::F_P + el * NQ * 9;
+      float2* pscr = fb + S::F_SCR + el * NQ * SCR2;
 #pragma unroll
-    for (int m = 0; m < 24; ++m) s_dNX[q * 24 + m] = df64_split(dNX[m]);
+      for (int m = 0; m < 24; ++m) pdNX[q * 24 + m] = df64_split(dNX[m]);
 #pragma unroll
-    for (int m = 0; m < 9; ++m) s_P[q * 9 + m] = df64_split(P9[m]);
-    Model::split_scratch(scr, s_scr + q * SCR2);
+      for (int m = 0; m < 9; ++m) pP[q * 9 + m] = df64_split(P9[m]);
+      Model::split_scratch(scr, pscr + q * SCR2);
+    }
   }
   __syncthreads();
   if (WANT_K && live) {
