@@ -451,6 +451,7 @@ def run_batched(args) -> None:
         "dtype": "f64" if args.precision == "fp64" else "f32-element/f64-accumulate", "data": "synthetic",
         "config": {"workload": WORKLOADS["batched"]["name"], "elements": total_ne, "systems": info,
                    "newton_iterations": iters, "execution": "one CUDA graph replay per step",
+                   "autotune": fec.autotune_report(),
                    "precision": args.precision, "l2": "inputs larger than L2"},
         "eager_ms_per_step": t_eager / args.steps,
         "roofline": {"bound": "hbm", "kernel": "all kernels of one R+K pass of both systems",

@@ -19,8 +19,39 @@
 #pragma once
 #include <type_traits>
 #include "fec_kernels.cuh"
+#include "fec_tc.cuh"
 
 namespace fec {
+
+// Stages the hex8 reference tables (shape-function values and gradients, 264
+// doubles) and the connectivity of the CTA's `nlive` elements into shared
+// memory with bulk (TMA) copies that complete on an mbarrier.  Connectivity of
+// a block that does not start on a 16-byte boundary, or a wait that gives up,
+// falls back to plain loads.  Ends with a barrier.
+__device__ __forceinline__ void stage_hex8_tables(const double* gref, double* s_ref, const int32_t* gconn, int nlive,
+                                                  int* s_conn, uint64_t* bar, int tid, int nthr) {
+  constexpr int NREF = RefLayout<1>::SIZE;
+  const bool bulk = ((reinterpret_cast<uintptr_t>(gref) | reinterpret_cast<uintptr_t>(gconn)) & 15) == 0;
+  bool done = false;
+  if (bulk) {
+    if (tid == 0) {
+      tc::mbar_init(bar, 1);
+      tc::mbar_fence_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      tc::mbar_expect_tx(bar, uint32_t(NREF * 8 + nlive * 32));
+      tc::bulk_g2s(s_ref, gref, NREF * 8, bar);
+      tc::bulk_g2s(s_conn, gconn, uint32_t(nlive * 32), bar);
+    }
+    done = tc::mbar_wait(bar, 0, 2000000000LL);
+  }
+  if (!done) {
+    for (int i = tid; i < NREF; i += nthr) s_ref[i] = gref[i];
+    for (int i = tid; i < nlive * 8; i += nthr) s_conn[i] = gconn[i];
+  }
+  __syncthreads();
+}
 
 // (r1, r2), r1 <= r2, of the m-th unique entry of a symmetric 9x9 matrix
 __device__ __forceinline__ void sym_pair(int m, int& r1, int& r2) {
@@ -98,7 +129,7 @@ struct Hex8Smem {
   static constexpr int R_A = (R_SCR + EPB * NQ * SCR + 3) & ~3;     // 16-byte aligned for the vector copy-out
   static constexpr int A_STRIDE = NQ * 81;                          // per element; >= 576 for the K staging
   static constexpr int N_REAL = R_A + EPB * A_STRIDE;
-  static constexpr size_t BYTES = sizeof(double) * N_DOUBLE + sizeof(Real) * N_REAL + sizeof(int) * EPB * 8;
+  static constexpr size_t BYTES = sizeof(double) * N_DOUBLE + sizeof(Real) * N_REAL + sizeof(int) * EPB * 8 + 16;
 };
 
 template <class Model, typename Real, int EPB, bool WANT_R, bool WANT_K>
@@ -311,13 +342,12 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_rows2_kernel(ElemArgs g) {
   Real* s_A = rb + S::R_A + ty * S::A_STRIDE;
   int* s_conn = s_conn_all + ty * 8;
 
-  for (int i = tid; i < L::SIZE; i += nthr) {
-    const double v = g.ref[i];
-    s_ref[i] = v;
-    s_reff[i] = Real(v);
+  {
+    const int64_t left = g.ne - e0;
+    stage_hex8_tables(g.ref, s_ref, g.conn + e0 * 8, left < EPB ? int(left) : EPB, s_conn_all,
+                      reinterpret_cast<uint64_t*>(s_conn_all + EPB * 8), tid, nthr);
   }
-  if (live && tx < 8) s_conn[tx] = g.conn[e * 8 + tx];
-  __syncthreads();
+  for (int i = tid; i < L::SIZE; i += nthr) s_reff[i] = Real(s_ref[i]);
   if (live) {
     for (int i = tx; i < 24; i += TPE) {
       const int a = i / 3, d = i % 3;
@@ -453,7 +483,7 @@ struct Hex8Df64Smem {
   static constexpr int F_A = (F_SCR + EPB * NQ * SCR2 + 1) & ~1;  // 16-byte aligned
   static constexpr int A_STRIDE = NQ * 81;              // >= 576 doubles of K staging
   static constexpr int N_F2 = F_A + EPB * A_STRIDE;
-  static constexpr size_t BYTES = sizeof(double) * N_DOUBLE + sizeof(float2) * N_F2 + sizeof(int) * EPB * 8;
+  static constexpr size_t BYTES = sizeof(double) * N_DOUBLE + sizeof(float2) * N_F2 + sizeof(int) * EPB * 8 + 16;
 };
 
 template <class Model, int EPB, bool WANT_R, bool WANT_K>
@@ -480,9 +510,11 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
   float2* s_A = fb + S::F_A + ty * S::A_STRIDE;
   int* s_conn = s_conn_all + ty * 8;
 
-  for (int i = tid; i < L::SIZE; i += nthr) s_ref[i] = g.ref[i];
-  if (live && tx < 8) s_conn[tx] = g.conn[e * 8 + tx];
-  __syncthreads();
+  {
+    const int64_t left = g.ne - e0;
+    stage_hex8_tables(g.ref, s_ref, g.conn + e0 * 8, left < EPB ? int(left) : EPB, s_conn_all,
+                      reinterpret_cast<uint64_t*>(s_conn_all + EPB * 8), tid, nthr);
+  }
   if (live) {
     for (int i = tx; i < 24; i += TPE) {
       const int a = i / 3, d = i % 3;

@@ -1,6 +1,9 @@
 // fec_mech_neohookean.cu -- instantiations of the mechanics element kernel for the
 // NeoHookean constitutive model.
 #include <cstdlib>
+#include <cstdio>
+#include <type_traits>
+#include "fec_autotune.h"
 #include "fec_launch.h"
 #include "fec_mech_hex8.cuh"
 
@@ -34,6 +37,45 @@ cudaError_t by_prec(int precision, bool want_r, bool want_k, const ElemArgs& a, 
   if (precision == 0) return go<ET, EPB, CSPLIT, double>(want_r, want_k, a, s, launches);
   if (precision == 1) return go<ET, EPB, CSPLIT, float>(want_r, want_k, a, s, launches);
   return cudaErrorNotSupported;
+}
+
+// Autotuned generic kernels: elements per CTA for tet4/tet10, column split
+// (threads per element) for hex27.
+template <int ET, typename Real, bool R, bool K>
+cudaError_t tuned1(const ElemArgs& a, cudaStream_t s) {
+  constexpr const char* P = std::is_same<Real, double>::value ? "fp64" : "fp32_element";
+  char fam[96];
+  snprintf(fam, sizeof fam, "neohookean/%s/%s/%s", ET == 6 ? "tet4" : (ET == 7 ? "tet10" : "hex27"), P,
+           R && K ? "R+K" : (R ? "R" : "K"));
+  if constexpr (ET == 6) {
+    static const TuneCandidate c[] = {{"EPB=8", go1<6, 8, 1, Real, R, K>}, {"EPB=16", go1<6, 16, 1, Real, R, K>},
+                                      {"EPB=32", go1<6, 32, 1, Real, R, K>}};
+    return tuned_launch(fam, c, 3, 1, a, s);
+  } else if constexpr (ET == 7) {
+    static const TuneCandidate c[] = {{"EPB=4", go1<7, 4, 1, Real, R, K>}, {"EPB=8", go1<7, 8, 1, Real, R, K>},
+                                      {"EPB=16", go1<7, 16, 1, Real, R, K>}};
+    return tuned_launch(fam, c, 3, 1, a, s);
+  } else {
+    static const TuneCandidate c[] = {{"EPB=1 CSPLIT=3", go1<8, 1, 3, Real, R, K>},
+                                      {"EPB=2 CSPLIT=3", go1<8, 2, 3, Real, R, K>},
+                                      {"EPB=1 CSPLIT=9", go1<8, 1, 9, Real, R, K>}};
+    return tuned_launch(fam, c, 3, 0, a, s);
+  }
+}
+
+template <int ET>
+cudaError_t tuned(int precision, bool want_r, bool want_k, const ElemArgs& a, cudaStream_t s, int* launches) {
+  if (precision != 0 && precision != 1) return cudaErrorNotSupported;
+  if (a.ne <= 0 || (!want_r && !want_k)) return cudaSuccess;
+  ++*launches;
+  if (precision == 0) {
+    if (want_r && want_k) return tuned1<ET, double, true, true>(a, s);
+    if (want_r) return tuned1<ET, double, true, false>(a, s);
+    return tuned1<ET, double, false, true>(a, s);
+  }
+  if (want_r && want_k) return tuned1<ET, float, true, true>(a, s);
+  if (want_r) return tuned1<ET, float, true, false>(a, s);
+  return tuned1<ET, float, false, true>(a, s);
 }
 
 template <typename Real, int EPB, bool R, bool K>
@@ -120,9 +162,9 @@ cudaError_t launch_mech_neohookean(int elem_type, int precision, bool want_r, bo
                              : hex8_df64<8>(want_r, want_k, a, s, launches);
       if (precision == 1) return hex8_f32<16>(want_r, want_k, a, s, launches);
       return cudaErrorNotSupported;
-    case 6: return by_prec<6, 16, 1>(precision, want_r, want_k, a, s, launches);
-    case 7: return by_prec<7, 8, 1>(precision, want_r, want_k, a, s, launches);
-    case 8: return by_prec<8, 1, 3>(precision, want_r, want_k, a, s, launches);
+    case 6: return tuned<6>(precision, want_r, want_k, a, s, launches);
+    case 7: return tuned<7>(precision, want_r, want_k, a, s, launches);
+    case 8: return tuned<8>(precision, want_r, want_k, a, s, launches);
     default: return cudaErrorNotSupported;
   }
 }

@@ -311,3 +311,12 @@ def assemble_residual_and_stiffness(asm: SparseMatrixAssembler, Uu, p: Parameter
 __all__ = ["SparseMatrixAssembler", "CSCMatrix", "Parameters", "create_parameters", "update_dofs_bcs",
            "assemble_vector", "assemble_stiffness", "assemble_matrix", "assemble_residual_and_stiffness",
            "residual", "stiffness", "ELEMENT_IDS"]
+
+
+def autotune_report() -> list[str]:
+    """Launch configurations chosen by the library's autotuner (one line per
+    kernel family and problem-size bucket, with every candidate's time)."""
+    lib = _lib.load()
+    buf = C.create_string_buffer(1 << 16)
+    lib.fec_autotune_report(buf, len(buf))
+    return [ln for ln in buf.value.decode().splitlines() if ln]

@@ -224,6 +224,13 @@ int fec_kernel_times(fec_ctx* ctx, float* ms, int cap, char* names, size_t len);
 int fec_probe_fma_rate(int device, int precision, double* tflops);
 
 /* Sizes the context knows (any pointer may be NULL). */
+/* Launch configurations the autotuner chose for the generic element kernels
+ * (tet4/tet10/hex27: elements per CTA, threads per element), one text line per
+ * tuned kernel family and problem-size bucket with every candidate's time.
+ * Returns the number of lines.  Tuning happens on a family's first launch
+ * outside CUDA-graph capture; FEC_AUTOTUNE=0 keeps the defaults.  No
+ * counterpart in the reference. */
+int fec_autotune_report(char* buf, size_t len);
 int fec_sizes(const fec_ctx* ctx, int64_t* num_nodes, int64_t* num_elems, int64_t* num_unknowns, int64_t* nnz,
               int64_t* state_len);
 

@@ -83,3 +83,40 @@ def test_newton_loop_graph_replays_eager_bits(fec, precision):
     graph.replay()
     torch.cuda.synchronize()
     assert not torch.equal(eager.unknowns(0), graph.unknowns(0))
+
+
+def test_autotuned_generic_kernels_are_bitwise_identical(fec):
+    """Every launch configuration the autotuner may pick for the tet4/tet10/hex27
+    kernels (elements per CTA, threads per element) gives bitwise the same
+    residual and nzval, in FP64 and FP32-element arithmetic; the tuned run
+    reports its choices."""
+    import os
+    torch = _torch()
+    from fec_gb300 import batching
+    from helpers import stretch_field
+    mesh = batching.mixed_mesh(3, 3, 2)
+    results = {}
+    for precision in ("fp64", "fp32_element"):
+        for cand in ("0", "1", "2", None):
+            if cand is None:
+                os.environ.pop("FEC_AUTOTUNE_CANDIDATE", None)
+            else:
+                os.environ["FEC_AUTOTUNE_CANDIDATE"] = cand
+            try:
+                asm = fec.SparseMatrixAssembler(fec.VectorFunction(fec.FunctionSpace(mesh), "u"), device=0,
+                                                precision=precision)
+                p = fec.create_parameters(mesh, asm, fec.NeoHookean.from_youngs(1.0, 0.3))
+                U = stretch_field(mesh.nodal_coords, seed=2).ravel()
+                Uu = torch.from_numpy(U[asm.dof.unknown_dofs - 1].copy()).cuda()
+                R, K = fec.assemble_residual_and_stiffness(asm, Uu, p)
+                torch.cuda.synchronize()
+                results[(precision, cand)] = (R.cpu().numpy().copy(), K.nzval.cpu().numpy().copy())
+            finally:
+                os.environ.pop("FEC_AUTOTUNE_CANDIDATE", None)
+        ref = results[(precision, "0")]
+        for cand in ("1", "2", None):
+            assert np.array_equal(results[(precision, cand)][0], ref[0])
+            assert np.array_equal(results[(precision, cand)][1], ref[1])
+    report = fec.autotune_report()
+    print("\n".join(report))
+    assert any("hex27" in line for line in report) and any("tet10" in line for line in report)
