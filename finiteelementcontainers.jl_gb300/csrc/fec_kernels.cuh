@@ -151,6 +151,57 @@ __device__ __forceinline__ double map_point(const double* __restrict__ s_ref, in
   return det * s_ref[L::W_OFF + q];
 }
 
+// FP32 map of a 3-D point from FP64-differenced coordinates xd[a] = x[a] - x[0]
+// (J = sum_a xd_a (x) dN_a, since sum_a dN_a = 0); falls back to the FP64 map
+// for distorted elements (Hadamard ratio |det J| / prod |J col| < 0.25).
+// Returns JxW.
+template <int ET>
+__device__ __forceinline__ float map_point_mixed(const double* __restrict__ s_ref, const float* __restrict__ s_reff,
+                                                 int q, const double* __restrict__ x, const float* __restrict__ xd,
+                                                 float* __restrict__ dNX) {
+  using E = Elem<ET>;
+  using L = RefLayout<ET>;
+  constexpr int A = E::NNPE;
+  static_assert(E::DIM == 3, "3-D elements");
+  const float* dN = s_reff + L::DN_OFF + q * A * 3;
+  float J[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+#pragma unroll
+  for (int a = 1; a < A; ++a)
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) J[d][k] = fmaf(xd[a * 3 + d], dN[a * 3 + k], J[d][k]);
+  const float c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+  const float c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  const float c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  const float det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+  float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    n0 = fmaf(J[d][0], J[d][0], n0);
+    n1 = fmaf(J[d][1], J[d][1], n1);
+    n2 = fmaf(J[d][2], J[d][2], n2);
+  }
+  if (!(fabsf(det) >= 0.25f * sqrtf(n0 * n1 * n2))) return float(map_point<ET, float>(s_ref, q, x, dNX, nullptr));
+  const float r = 1.0f / det;
+  float Ji[3][3];
+  Ji[0][0] = c00 * r;
+  Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
+  Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+  Ji[1][0] = c01 * r;
+  Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+  Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
+  Ji[2][0] = c02 * r;
+  Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * r;
+  Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+#pragma unroll
+  for (int a = 0; a < A; ++a)
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      dNX[a * 3 + d] = fmaf(dN[a * 3], Ji[0][d], fmaf(dN[a * 3 + 1], Ji[1][d], dN[a * 3 + 2] * Ji[2][d]));
+  return det * s_reff[L::W_OFF + q];
+}
+
 // Copy the reference tables and gather X (and U) of each element of the CTA
 // into shared memory.  Threads of element slot ty use tx = 0..TPE-1.
 template <int ET, int NF, int EPB, int TPE>
@@ -510,6 +561,9 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
   // (hi, lo) splits of the shape gradients and of A (written over A in place)
   constexpr bool DF = std::is_same<Real, double>::value;
   float2* s_dNXf_all = reinterpret_cast<float2*>(s_conn_all + ((EPB * A + 3) & ~3));
+  // FP32-element: FP32 copy of the reference tables, FP64-differenced coordinates
+  float* s_reff = reinterpret_cast<float*>(s_conn_all + ((EPB * A + 3) & ~3));
+  float* s_xd_all = s_reff + ((L::SIZE + 3) & ~3);
 
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int64_t e = int64_t(blockIdx.x) * EPB + ty;
@@ -523,12 +577,23 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
   float2* s_dNXf = s_dNXf_all + ty * NQ * A * D;
   stage_element<ET, 3, EPB, TPE>(g, e, tx, ty, s_ref, s_conn_all + ty * A, s_x, s_u);
   const bool live = e < g.ne;
+  float* s_xd = s_xd_all + ty * A * D;
+  if constexpr (!DF) {
+    for (int i = ty * TPE + tx; i < L::SIZE; i += EPB * TPE) s_reff[i] = float(s_ref[i]);
+    if (live)
+      for (int i = tx; i < A * D; i += TPE) s_xd[i] = float(s_x[i] - s_x[i % D]);
+    __syncthreads();
+  }
 
   // quadrature-point kinematics + constitutive update (one thread per point)
   if (live) {
     for (int q = tx; q < NQ; q += TPE) {
       Real* dNX = s_dNX + q * A * D;
-      const double jxw = map_point<ET, Real>(s_ref, q, s_x, dNX, nullptr);
+      double jxw;
+      if constexpr (DF)
+        jxw = map_point<ET, Real>(s_ref, q, s_x, dNX, nullptr);
+      else
+        jxw = map_point_mixed<ET>(s_ref, s_reff, q, s_x, s_xd, dNX);
       s_jxw[q] = Real(jxw);
       Real gu[3][3];
 #pragma unroll
@@ -655,7 +720,8 @@ constexpr size_t mech_smem_bytes() {
   return sizeof(double) * (((RefLayout<ET>::SIZE + 1) & ~1) + 2 * EPB * A * 3) +
          sizeof(Real) * (EPB * NQ * A * 3 + EPB * NQ + EPB * NQ * 9 + EPB * NQ * Model::SCR +
                          (WANT_K ? EPB * NQ * 81 : 0)) +
-         sizeof(int) * ((EPB * A + 3) & ~3) + (DF && WANT_K ? sizeof(float2) * EPB * NQ * A * 3 : 0) + 16;
+         sizeof(int) * ((EPB * A + 3) & ~3) + (DF && WANT_K ? sizeof(float2) * EPB * NQ * A * 3 : 0) +
+         (DF ? 0 : sizeof(float) * (((RefLayout<ET>::SIZE + 3) & ~3) + EPB * A * 3)) + 16;
 }
 
 // ---------------------------------------------------------------------------
