@@ -29,6 +29,13 @@ cudaError_t launch_poisson(int elem_type, int precision, bool want_r, bool want_
 cudaError_t launch_mech(int physics, int elem_type, int precision, bool want_r, bool want_k, const ElemArgs& args,
                         cudaStream_t stream, int* launches);
 cudaError_t launch_gather(int precision, int nf, const GatherArgs& args, cudaStream_t stream, int* launches);
+// Hex27 FP32-element mechanics with the element-stiffness contraction on the
+// tensor cores (physics 2 Neo-Hookean, 3 J2); a wait that gives up sets the
+// flag fec_tensor_core_status reads.
+cudaError_t launch_hex27_tc(int physics, bool want_r, bool want_k, const ElemArgs& args, cudaStream_t stream,
+                            int* launches);
+// FEC_HEX27_ON_CUDA_CORES=1 keeps hex27 FP32-element blocks on the generic kernel.
+bool hex27_on_cuda_cores();
 
 // Reference-element tables (RefLayout order) for an element type, in double.
 // Returns the number of doubles written (0 for an unknown type).

@@ -164,7 +164,9 @@ cudaError_t launch_mech_j2(int elem_type, int precision, bool want_r, bool want_
       return cudaErrorNotSupported;
     case 6: return tuned<6>(precision, want_r, want_k, a, s, launches);
     case 7: return tuned<7>(precision, want_r, want_k, a, s, launches);
-    case 8: return tuned<8>(precision, want_r, want_k, a, s, launches);
+    case 8:
+      if (precision == 1 && !hex27_on_cuda_cores()) return launch_hex27_tc(3, want_r, want_k, a, s, launches);
+      return tuned<8>(precision, want_r, want_k, a, s, launches);
     default: return cudaErrorNotSupported;
   }
 }

@@ -231,6 +231,11 @@ int fec_probe_fma_rate(int device, int precision, double* tflops);
  * outside CUDA-graph capture; FEC_AUTOTUNE=0 keeps the defaults.  No
  * counterpart in the reference. */
 int fec_autotune_report(char* buf, size_t len);
+/* FEC_OK, or FEC_ERR_DEVICE if a tensor-core element kernel (hex27
+ * FP32-element) on the current device gave up waiting for its MMAs (its
+ * results are then invalid); reset clears the flag.  Synchronous.  No
+ * counterpart in the reference. */
+int fec_tensor_core_status(int reset);
 int fec_sizes(const fec_ctx* ctx, int64_t* num_nodes, int64_t* num_elems, int64_t* num_unknowns, int64_t* nnz,
               int64_t* state_len);
 

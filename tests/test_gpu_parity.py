@@ -176,6 +176,45 @@ def test_higher_order_and_simplex_elements(fec, orc, kind):
     assert max(rel_err(nz, nzo)) <= TOL64
 
 
+@pytest.mark.parametrize("kind", ["tet4", "tet10", "hex27"])
+@pytest.mark.parametrize("phys_name", ["neohookean", "j2"])
+def test_higher_order_fp32_element(fec, orc, kind, phys_name):
+    """FP32-element tet4/tet10/hex27 against the FP64 oracle.  Hex27 runs its
+    element-stiffness contraction on the tensor cores (tcgen05 kind::tf32 with a
+    two-term split); it is also checked against the CUDA-core kernel."""
+    import os
+    gen = {"tet4": fec.meshes.box_tet4, "tet10": fec.meshes.box_tet10, "hex27": fec.meshes.box_hex27}[kind]
+    mesh = gen((4, 4, 4))
+    if phys_name == "neohookean":
+        phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+        U = stretch_field(mesh.nodal_coords, seed=2).ravel()
+    else:
+        phys = fec.J2Plasticity(200.0, 0.3, 0.25, 2.0)
+        U = 3.0 * stretch_field(mesh.nodal_coords, seed=2, noise=1e-4, diag=(1.004, 0.999, 0.999)).ravel()
+    asm, p = _setup(fec, mesh, "vector", phys, precision="fp32_element")
+    R, nz, K = _run(fec, asm, p, U)
+    nq = {"tet4": 1, "tet10": 4, "hex27": 27}[kind]
+    ne = mesh.num_elements()
+    st = np.zeros(7 * nq * ne) if phys_name == "j2" else None
+    Ro, colptr, rowval, nzo = _oracle(orc, mesh, phys_name, phys.create_properties(), U, asm, st,
+                                      None if st is None else np.zeros_like(st))
+    assert np.array_equal(K.colptr, colptr) and np.array_equal(K.rowval, rowval)
+    e_r, e_k = rel_err(R, Ro), rel_err(nz, nzo)
+    print(kind, phys_name, "fp32-element vs FP64 oracle: residual", e_r, "nzval", e_k)
+    assert max(e_r) <= TOL32 and max(e_k) <= TOL32
+    if kind == "hex27":
+        assert fec.load_library().fec_tensor_core_status(1) == 0
+        os.environ["FEC_HEX27_ON_CUDA_CORES"] = "1"
+        try:
+            asm2, p2 = _setup(fec, mesh, "vector", phys, precision="fp32_element")
+            R2, nz2, _ = _run(fec, asm2, p2, U)
+        finally:
+            del os.environ["FEC_HEX27_ON_CUDA_CORES"]
+        print("hex27 tensor cores vs CUDA cores: residual", rel_err(R, R2), "nzval", rel_err(nz, nz2))
+        assert np.array_equal(R, R2)  # the residual is formed on the CUDA cores either way
+        assert max(rel_err(nz, nz2)) <= 2e-6
+
+
 def test_j2_one_load_step_with_state(fec, orc):
     torch = _torch()
     n = 6
