@@ -389,8 +389,12 @@ def run_batched(args) -> None:
     from fec_gb300 import batching
     from fec_gb300.workloads import stretch_field
     torch.cuda.set_device(0)
-    meshes = {"batch64": batching.box_batch(batching.lognormal_cube_sides()).mesh,
-              "tet4_tet10_hex27": batching.mixed_mesh(32, 32, 46)}
+    if args.n:  # reduced case (profiling): 8 meshes and an n^3-box mixed mesh
+        meshes = {"batch8": batching.box_batch(batching.lognormal_cube_sides(count=8)).mesh,
+                  "tet4_tet10_hex27": batching.mixed_mesh(args.n, args.n, args.n)}
+    else:
+        meshes = {"batch64": batching.box_batch(batching.lognormal_cube_sides()).mesh,
+                  "tet4_tet10_hex27": batching.mixed_mesh(32, 32, 46)}
     phys = fec.NeoHookean.from_youngs(1.0, 0.3)
     systems, info = [], {}
     total_ne, alg = 0, 0

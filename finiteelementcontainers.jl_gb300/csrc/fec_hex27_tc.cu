@@ -5,10 +5,12 @@
 // C_q[(i,J),(b,k)] = sum_L A_q[iJkL] dN_bL(q) (A JxW-scaled).  Stacking i into
 // the rows makes it one GEMM per element:
 //     D[(i,b,k), a] = sum_{(q,J)} C[(i,b,k),(q,J)] * G[a,(q,J)],  K_(a,i),(b,k) = D[(i,b,k), a]
-// with M = 243 rows (two M = 128 tiles), N = 27 (padded to 32), K = 81 (q,J)
-// pairs (padded to 88).  The CUDA cores build C in K chunks of 8 (double
-// buffered) while the tensor cores (tcgen05.mma kind::tf32, FP32 accumulators
-// in tensor memory) consume the previous chunk; every operand is a two-term
+// with M = 243 rows (two M = 128 tiles), N = 27 (padded to 32) and K = (q,J)
+// with J padded to 4, so that one K chunk of 8 is exactly two quadrature points
+// (K = 28 x 4 = 112).  The CUDA cores build C chunk by chunk (double buffered,
+// shape gradients and tangent entries packed as float4) while the tensor cores
+// (tcgen05.mma kind::tf32, FP32 accumulators in tensor memory) consume the
+// previous chunk; every operand is a two-term
 // TF32 split hi + lo and each product takes hi*hi + lo*hi + hi*lo, which keeps
 // the contraction at FP32 accuracy.  The per-point map, constitutive update and
 // the residual stay on the CUDA cores, as in the generic kernel.
@@ -20,26 +22,27 @@
 namespace fec {
 namespace h27 {
 
-constexpr int A = 27, NQ = 27, ND = 81, KP = 88;          // nodes, points, dofs, padded (q, J) count
+constexpr int A = 27, NQ = 27, ND = 81, KP = 112;         // nodes, points, dofs, padded (q, J) count
+constexpr int NCHUNK = KP / 8;                            // 14 chunks of two points
 constexpr int NTHR = 256;
-constexpr uint32_t SBO_G = (KP / 4) * 128;                // 2816: 8-row groups of the G operand
-constexpr uint32_t S_GHI = 0, S_GLO = S_GHI + 4 * SBO_G;  // 32 x 88 tf32 each
+constexpr uint32_t SBO_G = (KP / 4) * 128;                // 3584: 8-row groups of the G operand
+constexpr uint32_t S_GHI = 0, S_GLO = S_GHI + 4 * SBO_G;  // 32 x 112 tf32 each
 constexpr uint32_t S_AOP = S_GLO + 4 * SBO_G;             // 2 buffers x (hi, lo) x 256 x 8 tf32
 __host__ __device__ constexpr uint32_t AOP(int buf, int term) { return S_AOP + uint32_t(buf * 2 + term) * 8192; }
 constexpr uint32_t S_REFF = S_AOP + 4 * 8192;             // floats: reference tables
 constexpr int REF = RefLayout<8>::SIZE;
 constexpr uint32_t S_X = S_REFF + ((REF * 4 + 15) & ~15);  // doubles: 81 coordinates
-constexpr uint32_t S_U = S_X + ND * 8;                     // doubles: 81 displacements
-constexpr uint32_t S_XD = S_U + ND * 8;                    // floats: 81 differenced coordinates
+constexpr uint32_t S_U = S_X + ND * 8;                     // floats: 81 displacements
+constexpr uint32_t S_XD = S_U + 336;                       // floats: 81 differenced coordinates
 constexpr uint32_t S_CONN = S_XD + 336;                    // 27 ints
-constexpr uint32_t S_DNX = S_CONN + 112;                   // floats: 27 points x 81
-constexpr uint32_t S_P = S_DNX + NQ * ND * 4;              // floats: 27 x 9
+constexpr uint32_t S_DN4 = (S_CONN + 112 + 15) & ~15u;     // float4 [q][a]: dN_a(q) (x, y, z, 0)
+constexpr uint32_t S_P = S_DN4 + NQ * A * 16;              // floats: 27 x 9
 constexpr uint32_t S_SCR = S_P + NQ * 9 * 4;               // floats: 27 x 24 (model scratch)
-constexpr uint32_t S_AT = S_SCR + NQ * 24 * 4;             // floats: 27 x 81 tangent entries
-constexpr uint32_t S_BAR = (S_AT + NQ * ND * 4 + 15) & ~15u; // 2 mbarriers
+constexpr uint32_t S_A4 = (S_SCR + NQ * 24 * 4 + 15) & ~15u;  // float4 [q][i][J][k]: A_iJk(0..2)
+constexpr uint32_t S_BAR = S_A4 + NQ * 27 * 16;            // 2 mbarriers
 constexpr uint32_t S_TSLOT = S_BAR + 16;
 constexpr uint32_t SMEM = S_TSLOT + 16;
-static_assert(S_X % 16 == 0 && S_DNX % 16 == 0 && S_BAR % 8 == 0, "alignment");
+static_assert(S_X % 16 == 0 && S_DN4 % 16 == 0 && S_A4 % 16 == 0 && S_BAR % 8 == 0, "alignment");
 static_assert(SMEM <= 113 * 1024, "two CTAs per SM");
 constexpr long long WAIT_BUDGET = 2000000000LL;
 
@@ -68,19 +71,18 @@ constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(32 >> 
 template <class Model, bool WANT_R, bool WANT_K>
 __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err) {
   using namespace tc;
-  using L = RefLayout<8>;
   constexpr int NS = Model::NS, SCR = Model::SCR;
   static_assert(SCR <= 24, "model scratch");
   extern __shared__ __align__(1024) unsigned char sm[];
   float* s_reff = reinterpret_cast<float*>(sm + S_REFF);
   double* s_x = reinterpret_cast<double*>(sm + S_X);
-  double* s_u = reinterpret_cast<double*>(sm + S_U);
+  float* s_u = reinterpret_cast<float*>(sm + S_U);
   float* s_xd = reinterpret_cast<float*>(sm + S_XD);
   int* s_conn = reinterpret_cast<int*>(sm + S_CONN);
-  float* s_dnx = reinterpret_cast<float*>(sm + S_DNX);
+  float4* s_dn4 = reinterpret_cast<float4*>(sm + S_DN4);
   float* s_P = reinterpret_cast<float*>(sm + S_P);
   float* s_scr = reinterpret_cast<float*>(sm + S_SCR);
-  float* s_A = reinterpret_cast<float*>(sm + S_AT);
+  float4* s_a4 = reinterpret_cast<float4*>(sm + S_A4);
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + S_BAR);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t s0 = smem_u32(sm);
@@ -100,6 +102,8 @@ __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err)
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + S_TSLOT);
   uint32_t ph[2] = {0u, 0u};
   bool failed = false;
+  // this thread's row of C: (i, b, k)
+  const int row = tid, ri = row / ND, rb = (row % ND) / 3, rk = row % 3;
 
   for (int64_t e = blockIdx.x; e < g.ne && !failed; e += gridDim.x) {
     // ---- staging ----
@@ -108,7 +112,7 @@ __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err)
     if (tid < ND) {
       const int a = tid / 3, d = tid % 3;
       s_x[tid] = __ldg(&g.coords[int64_t(s_conn[a]) * 3 + d]);
-      s_u[tid] = __ldg(&g.U[int64_t(s_conn[a]) * 3 + d]);
+      s_u[tid] = float(__ldg(&g.U[int64_t(s_conn[a]) * 3 + d]));
     }
     __syncthreads();
     if (tid < ND) s_xd[tid] = float(s_x[tid] - s_x[tid % 3]);
@@ -116,7 +120,7 @@ __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err)
     // ---- per point: map, displacement gradient, constitutive update ----
     if (tid < NQ) {
       const int q = tid;
-      float* dNX = s_dnx + q * ND;
+      float dNX[ND];
       const float jxw = map_point_mixed<8>(g.ref, s_reff, q, s_x, s_xd, dNX);
       float gu[3][3];
 #pragma unroll
@@ -124,48 +128,49 @@ __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err)
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
           float s = 0.f;
-          for (int a = 0; a < A; ++a) s = fmaf(float(s_u[a * 3 + i]), dNX[a * 3 + j], s);
+#pragma unroll
+          for (int a = 0; a < A; ++a) s = fmaf(s_u[a * 3 + i], dNX[a * 3 + j], s);
           gu[i][j] = s;
         }
+#pragma unroll
+      for (int a = 0; a < A; ++a) s_dn4[q * A + a] = make_float4(dNX[a * 3], dNX[a * 3 + 1], dNX[a * 3 + 2], 0.f);
       const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
       double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
       Model::point(g.props, gu, jxw, so, sn, s_P + q * 9, s_scr + q * SCR);
     }
     __syncthreads();
-    // ---- tangent entries, G operand, residual ----
+    // ---- tangent entries (float4 per (q,i,J,k)), G operand, residual ----
     if (WANT_K && tid < NQ * 3) {
       const int q = tid / 3, i = tid % 3;
-      Model::aentries(s_scr + q * SCR, i, s_A + q * ND + i * 27);
+      float out[27];
+      Model::aentries(s_scr + q * SCR, i, out);
+#pragma unroll
+      for (int jk = 0; jk < 9; ++jk)
+        s_a4[(q * 3 + i) * 9 + jk] = make_float4(out[jk * 3], out[jk * 3 + 1], out[jk * 3 + 2], 0.f);
     }
     if (WANT_K) {
-      // G[a, (q,J)] = dN_aJ(q), (q,J) = 3q + J
-      for (int w = tid; w < A * (ND / 4 + 1); w += NTHR) {
-        const int a = w / (ND / 4 + 1), c4 = w % (ND / 4 + 1);
-        float v[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int kk = 4 * c4 + j;
-          v[j] = kk < ND ? s_dnx[(kk / 3) * ND + a * 3 + kk % 3] : 0.f;
-        }
-        store4_split(sm + S_GHI, sm + S_GLO, a, 4 * c4, SBO_G, v);
+      // G[a, 4q + J] = dN_aJ(q), J = 3 a zero pad
+      for (int w = tid; w < A * NQ; w += NTHR) {
+        const int a = w / NQ, q = w % NQ;
+        const float4 d = s_dn4[q * A + a];
+        const float v[4] = {d.x, d.y, d.z, 0.f};
+        store4_split(sm + S_GHI, sm + S_GLO, a, 4 * q, SBO_G, v);
       }
     }
     if (WANT_R && tid < ND) {
       const int a = tid / 3, i = tid % 3;
       float R = 0.f;
       for (int q = 0; q < NQ; ++q) {
-        const float* dN = s_dnx + q * ND + a * 3;
+        const float4 dN = s_dn4[q * A + a];
         const float* P = s_P + q * 9 + i * 3;
-        R = fmaf(dN[0], P[0], fmaf(dN[1], P[1], fmaf(dN[2], P[2], R)));
+        R = fmaf(dN.x, P[0], fmaf(dN.y, P[1], fmaf(dN.z, P[2], R)));
       }
       static_cast<float*>(g.Re)[e * ND + tid] = R;
     }
     __syncthreads();
     if (!WANT_K) continue;
-    // ---- C chunks of 8 (q,J) pairs, double buffered against the MMAs ----
-    const int row = tid;  // (i, b, k) for row < 243
-    const int ri = row / ND, rb = (row % ND) / 3, rk = row % 3;
-    for (int c = 0; c < KP / 8; ++c) {
+    // ---- C chunks (two points each), double buffered against the MMAs ----
+    for (int c = 0; c < NCHUNK; ++c) {
       const int buf = c & 1;
       if (c >= 2) {
         const bool ok = mbar_wait(&bar[buf], ph[buf], WAIT_BUDGET);
@@ -178,16 +183,20 @@ __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err)
       if (row < 3 * ND) {
         float v[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int kk = 8 * c + j;
-          float s = 0.f;
-          if (kk < ND) {
-            const int q = kk / 3, J = kk % 3;
-            const float* Aq = s_A + q * ND + ri * 27 + J * 9 + rk * 3;
-            const float* dN = s_dnx + q * ND + rb * 3;
-            s = fmaf(Aq[0], dN[0], fmaf(Aq[1], dN[1], Aq[2] * dN[2]));
+        for (int h = 0; h < 2; ++h) {
+          const int q = 2 * c + h;
+          if (q < NQ) {
+            const float4 d = s_dn4[q * A + rb];
+#pragma unroll
+            for (int J = 0; J < 3; ++J) {
+              const float4 t = s_a4[((q * 3 + ri) * 3 + J) * 3 + rk];
+              v[4 * h + J] = fmaf(t.x, d.x, fmaf(t.y, d.y, t.z * d.z));
+            }
+            v[4 * h + 3] = 0.f;
+          } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) v[4 * h + j] = 0.f;
           }
-          v[j] = s;
         }
         store4_split(sm + AOP(buf, 0), sm + AOP(buf, 1), row, 0, 256, v);
         store4_split(sm + AOP(buf, 0), sm + AOP(buf, 1), row, 4, 256, v + 4);
@@ -211,12 +220,12 @@ __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err)
       }
     }
     if (failed) break;
-    // the last two chunks' barriers (chunk 9 on buffer 1, chunk 10 on buffer 0)
+    // the last two chunks' barriers (chunk 12 on buffer 0, chunk 13 on buffer 1)
     {
-      bool ok = mbar_wait(&bar[1], ph[1], WAIT_BUDGET);
-      ph[1] ^= 1u;
-      ok = mbar_wait(&bar[0], ph[0], WAIT_BUDGET) && ok;
+      bool ok = mbar_wait(&bar[0], ph[0], WAIT_BUDGET);
       ph[0] ^= 1u;
+      ok = mbar_wait(&bar[1], ph[1], WAIT_BUDGET) && ok;
+      ph[1] ^= 1u;
       if (__syncthreads_or(!ok)) {
         failed = true;
         break;
