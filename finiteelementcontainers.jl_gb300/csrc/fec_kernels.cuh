@@ -894,9 +894,9 @@ __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo&
 // blocks have different element sizes).
 template <typename Real, int NF>
 __device__ __forceinline__ void gather_run_generic(const GatherArgs& g, const BlockInfo& B, int64_t p, int64_t pend,
-                                                   unsigned um, int Ln, float* acc, float2& racc, int lane,
+                                                   unsigned um, bool fast, int Ln, float* acc, float2& racc, int lane,
                                                    bool wantK, bool wantR) {
-  const int A = B.nnpe, NDOF = B.ndof, TOTAL = NF * B.ndof;
+  const int A = B.nnpe, NDOF = B.ndof;
   const bool node_rows = B.layout == KE_NODE_ROWS;
   const Real* Ke = static_cast<const Real*>(g.Ke) + B.ke_off;
   const Real* Re = static_cast<const Real*>(g.Re) + B.re_off;
@@ -908,15 +908,24 @@ __device__ __forceinline__ void gather_run_generic(const GatherArgs& g, const Bl
     if (wantK) {
       const Real* Krows = Ke + (le * NDOF + int64_t(a) * NF) * NDOF;
       const uint16_t* ep = g.epos + B.epos_off + (le * A + a) * A;
-      for (int t = lane; t < TOTAL; t += 32) {
-        const int k = t / NDOF, rem = t - k * NDOF;
-        const int b = rem / NF, i = rem - b * NF;
+      const int32_t* cn = g.conn + B.conn_off + le * A;
+#pragma unroll
+      for (int k = 0; k < NF; ++k) {
         if (!((um >> k) & 1u)) continue;
-        const unsigned umm = g.umask[g.conn[B.conn_off + le * A + b]] & ~UMASK_FULL_NBR;
-        if (!((umm >> i) & 1u)) continue;
-        const int off = node_rows ? (k * NF + i) * A + b : t;
-        GatherAcc::add(acc, __popc(um & ((1u << k) - 1u)) * Ln + ep[b] + __popc(umm & ((1u << i) - 1u)),
-                             Krows[off]);
+        const int kb = __popc(um & ((1u << k) - 1u)) * Ln;
+        // lanes over the element's columns (b, i) of row component k
+        for (int rem = lane; rem < NDOF; rem += 32) {
+          const int b = rem / NF, i = rem - b * NF;
+          int pos;
+          if (fast) {  // every neighbour component is unknown: no mask lookups
+            pos = kb + ep[b] + i;
+          } else {
+            const unsigned umm = g.umask[cn[b]] & ~UMASK_FULL_NBR;
+            if (!((umm >> i) & 1u)) continue;
+            pos = kb + ep[b] + __popc(umm & ((1u << i) - 1u));
+          }
+          GatherAcc::add(acc, pos, Krows[node_rows ? (k * NF + i) * A + b : k * NDOF + rem]);
+        }
       }
       __syncwarp();
     }
@@ -1026,11 +1035,11 @@ __global__ void __launch_bounds__(WPB * 32, MINB) node_gather_kernel(GatherArgs 
       if (fast && B.layout == KE_NODE_ROWS)
         gather_run_hex8v<Real>(g, B, p, q, Ln, acc, racc, lane, wantK, wantR);
       else
-        gather_run_generic<Real, NF>(g, B, p, q, um, Ln, acc, racc, lane, wantK, wantR);
+        gather_run_generic<Real, NF>(g, B, p, q, um, fast, Ln, acc, racc, lane, wantK, wantR);
     } else if constexpr (A > 0) {
       gather_run<Real, NF, A, BUDGET>(g, B, p, q, um, fast, Ln, acc, racc, lane, wantK, wantR);
     } else {
-      gather_run_generic<Real, NF>(g, B, p, q, um, Ln, acc, racc, lane, wantK, wantR);
+      gather_run_generic<Real, NF>(g, B, p, q, um, fast, Ln, acc, racc, lane, wantK, wantR);
     }
     p = q;
   }
