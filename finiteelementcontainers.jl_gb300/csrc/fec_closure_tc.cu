@@ -1,6 +1,6 @@
 // fec_closure_tc.cu -- the learned J2 closure on the 5th-generation tensor cores.
 //
-// A persistent CTA of 256 threads takes 16 hex8 elements (128 quadrature points,
+// A persistent CTA of 512 threads takes 16 hex8 elements (128 quadrature points,
 // the M = 128 of one tcgen05 MMA) at a time:
 //   A  element staging, isoparametric map and displacement gradient per point,
 //      trial state; elastic points are completed exactly, plastic points write
@@ -11,7 +11,7 @@
 //      accumulators in tensor memory.  The activation row uses a two-term BF16
 //      split of activations and weights (hi*Whi + lo*Whi + hi*Wlo), which keeps
 //      the stress near FP32 accuracy; tangent rows use one BF16 term.  Between
-//      layers the 8 warps read the accumulators back (tcgen05.ld), apply bias,
+//      layers the 16 warps read the accumulators back (tcgen05.ld), apply bias,
 //      SiLU and SiLU' and write the next operand tiles;
 //   C  per plastic point: stress and tangent from the outputs, the consistency
 //      check, and the exact return map where the check fails.
@@ -53,10 +53,13 @@ __host__ __device__ constexpr uint32_t S_TAN(int j) { return S_TAN0 + uint32_t(j
 constexpr uint32_t S_X0_H = S_TAN0 + 5 * 16384, S_X0_L = S_X0_H + 4096;  // 128 x 16 input rows (alias tangent 5)
 constexpr uint32_t S_BAR = S_TAN0 + 6 * 16384;                   // mbarriers: activation MMAs, tangent MMAs
 constexpr uint32_t S_TSLOT = S_BAR + 16;                         // TMEM base address
+constexpr uint32_t S_ABORT = S_BAR + 20;                         // set when an epilogue wait gave up
 constexpr uint32_t S_USER = S_BAR + 128;                         // 191,616: caller's region
 static_assert(S_IMG + IMG_BYTES <= S_ACT_H, "image overlaps the operand tiles");
 
-constexpr int NTHR = 256;
+constexpr int NEPI = 256;          // epilogue / point threads (warps 0..7)
+constexpr int NTHR = NEPI + 32;    // + one warp that only issues MMAs (warp 8)
+constexpr int CW = 64 * 128 / NEPI;  // hidden columns per thread in an epilogue (32)
 constexpr uint32_t TMEM_COLS = 512;          // 7 accumulators x 64 columns
 constexpr long long WAIT_BUDGET = 2000000000LL;  // SM clocks (about 1 s) before a wait gives up
 
@@ -168,60 +171,72 @@ __device__ __forceinline__ void silu_and_prime(float z, float& a, float& d) {
   d = s * (1.0f + z * (1.0f - s));
 }
 
-// Hidden layer l (0..3) epilogues, all 8 warps: warp w reads lanes 32 (w % 4) ..
+// Hidden layer l (0..3) epilogues, epilogue warps 0..7: warp w reads lanes 32 (w % 4) ..
 // (points), columns 32 (w / 4) .. +31 of the layer's 64 outputs.  The
 // activation part writes the next activation tiles and keeps SiLU' in d; the
 // tangent part scales the tangent accumulators by it (layer 0: the input seeds).
-__device__ __forceinline__ void epilogue_act(const Ctx& c, int l, float d[32]) {
+__device__ __forceinline__ void epilogue_act(const Ctx& c, int l, float d[CW]) {
   using namespace tc;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int qd = warp & 3, m = 32 * qd + lane, c0 = 32 * (warp >> 2);
+  const int qd = warp & 3, m = 32 * qd + lane, c0 = CW * (warp >> 2);
   const float* f = reinterpret_cast<const float*>(c.sm + S_IMG + F32);
   const uint32_t row = c.tmem + (uint32_t(32 * qd) << 16);
-  float z[32];
+  float z[CW];
   tmem_ld32(row + c0, z);
 #pragma unroll
-  for (int i = 0; i < 32; ++i) silu_and_prime(z[i] + f[FB + 64 * l + c0 + i], z[i], d[i]);
+  for (int i = 0; i < CW; ++i) silu_and_prime(z[i] + f[FB + 64 * l + c0 + i], z[i], d[i]);
 #pragma unroll
-  for (int k8 = 0; k8 < 4; ++k8) store8_split(c.sm + S_ACT_H, c.sm + S_ACT_L, m, c0 + 8 * k8, 64, z + 8 * k8);
+  for (int k8 = 0; k8 < CW / 8; ++k8) store8_split(c.sm + S_ACT_H, c.sm + S_ACT_L, m, c0 + 8 * k8, 64, z + 8 * k8);
 }
-__device__ __forceinline__ void epilogue_tan(const Ctx& c, int l, const float d[32]) {
+__device__ __forceinline__ void epilogue_tan(const Ctx& c, int l, const float d[CW]) {
   using namespace tc;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int qd = warp & 3, m = 32 * qd + lane, c0 = 32 * (warp >> 2);
+  const int qd = warp & 3, m = 32 * qd + lane, c0 = CW * (warp >> 2);
   const float* f = reinterpret_cast<const float*>(c.sm + S_IMG + F32);
   const uint32_t row = c.tmem + (uint32_t(32 * qd) << 16);
 #pragma unroll 1
   for (int j = 0; j < 6; j += 2) {
-    float t[2][32];
+    float t[2][CW];
     if (l == 0) {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
+      for (int i = 0; i < CW; ++i) {
         t[0][i] = d[i] * f[FW0T + (c0 + i) * 6 + j];
         t[1][i] = d[i] * f[FW0T + (c0 + i) * 6 + j + 1];
       }
     } else {
       tmem_ld32x2(row + 64u * (1 + j) + c0, row + 64u * (2 + j) + c0, t[0], t[1]);
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
+      for (int i = 0; i < CW; ++i) {
         t[0][i] *= d[i];
         t[1][i] *= d[i];
       }
     }
 #pragma unroll
-    for (int k8 = 0; k8 < 4; ++k8) {
+    for (int k8 = 0; k8 < CW / 8; ++k8) {
       store8(c.sm + S_TAN(j), m, c0 + 8 * k8, 64, t[0] + 8 * k8);
       store8(c.sm + S_TAN(j + 1), m, c0 + 8 * k8, 64, t[1] + 8 * k8);
     }
   }
 }
 
-// Operand tiles written by this thread -> visible to the tensor core; all
-// threads' TMEM reads done; then one thread may issue.
-__device__ __forceinline__ void sync_for_issue() {
+// Named barriers between the epilogue warps (arrive) and the issuer warp (sync):
+// 1 = activation operand tiles (or the input rows) ready, 2 = tangent tiles
+// ready; 3 = the epilogue warps among themselves.
+__device__ __forceinline__ void named_arrive(int id, int n) { asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+__device__ __forceinline__ void named_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+__device__ __forceinline__ void epi_sync() { named_sync(3, NEPI); }
+
+// Epilogue warps: operand tiles written by this thread visible to the tensor
+// core, this thread's TMEM reads complete, then signal the issuer.  After an
+// abort the epilogue warps wait for the issuer at each barrier instead of
+// arriving ahead of it, so no barrier generation is overrun.
+__device__ __forceinline__ void release_to_issuer(int id, bool ok) {
   tc::fence_async_smem();
   tc::tc_fence_before();
-  __syncthreads();
+  if (ok)
+    named_arrive(id, NTHR);
+  else
+    named_sync(id, NTHR);
 }
 
 __device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t& phase) {
@@ -230,46 +245,77 @@ __device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t& phase) {
   return ok;
 }
 
-// Runs the five layers on the operand rows already in S_X0_H/L.  Leaves the
-// output layer's accumulators in TMEM.  False (uniformly) if a wait gave up.
-// Schedule per layer: the activation MMAs of layer l+1 run while the warps
-// work through the tangent epilogue of layer l, and the tangent MMAs of layer
-// l+1 while they work through the activation epilogue of layer l+1.
-__device__ bool run_layers(Ctx& c) {
+// The issuer warp's part of one tile: layer l's MMAs as soon as the epilogue
+// warps release their operand tiles.  Issues nothing once the epilogue warps
+// have flagged an abort, but keeps the barrier sequence.
+__device__ void issue_tile(Ctx& c) {
   using namespace tc;
-  sync_for_issue();
-  if (threadIdx.x == 0) {
-    tc_fence_after();
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(c.sm + S_ABORT);
+  const bool leader = (threadIdx.x & 31) == 0;
+  named_sync(1, NTHR);  // input rows
+  tc_fence_after();
+  if (leader && !*abort_flag) {
     issue_act(c, 0);
     mma_commit(c.bar_a);
   }
   for (int l = 0; l < MLP_LAYERS - 1; ++l) {
-    if (__syncthreads_or(!wait_bar(c.bar_a, c.phase_a))) return false;
+    named_sync(1, NTHR);  // activation tiles of layer l
     tc_fence_after();
-    float d[32];
-    epilogue_act(c, l, d);
-    sync_for_issue();
-    if (threadIdx.x == 0) {
-      tc_fence_after();
+    if (leader && !*abort_flag) {
       issue_act(c, l + 1);
       mma_commit(c.bar_a);
     }
-    if (l > 0) {
-      if (__syncthreads_or(!wait_bar(c.bar_t, c.phase_t))) return false;
-      tc_fence_after();
-    }
-    epilogue_tan(c, l, d);
-    sync_for_issue();
-    if (threadIdx.x == 0) {
-      tc_fence_after();
+    named_sync(2, NTHR);  // tangent tiles of layer l
+    tc_fence_after();
+    if (leader && !*abort_flag) {
       issue_tan(c, l + 1);
       mma_commit(c.bar_t);
     }
   }
-  if (__syncthreads_or(!wait_bar(c.bar_a, c.phase_a))) return false;
-  if (__syncthreads_or(!wait_bar(c.bar_t, c.phase_t))) return false;
+}
+
+// The epilogue warps' part of one tile, after they wrote the input rows: the
+// five layers, leaving the output layer's accumulators in TMEM.  Schedule per
+// layer: the activation MMAs of layer l+1 run while the epilogue warps work
+// through the tangent epilogue of layer l, the tangent MMAs of layer l+1 while
+// they work through the activation epilogue of layer l+1, and the issuer warp
+// issues in parallel with both.  `ok` goes (uniformly) false when a wait gives
+// up; the barrier sequence is kept so that the issuer warp never blocks.
+__device__ void epilogue_tile(Ctx& c, bool& ok) {
+  using namespace tc;
+  int* abort_flag = reinterpret_cast<int*>(c.sm + S_ABORT);
+  release_to_issuer(1, ok);
+  for (int l = 0; l < MLP_LAYERS - 1; ++l) {
+    if (ok) {
+      const bool w = wait_bar(c.bar_a, c.phase_a);
+      if (!w) *abort_flag = 1;
+    }
+    epi_sync();
+    ok = ok && !*reinterpret_cast<volatile int*>(abort_flag);
+    tc_fence_after();
+    float d[CW];
+    if (ok) epilogue_act(c, l, d);
+    release_to_issuer(1, ok);
+    if (l > 0) {
+      if (ok) {
+        const bool w = wait_bar(c.bar_t, c.phase_t);
+        if (!w) *abort_flag = 1;
+      }
+      epi_sync();
+      ok = ok && !*reinterpret_cast<volatile int*>(abort_flag);
+      tc_fence_after();
+    }
+    if (ok) epilogue_tan(c, l, d);
+    release_to_issuer(2, ok);
+  }
+  if (ok) {
+    const bool wa = wait_bar(c.bar_a, c.phase_a);
+    const bool wt = wait_bar(c.bar_t, c.phase_t);
+    if (!(wa && wt)) *abort_flag = 1;
+  }
+  epi_sync();
+  ok = ok && !*reinterpret_cast<volatile int*>(abort_flag);
   tc_fence_after();
-  return true;
 }
 
 // Output layer epilogue for point m = threadIdx.x (warps 0..3 only): outputs y in
@@ -313,6 +359,7 @@ __device__ void setup(Ctx& c, unsigned char* sm, const unsigned char* image) {
   uint4* dst = reinterpret_cast<uint4*>(sm + S_IMG);
   for (int i = threadIdx.x; i < int(IMG_BYTES / 16); i += blockDim.x) dst[i] = src[i];
   if (threadIdx.x == 0) {
+    *reinterpret_cast<int*>(sm + S_ABORT) = 0;
     mbar_init(c.bar_a, 1);
     mbar_init(c.bar_t, 1);
     mbar_fence_init();
@@ -347,31 +394,36 @@ __global__ void __launch_bounds__(NTHR, 1)
   extern __shared__ __align__(1024) unsigned char sm[];
   Ctx c;
   setup(c, sm, image);
-  bool failed = false;
+  bool ok = true;
+  const bool issuer = threadIdx.x >= NEPI;
   const int64_t tiles = (n + 127) / 128;
   for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
-    const int64_t r = t * 128 + threadIdx.x;
-    if (threadIdx.x < 128) {
-      float x[MLP_IN];
-      if (r < n)
-        for (int i = 0; i < MLP_IN; ++i) x[i] = X[r * MLP_IN + i];
-      write_input_row(c, threadIdx.x, r < n ? x : nullptr);
-    }
-    if (!run_layers(c)) {
-      failed = true;
-      break;
-    }
-    if (threadIdx.x < 128) {
-      float y[MLP_OUT], Js[6][6];
-      epilogue_output(c, y, Js);
-      if (r < n) {
-        for (int o = 0; o < MLP_OUT; ++o) Y[r * MLP_OUT + o] = y[o];
-        for (int o = 0; o < 6; ++o)
-          for (int j = 0; j < 6; ++j) Jac[r * 36 + o * 6 + j] = Js[o][j];
+    if (issuer) {
+      issue_tile(c);
+    } else {
+      const int64_t r = t * 128 + threadIdx.x;
+      if (threadIdx.x < 128) {
+        float x[MLP_IN];
+        if (r < n)
+          for (int i = 0; i < MLP_IN; ++i) x[i] = X[r * MLP_IN + i];
+        write_input_row(c, threadIdx.x, r < n ? x : nullptr);
+      }
+      epilogue_tile(c, ok);
+      if (ok && threadIdx.x < 128) {
+        float y[MLP_OUT], Js[6][6];
+        epilogue_output(c, y, Js);
+        if (r < n) {
+          for (int o = 0; o < MLP_OUT; ++o) Y[r * MLP_OUT + o] = y[o];
+          for (int o = 0; o < 6; ++o)
+            for (int j = 0; j < 6; ++j) Jac[r * 36 + o * 6 + j] = Js[o][j];
+        }
       }
     }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (*reinterpret_cast<volatile int*>(sm + S_ABORT)) break;
   }
-  teardown(c, failed, err);
+  teardown(c, *reinterpret_cast<volatile int*>(sm + S_ABORT) != 0, err);
 }
 
 // ---- the closure over hex8 elements: point table and state ----------------------------
@@ -418,100 +470,104 @@ __global__ void __launch_bounds__(NTHR, 1) j2mlp_points_tc_kernel(ElemArgs g, Tc
     s_ref[i] = g.ref[i];
     s_reff[i] = float(g.ref[i]);
   }
-  bool failed = false;
+  __syncthreads();
+  bool ok = true;
+  const bool issuer = tid >= NEPI;
   const int64_t tiles = (g.ne + EPT - 1) / EPT;
   for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
-    const int64_t e0 = t * EPT;
-    // ---- A: staging, kinematics, trial state ----
-    if (tid < 128) {
-      const int64_t e = e0 + tid / 8;
-      s_conn[tid] = e < g.ne ? g.conn[e * 8 + (tid & 7)] : 0;
-    }
-    __syncthreads();
-    for (int i = tid; i < EPT * 24; i += NTHR) {
-      const int el = i / 24, k = i % 24, a = k / 3, d = k % 3;
-      if (e0 + el < g.ne) {
-        const double xv = __ldg(&g.coords[int64_t(s_conn[el * 8 + a]) * 3 + d]);
-        s_x[i] = xv;
-        s_xd[i] = float(xv - __ldg(&g.coords[int64_t(s_conn[el * 8]) * 3 + d]));
-        s_u[i] = float(__ldg(&g.U[int64_t(s_conn[el * 8 + a]) * 3 + d]));
+    if (issuer) {
+      issue_tile(c);
+    } else {
+      const int64_t e0 = t * EPT;
+      // ---- A: staging, kinematics, trial state ----
+      if (tid < 128) {
+        const int64_t e = e0 + tid / 8;
+        s_conn[tid] = e < g.ne ? g.conn[e * 8 + (tid & 7)] : 0;
       }
-    }
-    __syncthreads();
-    int plastic = 0;
-    if (tid < 128) {
-      const int el = tid / 8, q = tid & 7;
-      const int64_t e = e0 + el, p = e * 8 + q;
-      int flag = -1;  // -1: no element, 0: elastic (done), 1: plastic
-      float x[MLP_IN];
-      if (e < g.ne) {
-        float dNX[24];
-        map_hex8_mixed(s_ref, s_reff, q, s_x + el * 24, s_xd + el * 24, dNX);
-        float gu[3][3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-          for (int j = 0; j < 3; ++j) {
-            float s = 0.f;
-#pragma unroll
-            for (int a = 0; a < 8; ++a) s = fmaf(s_u[el * 24 + a * 3 + i], dNX[a * 3 + j], s);
-            gu[i][j] = s;
-            s_gu[tid * 9 + i * 3 + j] = s;
-          }
-        const double* so = g.state_old + p * 7;
-        double* sn = g.state_new ? g.state_new + p * 7 : nullptr;
-        float etr[6];
-        if (J2MLP::trial(g.props, gu, so, etr, x)) {
-          flag = 1;
-        } else {
-          float P9[9], C36[36];
-          J2MLP::exact(g.props, gu, 1.0f, so, sn, P9, C36);
-          write_row(cl.table, p, P9, C36);
-          flag = 0;
+      epi_sync();
+      for (int i = tid; i < EPT * 24; i += NEPI) {
+        const int el = i / 24, k = i % 24, a = k / 3, d = k % 3;
+        if (e0 + el < g.ne) {
+          const double xv = __ldg(&g.coords[int64_t(s_conn[el * 8 + a]) * 3 + d]);
+          s_x[i] = xv;
+          s_xd[i] = float(xv - __ldg(&g.coords[int64_t(s_conn[el * 8]) * 3 + d]));
+          s_u[i] = float(__ldg(&g.U[int64_t(s_conn[el * 8 + a]) * 3 + d]));
         }
       }
-      s_flag[tid] = flag;
-      plastic = flag == 1;
-      write_input_row(c, tid, plastic ? x : nullptr);
-    }
-    // ---- B: the network on all 128 rows ----
-    if (!run_layers(c)) {
-      failed = true;
-      break;
-    }
-    // ---- C: plastic points from the network, with the consistency check ----
-    if (tid < 128) {
-      float y[MLP_OUT], Js[6][6];
-      epilogue_output(c, y, Js);
-      int fell_back = 0;
-      if (plastic) {
-        const int64_t p = (e0 + tid / 8) * 8 + (tid & 7);
-        const double* so = g.state_old + p * 7;
-        double* sn = g.state_new ? g.state_new + p * 7 : nullptr;
-        float gu[3][3];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) gu[i / 3][i % 3] = s_gu[tid * 9 + i];
-        float etr[6];
+      epi_sync();
+      int plastic = 0;
+      if (tid < 128) {
+        const int el = tid / 8, q = tid & 7;
+        const int64_t e = e0 + el, p = e * 8 + q;
+        int flag = -1;  // -1: no element, 0: elastic (done), 1: plastic
         float x[MLP_IN];
-        J2MLP::trial(g.props, gu, so, etr, x);
-        float P9[9], C36[36];
-        if (!J2MLP::finish(g.props, etr, cl.tol, y, Js, 1.0f, so, sn, P9, C36)) {
-          fell_back = 1;
-          J2MLP::exact(g.props, gu, 1.0f, so, sn, P9, C36);
+        if (e < g.ne) {
+          float dNX[24];
+          map_hex8_mixed(s_ref, s_reff, q, s_x + el * 24, s_xd + el * 24, dNX);
+          float gu[3][3];
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+              float s = 0.f;
+#pragma unroll
+              for (int a = 0; a < 8; ++a) s = fmaf(s_u[el * 24 + a * 3 + i], dNX[a * 3 + j], s);
+              gu[i][j] = s;
+              s_gu[tid * 9 + i * 3 + j] = s;
+            }
+          const double* so = g.state_old + p * 7;
+          double* sn = g.state_new ? g.state_new + p * 7 : nullptr;
+          float etr[6];
+          if (J2MLP::trial(g.props, gu, so, etr, x)) {
+            flag = 1;
+          } else {
+            float P9[9], C36[36];
+            J2MLP::exact(g.props, gu, 1.0f, so, sn, P9, C36);
+            write_row(cl.table, p, P9, C36);
+            flag = 0;
+          }
         }
-        write_row(cl.table, p, P9, C36);
+        s_flag[tid] = flag;
+        plastic = flag == 1;
+        write_input_row(c, tid, plastic ? x : nullptr);
       }
-      const unsigned np = __popc(__ballot_sync(0xffffffffu, plastic));
-      const unsigned nf = __popc(__ballot_sync(0xffffffffu, fell_back));
-      if ((tid & 31) == 0 && np) {
-        atomicAdd(&cl.counters[0], (unsigned long long)np);
-        if (nf) atomicAdd(&cl.counters[1], (unsigned long long)nf);
+      // ---- B: the network on all 128 rows (the issuer warp issues the MMAs) ----
+      epilogue_tile(c, ok);
+      // ---- C: plastic points from the network, with the consistency check ----
+      if (ok && tid < 128) {
+        float y[MLP_OUT], Js[6][6];
+        epilogue_output(c, y, Js);
+        int fell_back = 0;
+        if (plastic) {
+          const int64_t p = (e0 + tid / 8) * 8 + (tid & 7);
+          const double* so = g.state_old + p * 7;
+          double* sn = g.state_new ? g.state_new + p * 7 : nullptr;
+          float gu[3][3];
+#pragma unroll
+          for (int i = 0; i < 9; ++i) gu[i / 3][i % 3] = s_gu[tid * 9 + i];
+          float etr[6];
+          float x[MLP_IN];
+          J2MLP::trial(g.props, gu, so, etr, x);
+          float P9[9], C36[36];
+          if (!J2MLP::finish(g.props, etr, cl.tol, y, Js, 1.0f, so, sn, P9, C36)) {
+            fell_back = 1;
+            J2MLP::exact(g.props, gu, 1.0f, so, sn, P9, C36);
+          }
+          write_row(cl.table, p, P9, C36);
+        }
+        const unsigned np = __popc(__ballot_sync(0xffffffffu, plastic));
+        const unsigned nf = __popc(__ballot_sync(0xffffffffu, fell_back));
+        if ((tid & 31) == 0 && np) {
+          atomicAdd(&cl.counters[0], (unsigned long long)np);
+          if (nf) atomicAdd(&cl.counters[1], (unsigned long long)nf);
+        }
       }
     }
     tc::tc_fence_before();
     __syncthreads();
+    if (*reinterpret_cast<volatile int*>(sm + S_ABORT)) break;
   }
-  teardown(c, failed, reinterpret_cast<int*>(&cl.counters[2]));
+  teardown(c, *reinterpret_cast<volatile int*>(sm + S_ABORT) != 0, reinterpret_cast<int*>(&cl.counters[2]));
 }
 
 // Point-table model for the FP32 hex8 element kernel: stress and tangent read
