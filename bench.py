@@ -53,8 +53,11 @@ WORKLOADS = {
     # a 5-iteration Newton-type loop replayed as one CUDA graph per step
     "batched": dict(n=0, kind="vector", name="batched_64_hex8_plus_tet4_tet10_hex27_newton5_graph",
                     flop_per_elem=48e3, state=0),
+    # matrix-free tangent action K v of the Neo-Hookean 128^3 system (no K formed)
+    "action": dict(n=128, kind="vector", name="neohookean_hex8_128cubed_matrix_free_action", flop_per_elem=5.5e3,
+                   state=0),
 }
-CPU_SAMPLE_N = {"neohookean": 40, "poisson": 32, "j2": 40, "batched": 40, "j2mlp": 40}
+CPU_SAMPLE_N = {"neohookean": 40, "poisson": 32, "j2": 40, "batched": 40, "j2mlp": 40, "action": 40}
 J2_STEPS = 20
 J2_PROPS = (200.0, 0.3, 0.25, 2.0)   # E, nu, yield stress, linear hardening
 
@@ -222,6 +225,10 @@ def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    if args.workload in ("action", "j2mlp", "batched"):
+        print(json.dumps({"impl": "reference", "unavailable": f"the CPU port times the assembly workloads only "
+                                                                f"(neohookean, poisson, j2), not {args.workload}"}))
+        return
     from oracle import oracle
     threads = oracle.max_threads()
     n = CPU_SAMPLE_N[args.workload]
@@ -377,6 +384,75 @@ def run_closure(args) -> None:
                   "fp32_element_max_rel_err_vs_fp64": x32_err, "kernels_ms": x_kernels,
                   "speedup_closure_vs_exact_fp64": t_x64 / main_t, "speedup_closure_vs_exact_fp32": t_x32 / main_t},
         "clocks": clk.summary(), "e2e": None, "gpu_launches": int(main_launches), "cpu_baseline": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_action(args) -> None:
+    """Matrix-free tangent action of the Neo-Hookean 128^3 system: one step is
+    field update + element action kernel + node gather (K v over the unknowns)."""
+    import torch
+    import __graft_entry__ as ge
+    fec = ge.load_package()
+    torch.cuda.set_device(0)
+    n = args.n or WORKLOADS["action"]["n"]
+    mesh, asm, p, inputs = build_workload(fec, "neohookean", n, 0, args.precision)
+    ne, nn = mesh.num_elements(), mesh.num_nodes
+    n_u = int(asm.dof.unknown_dofs.size)
+    Uu = torch.from_numpy(inputs[0][0]).cuda()
+    Vu = torch.from_numpy(np.random.default_rng(4).standard_normal(n_u)).cuda()
+    stream = torch.cuda.current_stream()
+
+    def step(u=Uu, v=Vu):
+        return fec.assemble_matrix_free_action(asm, fec.stiffness_action, u, v, p)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    asm.set_profiling(True)
+    step()
+    kernels = {k: ms for k, ms in asm.kernel_times()}
+    asm.set_profiling(False)
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    t_ms = e0.elapsed_time(e1) / args.steps
+    # end to end: host Uu, Vu in (pinned), K v out (pinned)
+    hU, hV = Uu.cpu().pin_memory(), Vu.cpu().pin_memory()
+    hK = torch.empty(n_u, dtype=torch.float64).pin_memory()
+    for _ in range(2):
+        step(hU.cuda(non_blocking=True), hV.cuda(non_blocking=True))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        kv = step(hU.cuda(non_blocking=True), hV.cuda(non_blocking=True))
+        hK.copy_(kv, non_blocking=True)
+    torch.cuda.synchronize()
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    # compulsory traffic: connectivity, X, U and V per node, K v over the unknowns
+    alg = 4 * 8 * ne + 8 * 3 * nn * 3 + 8 * n_u
+    dom = max((k for k in kernels if k != "update_field"), key=kernels.get)
+    peaks = measured_peaks()
+    achieved = alg / (t_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": ne / (t_ms * 1e-3) / 1e6, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32-element/f64-accumulate",
+        "data": "synthetic",
+        "config": {"workload": WORKLOADS["action"]["name"], "elements": ne, "unknowns": n_u,
+                   "precision": args.precision, "direction": "N(0,1) seed 4",
+                   "l2": "inputs larger than L2 (X, U, V 155 MB; element workspace 403 MB)"},
+        "roofline": {"bound": "hbm", "kernel": "whole step", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                     "algorithmic_bytes_per_elem": alg / ne, "kernels_ms": kernels, "dominant": dom},
+        "e2e": {"value": ne / t_e2e / 1e6, "unit": UNIT, "h2d_bytes_per_step": 16 * n_u,
+                "d2h_bytes_per_step": 8 * n_u},
+        "clocks": clk.summary(), "gpu_launches": int(asm.last_launch_count() + 2) * args.steps,
+        "cpu_baseline": None,
     }
     print(json.dumps(line), flush=True)
 
@@ -699,6 +775,8 @@ def main() -> None:
         run_batched(args)
     elif args.workload == "j2mlp":
         run_closure(args)
+    elif args.workload == "action":
+        run_action(args)
     else:
         run_ours(args)
 

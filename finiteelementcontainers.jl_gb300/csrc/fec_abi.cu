@@ -80,6 +80,7 @@ struct fec_ctx {
   // ClosureArgs struct the kernels read
   DevBuf d_cl_w, d_cl_norm, d_cl_cnt, d_cl_args;
   DevBuf d_cl_img, d_cl_table;  // tensor-core closure: packed parameters, per-point table
+  DevBuf d_V;                   // matrix-free action: the direction as a full field
   float cl_tol = 0.f;
   // optional per-launch timing (CUDA events on the caller's stream)
   bool profiling = false;
@@ -238,7 +239,7 @@ int fec_ctx_destroy(fec_ctx* c) {
   for (cudaEvent_t e : c->events) cudaEventDestroy(e);
   for (DevBuf* b : {&c->d_coords, &c->d_conn, &c->d_ref, &c->d_nadj_ptr, &c->d_nadj, &c->d_epos, &c->d_umask,
                     &c->d_col_base, &c->d_col_len, &c->d_dtu, &c->d_unknown_dofs, &c->d_Ke, &c->d_Re, &c->d_cl_w,
-                    &c->d_cl_norm, &c->d_cl_cnt, &c->d_cl_args, &c->d_cl_img, &c->d_cl_table})
+                    &c->d_cl_norm, &c->d_cl_cnt, &c->d_cl_args, &c->d_cl_img, &c->d_cl_table, &c->d_V})
     b->release();
   delete c;
   return FEC_OK;
@@ -742,6 +743,109 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
   ga.Re = c->d_Re.p;
   ga.nzval = want_k ? nzval : nullptr;
   ga.R_u = want_r ? R_u : nullptr;
+  ga.acc_stride = c->acc_stride;
+  cudaError_t e;
+  {
+    LaunchTimer timer(c, s, "node_gather");
+    e = fec::launch_gather(precision, c->nf, ga, s, &c->last_launches);
+  }
+  if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "gather launch: %s", cudaGetErrorString(e));
+  return ok(c);
+}
+
+int fec_assemble_action(fec_ctx* c, int precision, double t, double dt, const double* U, const double* state_old,
+                        const double* Vu, double* Kv_u, void* stream) {
+  (void)t;
+  (void)dt;
+  if (!c) return FEC_ERR_ARG;
+  c->last_launches = 0;
+  if (!c->pattern_ready) return fail(c, FEC_ERR_STATE, "fec_assemble_action before fec_pattern_build");
+  if (c->device < 0) return fail(c, FEC_ERR_STATE, "host-only context (device -1) cannot run kernels");
+  if (precision != FEC_FP64 && precision != FEC_FP32_ELEMENT)
+    return fail(c, FEC_ERR_ARG, "unknown precision %d", precision);
+  if (!U) return fail(c, FEC_ERR_ARG, "U is NULL");
+  if (c->n_unknowns > 0 && (!Vu || !Kv_u)) return fail(c, FEC_ERR_ARG, "Vu or Kv_u is NULL");
+  bool any_state = false;
+  for (size_t b = 0; b < c->blocks.size(); ++b) {
+    const Block& B = c->blocks[b];
+    if (!B.physics) return fail(c, FEC_ERR_STATE, "block %d has no physics", int(b) + 1);
+    if (num_fields_of(B.physics) != c->nf)
+      return fail(c, FEC_ERR_ARG, "block %d physics has %d fields but the dofs have %d", int(b) + 1,
+                  num_fields_of(B.physics), c->nf);
+    if (num_states_of(B.physics)) any_state = true;
+  }
+  if (any_state && !state_old) return fail(c, FEC_ERR_ARG, "state_old is NULL for a physics with state");
+  cudaSetDevice(c->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  c->n_timed = 0;
+  const size_t rsz = precision == FEC_FP64 ? sizeof(double) : sizeof(float);
+  int64_t re_total = 0;
+  for (const Block& B : c->blocks) re_total += B.ne * c->nf * B.nnpe;
+  int rc;
+  if ((rc = ensure(c, c->d_Re, rsz * size_t(re_total)))) return rc;
+  // the direction as a full field: the unknowns' values, zero on Dirichlet dofs
+  const int64_t ndofs = c->nn * c->nf;
+  if ((rc = ensure(c, c->d_V, sizeof(double) * size_t(ndofs)))) return rc;
+  double* V = static_cast<double*>(c->d_V.p);
+  FEC_CUDA(c, cudaMemsetAsync(V, 0, sizeof(double) * size_t(ndofs), s));
+  if (c->n_unknowns > 0) {
+    set_unknowns_kernel<<<unsigned((c->n_unknowns + 255) / 256), 256, 0, s>>>(
+        V, c->n_unknowns, static_cast<const int64_t*>(c->d_unknown_dofs.p), Vu);
+    FEC_CUDA(c, cudaGetLastError());
+    ++c->last_launches;
+  }
+  GatherArgs ga;
+  memset(&ga, 0, sizeof ga);
+  int64_t re_off = 0, st_off = 0;
+  for (size_t b = 0; b < c->blocks.size(); ++b) {
+    const Block& B = c->blocks[b];
+    const int ndof = c->nf * B.nnpe;
+    ElemArgs ea;
+    memset(&ea, 0, sizeof ea);
+    ea.conn = static_cast<const int32_t*>(c->d_conn.p) + B.conn_off;
+    ea.ne = B.ne;
+    ea.coords = static_cast<const double*>(c->d_coords.p);
+    ea.U = U;
+    ea.ref = static_cast<const double*>(c->d_ref.p) + c->ref_off[b];
+    for (int i = 0; i < 8; ++i) ea.props[i] = B.props[i];
+    const int ns = num_states_of(B.physics);
+    ea.state_old = ns ? state_old + st_off : nullptr;
+    ea.Re = static_cast<char*>(c->d_Re.p) + rsz * size_t(re_off);
+    cudaError_t e;
+    {
+      LaunchTimer timer(c, s, "element_action");
+      e = fec::launch_action(B.physics, B.elem_type, precision, ea, V, s, &c->last_launches);
+    }
+    if (e == cudaErrorNotSupported)
+      return fail(c, FEC_ERR_UNSUPPORTED, "block %d: matrix-free action of physics %d on element type %d is not built",
+                  int(b) + 1, B.physics, B.elem_type);
+    if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "action kernel launch: %s", cudaGetErrorString(e));
+    BlockInfo& bi = ga.blk[b];
+    bi.elem_start = B.elem_start;
+    bi.ke_off = 0;
+    bi.re_off = re_off;
+    bi.conn_off = B.conn_off;
+    bi.epos_off = B.epos_off;
+    bi.nnpe = B.nnpe;
+    bi.ndof = ndof;
+    bi.layout = fec::KE_ROW_MAJOR;
+    re_off += B.ne * ndof;
+    st_off += int64_t(ns) * B.nq * B.ne;
+  }
+  ga.nn = c->nn;
+  ga.nf = c->nf;
+  ga.nblocks = int(c->blocks.size());
+  ga.nadj_ptr = static_cast<const int64_t*>(c->d_nadj_ptr.p);
+  ga.nadj = static_cast<const uint32_t*>(c->d_nadj.p);
+  ga.conn = static_cast<const int32_t*>(c->d_conn.p);
+  ga.epos = static_cast<const uint16_t*>(c->d_epos.p);
+  ga.umask = static_cast<const uint8_t*>(c->d_umask.p);
+  ga.col_base = static_cast<const int64_t*>(c->d_col_base.p);
+  ga.col_len = static_cast<const int32_t*>(c->d_col_len.p);
+  ga.dof_to_unknown = static_cast<const int64_t*>(c->d_dtu.p);
+  ga.Re = c->d_Re.p;
+  ga.nzval = nullptr;
+  ga.R_u = Kv_u;
   ga.acc_stride = c->acc_stride;
   cudaError_t e;
   {

@@ -376,6 +376,35 @@ struct NeoHookean {
     if (i == k && J == L) v += scr[20];
     return v;
   }
+  // JxW (A : G)_iJ = sum_kL A_iJkL G_kL for a direction gradient G, without forming A:
+  // a1 (H:G) H + a2 H G^T H - 2/3 c2 ((H:G) F + (F:G) H) + c2 G
+  template <typename Real>
+  __device__ static void action(const Real* scr, const Real G[3][3], Real out[3][3]) {
+    const Real* F = scr;
+    const Real* H = scr + 9;
+    Real hg = 0, fg = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int L = 0; L < 3; ++L) {
+        hg = fma(H[k * 3 + L], G[k][L], hg);
+        fg = fma(F[k * 3 + L], G[k][L], fg);
+      }
+    Real M[3][3];  // (G^T H)_LJ
+#pragma unroll
+    for (int L = 0; L < 3; ++L)
+#pragma unroll
+      for (int J = 0; J < 3; ++J) M[L][J] = G[0][L] * H[J] + G[1][L] * H[3 + J] + G[2][L] * H[6 + J];
+    const Real m23 = Real(-2.0 / 3.0) * scr[20];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int J = 0; J < 3; ++J) {
+        const Real hgh = H[i * 3] * M[0][J] + H[i * 3 + 1] * M[1][J] + H[i * 3 + 2] * M[2][J];
+        out[i][J] = scr[18] * hg * H[i * 3 + J] + scr[19] * hgh + m23 * (hg * F[i * 3 + J] + fg * H[i * 3 + J]) +
+                    scr[20] * G[i][J];
+      }
+  }
   // df64 form of the scratch: F(9), H(9), a1, a2, c2, -2/3 c2 (all JxW-scaled where scr is)
   static constexpr int SCR2 = 22;
   __device__ static void split_scratch(const double* scr, float2* out) {
@@ -495,6 +524,25 @@ struct J2 {
     const Real dij = (i == J) ? Real(1) : Real(0), dkl = (k == L) ? Real(1) : Real(0);
     const Real isym = Real(0.5) * (Real((i == k) && (J == L)) + Real((i == L) && (J == k)));
     return scr[9] * dij * dkl + scr[10] * (isym - dij * dkl / Real(3)) - scr[11] * scr[i * 3 + J] * scr[k * 3 + L];
+  }
+  // JxW (A : G)_iJ = kap' tr(G) d_iJ + 2 mu th' (sym(G) - tr(G)/3 I)_iJ - 2 mu thb' n_iJ (n : G)
+  template <typename Real>
+  __device__ static void action(const Real* scr, const Real G[3][3], Real out[3][3]) {
+    const Real* n = scr;
+    const Real tr = G[0][0] + G[1][1] + G[2][2];
+    Real ng = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int L = 0; L < 3; ++L) ng = fma(n[k * 3 + L], G[k][L], ng);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int J = 0; J < 3; ++J) {
+        const Real d = i == J ? Real(1) : Real(0);
+        out[i][J] = scr[9] * tr * d + scr[10] * (Real(0.5) * (G[i][J] + G[J][i]) - tr / Real(3) * d) -
+                    scr[11] * n[i * 3 + J] * ng;
+      }
   }
   // df64 form: n(9), c_a = kap' - mt'/3 (d_iJ d_kL), c_b = mt'/2 (each I_sym term), mb'
   static constexpr int SCR2 = 12;

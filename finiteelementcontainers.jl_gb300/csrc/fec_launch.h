@@ -29,6 +29,11 @@ cudaError_t launch_poisson(int elem_type, int precision, bool want_r, bool want_
 cudaError_t launch_mech(int physics, int elem_type, int precision, bool want_r, bool want_k, const ElemArgs& args,
                         cudaStream_t stream, int* launches);
 cudaError_t launch_gather(int precision, int nf, const GatherArgs& args, cudaStream_t stream, int* launches);
+// Matrix-free tangent action: element contributions K_e v_e (summed over points
+// in point order) into the residual workspace args.Re; V is the full direction
+// field (zero on Dirichlet dofs).  The state is read only.
+cudaError_t launch_action(int physics, int elem_type, int precision, const ElemArgs& args, const double* V,
+                          cudaStream_t stream, int* launches);
 // Hex27 FP32-element mechanics with the element-stiffness contraction on the
 // tensor cores (physics 2 Neo-Hookean, 3 J2); a wait that gives up sets the
 // flag fec_tensor_core_status reads.

@@ -11,7 +11,8 @@ from .bcs import DirichletBC, dirichlet_dofs
 from .physics import Poisson, NeoHookean, J2Plasticity, num_fields, num_properties, num_states
 from .assemblers import (SparseMatrixAssembler, CSCMatrix, Parameters, create_parameters, update_dofs_bcs,
                          assemble_vector, assemble_stiffness, assemble_matrix, assemble_residual_and_stiffness,
-                         residual, stiffness, autotune_report)
+                         residual, stiffness, autotune_report, assemble_matrix_free_action, stiffness_action,
+                         hvp)
 from ._lib import FECError, load as load_library
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -258,7 +258,8 @@ def _as_device_unknowns(asm, Uu):
     return Uu
 
 
-def _assemble(asm: SparseMatrixAssembler, want: int, Uu, p: Parameters, precision: str | None):
+def _prepare(asm: SparseMatrixAssembler, Uu, p: Parameters):
+    """Physics set-up (once per change) and _update_for_assembly! (src/Parameters.jl:404-413)."""
     torch = _torch()
     asm._ensure_pattern()
     key = tuple((ph.ID, pr.tobytes(), id(getattr(ph, "closure", None))) for ph, pr in zip(p.physics, p.props))
@@ -276,6 +277,11 @@ def _assemble(asm: SparseMatrixAssembler, want: int, Uu, p: Parameters, precisio
     asm._call("fec_update_field", _lib.ptr(p.field), _lib.ptr(Uu_d), int(p.bc_dofs.numel()),
               _lib.ptr(p.bc_dofs) if p.bc_dofs.numel() else None,
               _lib.ptr(p.bc_vals) if p.bc_vals.numel() else None, stream)
+    return stream
+
+
+def _assemble(asm: SparseMatrixAssembler, want: int, Uu, p: Parameters, precision: str | None):
+    stream = _prepare(asm, Uu, p)
     R = residual(asm) if want & _lib.FEC_WANT_RESIDUAL else None
     K = stiffness(asm) if want & _lib.FEC_WANT_STIFFNESS else None
     has_state = any(ph.NS for ph in p.physics)
@@ -308,9 +314,43 @@ def assemble_residual_and_stiffness(asm: SparseMatrixAssembler, Uu, p: Parameter
     return _assemble(asm, _lib.FEC_WANT_RESIDUAL | _lib.FEC_WANT_STIFFNESS, Uu, p, precision)
 
 
+def stiffness_action(*_):
+    """Marker of the physics' tangent action (stiffness_action in the reference)."""
+    raise TypeError("stiffness_action is a marker for assemble_matrix_free_action")
+
+
+def assemble_matrix_free_action(asm: SparseMatrixAssembler, func, Uu, Vu, p: Parameters, *,
+                                precision: str | None = None):
+    """assemble_matrix_free_action!(asm, stiffness_action, Uu, Vu, p)
+    (src/assemblers/MatrixAction.jl:9-77): K v over the unknowns without forming
+    K; read it with hvp(asm).  Dirichlet components of the direction are zero."""
+    torch = _torch()
+    if func is not stiffness_action:
+        raise NotImplementedError("assemble_matrix_free_action supports the physics `stiffness_action` method")
+    stream = _prepare(asm, Uu, p)
+    n_u = int(asm.dof.unknown_dofs.size)
+    Vu_d = _as_device_unknowns(asm, Vu)
+    if Vu_d.numel() != n_u:
+        raise ValueError(f"Vu has {Vu_d.numel()} entries, expected {n_u}")
+    if getattr(asm, "_hvp", None) is None or asm._hvp.numel() != n_u:
+        asm._hvp = torch.empty(n_u, dtype=torch.float64, device=asm._torch_device())
+    has_state = any(ph.NS for ph in p.physics)
+    asm._call("fec_assemble_action", PRECISIONS[precision or asm.precision], p.t, p.dt, _lib.ptr(p.field),
+              _lib.ptr(p.state_old) if has_state else None, _lib.ptr(Vu_d), _lib.ptr(asm._hvp), stream)
+    return asm._hvp
+
+
+def hvp(asm: SparseMatrixAssembler, Vu=None):
+    """hvp(asm, v) (src/assemblers/Assemblers.jl:310-324): the last matrix-free action
+    over the unknowns (a device view)."""
+    if getattr(asm, "_hvp", None) is None:
+        raise RuntimeError("hvp before assemble_matrix_free_action")
+    return asm._hvp
+
+
 __all__ = ["SparseMatrixAssembler", "CSCMatrix", "Parameters", "create_parameters", "update_dofs_bcs",
            "assemble_vector", "assemble_stiffness", "assemble_matrix", "assemble_residual_and_stiffness",
-           "residual", "stiffness", "ELEMENT_IDS"]
+           "assemble_matrix_free_action", "stiffness_action", "hvp", "residual", "stiffness", "ELEMENT_IDS"]
 
 
 def autotune_report() -> list[str]:

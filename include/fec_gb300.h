@@ -140,6 +140,18 @@ int fec_assemble(fec_ctx* ctx, int want, int precision, double t, double dt, con
                  const double* U_old_dev, const double* state_old_dev, double* state_new_dev, double* R_u_dev,
                  double* nzval_dev, void* stream);
 
+/* Matrix-free tangent action: Kv_u = K_uu Vu without forming K.  U is the full
+ * field (after fec_update_field), Vu the direction over the unknowns (its
+ * Dirichlet components are zero), Kv_u the product over the unknowns (device,
+ * caller-owned).  Element contributions are summed over quadrature points in
+ * point order and over elements in element order (deterministic).  The state is
+ * read, never written.  Replaces assemble_matrix_free_action!(asm,
+ * stiffness_action, Uu, Vu, p) followed by hvp(asm, Vu)
+ * (src/assemblers/MatrixAction.jl:9-77, src/assemblers/Assemblers.jl:310-324).
+ * Poisson, Neo-Hookean and J2 on hex8/tet4/tet10/hex27 (quad4 for Poisson). */
+int fec_assemble_action(fec_ctx* ctx, int precision, double t, double dt, const double* U_dev,
+                        const double* state_old_dev, const double* Vu_dev, double* Kv_u_dev, void* stream);
+
 /* Assembly that allocates no device memory.  No counterpart in the reference.
  *
  * fec_assemble keeps its element-matrix workspace in memory it cudaMallocs on
