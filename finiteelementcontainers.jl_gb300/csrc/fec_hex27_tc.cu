@@ -71,6 +71,7 @@ constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(32 >> 
 template <class Model, bool WANT_R, bool WANT_K>
 __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err) {
   using namespace tc;
+  static_assert(WANT_K, "the tensor-core kernel forms K_e");
   constexpr int NS = Model::NS, SCR = Model::SCR;
   static_assert(SCR <= 24, "model scratch");
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -168,7 +169,6 @@ __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err)
       static_cast<float*>(g.Re)[e * ND + tid] = R;
     }
     __syncthreads();
-    if (!WANT_K) continue;
     // ---- C chunks (two points each), double buffered against the MMAs ----
     for (int c = 0; c < NCHUNK; ++c) {
       const int buf = c & 1;
@@ -281,10 +281,10 @@ cudaError_t go(const ElemArgs& a, int* err, cudaStream_t s) {
 
 template <class Model>
 cudaError_t launch(bool want_r, bool want_k, const ElemArgs& a, int* err, cudaStream_t s, int* launches) {
-  if (a.ne <= 0 || (!want_r && !want_k)) return cudaSuccess;
+  if (!want_k) return cudaErrorNotSupported;  // residual only: no contraction, the generic kernel serves it
+  if (a.ne <= 0) return cudaSuccess;
   ++*launches;
-  if (want_r && want_k) return go<Model, true, true>(a, err, s);
-  if (want_r) return go<Model, true, false>(a, err, s);
+  if (want_r) return go<Model, true, true>(a, err, s);
   return go<Model, false, true>(a, err, s);
 }
 

@@ -633,33 +633,40 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
     __syncthreads();
   }
 
-  // quadrature-point kinematics + constitutive update (one thread per point)
-  if (live) {
-    for (int q = tx; q < NQ; q += TPE) {
-      Real* dNX = s_dNX + q * A * D;
-      double jxw;
-      if constexpr (DF)
-        jxw = map_point<ET, Real>(s_ref, q, s_x, dNX, nullptr);
-      else
-        jxw = map_point_mixed<ET>(s_ref, s_reff, q, s_x, s_xd, dNX);
-      s_jxw[q] = Real(jxw);
-      Real gu[3][3];
+  // quadrature-point kinematics + constitutive update, one thread per point: the
+  // CTA's EPB * NQ points go to its first threads so that every warp issuing this
+  // (FP64 in the FP64 variant) work has all its lanes busy
+  for (int w = ty * TPE + tx; w < EPB * NQ; w += EPB * TPE) {
+    const int el = w / NQ, q = w % NQ;
+    const int64_t ee = int64_t(blockIdx.x) * EPB + el;
+    if (ee >= g.ne) continue;
+    const double* px = s_x_all + el * A * D;
+    const double* pu = s_u_all + el * A * D;
+    Real* dNX = s_dNX_all + (el * NQ + q) * A * D;
+    double jxw;
+    if constexpr (DF)
+      jxw = map_point<ET, Real>(s_ref, q, px, dNX, nullptr);
+    else
+      jxw = map_point_mixed<ET>(s_ref, s_reff, q, px, s_xd_all + el * A * D, dNX);
+    s_jxw_all[el * NQ + q] = Real(jxw);
+    Real gu[3][3];
 #pragma unroll
-      for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          Real s = 0;
+      for (int j = 0; j < 3; ++j) {
+        Real s = 0;
 #pragma unroll
-          for (int a = 0; a < A; ++a) s = fma(Real(s_u[a * 3 + i]), dNX[a * 3 + j], s);
-          gu[i][j] = s;
-        }
-      const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
-      double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
-      if constexpr (Model::USES_CLOSURE)
-        Model::point_closure(g.closure, g.props, gu, Real(jxw), so, sn, s_P + q * 9, s_scr + q * SCR);
-      else
-        Model::point(g.props, gu, Real(jxw), so, sn, s_P + q * 9, s_scr + q * SCR);
-    }
+        for (int a = 0; a < A; ++a) s = fma(Real(pu[a * 3 + i]), dNX[a * 3 + j], s);
+        gu[i][j] = s;
+      }
+    const double* so = NS ? g.state_old + (ee * NQ + q) * NS : nullptr;
+    double* sn = (NS && g.state_new) ? g.state_new + (ee * NQ + q) * NS : nullptr;
+    Real* pP = s_P_all + (el * NQ + q) * 9;
+    Real* pscr = s_scr_all + (el * NQ + q) * SCR;
+    if constexpr (Model::USES_CLOSURE)
+      Model::point_closure(g.closure, g.props, gu, Real(jxw), so, sn, pP, pscr);
+    else
+      Model::point(g.props, gu, Real(jxw), so, sn, pP, pscr);
   }
   __syncthreads();
   // JxW-scaled tangent entries A'_iJkL, one (q, i) per thread

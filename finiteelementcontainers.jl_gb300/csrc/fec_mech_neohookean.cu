@@ -165,7 +165,8 @@ cudaError_t launch_mech_neohookean(int elem_type, int precision, bool want_r, bo
     case 6: return tuned<6>(precision, want_r, want_k, a, s, launches);
     case 7: return tuned<7>(precision, want_r, want_k, a, s, launches);
     case 8:
-      if (precision == 1 && !hex27_on_cuda_cores()) return launch_hex27_tc(2, want_r, want_k, a, s, launches);
+      if (precision == 1 && want_k && !hex27_on_cuda_cores())
+        return launch_hex27_tc(2, want_r, want_k, a, s, launches);
       return tuned<8>(precision, want_r, want_k, a, s, launches);
     default: return cudaErrorNotSupported;
   }
