@@ -3,6 +3,7 @@
 // pattern and the element -> nzval maps, and the assembly driver.
 #include <algorithm>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -17,6 +18,7 @@
 #include "fec_closure.cuh"
 #include "fec_closure_tc.h"
 #include "fec_launch.h"
+#include "fec_solver.h"
 #include <cuda_bf16.h>
 
 using fec::BlockInfo;
@@ -81,6 +83,7 @@ struct fec_ctx {
   DevBuf d_cl_w, d_cl_norm, d_cl_cnt, d_cl_args;
   DevBuf d_cl_img, d_cl_table;  // tensor-core closure: packed parameters, per-point table
   DevBuf d_V;                   // matrix-free action: the direction as a full field
+  DevBuf d_colptr0, d_rowval32, d_cg;  // linear solve: 0-based CSC pattern, CG scratch
   float cl_tol = 0.f;
   // optional per-launch timing (CUDA events on the caller's stream)
   bool profiling = false;
@@ -197,6 +200,8 @@ struct LaunchTimer {
 void invalidate_pattern(fec_ctx* c) {
   c->pattern_ready = false;
   c->nnz = 0;
+  c->d_colptr0.release();
+  c->d_rowval32.release();
   c->d_nadj_ptr.release();
   c->d_nadj.release();
   c->d_epos.release();
@@ -239,7 +244,8 @@ int fec_ctx_destroy(fec_ctx* c) {
   for (cudaEvent_t e : c->events) cudaEventDestroy(e);
   for (DevBuf* b : {&c->d_coords, &c->d_conn, &c->d_ref, &c->d_nadj_ptr, &c->d_nadj, &c->d_epos, &c->d_umask,
                     &c->d_col_base, &c->d_col_len, &c->d_dtu, &c->d_unknown_dofs, &c->d_Ke, &c->d_Re, &c->d_cl_w,
-                    &c->d_cl_norm, &c->d_cl_cnt, &c->d_cl_args, &c->d_cl_img, &c->d_cl_table, &c->d_V})
+                    &c->d_cl_norm, &c->d_cl_cnt, &c->d_cl_args, &c->d_cl_img, &c->d_cl_table, &c->d_V, &c->d_colptr0, &c->d_rowval32,
+                    &c->d_cg})
     b->release();
   delete c;
   return FEC_OK;
@@ -853,6 +859,45 @@ int fec_assemble_action(fec_ctx* c, int precision, double t, double dt, const do
     e = fec::launch_gather(precision, c->nf, ga, s, &c->last_launches);
   }
   if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "gather launch: %s", cudaGetErrorString(e));
+  return ok(c);
+}
+
+int fec_cg_solve(fec_ctx* c, const double* nzval, const double* b, double* x, int max_iter, double rtol,
+                 int preconditioner, int* iterations, double* rel_residual, void* stream) {
+  if (!c) return FEC_ERR_ARG;
+  if (!c->pattern_ready) return fail(c, FEC_ERR_STATE, "fec_cg_solve before fec_pattern_build");
+  if (c->device < 0) return fail(c, FEC_ERR_STATE, "host-only context (device -1) cannot run kernels");
+  if (c->n_unknowns > 0 && (!nzval || !b || !x)) return fail(c, FEC_ERR_ARG, "nzval, b or x is NULL");
+  if (max_iter < 0 || !(rtol >= 0.0) || (preconditioner != 0 && preconditioner != 1))
+    return fail(c, FEC_ERR_ARG, "max_iter >= 0, rtol >= 0, preconditioner 0 (none) or 1 (Jacobi)");
+  if (c->n_unknowns > INT32_MAX) return fail(c, FEC_ERR_UNSUPPORTED, "more than 2^31 unknowns");
+  cudaSetDevice(c->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int64_t n = c->n_unknowns;
+  int rc;
+  if (!c->d_rowval32.p && c->nnz > 0) {  // the pattern, 0-based, once per pattern
+    std::vector<int64_t> colptr(size_t(n) + 1);
+    std::vector<int64_t> rv(size_t(c->nnz));
+    if ((rc = fec_pattern_get(c, colptr.data(), rv.data()))) return rc;
+    std::vector<int32_t> rv32(rv.size());
+    for (size_t i = 0; i < rv.size(); ++i) rv32[i] = int32_t(rv[i] - 1);
+    for (auto& v : colptr) v -= 1;
+    if ((rc = upload(c, c->d_colptr0, colptr.data(), sizeof(int64_t) * colptr.size()))) return rc;
+    if ((rc = upload(c, c->d_rowval32, rv32.data(), sizeof(int32_t) * rv32.size()))) return rc;
+  }
+  if ((rc = ensure(c, c->d_cg, sizeof(double) * fec::pcg_scratch_doubles(n)))) return rc;
+  fec::CscSym A;
+  A.n = n;
+  A.colptr = static_cast<const int64_t*>(c->d_colptr0.p);
+  A.rowval = static_cast<const int32_t*>(c->d_rowval32.p);
+  A.val = nzval;
+  int it = 0;
+  double rr = 0.0;
+  const cudaError_t e = fec::pcg(A, b, x, static_cast<double*>(c->d_cg.p), max_iter, rtol, 10, preconditioner == 1,
+                                 &it, &rr, s);
+  if (iterations) *iterations = it;
+  if (rel_residual) *rel_residual = rr;
+  if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "conjugate gradients: %s", cudaGetErrorString(e));
   return ok(c);
 }
 

@@ -174,7 +174,7 @@ cudaError_t by_element(int elem_type, int precision, const ElemArgs& a, const do
 }
 
 struct ScalarModel {  // the Poisson stiffness needs no constitutive state
-  static constexpr int NS = 0, SCR = 1;
+  static constexpr int SCR = 1;
 };
 
 }  // namespace

@@ -12,7 +12,7 @@ from .physics import Poisson, NeoHookean, J2Plasticity, num_fields, num_properti
 from .assemblers import (SparseMatrixAssembler, CSCMatrix, Parameters, create_parameters, update_dofs_bcs,
                          assemble_vector, assemble_stiffness, assemble_matrix, assemble_residual_and_stiffness,
                          residual, stiffness, autotune_report, assemble_matrix_free_action, stiffness_action,
-                         hvp)
+                         hvp, IterativeLinearSolver)
 from ._lib import FECError, load as load_library
 
 __all__ = [n for n in dir() if not n.startswith("_")]

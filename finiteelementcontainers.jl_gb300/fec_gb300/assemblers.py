@@ -348,9 +348,45 @@ def hvp(asm: SparseMatrixAssembler, Vu=None):
     return asm._hvp
 
 
+class IterativeLinearSolver:
+    """IterativeLinearSolver (src/Solvers.jl:88-152) on the device: solve! assembles
+    the residual and the stiffness (one fused pass), solves K x = R by conjugate
+    gradients on the assembled CSC (fec_cg_solve), and updates Uu -= x.
+    preconditioner "none" is the reference's Krylov CG; "jacobi" scales by the
+    diagonal."""
+
+    def __init__(self, assembler: SparseMatrixAssembler, *, preconditioner: str = "jacobi", rtol: float = 1e-10,
+                 max_iter: int = 10000):
+        if preconditioner not in ("none", "jacobi"):
+            raise ValueError("preconditioner is 'none' or 'jacobi'")
+        self.assembler = assembler
+        self.preconditioner = preconditioner
+        self.rtol, self.max_iter = float(rtol), int(max_iter)
+        self.iterations, self.rel_residual = 0, float("nan")
+        self.dUu = None
+
+    def solve(self, Uu, p: Parameters):
+        """solve!(solver, Uu, p): one Newton update of the device unknowns Uu in place."""
+        torch = _torch()
+        asm = self.assembler
+        R, K = assemble_residual_and_stiffness(asm, Uu, p)
+        if self.dUu is None or self.dUu.numel() != R.numel():
+            self.dUu = torch.zeros_like(R)
+        else:
+            self.dUu.zero_()
+        it, rr = C.c_int(0), C.c_double(0.0)
+        stream = C.c_void_p(torch.cuda.current_stream(asm.device).cuda_stream)
+        asm._call("fec_cg_solve", _lib.ptr(K.nzval), _lib.ptr(R), _lib.ptr(self.dUu), self.max_iter, self.rtol,
+                  1 if self.preconditioner == "jacobi" else 0, C.byref(it), C.byref(rr), stream)
+        self.iterations, self.rel_residual = it.value, rr.value
+        Uu.sub_(self.dUu)
+        return Uu
+
+
 __all__ = ["SparseMatrixAssembler", "CSCMatrix", "Parameters", "create_parameters", "update_dofs_bcs",
            "assemble_vector", "assemble_stiffness", "assemble_matrix", "assemble_residual_and_stiffness",
-           "assemble_matrix_free_action", "stiffness_action", "hvp", "residual", "stiffness", "ELEMENT_IDS"]
+           "assemble_matrix_free_action", "stiffness_action", "hvp", "residual", "stiffness", "ELEMENT_IDS",
+           "IterativeLinearSolver"]
 
 
 def autotune_report() -> list[str]:

@@ -152,6 +152,16 @@ int fec_assemble(fec_ctx* ctx, int want, int precision, double t, double dt, con
 int fec_assemble_action(fec_ctx* ctx, int precision, double t, double dt, const double* U_dev,
                         const double* state_old_dev, const double* Vu_dev, double* Kv_u_dev, void* stream);
 
+/* Linear solve after assembly: conjugate gradients on the assembled CSC
+ * stiffness over the unknowns (nzval from fec_assemble; symmetric), K x = b,
+ * starting from x.  preconditioner 0: none (the reference's Krylov CG), 1:
+ * Jacobi.  Stops at ||b - K x|| <= rtol ||b|| (checked every 10 iterations) or
+ * after max_iter; reports the iterations and the final relative residual.
+ * Bitwise repeatable.  Synchronises the stream.  Replaces the Krylov solve of
+ * IterativeLinearSolver (src/Solvers.jl:88-152). */
+int fec_cg_solve(fec_ctx* ctx, const double* nzval_dev, const double* b_dev, double* x_dev, int max_iter,
+                 double rtol, int preconditioner, int* iterations, double* rel_residual, void* stream);
+
 /* Assembly that allocates no device memory.  No counterpart in the reference.
  *
  * fec_assemble keeps its element-matrix workspace in memory it cudaMallocs on
