@@ -35,10 +35,23 @@ struct J2MLP {
                                Real* P9, Real* scr) {
     Real s13[J2::SCR];
     J2::point(props, gu, jxw, st_old, st_new, P9, s13);
-    float C6[36];
-    tangent6_from([&](int i, int J, int k, int L) { return float(J2::aentry(s13, i, J, k, L)); }, C6);
+    // the consistent tangent in Voigt form, d sigma_m / d eps_n (tensor strain
+    // components): (kap' - mt'/3) [m,n normal] + mt' I_mn (1/2 for shear m = n)
+    // - mb' n_m n_n, shear columns counting both (k,L) and (L,k)
+    const int ii[6] = {0, 1, 2, 1, 0, 0}, jj[6] = {0, 1, 2, 2, 2, 1};
+    const Real ca = s13[9] - s13[10] / Real(3), mt = s13[10], mb = s13[11];
 #pragma unroll
-    for (int m = 0; m < 36; ++m) scr[m] = Real(C6[m]);
+    for (int m = 0; m < 6; ++m) {
+      const Real nm = s13[ii[m] * 3 + jj[m]];
+#pragma unroll
+      for (int n = 0; n < 6; ++n) {
+        const Real nn = s13[ii[n] * 3 + jj[n]];
+        Real c = -mb * nm * nn;
+        if (m < 3 && n < 3) c += ca;
+        if (m == n) c += m < 3 ? mt : Real(0.5) * mt;
+        scr[m * 6 + n] = n >= 3 ? Real(2) * c : c;
+      }
+    }
   }
 
   // Trial state of a point: e_tr = eps - eps_p_old, the network's input row x
