@@ -40,7 +40,7 @@ for _p in (str(ROOT / "finiteelementcontainers.jl_gb300"), str(ROOT)):
 METRIC = "R+K assembly Melem/s & % HBM roofline; MLP closure vs exact at 1e-3 stress err"
 UNIT = "Melem/s"
 # compulsory HBM bytes per element of one R+K pass (int32 connectivity, X and U
-# gathers, residual and nzval written once), see the design doc
+# gathers, residual and nzval written once)
 WORKLOADS = {
     "neohookean": dict(n=128, kind="vector", name="neohookean_hex8_128cubed", flop_per_elem=48e3, state=0),
     "poisson": dict(n=32, kind="scalar", name="poisson_hex8_32cubed", flop_per_elem=8e3, state=0),

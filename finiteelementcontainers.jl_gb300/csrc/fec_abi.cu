@@ -84,6 +84,7 @@ struct fec_ctx {
   DevBuf d_cl_img, d_cl_table;  // tensor-core closure: packed parameters, per-point table
   DevBuf d_V;                   // matrix-free action: the direction as a full field
   DevBuf d_colptr0, d_rowval32, d_cg;  // linear solve: 0-based CSC pattern, CG scratch
+  DevBuf d_flag;                       // non-finite scan result
   float cl_tol = 0.f;
   // optional per-launch timing (CUDA events on the caller's stream)
   bool profiling = false;
@@ -171,6 +172,12 @@ __global__ void set_unknowns_kernel(double* U, int64_t n, const int64_t* unknown
   if (k < n) U[unknown_dofs[k]] = Uu[k];
 }
 
+// Smallest index of a non-finite entry of x[0..n) into *first (atomicMin).
+__global__ void first_nonfinite_kernel(const double* x, int64_t n, unsigned long long* first) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    if (!isfinite(x[i])) atomicMin(first, (unsigned long long)i);
+}
+
 // Records an event pair around launch `name` when profiling is on.
 struct LaunchTimer {
   fec_ctx* c;
@@ -245,7 +252,7 @@ int fec_ctx_destroy(fec_ctx* c) {
   for (DevBuf* b : {&c->d_coords, &c->d_conn, &c->d_ref, &c->d_nadj_ptr, &c->d_nadj, &c->d_epos, &c->d_umask,
                     &c->d_col_base, &c->d_col_len, &c->d_dtu, &c->d_unknown_dofs, &c->d_Ke, &c->d_Re, &c->d_cl_w,
                     &c->d_cl_norm, &c->d_cl_cnt, &c->d_cl_args, &c->d_cl_img, &c->d_cl_table, &c->d_V, &c->d_colptr0, &c->d_rowval32,
-                    &c->d_cg})
+                    &c->d_cg, &c->d_flag})
     b->release();
   delete c;
   return FEC_OK;
@@ -898,6 +905,29 @@ int fec_cg_solve(fec_ctx* c, const double* nzval, const double* b, double* x, in
   if (iterations) *iterations = it;
   if (rel_residual) *rel_residual = rr;
   if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "conjugate gradients: %s", cudaGetErrorString(e));
+  return ok(c);
+}
+
+int fec_check_finite(fec_ctx* c, const double* R_u, const double* nzval, int64_t* first_bad, void* stream) {
+  if (!c) return FEC_ERR_ARG;
+  if (c->device < 0) return fail(c, FEC_ERR_STATE, "host-only context (device -1) cannot run kernels");
+  if (!c->pattern_ready) return fail(c, FEC_ERR_STATE, "fec_check_finite before fec_pattern_build");
+  cudaSetDevice(c->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc;
+  if ((rc = ensure(c, c->d_flag, 2 * sizeof(unsigned long long)))) return rc;
+  unsigned long long* d = static_cast<unsigned long long*>(c->d_flag.p);
+  FEC_CUDA(c, cudaMemsetAsync(d, 0xFF, 2 * sizeof(unsigned long long), s));
+  if (R_u && c->n_unknowns > 0) first_nonfinite_kernel<<<1216, 256, 0, s>>>(R_u, c->n_unknowns, d);
+  if (nzval && c->nnz > 0) first_nonfinite_kernel<<<1216, 256, 0, s>>>(nzval, c->nnz, d + 1);
+  FEC_CUDA(c, cudaGetLastError());
+  unsigned long long h[2];
+  FEC_CUDA(c, cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost, s));
+  FEC_CUDA(c, cudaStreamSynchronize(s));
+  const unsigned long long none = ~0ull;
+  if (first_bad) *first_bad = h[0] != none ? int64_t(h[0]) : (h[1] != none ? int64_t(h[1]) : -1);
+  if (h[0] != none) return fail(c, FEC_ERR_NONFINITE, "residual entry %lld is not finite", (long long)h[0]);
+  if (h[1] != none) return fail(c, FEC_ERR_NONFINITE, "nzval entry %lld is not finite", (long long)h[1]);
   return ok(c);
 }
 

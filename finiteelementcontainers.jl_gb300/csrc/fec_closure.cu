@@ -1,5 +1,5 @@
 // fec_closure.cu -- the learned J2 closure: exact return-map batches (training
-// data and the judge), the MLP's training kernels (forward/backward, Adam) and
+// data and the reference for its error), the MLP's training kernels (forward/backward, Adam) and
 // the closure physics inside the element kernel.
 #include <cmath>
 #include "../../include/fec_gb300.h"
@@ -42,7 +42,7 @@ struct J2Params {
   double p[4];
 };
 
-// exact J2 update of a batch of points (FP64): data generation and the judge
+// exact J2 update of a batch of points (FP64): data generation and the error reference
 __global__ void j2_points_kernel(J2Params P, int64_t n, const double* strain, const double* st_old, double* stress,
                                  double* st_new, double* tangent) {
   const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;

@@ -53,6 +53,7 @@ SIGNATURES = {
     "fec_mlp_eval_tc": (C.c_int, [_vp, _vp, _vp, C.c_int64, _vp, _vp, _vp]),
     "fec_autotune_report": (C.c_int, [C.c_char_p, C.c_size_t]),
     "fec_assemble_action": (C.c_int, [_vp, C.c_int, C.c_double, C.c_double, _vp, _vp, _vp, _vp, _vp]),
+    "fec_check_finite": (C.c_int, [_vp, _vp, _vp, C.POINTER(C.c_int64), _vp]),
     "fec_cg_solve": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int),
                                C.POINTER(C.c_double), _vp]),
     "fec_tensor_core_status": (C.c_int, [C.c_int]),

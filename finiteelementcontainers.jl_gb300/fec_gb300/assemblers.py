@@ -308,10 +308,23 @@ def assemble_stiffness(asm: SparseMatrixAssembler, func, Uu, p: Parameters, *, p
 assemble_matrix = assemble_stiffness
 
 
-def assemble_residual_and_stiffness(asm: SparseMatrixAssembler, Uu, p: Parameters, *, precision: str | None = None):
+def assemble_residual_and_stiffness(asm: SparseMatrixAssembler, Uu, p: Parameters, *, precision: str | None = None,
+                                    check_finite: bool = False):
     """One fused pass producing both residual(asm) and stiffness(asm), the pair a
-    Newton iteration assembles (src/Solvers.jl:128-153)."""
-    return _assemble(asm, _lib.FEC_WANT_RESIDUAL | _lib.FEC_WANT_STIFFNESS, Uu, p, precision)
+    Newton iteration assembles (src/Solvers.jl:128-153).  check_finite raises
+    FECError (FEC_ERR_NONFINITE) when an output holds NaN/Inf (synchronises)."""
+    R, K = _assemble(asm, _lib.FEC_WANT_RESIDUAL | _lib.FEC_WANT_STIFFNESS, Uu, p, precision)
+    if check_finite:
+        check_finite_outputs(asm, R, K)
+    return R, K
+
+
+def check_finite_outputs(asm: SparseMatrixAssembler, R=None, K=None) -> None:
+    """Raise FECError (FEC_ERR_NONFINITE) if the residual or the stiffness values hold NaN/Inf."""
+    torch = _torch()
+    bad = C.c_int64(-1)
+    stream = C.c_void_p(torch.cuda.current_stream(asm.device).cuda_stream)
+    asm._call("fec_check_finite", _lib.ptr(R), _lib.ptr(K.nzval) if K is not None else None, C.byref(bad), stream)
 
 
 def stiffness_action(*_):
@@ -386,7 +399,7 @@ class IterativeLinearSolver:
 __all__ = ["SparseMatrixAssembler", "CSCMatrix", "Parameters", "create_parameters", "update_dofs_bcs",
            "assemble_vector", "assemble_stiffness", "assemble_matrix", "assemble_residual_and_stiffness",
            "assemble_matrix_free_action", "stiffness_action", "hvp", "residual", "stiffness", "ELEMENT_IDS",
-           "IterativeLinearSolver"]
+           "IterativeLinearSolver", "check_finite_outputs"]
 
 
 def autotune_report() -> list[str]:

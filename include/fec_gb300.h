@@ -162,6 +162,13 @@ int fec_assemble_action(fec_ctx* ctx, int precision, double t, double dt, const 
 int fec_cg_solve(fec_ctx* ctx, const double* nzval_dev, const double* b_dev, double* x_dev, int max_iter,
                  double rtol, int preconditioner, int* iterations, double* rel_residual, void* stream);
 
+/* Scans assembled outputs (either may be NULL) for NaN/Inf: FEC_OK, or
+ * FEC_ERR_NONFINITE with the first offending index (residual first, then nzval;
+ * -1 if none) and a message naming the array.  Synchronises the stream.  The
+ * boundary's non-finite check; the reference does not check. */
+int fec_check_finite(fec_ctx* ctx, const double* R_u_dev, const double* nzval_dev, int64_t* first_bad,
+                     void* stream);
+
 /* Assembly that allocates no device memory.  No counterpart in the reference.
  *
  * fec_assemble keeps its element-matrix workspace in memory it cudaMallocs on
@@ -196,7 +203,7 @@ int fec_mlp_param_count(void);
 /* Exact J2 radial return of n points (FP64, device arrays): strain (6 tensor
  * components xx yy zz yz xz xy per point), state (7) -> stress (6), new state
  * (7), and optionally the 6x6 consistent tangent d sigma / d eps.  props as
- * FEC_PHYS_J2.  Used to generate training data and to judge the closure. */
+ * FEC_PHYS_J2.  Used to generate training data and as the reference for the closure's error. */
 int fec_j2_points(const double* props, int64_t n, const double* strain_dev, const double* state_old_dev,
                   double* stress_dev, double* state_new_dev, double* tangent_dev, void* stream);
 /* MLP forward pass on n normalised samples X (n x 14) -> Y (n x 13), FP32. */

@@ -134,7 +134,7 @@ def test_training_gains_over_untrained_network(fec):
     assert val["fp32_params"]["deviatoric_stress"] < 0.1 * val_un["fp32_params"]["deviatoric_stress"]
     assert val["fp32_params"]["stress"] < 1e-2
     # inside assembly, along a 10-step load path with state carried (the closure serves the
-    # plastic points; the exact return map judges it)
+    # plastic points; the exact return map is the reference)
     exact, _ = _j2_path(fec, fec.J2Plasticity(*PROPS))
     runs = {}
     loose = closure.TrainedClosure(trained.params, trained.normalisation, [], 5e-2)

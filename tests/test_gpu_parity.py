@@ -266,3 +266,18 @@ def test_j2_load_path_with_state(fec, orc, precision):
         # the library reads state_old from the parameters; keep it equal to the oracle's
         p.state_old.copy_(torch.from_numpy(so))
     assert yielded > 0
+
+
+def test_nonfinite_outputs_are_reported(fec):
+    """The boundary's NaN/Inf check: a NaN in the unknowns reaches the residual and
+    nzval, and fec_check_finite reports FEC_ERR_NONFINITE naming the array."""
+    torch = _torch()
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (4, 4, 4))
+    asm, p = _setup(fec, mesh, "vector", fec.NeoHookean.from_youngs(1.0, 0.3))
+    U = stretch_field(mesh.nodal_coords, seed=2).ravel()
+    Uu = torch.from_numpy(U[asm.dof.unknown_dofs - 1].copy()).cuda()
+    fec.assemble_residual_and_stiffness(asm, Uu, p, check_finite=True)   # finite: no error
+    Uu[7] = float("nan")
+    with pytest.raises(fec.FECError) as info:
+        fec.assemble_residual_and_stiffness(asm, Uu, p, check_finite=True)
+    assert info.value.status == -5 and "residual" in str(info.value)

@@ -162,6 +162,13 @@ def test_abi_error_paths_host_only(fec):
         assert lib.fec_pattern_build(h, C.byref(nnz)) == 0 and nnz.value == 49
         st = lib.fec_assemble(h, 3, 0, 0.0, 0.0, None, None, None, None, None, None, None)
         assert st == _lib.FEC_ERR_STATE and "host-only" in _lib.last_error(lib, h)
+        # every device entry point refuses a host-only context instead of touching a GPU
+        bad_index = C.c_int64()
+        assert lib.fec_check_finite(h, None, None, C.byref(bad_index), None) == _lib.FEC_ERR_STATE
+        assert lib.fec_assemble_action(h, 0, 0.0, 0.0, None, None, None, None, None) == _lib.FEC_ERR_STATE
+        it, rr = C.c_int(), C.c_double()
+        assert lib.fec_cg_solve(h, None, None, None, 10, 1e-8, 0, C.byref(it), C.byref(rr), None) == \
+            _lib.FEC_ERR_STATE
         props = np.array([1.0])
         assert lib.fec_physics_set(h, 2, 1, props.ctypes.data, 1) == _lib.FEC_ERR_ARG
         assert lib.fec_physics_set(h, 1, 99, props.ctypes.data, 1) == _lib.FEC_ERR_UNSUPPORTED
