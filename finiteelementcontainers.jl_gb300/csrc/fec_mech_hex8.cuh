@@ -68,6 +68,13 @@ __device__ __forceinline__ void sym_pair(int m, int& r1, int& r2) {
   r2 = r + m;
 }
 
+// Packed upper-triangle index of entry (r1, r2) of a symmetric 9x9 matrix (the
+// order sym_pair enumerates).
+__device__ __forceinline__ int sym_index(int r1, int r2) {
+  const int lo = r1 < r2 ? r1 : r2, hi = r1 < r2 ? r2 : r1;
+  return 9 * lo - (lo * (lo - 1)) / 2 + (hi - lo);
+}
+
 // FP32 map of a hex8 point from FP64-differenced coordinates; falls back to the
 // FP64 map for distorted elements.  Returns JxW.
 __device__ __forceinline__ float map_hex8_mixed(const double* __restrict__ s_ref, const float* __restrict__ s_reff,
@@ -480,9 +487,11 @@ struct Hex8Df64Smem {
   static constexpr int F_DNX = 0;                       // float2 entries, after the doubles
   static constexpr int F_P = F_DNX + EPB * NQ * 24;
   static constexpr int F_SCR = F_P + EPB * NQ * 9;
-  static constexpr int F_A = (F_SCR + EPB * NQ * SCR2 + 1) & ~1;  // 16-byte aligned
-  static constexpr int A_STRIDE = NQ * 81;              // >= 576 doubles of K staging
-  static constexpr int N_F2 = F_A + EPB * A_STRIDE;
+  static constexpr int F_A = (F_SCR + EPB * NQ * SCR2 + 1) & ~1;  // 45 unique tangent entries per point
+  static constexpr int A_STRIDE = NQ * 45;
+  static constexpr int K_STRIDE = 576;                  // K staging per element, over the whole float2 region
+  static constexpr int N_F2_USE = F_A + EPB * A_STRIDE;
+  static constexpr int N_F2 = N_F2_USE > EPB * K_STRIDE ? N_F2_USE : EPB * K_STRIDE;
   static constexpr size_t BYTES = sizeof(double) * N_DOUBLE + sizeof(float2) * N_F2 + sizeof(int) * EPB * 8 + 16;
 };
 
@@ -560,14 +569,11 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
   }
   __syncthreads();
   if (WANT_K && live) {
-    for (int w = tx; w < NQ * 45; w += TPE) {
+    for (int w = tx; w < NQ * 45; w += TPE) {  // w = 45 q + the packed upper-triangle index
       const int q = w / 45;
       int r1, r2;
       sym_pair(w - q * 45, r1, r2);
-      const float2 v = Model::aentry_df64(s_scr + q * SCR2, r1 / 3, r1 % 3, r2 / 3, r2 % 3);
-      float2* Aq = s_A + q * 81;
-      Aq[r1 * 9 + r2] = v;
-      Aq[r2 * 9 + r1] = v;
+      s_A[w] = Model::aentry_df64(s_scr + q * SCR2, r1 / 3, r1 % 3, r2 / 3, r2 % 3);
     }
   }
   __syncthreads();
@@ -575,6 +581,7 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
   const int pp = tx / 3, i = tx % 3;
   const int a1 = pp, a2 = 7 - pp;
   const int split = 8 - pp;
+  const int r1v[3] = {3 * i, 3 * i + 1, 3 * i + 2};  // rows (i, J) of A for this thread
   const float2 z = make_float2(0.f, 0.f);
   float2 K[27];
 #pragma unroll
@@ -591,11 +598,11 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
         R2 = df64_fma(g20, P[0], df64_fma(g21, P[1], df64_fma(g22, P[2], R2)));
       }
       if (WANT_K) {
-        const float2* Ai = s_A + q * 81 + i * 27;
+        const float2* Aq = s_A + q * 45;
         float2 t1[9], t2[9];
 #pragma unroll
         for (int kl = 0; kl < 9; ++kl) {
-          const float2 x0 = Ai[kl], x1 = Ai[9 + kl], x2 = Ai[18 + kl];
+          const float2 x0 = Aq[sym_index(r1v[0], kl)], x1 = Aq[sym_index(r1v[1], kl)], x2 = Aq[sym_index(r1v[2], kl)];
           t1[kl] = df64_fma(g10, x0, df64_fma(g11, x1, df64_mul(g12, x2)));
           t2[kl] = df64_fma(g20, x0, df64_fma(g21, x1, df64_mul(g22, x2)));
         }
@@ -615,9 +622,9 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
       }
     }
   }
-  __syncthreads();  // s_A is reused for the K staging below (as doubles)
+  __syncthreads();  // the whole float2 region is reused for the K staging below
   if (WANT_K && live) {
-    float2* Ks = s_A;  // 576 double-float entries, KE_NODE_ROWS layout
+    float2* Ks = fb + ty * S::K_STRIDE;  // 576 double-float entries, KE_NODE_ROWS layout
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
       const bool first = j < split;
@@ -641,10 +648,10 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
     const int64_t left = g.ne - e0;
     const int nlive = left < EPB ? int(left) : EPB;
     double2* dst = reinterpret_cast<double2*>(static_cast<double*>(g.Ke) + e0 * 576);
-    const double* src = reinterpret_cast<const double*>(fb + S::F_A);
+    const double* src = reinterpret_cast<const double*>(fb);
     for (int idx = tid; idx < nlive * PER; idx += nthr) {
       const int el = idx / PER, off = idx - el * PER;
-      dst[idx] = *reinterpret_cast<const double2*>(src + el * S::A_STRIDE + off * 2);
+      dst[idx] = *reinterpret_cast<const double2*>(src + el * S::K_STRIDE + off * 2);
     }
   }
 }
