@@ -19,10 +19,41 @@
 
 namespace fec {
 
-__device__ __forceinline__ float2 df64_split(double x) {
+// Split by conversion: three FP64-pipe operations (two conversions, one
+// subtraction).  Used for zero, subnormal-range, huge and non-finite values.
+static __device__ __noinline__ float2 df64_split_fp64(double x) {
   const float hi = __double2float_rn(x);
   const float lo = __double2float_rn(x - double(hi));
   return make_float2(hi, lo);
+}
+
+// Split of a double into hi + lo on the integer and FP32 pipes.  For binary
+// exponents E in [949, 1149] (|x| in about [2^-74, 2^126)):
+//   hi: the mantissa rounded to 24 bits by adding half of the discarded field
+//       (2^28) to the bit pattern -- a carry into the exponent is the correct
+//       rounding -- then the exponent rebiased 1023 -> 127 by one subtraction
+//       on the funnel-shifted word;
+//   lo: x - hi is the difference of the two bit patterns in units of
+//       2^(E-1075) (the bit pattern is linear in the value within a binade and
+//       across the boundary the carry crosses), |diff| <= 2^28, converted to
+//       float (rounded to 24 bits) and scaled by the signed power of two.
+// |lo| <= ulp(hi)/2 (ties round away from zero), |hi + lo - x| <= 2^-48 |x|: the
+// same representation __double2float_rn gives up to the tie rule.  Signed
+// zeros are selected in place; everything else takes the conversion path.
+__device__ __forceinline__ float2 df64_split(double x) {
+  const uint64_t b = uint64_t(__double_as_longlong(x));
+  const uint32_t bh = uint32_t(b >> 32), bl = uint32_t(b);
+  const uint32_t E = (bh >> 20) & 0x7FFu;
+  const bool zero = ((bh & 0x7FFFFFFFu) | bl) == 0u;
+  if (E - 949u > 200u && !zero) return df64_split_fp64(x);
+  const uint64_t r = b + (uint64_t(1) << 28);
+  const uint32_t rh = uint32_t(r >> 32), rl = uint32_t(r);
+  const uint32_t fs = __funnelshift_l(rl, rh, 3);  // exponent (low 9 bits) | top 23 mantissa bits
+  const float hi = __uint_as_float(((fs - 0xC0000000u) & 0x7FFFFFFFu) | (rh & 0x80000000u));
+  const int32_t diff = int32_t(bl - (rl & 0xE0000000u));
+  const float scale = __uint_as_float(((E - 948u) << 23) | (bh & 0x80000000u));
+  const float lo = __fmul_rn(__int2float_rn(diff), scale);
+  return zero ? make_float2(__uint_as_float(bh & 0x80000000u), 0.f) : make_float2(hi, lo);
 }
 
 __device__ __forceinline__ float2 df64_fast2sum(float a, float b) {  // |a| >= |b|

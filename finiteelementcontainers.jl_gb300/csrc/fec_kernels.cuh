@@ -847,6 +847,17 @@ __device__ __forceinline__ double widen_exact(float f) {
   return __longlong_as_double(int64_t(bits));
 }
 
+// Float -> double widening for normal floats and zeros in six integer
+// operations (the exponent rebias is one add on the high word); subnormals,
+// inf and nan go through widen_exact.
+__device__ __forceinline__ double widen(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t mag = u & 0x7FFFFFFFu;
+  if (mag - 0x00800000u >= 0x7F000000u && mag != 0u) return widen_exact(f);
+  const uint32_t hiw = (u & 0x80000000u) | (mag == 0u ? 0u : (mag >> 3) + (896u << 20));
+  return __hiloint2double(int(hiw), int(u << 29));
+}
+
 // Accumulator of the node gather: a compensated FP32 pair (hi, lo).  Adding a
 // float recovers its rounding error exactly with TwoSum (Knuth); adding a
 // double-float pair is a df64 addition.  Either keeps the sum to about 2^-48
@@ -867,7 +878,7 @@ struct GatherAcc {
     float2* p = reinterpret_cast<float2*>(base) + j;
     *p = plus(*p, v);
   }
-  __device__ static double value(float2 a) { return widen_exact(a.x) + widen_exact(a.y); }
+  __device__ static double value(float2 a) { return widen(a.x) + widen(a.y); }
   __device__ static double value(const float* base, int j) { return value(reinterpret_cast<const float2*>(base)[j]); }
 };
 
@@ -934,9 +945,16 @@ __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo&
         if (c < nh) {
           racc = GatherAcc::plus(racc, rv[c]);
           if (wantK) {
+            // one element's values of this lane go to distinct positions: loads,
+            // additions and stores are batched
+            float2* A2 = reinterpret_cast<float2*>(acc);
+            float2 sv[VPL];
 #pragma unroll
             for (int j = 0; j < VPL; ++j)
-              if (pos[c][j] >= 0) GatherAcc::add(acc, pos[c][j], v[c][j]);
+              if (pos[c][j] >= 0) sv[j] = A2[pos[c][j]];
+#pragma unroll
+            for (int j = 0; j < VPL; ++j)
+              if (pos[c][j] >= 0) A2[pos[c][j]] = GatherAcc::plus(sv[j], v[c][j]);
             __syncwarp();
           }
         }
@@ -1039,10 +1057,21 @@ __device__ __forceinline__ void gather_run_hex8v(const GatherArgs& g, const Bloc
           racc = GatherAcc::plus(racc, rv[c]);
           if (wantK) {
             if (kl) {
-              GatherAcc::add(acc, base + int(ep[c].x & 0xffffu), v[c].x);
-              GatherAcc::add(acc, base + int(ep[c].x >> 16), v[c].y);
-              GatherAcc::add(acc, base + int(ep[c].y & 0xffffu), v[c].z);
-              GatherAcc::add(acc, base + int(ep[c].y >> 16), v[c].w);
+              // the four columns of one element go to four distinct positions, so
+              // their read-modify-writes are issued as one batch of loads, four
+              // independent additions and one batch of stores
+              float2* A2 = reinterpret_cast<float2*>(acc);
+              const int p0 = base + int(ep[c].x & 0xffffu), p1 = base + int(ep[c].x >> 16);
+              const int p2 = base + int(ep[c].y & 0xffffu), p3 = base + int(ep[c].y >> 16);
+              float2 s0 = A2[p0], s1 = A2[p1], s2 = A2[p2], s3 = A2[p3];
+              s0 = GatherAcc::plus(s0, v[c].x);
+              s1 = GatherAcc::plus(s1, v[c].y);
+              s2 = GatherAcc::plus(s2, v[c].z);
+              s3 = GatherAcc::plus(s3, v[c].w);
+              A2[p0] = s0;
+              A2[p1] = s1;
+              A2[p2] = s2;
+              A2[p3] = s3;
             }
             __syncwarp();
           }

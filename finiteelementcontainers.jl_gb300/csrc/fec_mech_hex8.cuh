@@ -3,11 +3,11 @@
 //
 // Compared with the generic mech_element_kernel (one thread per element row):
 //  * the tangent is symmetric for the hyperelastic and associative-plastic
-//    models here (A_iJkL = A_kLiJ), so each element is served by 12 threads,
-//    thread (p, i) owning rows (p, i) and (7-p, i) and only the column blocks
-//    b >= row node: 9 node blocks per thread, 36 of the 64 node pairs in all,
-//    which removes 32% of the contraction FMAs -- the work that binds the FP64
-//    variant to the GB300's FP64 pipe;
+//    models here (A_iJkL = A_kLiJ), so only 36 of the 64 node-pair blocks of
+//    K_e are contracted (32% fewer FMAs): in the FP32/FP64 kernels each
+//    element is served by 12 threads, thread (p, i) owning rows (p, i) and
+//    (7-p, i) and the column blocks b >= row node (9 blocks per thread); the
+//    df64 kernel uses 24 threads per element with a circulant cover (below);
 //  * the tangent tensor is evaluated from its 45 unique entries;
 //  * K_e is staged in shared memory (the mirrored half written there) in the
 //    KE_NODE_ROWS layout the node gather reads, and leaves the CTA as one
@@ -475,8 +475,7 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_rows2_kernel(ElemArgs g) {
 // constitutive update stay in FP64; the shape-function gradients, the stress and
 // the tangent scratch are split into double-float (hi + lo) once per point, the
 // tangent entries and the whole K_e / R_e contraction run in df64, and the
-// double-float results go to the workspace as they are.  Same thread mapping and
-// symmetry as mech_hex8_sym_kernel.
+// double-float results go to the workspace as they are.
 // ---------------------------------------------------------------------------
 template <class Model, int EPB>
 struct Hex8Df64Smem {
@@ -495,11 +494,17 @@ struct Hex8Df64Smem {
   static constexpr size_t BYTES = sizeof(double) * N_DOUBLE + sizeof(float2) * N_F2 + sizeof(int) * EPB * 8 + 16;
 };
 
+// 24 threads per element: thread (a, i) owns row (a, i) and the node blocks
+// b = a, a+1, a+2, a+3 (mod 8), plus b = a+4 for a < 4 -- a circulant cover of
+// the 36 symmetric node pairs, 4 or 5 blocks per row, the other half of K_e
+// mirrored in the staging.  Each thread forms the one tangent vector of its row
+// and holds 15 accumulators, which fits 4 CTAs (24 warps) on an SM: the df64
+// chains are latency-bound, and twice the warps of a 12-thread-per-element
+// layout (rows paired as in mech_hex8_sym_kernel) cut the kernel time by 21%.
 template <class Model, int EPB, bool WANT_R, bool WANT_K>
-__global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
-  constexpr int NQ = 8, TPE = 12, NS = Model::NS, SCR = Model::SCR, SCR2 = Model::SCR2;
+__global__ void __launch_bounds__(EPB * 24, 4) mech_hex8_df64_kernel(ElemArgs g) {
+  constexpr int NQ = 8, TPE = 24, NS = Model::NS, SCR = Model::SCR, SCR2 = Model::SCR2;
   using S = Hex8Df64Smem<Model, EPB>;
-  using L = RefLayout<1>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* dbase = reinterpret_cast<double*>(smem_raw);
   double* s_ref = dbase + S::D_REF;
@@ -513,9 +518,9 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
   const bool live = e < g.ne;
   double* s_x = dbase + S::D_X + ty * 24;
   double* s_u = dbase + S::D_U + ty * 24;
-  float2* s_dNX = fb + S::F_DNX + ty * NQ * 24;
-  float2* s_P = fb + S::F_P + ty * NQ * 9;
-  float2* s_scr = fb + S::F_SCR + ty * NQ * SCR2;
+  const float2* s_dNX = fb + S::F_DNX + ty * NQ * 24;
+  const float2* s_P = fb + S::F_P + ty * NQ * 9;
+  const float2* s_scr = fb + S::F_SCR + ty * NQ * SCR2;
   float2* s_A = fb + S::F_A + ty * S::A_STRIDE;
   int* s_conn = s_conn_all + ty * 8;
 
@@ -525,17 +530,12 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
                       reinterpret_cast<uint64_t*>(s_conn_all + EPB * 8), tid, nthr);
   }
   if (live) {
-    for (int i = tx; i < 24; i += TPE) {
-      const int a = i / 3, d = i % 3;
-      s_x[i] = __ldg(&g.coords[int64_t(s_conn[a]) * 3 + d]);
-      s_u[i] = __ldg(&g.U[int64_t(s_conn[a]) * 3 + d]);
-    }
+    const int a = tx / 3, d = tx % 3;
+    s_x[tx] = __ldg(&g.coords[int64_t(s_conn[a]) * 3 + d]);
+    s_u[tx] = __ldg(&g.U[int64_t(s_conn[a]) * 3 + d]);
   }
   __syncthreads();
-  // Per-point map and constitutive update in native FP64: the CTA's EPB * 8 points
-  // go to its first EPB * 8 threads, so every warp that issues this FP64 work has
-  // all 32 lanes busy (the FP64 pipe is the scarce one).
-  if (tid < EPB * NQ) {
+  if (tid < EPB * NQ) {  // per-point map and constitutive update, native FP64, full warps
     const int el = tid / NQ, q = tid % NQ;
     const int64_t ep = e0 + el;
     if (ep < g.ne) {
@@ -553,15 +553,15 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
           for (int a = 0; a < 8; ++a) s = fma(pu[a * 3 + i], dNX[a * 3 + j], s);
           gu[i][j] = s;
         }
+      float2* pdNX = fb + S::F_DNX + el * NQ * 24;
+#pragma unroll
+      for (int m = 0; m < 24; ++m) pdNX[q * 24 + m] = df64_split(dNX[m]);  // dNX dies before the model
       const double* so = NS ? g.state_old + (ep * NQ + q) * NS : nullptr;
       double* sn = (NS && g.state_new) ? g.state_new + (ep * NQ + q) * NS : nullptr;
       double P9[9], scr[SCR];
       Model::point(g.props, gu, jxw, so, sn, P9, scr);
-      float2* pdNX = fb + S::F_DNX + el * NQ * 24;
       float2* pP = fb + S::F_P + el * NQ * 9;
       float2* pscr = fb + S::F_SCR + el * NQ * SCR2;
-#pragma unroll
-      for (int m = 0; m < 24; ++m) pdNX[q * 24 + m] = df64_split(dNX[m]);
 #pragma unroll
       for (int m = 0; m < 9; ++m) pP[q * 9 + m] = df64_split(P9[m]);
       Model::split_scratch(scr, pscr + q * SCR2);
@@ -569,7 +569,7 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
   }
   __syncthreads();
   if (WANT_K && live) {
-    for (int w = tx; w < NQ * 45; w += TPE) {  // w = 45 q + the packed upper-triangle index
+    for (int w = tx; w < NQ * 45; w += TPE) {
       const int q = w / 45;
       int r1, r2;
       sym_pair(w - q * 45, r1, r2);
@@ -578,46 +578,38 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
   }
   __syncthreads();
 
-  const int pp = tx / 3, i = tx % 3;
-  const int a1 = pp, a2 = 7 - pp;
-  const int split = 8 - pp;
-  const int r1v[3] = {3 * i, 3 * i + 1, 3 * i + 2};  // rows (i, J) of A for this thread
+  const int a = tx / 3, i = tx % 3;
+  const bool fifth = a < 4;
+  const int r1v[3] = {3 * i, 3 * i + 1, 3 * i + 2};
   const float2 z = make_float2(0.f, 0.f);
-  float2 K[27];
+  float2 K[15];
 #pragma unroll
-  for (int c = 0; c < 27; ++c) K[c] = z;
-  float2 R1 = z, R2 = z;
+  for (int c = 0; c < 15; ++c) K[c] = z;
+  float2 R = z;
   if (live) {
+#pragma unroll 1
     for (int q = 0; q < NQ; ++q) {
       const float2* dNX = s_dNX + q * 24;
-      const float2 g10 = dNX[a1 * 3], g11 = dNX[a1 * 3 + 1], g12 = dNX[a1 * 3 + 2];
-      const float2 g20 = dNX[a2 * 3], g21 = dNX[a2 * 3 + 1], g22 = dNX[a2 * 3 + 2];
+      const float2 g0 = dNX[a * 3], g1 = dNX[a * 3 + 1], g2 = dNX[a * 3 + 2];
       if (WANT_R) {
         const float2* P = s_P + q * 9 + i * 3;
-        R1 = df64_fma(g10, P[0], df64_fma(g11, P[1], df64_fma(g12, P[2], R1)));
-        R2 = df64_fma(g20, P[0], df64_fma(g21, P[1], df64_fma(g22, P[2], R2)));
+        R = df64_fma(g0, P[0], df64_fma(g1, P[1], df64_fma(g2, P[2], R)));
       }
       if (WANT_K) {
         const float2* Aq = s_A + q * 45;
-        float2 t1[9], t2[9];
+        float2 t[9];
 #pragma unroll
-        for (int kl = 0; kl < 9; ++kl) {
-          const float2 x0 = Aq[sym_index(r1v[0], kl)], x1 = Aq[sym_index(r1v[1], kl)], x2 = Aq[sym_index(r1v[2], kl)];
-          t1[kl] = df64_fma(g10, x0, df64_fma(g11, x1, df64_mul(g12, x2)));
-          t2[kl] = df64_fma(g20, x0, df64_fma(g21, x1, df64_mul(g22, x2)));
-        }
+        for (int kl = 0; kl < 9; ++kl)
+          t[kl] = df64_fma(g0, Aq[sym_index(r1v[0], kl)],
+                           df64_fma(g1, Aq[sym_index(r1v[1], kl)], df64_mul(g2, Aq[sym_index(r1v[2], kl)])));
 #pragma unroll
-        for (int j = 0; j < 9; ++j) {
-          const bool first = j < split;
-          const int b = first ? pp + j : j - 1;
+        for (int d = 0; d < 5; ++d) {
+          if (d == 4 && !fifth) break;
+          const int b = (a + d) & 7;
           const float2 h0 = dNX[b * 3], h1 = dNX[b * 3 + 1], h2 = dNX[b * 3 + 2];
 #pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            const float2 u0 = first ? t1[k * 3] : t2[k * 3];
-            const float2 u1 = first ? t1[k * 3 + 1] : t2[k * 3 + 1];
-            const float2 u2 = first ? t1[k * 3 + 2] : t2[k * 3 + 2];
-            K[j * 3 + k] = df64_fma(u0, h0, df64_fma(u1, h1, df64_fma(u2, h2, K[j * 3 + k])));
-          }
+          for (int k = 0; k < 3; ++k)
+            K[d * 3 + k] = df64_fma(t[k * 3], h0, df64_fma(t[k * 3 + 1], h1, df64_fma(t[k * 3 + 2], h2, K[d * 3 + k])));
         }
       }
     }
@@ -626,22 +618,17 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_df64_kernel(ElemArgs g) {
   if (WANT_K && live) {
     float2* Ks = fb + ty * S::K_STRIDE;  // 576 double-float entries, KE_NODE_ROWS layout
 #pragma unroll
-    for (int j = 0; j < 9; ++j) {
-      const bool first = j < split;
-      const int an = first ? a1 : a2;
-      const int b = first ? pp + j : j - 1;
+    for (int d = 0; d < 5; ++d) {
+      if (d == 4 && !fifth) break;
+      const int b = (a + d) & 7;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        Ks[((an * 3 + i) * 3 + k) * 8 + b] = K[j * 3 + k];
-        if (b != an) Ks[((b * 3 + k) * 3 + i) * 8 + an] = K[j * 3 + k];
+        Ks[((a * 3 + i) * 3 + k) * 8 + b] = K[d * 3 + k];
+        if (d) Ks[((b * 3 + k) * 3 + i) * 8 + a] = K[d * 3 + k];
       }
     }
   }
-  if (WANT_R && live) {
-    float2* Re = static_cast<float2*>(g.Re) + e * 24;
-    Re[a1 * 3 + i] = R1;
-    Re[a2 * 3 + i] = R2;
-  }
+  if (WANT_R && live) static_cast<float2*>(g.Re)[e * 24 + tx] = R;
   if (WANT_K) {
     __syncthreads();
     constexpr int PER = 576 / 2;

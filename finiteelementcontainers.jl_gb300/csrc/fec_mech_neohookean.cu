@@ -93,12 +93,10 @@ cudaError_t hex8_1(const ElemArgs& a, cudaStream_t s) {
 template <int EPB, bool R, bool K>
 cudaError_t hex8_df64_1(const ElemArgs& a, cudaStream_t s) {
   constexpr size_t smem = Hex8Df64Smem<NeoHookean, EPB>::BYTES;
-  auto kern = mech_hex8_df64_kernel<NeoHookean, EPB, R, K>;
-  cudaError_t err = ensure_smem<mech_hex8_df64_kernel<NeoHookean, EPB, R, K>>(smem);
-  if (err != cudaSuccess) return err;
-  const dim3 block(12, EPB);
   const dim3 grid(unsigned((a.ne + EPB - 1) / EPB));
-  kern<<<grid, block, smem, s>>>(a);
+  cudaError_t err;
+  if ((err = ensure_smem<mech_hex8_df64_kernel<NeoHookean, EPB, R, K>>(smem)) != cudaSuccess) return err;
+  mech_hex8_df64_kernel<NeoHookean, EPB, R, K><<<grid, dim3(24, EPB), smem, s>>>(a);
   return cudaGetLastError();
 }
 
