@@ -254,6 +254,22 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def exact_fp64_native_ms(args, n) -> float | None:
+    """Milliseconds per load step of exact FP64 J2 assembly on the same path with
+    the element contraction in native FP64 arithmetic (the selection is fixed per
+    process, so it runs in a child process)."""
+    env = dict(os.environ, FEC_FP64_CONTRACTION="native")
+    cmd = [sys.executable, os.path.abspath(__file__), "--workload", "j2", "--n", str(n), "--steps", str(args.steps),
+           "--warmup", str(args.warmup), "--no-cpu-baseline", "--no-e2e", "--no-variants"]
+    r = subprocess.run(cmd, env=env, capture_output=True, text=True)
+    if r.returncode != 0:
+        return None
+    try:
+        return float(json.loads(r.stdout.strip().splitlines()[-1])["ms_per_step"])
+    except (ValueError, KeyError, IndexError):
+        return None
+
+
 def run_closure(args) -> None:
     """Learned closure vs exact return mapping on the 96^3 J2 load path (20 steps,
     state carried), each path timed whole; errors per step against exact FP64."""
@@ -365,6 +381,7 @@ def run_closure(args) -> None:
             "max_rel_err_vs_exact_fp64_over_path": err, "kernels_ms": kernels(a, p, d)}
     x32_err = errors(a32, p32, d32)
     x_kernels = {"fp32_element": kernels(a32, p32, d32), "fp64": kernels(a64, p64, d64)}
+    t_x64n = exact_fp64_native_ms(args, n)
     main_t = t_cl[1e-4]
     line = {
         "metric": METRIC, "value": ne / (main_t * 1e-3) / 1e6, "unit": UNIT, "n_gpus": 1,
@@ -382,7 +399,11 @@ def run_closure(args) -> None:
         "closure": {"validation_rel_err": val, **out},
         "exact": {"fp32_element_ms_per_load_step": t_x32, "fp64_ms_per_load_step": t_x64,
                   "fp32_element_max_rel_err_vs_fp64": x32_err, "kernels_ms": x_kernels,
-                  "speedup_closure_vs_exact_fp64": t_x64 / main_t, "speedup_closure_vs_exact_fp32": t_x32 / main_t},
+                  "fp64_native_ms_per_load_step": t_x64n,
+                  "fp64_native": "exact FP64 assembly with every product in native FP64 arithmetic "
+                                 "(the reference's arithmetic; FEC_FP64_CONTRACTION=native), same path",
+                  "speedup_closure_vs_exact_fp64": t_x64 / main_t, "speedup_closure_vs_exact_fp32": t_x32 / main_t,
+                  "speedup_closure_vs_exact_fp64_native": (t_x64n / main_t) if t_x64n else None},
         "clocks": clk.summary(), "e2e": None, "gpu_launches": int(main_launches), "cpu_baseline": None,
     }
     print(json.dumps(line), flush=True)

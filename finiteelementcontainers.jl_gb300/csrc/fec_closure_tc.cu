@@ -1,7 +1,8 @@
 // fec_closure_tc.cu -- the learned J2 closure on the 5th-generation tensor cores.
 //
-// A persistent CTA of 512 threads takes 16 hex8 elements (128 quadrature points,
-// the M = 128 of one tcgen05 MMA) at a time:
+// A persistent CTA of 288 threads (eight epilogue warps and one warp that
+// issues the MMAs) takes 16 hex8 elements (128 quadrature points, the M = 128 of
+// one tcgen05 MMA) at a time:
 //   A  element staging, isoparametric map and displacement gradient per point,
 //      trial state; elastic points are completed exactly, plastic points write
 //      their normalised input row to the first layer's operand tile;
@@ -11,10 +12,11 @@
 //      accumulators in tensor memory.  The activation row uses a two-term BF16
 //      split of activations and weights (hi*Whi + lo*Whi + hi*Wlo), which keeps
 //      the stress near FP32 accuracy; tangent rows use one BF16 term.  Between
-//      layers the 16 warps read the accumulators back (tcgen05.ld), apply bias,
-//      SiLU and SiLU' and write the next operand tiles;
+//      layers the eight epilogue warps read the accumulators back (tcgen05.ld),
+//      apply bias, SiLU and SiLU' and write the next operand tiles;
 //   C  per plastic point: stress and tangent from the outputs, the consistency
 //      check, and the exact return map where the check fails.
+// C of one tile (warps 0..3) runs concurrently with A of the next (warps 4..7).
 // Each point's stress (Voigt) and 6x6 tangent go to a point table; the FP32 hex8
 // element kernel (point-table model) then forms R_e and K_e from it.
 #include <cmath>
@@ -122,15 +124,27 @@ struct Ctx {
   uint32_t phase_a, phase_t;
 };
 
+// The shared-space base address as a value the compiler cannot treat as loop
+// invariant: the ~100 descriptors of a tile's MMAs are then formed just before
+// each issue (a few integer operations) instead of being hoisted out of the tile
+// loop and kept live -- which spilled them to local memory and made the single
+// issuing thread wait on L2 for every MMA.
+__device__ __forceinline__ uint32_t opaque(uint32_t v) {
+  uint32_t r;
+  asm volatile("mov.b32 %0, %1;" : "=r"(r) : "r"(v));
+  return r;
+}
+
 // MMAs of layer l, issued by one thread.  Accumulator of row vector v at
 // columns 64 v: v = 0 the activation row, v = 1 + j the tangent of input j.
 // Activation rows: hi*Whi + lo*Whi + hi*Wlo; tangent rows: t*Whi.
 __device__ __forceinline__ void issue_act(const Ctx& c, int l) {
   using namespace tc;
+  const uint32_t s0 = opaque(c.s0);
   if (l == 0) {
     const uint32_t id = idesc_bf16(128, 64);
-    const uint64_t xh = smem_desc(c.s0 + S_X0_H, 128, 256), xl = smem_desc(c.s0 + S_X0_L, 128, 256);
-    const uint64_t wh = smem_desc(c.s0 + S_IMG + W0H, 128, 256), wl = smem_desc(c.s0 + S_IMG + W0L, 128, 256);
+    const uint64_t xh = smem_desc(s0 + S_X0_H, 128, 256), xl = smem_desc(s0 + S_X0_L, 128, 256);
+    const uint64_t wh = smem_desc(s0 + S_IMG + W0H, 128, 256), wl = smem_desc(s0 + S_IMG + W0L, 128, 256);
     mma_bf16(c.tmem, xh, wh, id, 0);
     mma_bf16(c.tmem, xl, wh, id, 1);
     mma_bf16(c.tmem, xh, wl, id, 1);
@@ -142,8 +156,8 @@ __device__ __forceinline__ void issue_act(const Ctx& c, int l) {
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
     const uint32_t ko = uint32_t(s) * 256;
-    const uint64_t ah = smem_desc(c.s0 + S_ACT_H + ko, 128, 1024), al = smem_desc(c.s0 + S_ACT_L + ko, 128, 1024);
-    const uint64_t bh = smem_desc(c.s0 + wH + ko, 128, 1024), bl = smem_desc(c.s0 + wL + ko, 128, 1024);
+    const uint64_t ah = smem_desc(s0 + S_ACT_H + ko, 128, 1024), al = smem_desc(s0 + S_ACT_L + ko, 128, 1024);
+    const uint64_t bh = smem_desc(s0 + wH + ko, 128, 1024), bl = smem_desc(s0 + wL + ko, 128, 1024);
     mma_bf16(c.tmem, ah, bh, id, s > 0);
     mma_bf16(c.tmem, al, bh, id, 1);
     mma_bf16(c.tmem, ah, bl, id, 1);
@@ -151,16 +165,17 @@ __device__ __forceinline__ void issue_act(const Ctx& c, int l) {
 }
 __device__ __forceinline__ void issue_tan(const Ctx& c, int l) {  // l >= 1
   using namespace tc;
+  const uint32_t s0 = opaque(c.s0);
   const bool out = l == MLP_LAYERS - 1;
   const uint32_t id = idesc_bf16(128, out ? 16 : 64);
   const uint32_t wH = S_IMG + (out ? W4H : WH(l));
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
     const uint32_t ko = uint32_t(s) * 256;
-    const uint64_t bh = smem_desc(c.s0 + wH + ko, 128, 1024);
+    const uint64_t bh = smem_desc(s0 + wH + ko, 128, 1024);
 #pragma unroll
     for (int j = 0; j < 6; ++j)
-      mma_bf16(c.tmem + 64u * (1 + j), smem_desc(c.s0 + S_TAN(j) + ko, 128, 1024), bh, id, s > 0);
+      mma_bf16(c.tmem + 64u * (1 + j), smem_desc(s0 + S_TAN(j) + ko, 128, 1024), bh, id, s > 0);
   }
 }
 
@@ -433,10 +448,11 @@ constexpr uint32_t U_REFF = U_REF + 264 * 8;               // 264 floats
 constexpr uint32_t U_X = U_REFF + 1072;                    // EPT x 24 doubles
 constexpr uint32_t U_XD = U_X + EPT * 24 * 8;              // EPT x 24 floats
 constexpr uint32_t U_U = U_XD + EPT * 24 * 4;              // EPT x 24 floats
-constexpr uint32_t U_GU = U_U + EPT * 24 * 4;              // 128 x 9 floats
-constexpr uint32_t U_FLAG = U_GU + 128 * 9 * 4;            // 128 ints
-constexpr uint32_t U_CONN = U_FLAG + 128 * 4;              // 128 ints
+constexpr uint32_t U_GU = U_U + EPT * 24 * 4;              // 2 x 128 x 9 floats (tile parity)
+constexpr uint32_t U_FLAG = U_GU + 2 * 128 * 9 * 4;        // 2 x 128 ints
+constexpr uint32_t U_CONN = U_FLAG + 2 * 128 * 4;          // 128 ints
 constexpr uint32_t POINTS_SMEM = U_CONN + 128 * 4;
+constexpr int PREP_BAR = 4;                                // named barrier of the preparing warps 4..7
 static_assert(POINTS_SMEM <= 227 * 1024, "closure kernel shared memory");
 static_assert(RefLayout<1>::SIZE == 264, "hex8 reference tables");
 
@@ -453,18 +469,115 @@ __device__ __forceinline__ void write_row(float* table, int64_t p, const float* 
   for (int k = 0; k < POINT_TABLE_STRIDE / 4; ++k) dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
 }
 
+// Phase A of tile t on warps 4..7 (m = point of the tile): staging, map and
+// displacement gradient, trial state; elastic points are completed exactly,
+// plastic points write their input row (others a zero row).  Flags and grad u go
+// to the buffer of the tile's parity.
+__device__ void prep_tile(const ElemArgs& g, const TcClosure& cl, const Ctx& c, int64_t t, int buf, int m) {
+  unsigned char* sm = c.sm;
+  const double* s_ref = reinterpret_cast<const double*>(sm + U_REF);
+  const float* s_reff = reinterpret_cast<const float*>(sm + U_REFF);
+  double* s_x = reinterpret_cast<double*>(sm + U_X);
+  float* s_xd = reinterpret_cast<float*>(sm + U_XD);
+  float* s_u = reinterpret_cast<float*>(sm + U_U);
+  float* s_gu = reinterpret_cast<float*>(sm + U_GU) + buf * 128 * 9;
+  int* s_flag = reinterpret_cast<int*>(sm + U_FLAG) + buf * 128;
+  int* s_conn = reinterpret_cast<int*>(sm + U_CONN);
+  const int64_t e0 = t * EPT;
+  {
+    const int64_t e = e0 + m / 8;
+    s_conn[m] = e < g.ne ? g.conn[e * 8 + (m & 7)] : 0;
+  }
+  named_sync(PREP_BAR, 128);
+  for (int i = m; i < EPT * 24; i += 128) {
+    const int el = i / 24, k = i % 24, a = k / 3, d = k % 3;
+    if (e0 + el < g.ne) {
+      const double xv = __ldg(&g.coords[int64_t(s_conn[el * 8 + a]) * 3 + d]);
+      s_x[i] = xv;
+      s_xd[i] = float(xv - __ldg(&g.coords[int64_t(s_conn[el * 8]) * 3 + d]));
+      s_u[i] = float(__ldg(&g.U[int64_t(s_conn[el * 8 + a]) * 3 + d]));
+    }
+  }
+  named_sync(PREP_BAR, 128);
+  const int el = m / 8, q = m & 7;
+  const int64_t e = e0 + el, p = e * 8 + q;
+  int flag = -1;  // -1: no element, 0: elastic (done), 1: plastic
+  float x[MLP_IN];
+  if (e < g.ne) {
+    float dNX[24];
+    map_hex8_mixed(s_ref, s_reff, q, s_x + el * 24, s_xd + el * 24, dNX);
+    float gu[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        float sum = 0.f;
+#pragma unroll
+        for (int a = 0; a < 8; ++a) sum = fmaf(s_u[el * 24 + a * 3 + i], dNX[a * 3 + j], sum);
+        gu[i][j] = sum;
+        s_gu[m * 9 + i * 3 + j] = sum;
+      }
+    const double* so = g.state_old + p * 7;
+    double* sn = g.state_new ? g.state_new + p * 7 : nullptr;
+    float etr[6];
+    if (J2MLP::trial(g.props, gu, so, etr, x)) {
+      flag = 1;
+    } else {
+      float P9[9], C36[36];
+      J2MLP::exact(g.props, gu, 1.0f, so, sn, P9, C36);
+      write_row(cl.table, p, P9, C36);
+      flag = 0;
+    }
+  }
+  s_flag[m] = flag;
+  write_input_row(c, m, flag == 1 ? x : nullptr);
+  named_sync(PREP_BAR, 128);  // the staging arrays are free for the next tile
+}
+
+// Phase C of tile t on warps 0..3 (m = point of the tile): plastic points from
+// the network's outputs, with the consistency check and the exact fallback.
+__device__ void complete_tile(const ElemArgs& g, const TcClosure& cl, const Ctx& c, int64_t t, int buf, int m) {
+  const float* s_gu = reinterpret_cast<const float*>(c.sm + U_GU) + buf * 128 * 9;
+  const int* s_flag = reinterpret_cast<const int*>(c.sm + U_FLAG) + buf * 128;
+  float y[MLP_OUT], Js[6][6];
+  epilogue_output(c, y, Js);
+  const int plastic = s_flag[m] == 1;
+  int fell_back = 0;
+  if (plastic) {
+    const int64_t p = (t * EPT + m / 8) * 8 + (m & 7);
+    const double* so = g.state_old + p * 7;
+    double* sn = g.state_new ? g.state_new + p * 7 : nullptr;
+    float gu[3][3];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) gu[i / 3][i % 3] = s_gu[m * 9 + i];
+    float etr[6];
+    float x[MLP_IN];
+    J2MLP::trial(g.props, gu, so, etr, x);
+    float P9[9], C36[36];
+    if (!J2MLP::finish(g.props, etr, cl.tol, y, Js, 1.0f, so, sn, P9, C36)) {
+      fell_back = 1;
+      J2MLP::exact(g.props, gu, 1.0f, so, sn, P9, C36);
+    }
+    write_row(cl.table, p, P9, C36);
+  }
+  const unsigned np = __popc(__ballot_sync(0xffffffffu, plastic));
+  const unsigned nf = __popc(__ballot_sync(0xffffffffu, fell_back));
+  if ((m & 31) == 0 && np) {
+    atomicAdd(&cl.counters[0], (unsigned long long)np);
+    if (nf) atomicAdd(&cl.counters[1], (unsigned long long)nf);
+  }
+}
+
+// Tiles of 16 elements.  Per tile the network runs on all eight epilogue warps
+// (B); after it, warps 0..3 complete the tile's points (C) while warps 4..7
+// already prepare the CTA's next tile (A), into the other parity's buffers and
+// the input rows, which the tile's last MMAs no longer read.
 __global__ void __launch_bounds__(NTHR, 1) j2mlp_points_tc_kernel(ElemArgs g, TcClosure cl) {
   extern __shared__ __align__(1024) unsigned char sm[];
   Ctx c;
   setup(c, sm, cl.image);
   double* s_ref = reinterpret_cast<double*>(sm + U_REF);
   float* s_reff = reinterpret_cast<float*>(sm + U_REFF);
-  double* s_x = reinterpret_cast<double*>(sm + U_X);
-  float* s_xd = reinterpret_cast<float*>(sm + U_XD);
-  float* s_u = reinterpret_cast<float*>(sm + U_U);
-  float* s_gu = reinterpret_cast<float*>(sm + U_GU);
-  int* s_flag = reinterpret_cast<int*>(sm + U_FLAG);
-  int* s_conn = reinterpret_cast<int*>(sm + U_CONN);
   const int tid = threadIdx.x;
   for (int i = tid; i < RefLayout<1>::SIZE; i += NTHR) {
     s_ref[i] = g.ref[i];
@@ -474,93 +587,17 @@ __global__ void __launch_bounds__(NTHR, 1) j2mlp_points_tc_kernel(ElemArgs g, Tc
   bool ok = true;
   const bool issuer = tid >= NEPI;
   const int64_t tiles = (g.ne + EPT - 1) / EPT;
-  for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+  int64_t t = blockIdx.x;
+  if (tid >= 128 && tid < NEPI && t < tiles) prep_tile(g, cl, c, t, 0, tid - 128);
+  for (int it = 0; t < tiles; t += gridDim.x, ++it) {
     if (issuer) {
       issue_tile(c);
     } else {
-      const int64_t e0 = t * EPT;
-      // ---- A: staging, kinematics, trial state ----
-      if (tid < 128) {
-        const int64_t e = e0 + tid / 8;
-        s_conn[tid] = e < g.ne ? g.conn[e * 8 + (tid & 7)] : 0;
-      }
-      epi_sync();
-      for (int i = tid; i < EPT * 24; i += NEPI) {
-        const int el = i / 24, k = i % 24, a = k / 3, d = k % 3;
-        if (e0 + el < g.ne) {
-          const double xv = __ldg(&g.coords[int64_t(s_conn[el * 8 + a]) * 3 + d]);
-          s_x[i] = xv;
-          s_xd[i] = float(xv - __ldg(&g.coords[int64_t(s_conn[el * 8]) * 3 + d]));
-          s_u[i] = float(__ldg(&g.U[int64_t(s_conn[el * 8 + a]) * 3 + d]));
-        }
-      }
-      epi_sync();
-      int plastic = 0;
-      if (tid < 128) {
-        const int el = tid / 8, q = tid & 7;
-        const int64_t e = e0 + el, p = e * 8 + q;
-        int flag = -1;  // -1: no element, 0: elastic (done), 1: plastic
-        float x[MLP_IN];
-        if (e < g.ne) {
-          float dNX[24];
-          map_hex8_mixed(s_ref, s_reff, q, s_x + el * 24, s_xd + el * 24, dNX);
-          float gu[3][3];
-#pragma unroll
-          for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-              float s = 0.f;
-#pragma unroll
-              for (int a = 0; a < 8; ++a) s = fmaf(s_u[el * 24 + a * 3 + i], dNX[a * 3 + j], s);
-              gu[i][j] = s;
-              s_gu[tid * 9 + i * 3 + j] = s;
-            }
-          const double* so = g.state_old + p * 7;
-          double* sn = g.state_new ? g.state_new + p * 7 : nullptr;
-          float etr[6];
-          if (J2MLP::trial(g.props, gu, so, etr, x)) {
-            flag = 1;
-          } else {
-            float P9[9], C36[36];
-            J2MLP::exact(g.props, gu, 1.0f, so, sn, P9, C36);
-            write_row(cl.table, p, P9, C36);
-            flag = 0;
-          }
-        }
-        s_flag[tid] = flag;
-        plastic = flag == 1;
-        write_input_row(c, tid, plastic ? x : nullptr);
-      }
-      // ---- B: the network on all 128 rows (the issuer warp issues the MMAs) ----
       epilogue_tile(c, ok);
-      // ---- C: plastic points from the network, with the consistency check ----
-      if (ok && tid < 128) {
-        float y[MLP_OUT], Js[6][6];
-        epilogue_output(c, y, Js);
-        int fell_back = 0;
-        if (plastic) {
-          const int64_t p = (e0 + tid / 8) * 8 + (tid & 7);
-          const double* so = g.state_old + p * 7;
-          double* sn = g.state_new ? g.state_new + p * 7 : nullptr;
-          float gu[3][3];
-#pragma unroll
-          for (int i = 0; i < 9; ++i) gu[i / 3][i % 3] = s_gu[tid * 9 + i];
-          float etr[6];
-          float x[MLP_IN];
-          J2MLP::trial(g.props, gu, so, etr, x);
-          float P9[9], C36[36];
-          if (!J2MLP::finish(g.props, etr, cl.tol, y, Js, 1.0f, so, sn, P9, C36)) {
-            fell_back = 1;
-            J2MLP::exact(g.props, gu, 1.0f, so, sn, P9, C36);
-          }
-          write_row(cl.table, p, P9, C36);
-        }
-        const unsigned np = __popc(__ballot_sync(0xffffffffu, plastic));
-        const unsigned nf = __popc(__ballot_sync(0xffffffffu, fell_back));
-        if ((tid & 31) == 0 && np) {
-          atomicAdd(&cl.counters[0], (unsigned long long)np);
-          if (nf) atomicAdd(&cl.counters[1], (unsigned long long)nf);
-        }
+      if (tid < 128) {
+        if (ok) complete_tile(g, cl, c, t, it & 1, tid);
+      } else if (t + gridDim.x < tiles) {
+        prep_tile(g, cl, c, t + gridDim.x, (it + 1) & 1, tid - 128);
       }
     }
     tc::tc_fence_before();
