@@ -296,7 +296,13 @@ __device__ void issue_tile(Ctx& c) {
 // they work through the activation epilogue of layer l+1, and the issuer warp
 // issues in parallel with both.  `ok` goes (uniformly) false when a wait gives
 // up; the barrier sequence is kept so that the issuer warp never blocks.
-__device__ void epilogue_tile(Ctx& c, bool& ok) {
+// `mid` runs once on every epilogue thread after layer 0 (a point where the
+// caller can issue background work).
+struct NoMid {
+  __device__ void operator()() const {}
+};
+template <class Mid = NoMid>
+__device__ void epilogue_tile(Ctx& c, bool& ok, const Mid& mid = Mid()) {
   using namespace tc;
   int* abort_flag = reinterpret_cast<int*>(c.sm + S_ABORT);
   release_to_issuer(1, ok);
@@ -322,6 +328,7 @@ __device__ void epilogue_tile(Ctx& c, bool& ok) {
     }
     if (ok) epilogue_tan(c, l, d);
     release_to_issuer(2, ok);
+    if (l == 0) mid();
   }
   if (ok) {
     const bool wa = wait_bar(c.bar_a, c.phase_a);
@@ -445,12 +452,14 @@ __global__ void __launch_bounds__(NTHR, 1)
 constexpr int EPT = 16;  // elements per tile (x 8 points = 128)
 constexpr uint32_t U_REF = S_USER;                         // 264 doubles
 constexpr uint32_t U_REFF = U_REF + 264 * 8;               // 264 floats
-constexpr uint32_t U_X = U_REFF + 1072;                    // EPT x 24 doubles
-constexpr uint32_t U_XD = U_X + EPT * 24 * 8;              // EPT x 24 floats
+constexpr uint32_t U_X = U_REFF + 1072;                    // EPT x 24 doubles (prefetched)
+constexpr uint32_t U_UD = U_X + EPT * 24 * 8;              // EPT x 24 doubles (prefetched)
+constexpr uint32_t U_ST = U_UD + EPT * 24 * 8;             // 128 x 7 doubles: state_old (prefetched)
+constexpr uint32_t U_XD = U_ST + 128 * 7 * 8;              // EPT x 24 floats
 constexpr uint32_t U_U = U_XD + EPT * 24 * 4;              // EPT x 24 floats
 constexpr uint32_t U_GU = U_U + EPT * 24 * 4;              // 2 x 128 x 9 floats (tile parity)
 constexpr uint32_t U_FLAG = U_GU + 2 * 128 * 9 * 4;        // 2 x 128 ints
-constexpr uint32_t U_CONN = U_FLAG + 2 * 128 * 4;          // 128 ints
+constexpr uint32_t U_CONN = U_FLAG + 2 * 128 * 4;          // 128 ints (prefetched)
 constexpr uint32_t POINTS_SMEM = U_CONN + 128 * 4;
 constexpr int PREP_BAR = 4;                                // named barrier of the preparing warps 4..7
 static_assert(POINTS_SMEM <= 227 * 1024, "closure kernel shared memory");
@@ -469,33 +478,66 @@ __device__ __forceinline__ void write_row(float* table, int64_t p, const float* 
   for (int k = 0; k < POINT_TABLE_STRIDE / 4; ++k) dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
 }
 
-// Phase A of tile t on warps 4..7 (m = point of the tile): staging, map and
-// displacement gradient, trial state; elastic points are completed exactly,
-// plastic points write their input row (others a zero row).  Flags and grad u go
-// to the buffer of the tile's parity.
+// Background staging of tile t by warps 4..7 (m = 0..127), in two steps so that
+// their latency hides under the previous tile's network: the connectivity (at
+// the start of the previous tile), then -- it has landed by the end of that
+// tile's first layer -- the coordinates, displacements and old state.
+__device__ void prefetch_conn(const ElemArgs& g, const Ctx& c, int64_t t, int m) {
+  int* s_conn = reinterpret_cast<int*>(c.sm + U_CONN);
+  const int64_t e = t * EPT + m / 8;
+  if (e < g.ne)
+    tc::cp_async4(&s_conn[m], &g.conn[e * 8 + (m & 7)]);
+  else
+    s_conn[m] = 0;
+  tc::cp_async_commit();
+}
+__device__ void prefetch_data(const ElemArgs& g, const Ctx& c, int64_t t, int m) {
+  unsigned char* sm = c.sm;
+  const int* s_conn = reinterpret_cast<const int*>(sm + U_CONN);
+  double* s_x = reinterpret_cast<double*>(sm + U_X);
+  double* s_ud = reinterpret_cast<double*>(sm + U_UD);
+  double* s_st = reinterpret_cast<double*>(sm + U_ST);
+  tc::cp_async_wait_all();
+  named_sync(PREP_BAR, 128);
+  const int64_t e0 = t * EPT;
+  for (int i = m; i < EPT * 24; i += 128) {
+    const int el = i / 24, k = i % 24, a = k / 3, d = k % 3;
+    if (e0 + el < g.ne) {
+      const int64_t dof = int64_t(s_conn[el * 8 + a]) * 3 + d;
+      tc::cp_async8(&s_x[i], &g.coords[dof]);
+      tc::cp_async8(&s_ud[i], &g.U[dof]);
+    }
+  }
+  const int64_t left = (g.ne - e0) * 8;
+  const int nst = 7 * int(left < 128 ? left : 128);
+  const double* so = g.state_old + e0 * 8 * 7;
+  for (int j = m; j < nst; j += 128) tc::cp_async8(&s_st[j], &so[j]);
+  tc::cp_async_commit();
+}
+
+// Phase A of tile t on warps 4..7 (m = point of the tile), from the staged
+// data: map and displacement gradient, trial state; elastic points are
+// completed exactly, plastic points write their input row (others a zero row).
+// Flags and grad u go to the buffer of the tile's parity.
 __device__ void prep_tile(const ElemArgs& g, const TcClosure& cl, const Ctx& c, int64_t t, int buf, int m) {
   unsigned char* sm = c.sm;
   const double* s_ref = reinterpret_cast<const double*>(sm + U_REF);
   const float* s_reff = reinterpret_cast<const float*>(sm + U_REFF);
-  double* s_x = reinterpret_cast<double*>(sm + U_X);
+  const double* s_x = reinterpret_cast<const double*>(sm + U_X);
+  const double* s_ud = reinterpret_cast<const double*>(sm + U_UD);
+  const double* s_st = reinterpret_cast<const double*>(sm + U_ST);
   float* s_xd = reinterpret_cast<float*>(sm + U_XD);
   float* s_u = reinterpret_cast<float*>(sm + U_U);
   float* s_gu = reinterpret_cast<float*>(sm + U_GU) + buf * 128 * 9;
   int* s_flag = reinterpret_cast<int*>(sm + U_FLAG) + buf * 128;
-  int* s_conn = reinterpret_cast<int*>(sm + U_CONN);
   const int64_t e0 = t * EPT;
-  {
-    const int64_t e = e0 + m / 8;
-    s_conn[m] = e < g.ne ? g.conn[e * 8 + (m & 7)] : 0;
-  }
+  tc::cp_async_wait_all();
   named_sync(PREP_BAR, 128);
   for (int i = m; i < EPT * 24; i += 128) {
-    const int el = i / 24, k = i % 24, a = k / 3, d = k % 3;
+    const int el = i / 24, d = i % 3;
     if (e0 + el < g.ne) {
-      const double xv = __ldg(&g.coords[int64_t(s_conn[el * 8 + a]) * 3 + d]);
-      s_x[i] = xv;
-      s_xd[i] = float(xv - __ldg(&g.coords[int64_t(s_conn[el * 8]) * 3 + d]));
-      s_u[i] = float(__ldg(&g.U[int64_t(s_conn[el * 8 + a]) * 3 + d]));
+      s_xd[i] = float(s_x[i] - s_x[el * 24 + d]);
+      s_u[i] = float(s_ud[i]);
     }
   }
   named_sync(PREP_BAR, 128);
@@ -517,7 +559,7 @@ __device__ void prep_tile(const ElemArgs& g, const TcClosure& cl, const Ctx& c, 
         gu[i][j] = sum;
         s_gu[m * 9 + i * 3 + j] = sum;
       }
-    const double* so = g.state_old + p * 7;
+    const double* so = s_st + m * 7;
     double* sn = g.state_new ? g.state_new + p * 7 : nullptr;
     float etr[6];
     if (J2MLP::trial(g.props, gu, so, etr, x)) {
@@ -531,7 +573,7 @@ __device__ void prep_tile(const ElemArgs& g, const TcClosure& cl, const Ctx& c, 
   }
   s_flag[m] = flag;
   write_input_row(c, m, flag == 1 ? x : nullptr);
-  named_sync(PREP_BAR, 128);  // the staging arrays are free for the next tile
+  named_sync(PREP_BAR, 128);  // the staged data is free for the next tile
 }
 
 // Phase C of tile t on warps 0..3 (m = point of the tile): plastic points from
@@ -571,7 +613,8 @@ __device__ void complete_tile(const ElemArgs& g, const TcClosure& cl, const Ctx&
 // Tiles of 16 elements.  Per tile the network runs on all eight epilogue warps
 // (B); after it, warps 0..3 complete the tile's points (C) while warps 4..7
 // already prepare the CTA's next tile (A), into the other parity's buffers and
-// the input rows, which the tile's last MMAs no longer read.
+// the input rows, which the tile's last MMAs no longer read.  The next tile's
+// inputs are copied in the background during the current tile's network.
 __global__ void __launch_bounds__(NTHR, 1) j2mlp_points_tc_kernel(ElemArgs g, TcClosure cl) {
   extern __shared__ __align__(1024) unsigned char sm[];
   Ctx c;
@@ -588,16 +631,26 @@ __global__ void __launch_bounds__(NTHR, 1) j2mlp_points_tc_kernel(ElemArgs g, Tc
   const bool issuer = tid >= NEPI;
   const int64_t tiles = (g.ne + EPT - 1) / EPT;
   int64_t t = blockIdx.x;
-  if (tid >= 128 && tid < NEPI && t < tiles) prep_tile(g, cl, c, t, 0, tid - 128);
+  const bool preparer = tid >= 128 && tid < NEPI;
+  if (preparer && t < tiles) {
+    prefetch_conn(g, c, t, tid - 128);
+    prefetch_data(g, c, t, tid - 128);
+    prep_tile(g, cl, c, t, 0, tid - 128);
+  }
   for (int it = 0; t < tiles; t += gridDim.x, ++it) {
+    const int64_t tn = t + gridDim.x;
+    const bool next = tn < tiles;
     if (issuer) {
       issue_tile(c);
     } else {
-      epilogue_tile(c, ok);
+      if (preparer && next) prefetch_conn(g, c, tn, tid - 128);
+      epilogue_tile(c, ok, [&] {
+        if (preparer && next) prefetch_data(g, c, tn, tid - 128);
+      });
       if (tid < 128) {
         if (ok) complete_tile(g, cl, c, t, it & 1, tid);
-      } else if (t + gridDim.x < tiles) {
-        prep_tile(g, cl, c, t + gridDim.x, (it + 1) & 1, tid - 128);
+      } else if (next) {
+        prep_tile(g, cl, c, tn, (it + 1) & 1, tid - 128);
       }
     }
     tc::tc_fence_before();
