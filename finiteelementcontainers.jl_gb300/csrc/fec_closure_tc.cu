@@ -454,8 +454,8 @@ constexpr uint32_t U_REF = S_USER;                         // 264 doubles
 constexpr uint32_t U_REFF = U_REF + 264 * 8;               // 264 floats
 constexpr uint32_t U_X = U_REFF + 1072;                    // EPT x 24 doubles (prefetched)
 constexpr uint32_t U_UD = U_X + EPT * 24 * 8;              // EPT x 24 doubles (prefetched)
-constexpr uint32_t U_ST = U_UD + EPT * 24 * 8;             // 128 x 7 doubles: state_old (prefetched)
-constexpr uint32_t U_XD = U_ST + 128 * 7 * 8;              // EPT x 24 floats
+constexpr uint32_t U_ST = U_UD + EPT * 24 * 8;             // 2 x 128 x 7 doubles: state_old (prefetched, parity)
+constexpr uint32_t U_XD = U_ST + 2 * 128 * 7 * 8;          // EPT x 24 floats
 constexpr uint32_t U_U = U_XD + EPT * 24 * 4;              // EPT x 24 floats
 constexpr uint32_t U_GU = U_U + EPT * 24 * 4;              // 2 x 128 x 9 floats (tile parity)
 constexpr uint32_t U_FLAG = U_GU + 2 * 128 * 9 * 4;        // 2 x 128 ints
@@ -491,12 +491,12 @@ __device__ void prefetch_conn(const ElemArgs& g, const Ctx& c, int64_t t, int m)
     s_conn[m] = 0;
   tc::cp_async_commit();
 }
-__device__ void prefetch_data(const ElemArgs& g, const Ctx& c, int64_t t, int m) {
+__device__ void prefetch_data(const ElemArgs& g, const Ctx& c, int64_t t, int buf, int m) {
   unsigned char* sm = c.sm;
   const int* s_conn = reinterpret_cast<const int*>(sm + U_CONN);
   double* s_x = reinterpret_cast<double*>(sm + U_X);
   double* s_ud = reinterpret_cast<double*>(sm + U_UD);
-  double* s_st = reinterpret_cast<double*>(sm + U_ST);
+  double* s_st = reinterpret_cast<double*>(sm + U_ST) + buf * 128 * 7;
   tc::cp_async_wait_all();
   named_sync(PREP_BAR, 128);
   const int64_t e0 = t * EPT;
@@ -525,7 +525,7 @@ __device__ void prep_tile(const ElemArgs& g, const TcClosure& cl, const Ctx& c, 
   const float* s_reff = reinterpret_cast<const float*>(sm + U_REFF);
   const double* s_x = reinterpret_cast<const double*>(sm + U_X);
   const double* s_ud = reinterpret_cast<const double*>(sm + U_UD);
-  const double* s_st = reinterpret_cast<const double*>(sm + U_ST);
+  const double* s_st = reinterpret_cast<const double*>(sm + U_ST) + buf * 128 * 7;
   float* s_xd = reinterpret_cast<float*>(sm + U_XD);
   float* s_u = reinterpret_cast<float*>(sm + U_U);
   float* s_gu = reinterpret_cast<float*>(sm + U_GU) + buf * 128 * 9;
@@ -578,16 +578,20 @@ __device__ void prep_tile(const ElemArgs& g, const TcClosure& cl, const Ctx& c, 
 
 // Phase C of tile t on warps 0..3 (m = point of the tile): plastic points from
 // the network's outputs, with the consistency check and the exact fallback.
+// Each warp's 32 table rows are staged in shared memory (a tangent tile, idle
+// between networks) and leave as contiguous 128-byte segments.
 __device__ void complete_tile(const ElemArgs& g, const TcClosure& cl, const Ctx& c, int64_t t, int buf, int m) {
   const float* s_gu = reinterpret_cast<const float*>(c.sm + U_GU) + buf * 128 * 9;
   const int* s_flag = reinterpret_cast<const int*>(c.sm + U_FLAG) + buf * 128;
+  const double* s_st = reinterpret_cast<const double*>(c.sm + U_ST) + buf * 128 * 7;
+  float* stage = reinterpret_cast<float*>(c.sm + S_TAN(0)) + (m >> 5) * (32 * POINT_TABLE_STRIDE);
   float y[MLP_OUT], Js[6][6];
   epilogue_output(c, y, Js);
   const int plastic = s_flag[m] == 1;
   int fell_back = 0;
   if (plastic) {
-    const int64_t p = (t * EPT + m / 8) * 8 + (m & 7);
-    const double* so = g.state_old + p * 7;
+    const int64_t p = t * 128 + m;
+    const double* so = s_st + m * 7;
     double* sn = g.state_new ? g.state_new + p * 7 : nullptr;
     float gu[3][3];
 #pragma unroll
@@ -600,10 +604,24 @@ __device__ void complete_tile(const ElemArgs& g, const TcClosure& cl, const Ctx&
       fell_back = 1;
       J2MLP::exact(g.props, gu, 1.0f, so, sn, P9, C36);
     }
-    write_row(cl.table, p, P9, C36);
+    float* row = stage + (m & 31) * POINT_TABLE_STRIDE;
+    const int ii[6] = {0, 1, 2, 1, 0, 0}, jj[6] = {0, 1, 2, 2, 2, 1};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) row[k] = P9[ii[k] * 3 + jj[k]];
+#pragma unroll
+    for (int k = 0; k < 36; ++k) row[6 + k] = C36[k];
+    row[42] = row[43] = 0.f;
   }
-  const unsigned np = __popc(__ballot_sync(0xffffffffu, plastic));
+  const unsigned pmask = __ballot_sync(0xffffffffu, plastic);
+  const unsigned np = __popc(pmask);
   const unsigned nf = __popc(__ballot_sync(0xffffffffu, fell_back));
+  if (np) {
+    __syncwarp();
+    const int lane = m & 31;
+    float* dst = cl.table + (t * 128 + (m & ~31)) * POINT_TABLE_STRIDE;
+    for (int f = lane; f < 32 * POINT_TABLE_STRIDE; f += 32)
+      if ((pmask >> (f / POINT_TABLE_STRIDE)) & 1u) dst[f] = stage[f];
+  }
   if ((m & 31) == 0 && np) {
     atomicAdd(&cl.counters[0], (unsigned long long)np);
     if (nf) atomicAdd(&cl.counters[1], (unsigned long long)nf);
@@ -634,7 +652,7 @@ __global__ void __launch_bounds__(NTHR, 1) j2mlp_points_tc_kernel(ElemArgs g, Tc
   const bool preparer = tid >= 128 && tid < NEPI;
   if (preparer && t < tiles) {
     prefetch_conn(g, c, t, tid - 128);
-    prefetch_data(g, c, t, tid - 128);
+    prefetch_data(g, c, t, 0, tid - 128);
     prep_tile(g, cl, c, t, 0, tid - 128);
   }
   for (int it = 0; t < tiles; t += gridDim.x, ++it) {
@@ -645,7 +663,7 @@ __global__ void __launch_bounds__(NTHR, 1) j2mlp_points_tc_kernel(ElemArgs g, Tc
     } else {
       if (preparer && next) prefetch_conn(g, c, tn, tid - 128);
       epilogue_tile(c, ok, [&] {
-        if (preparer && next) prefetch_data(g, c, tn, tid - 128);
+        if (preparer && next) prefetch_data(g, c, tn, (it + 1) & 1, tid - 128);
       });
       if (tid < 128) {
         if (ok) complete_tile(g, cl, c, t, it & 1, tid);
