@@ -1044,9 +1044,30 @@ int probe(int device, int iters, double* tflops) {
   *tflops = 2.0 * double(blocks) * threads * iters * 8 / (double(ms) * 1e-3) / 1e12;
   return FEC_OK;
 }
+
+// df64_split and widen over an array: the device-side conversions of the FP64
+// path, exposed so that tests can check them against host arithmetic.
+__global__ void df64_split_check_kernel(const double* x, int64_t n, float* split, double* widened) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float2 s = fec::df64_split(x[i]);
+  split[2 * i] = s.x;
+  split[2 * i + 1] = s.y;
+  widened[2 * i] = fec::widen(s.x);
+  widened[2 * i + 1] = fec::widen(s.y);
+}
 }  // namespace
 
 extern "C" {
+
+int fec_df64_split_check(const double* x_dev, int64_t n, float* split_dev, double* widened_dev, void* stream) {
+  if (n < 0 || (n > 0 && (!x_dev || !split_dev || !widened_dev))) return FEC_ERR_ARG;
+  if (n == 0) return FEC_OK;
+  const int threads = 256;
+  const unsigned blocks = unsigned((n + threads - 1) / threads);
+  df64_split_check_kernel<<<blocks, threads, 0, static_cast<cudaStream_t>(stream)>>>(x_dev, n, split_dev, widened_dev);
+  return cudaGetLastError() == cudaSuccess ? FEC_OK : FEC_ERR_CUDA;
+}
 
 int fec_probe_fma_rate(int device, int precision, double* tflops) {
   if (!tflops) return FEC_ERR_ARG;

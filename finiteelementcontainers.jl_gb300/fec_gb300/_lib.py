@@ -64,6 +64,7 @@ SIGNATURES = {
     "fec_closure_stats": (C.c_int, [_vp, _i64p, _i64p, C.c_int]),
     "fec_kernel_times": (C.c_int, [_vp, C.POINTER(C.c_float), C.c_int, C.c_char_p, C.c_size_t]),
     "fec_probe_fma_rate": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    "fec_df64_split_check": (C.c_int, [_vp, C.c_int64, _vp, _vp, _vp]),
 }
 
 

@@ -251,6 +251,11 @@ int fec_kernel_times(fec_ctx* ctx, float* ms, int cap, char* names, size_t len);
  * (precision FEC_FP64) or FP32 (FEC_FP32_ELEMENT): the denominator of the
  * FP64-bound roofline of the element kernels. */
 int fec_probe_fma_rate(int device, int precision, double* tflops);
+/* Self-check of the FP64 path's conversions (device buffers, stream-ordered):
+ * for each x[i], split[2i], split[2i+1] = the double-float (hi, lo) the FP64
+ * kernels form from it, and widened[2i], widened[2i+1] = hi and lo widened back
+ * to double as the node gather does.  No reference counterpart. */
+int fec_df64_split_check(const double* x_dev, int64_t n, float* split_dev, double* widened_dev, void* stream);
 
 /* Sizes the context knows (any pointer may be NULL). */
 /* Launch configurations the autotuner chose for the generic element kernels
