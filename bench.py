@@ -56,8 +56,11 @@ WORKLOADS = {
     # matrix-free tangent action K v of the Neo-Hookean 128^3 system (no K formed)
     "action": dict(n=128, kind="vector", name="neohookean_hex8_128cubed_matrix_free_action", flop_per_elem=5.5e3,
                    state=0),
+    # the symbolic phase (CSC pattern + element maps) of the Neo-Hookean 128^3 system, host vs device
+    "symbolic": dict(n=128, kind="vector", name="neohookean_hex8_128cubed_symbolic_phase", flop_per_elem=0,
+                     state=0),
 }
-CPU_SAMPLE_N = {"neohookean": 40, "poisson": 32, "j2": 40, "batched": 40, "j2mlp": 40, "action": 40}
+CPU_SAMPLE_N = {"neohookean": 40, "poisson": 32, "j2": 40, "batched": 40, "j2mlp": 40, "action": 40, "symbolic": 40}
 J2_STEPS = 20
 J2_PROPS = (200.0, 0.3, 0.25, 2.0)   # E, nu, yield stress, linear hardening
 
@@ -225,7 +228,7 @@ def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    if args.workload in ("action", "j2mlp", "batched"):
+    if args.workload in ("action", "j2mlp", "batched", "symbolic"):
         print(json.dumps({"impl": "reference", "unavailable": f"the CPU port times the assembly workloads only "
                                                                 f"(neohookean, poisson, j2), not {args.workload}"}))
         return
@@ -406,6 +409,54 @@ def run_closure(args) -> None:
                   "speedup_closure_vs_exact_fp64_native": (t_x64n / main_t) if t_x64n else None},
         "clocks": clk.summary(), "e2e": None, "gpu_launches": int(main_launches), "cpu_baseline": None,
     }
+    print(json.dumps(line), flush=True)
+
+
+def run_symbolic(args) -> None:
+    """The symbolic phase of the Neo-Hookean 128^3 system (no Dirichlet dofs): CSC
+    pattern, node adjacency, neighbour lists, column offsets and the element map,
+    built by the host threads (fec_pattern_build) and by kernels
+    (fec_pattern_build_device); each timed from the call to its return."""
+    import ctypes as C
+    import torch
+    import __graft_entry__ as ge
+    fec = ge.load_package()
+    torch.cuda.set_device(0)
+    n = args.n or WORKLOADS["symbolic"]["n"]
+    mesh, asm, p, inputs = build_workload(fec, "neohookean", n, 0, "fp64")
+    lib = fec.load_library()
+    ctx = asm._ctx
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    nnz = C.c_int64()
+
+    def host():
+        assert lib.fec_pattern_build(ctx, C.byref(nnz)) == 0
+        return int(nnz.value)
+
+    def device():
+        assert lib.fec_pattern_build_device(ctx, C.byref(nnz), s) == 0
+        return int(nnz.value)
+
+    times = {}
+    sizes = {}
+    for name, fn in (("host", host), ("device", device)):
+        for _ in range(max(1, args.warmup)):
+            sizes[name] = fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            fn()
+        torch.cuda.synchronize()
+        times[name] = (time.perf_counter() - t0) / args.steps
+    assert sizes["host"] == sizes["device"]
+    cores = os.cpu_count() or 1
+    line = {"metric": "symbolic phase seconds (CSC pattern + element maps)", "value": times["device"], "unit": "s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": times["device"] * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+            "config": {"workload": WORKLOADS["symbolic"]["name"], "elements": mesh.num_elements(),
+                       "nodes": mesh.num_nodes, "nnz": sizes["device"]},
+            "host_threads_s": times["host"], "host_threads": cores, "speedup_device_vs_host": times["host"] / times["device"],
+            "e2e": None, "gpu_launches": None, "cpu_baseline": None}
     print(json.dumps(line), flush=True)
 
 
@@ -817,6 +868,8 @@ def main() -> None:
         run_closure(args)
     elif args.workload == "action":
         run_action(args)
+    elif args.workload == "symbolic":
+        run_symbolic(args)
     else:
         run_ours(args)
 

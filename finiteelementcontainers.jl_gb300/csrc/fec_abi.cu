@@ -18,6 +18,7 @@
 #include "fec_closure.cuh"
 #include "fec_closure_tc.h"
 #include "fec_launch.h"
+#include "fec_pattern.h"
 #include "fec_solver.h"
 #include <cuda_bf16.h>
 
@@ -85,6 +86,7 @@ struct fec_ctx {
   DevBuf d_V;                   // matrix-free action: the direction as a full field
   DevBuf d_colptr0, d_rowval32, d_cg;  // linear solve: 0-based CSC pattern, CG scratch
   DevBuf d_flag;                       // non-finite scan result
+  DevBuf d_nbr_ptr, d_nbr;             // neighbour lists on the device (device symbolic phase, CSC fill)
   float cl_tol = 0.f;
   // optional per-launch timing (CUDA events on the caller's stream)
   bool profiling = false;
@@ -214,6 +216,8 @@ void invalidate_pattern(fec_ctx* c) {
   c->d_epos.release();
   c->d_col_base.release();
   c->d_col_len.release();
+  c->d_nbr_ptr.release();
+  c->d_nbr.release();
 }
 
 }  // namespace
@@ -426,6 +430,8 @@ int fec_pattern_build(fec_ctx* c, int64_t* nnz_out) {
   if (!c) return FEC_ERR_ARG;
   if (c->n_unknowns < 0) return fail(c, FEC_ERR_STATE, "fec_pattern_build before fec_dofs_set");
   if (c->device >= 0) cudaSetDevice(c->device);
+  c->d_nbr_ptr.release();  // device copies of the neighbour lists go with the pattern
+  c->d_nbr.release();
   const int64_t nn = c->nn;
   // node -> (element, local node) adjacency, elements ascending
   std::vector<int64_t> nadj_ptr(nn + 1, 0);
@@ -563,6 +569,149 @@ int fec_pattern_build(fec_ctx* c, int64_t* nnz_out) {
   c->acc_stride = acc_stride;
   c->pattern_ready = true;
   if (nnz_out) *nnz_out = nnz;
+  return ok(c);
+}
+
+int fec_pattern_build_device(fec_ctx* c, int64_t* nnz_out, void* stream) {
+  if (!c) return FEC_ERR_ARG;
+  if (c->n_unknowns < 0) return fail(c, FEC_ERR_STATE, "fec_pattern_build_device before fec_dofs_set");
+  if (c->device < 0) return fail(c, FEC_ERR_STATE, "host-only context (device -1) cannot run kernels");
+  if (c->blocks.size() > size_t(fec::PATTERN_MAX_BLOCKS))
+    return fail(c, FEC_ERR_UNSUPPORTED, "the device symbolic phase takes at most %d element blocks",
+                fec::PATTERN_MAX_BLOCKS);
+  if (c->ne_total >= (int64_t(1) << 27))
+    return fail(c, FEC_ERR_UNSUPPORTED, "more than 2^27 elements (%lld)", (long long)c->ne_total);
+  cudaSetDevice(c->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  invalidate_pattern(c);
+  const int64_t nn = c->nn;
+  const int64_t nent = int64_t(c->conn.size());
+  fec::PatternBlocks PB{};
+  PB.nblocks = int(c->blocks.size());
+  int64_t epos_total = 0;
+  for (size_t b = 0; b < c->blocks.size(); ++b) {
+    const Block& B = c->blocks[b];
+    PB.nnpe[b] = B.nnpe;
+    PB.ne[b] = B.ne;
+    PB.elem_start[b] = B.elem_start;
+    PB.conn_off[b] = B.conn_off;
+    PB.epos_off[b] = B.epos_off;
+    epos_total += (B.ne * B.nnpe * B.nnpe + 3) & ~int64_t(3);
+  }
+  // scratch: counts/cursors (int32 nn), scan partials, flags
+  DevBuf t_cnt, t_cur, t_scan, t_flags, t_w, t_rowoff, t_um;
+  struct Frees {
+    DevBuf* b[7];
+    ~Frees() {
+      for (DevBuf* x : b) x->release();
+    }
+  } frees{{&t_cnt, &t_cur, &t_scan, &t_flags, &t_w, &t_rowoff, &t_um}};
+  const size_t scan_n = fec::pattern_scan_scratch(nn + 1);
+  FEC_CUDA(c, cudaMalloc(&t_cnt.p, sizeof(int32_t) * size_t(nn + 1)));
+  FEC_CUDA(c, cudaMalloc(&t_cur.p, sizeof(int32_t) * size_t(nn + 1)));
+  FEC_CUDA(c, cudaMalloc(&t_scan.p, sizeof(int64_t) * scan_n));
+  FEC_CUDA(c, cudaMalloc(&t_flags.p, sizeof(int) * 4));
+  FEC_CUDA(c, cudaMalloc(&t_w.p, sizeof(int64_t) * size_t(nn + 1)));
+  FEC_CUDA(c, cudaMalloc(&t_um.p, size_t(nn + 1)));
+  int32_t* cnt = static_cast<int32_t*>(t_cnt.p);
+  int32_t* cur = static_cast<int32_t*>(t_cur.p);
+  int64_t* scan = static_cast<int64_t*>(t_scan.p);
+  int* flags = static_cast<int*>(t_flags.p);  // [0] overflow, [1] max column length, [2] max entries of a node
+  const uint8_t* um = static_cast<const uint8_t*>(c->d_umask.p);
+  const int32_t* conn = static_cast<const int32_t*>(c->d_conn.p);
+  FEC_CUDA(c, cudaMemsetAsync(flags, 0, sizeof(int) * 4, s));
+  // node -> (element, local node) adjacency, elements ascending
+  FEC_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * size_t(nn + 1), s));
+  FEC_CUDA(c, fec::pattern_count_adjacency(conn, nent, cnt, s));
+  int rc;
+  if ((rc = ensure(c, c->d_nadj_ptr, sizeof(int64_t) * size_t(nn + 1)))) return rc;
+  if ((rc = ensure(c, c->d_nadj, sizeof(uint32_t) * size_t(nent > 0 ? nent : 1)))) return rc;
+  int64_t* adj_ptr = static_cast<int64_t*>(c->d_nadj_ptr.p);
+  uint32_t* nadj = static_cast<uint32_t*>(c->d_nadj.p);
+  FEC_CUDA(c, fec::pattern_scan(cnt, nullptr, nn, adj_ptr, scan, s));
+  FEC_CUDA(c, cudaMemsetAsync(cur, 0, sizeof(int32_t) * size_t(nn + 1), s));
+  FEC_CUDA(c, fec::pattern_fill_adjacency(PB, conn, adj_ptr, nn, cur, nadj, s));
+  // neighbour counts and column lengths, then the lists
+  if ((rc = ensure(c, c->d_col_len, sizeof(int32_t) * size_t(nn + 1)))) return rc;
+  int32_t* col_len = static_cast<int32_t*>(c->d_col_len.p);
+  FEC_CUDA(c, fec::pattern_neighbours(PB, conn, adj_ptr, nadj, nn, um, cnt, col_len, nullptr, nullptr, nullptr,
+                                      flags, s));
+  if ((rc = ensure(c, c->d_nbr_ptr, sizeof(int64_t) * size_t(nn + 1)))) return rc;
+  int64_t* nbr_ptr = static_cast<int64_t*>(c->d_nbr_ptr.p);
+  FEC_CUDA(c, fec::pattern_scan(cnt, nullptr, nn, nbr_ptr, scan, s));
+  int64_t n_nbr = 0;
+  int overflow = 0;
+  FEC_CUDA(c, cudaMemcpyAsync(&n_nbr, nbr_ptr + nn, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  FEC_CUDA(c, cudaMemcpyAsync(&overflow, flags, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FEC_CUDA(c, cudaStreamSynchronize(s));
+  if (overflow)
+    return fail(c, FEC_ERR_UNSUPPORTED, "a node gathers more than %d element nodes; use fec_pattern_build",
+                fec::PATTERN_CAND_CAP);
+  if ((rc = ensure(c, c->d_nbr, sizeof(int32_t) * size_t(n_nbr > 0 ? n_nbr : 1)))) return rc;
+  FEC_CUDA(c, cudaMalloc(&t_rowoff.p, sizeof(int32_t) * size_t(n_nbr > 0 ? n_nbr : 1)));
+  int32_t* nbr = static_cast<int32_t*>(c->d_nbr.p);
+  int32_t* rowoff = static_cast<int32_t*>(t_rowoff.p);
+  FEC_CUDA(c, fec::pattern_neighbours(PB, conn, adj_ptr, nadj, nn, um, cnt, col_len, nbr_ptr, nbr, rowoff, flags, s));
+  // column sizes and offsets
+  int64_t* w = static_cast<int64_t*>(t_w.p);
+  FEC_CUDA(c, fec::pattern_column_sizes(nn, um, col_len, w, flags + 1, flags + 2, s));
+  if ((rc = ensure(c, c->d_col_base, sizeof(int64_t) * size_t(nn + 1)))) return rc;
+  int64_t* col_base = static_cast<int64_t*>(c->d_col_base.p);
+  FEC_CUDA(c, fec::pattern_scan(nullptr, w, nn, col_base, scan, s));
+  int host_flags[4] = {0, 0, 0, 0};
+  int64_t nnz = 0;
+  FEC_CUDA(c, cudaMemcpyAsync(host_flags, flags, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
+  FEC_CUDA(c, cudaMemcpyAsync(&nnz, col_base + nn, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  FEC_CUDA(c, cudaStreamSynchronize(s));
+  if (host_flags[1] >= 65535)
+    return fail(c, FEC_ERR_UNSUPPORTED, "a node couples to %d dofs (limit 65534)", host_flags[1]);
+  const int max_cols = host_flags[2];
+  const int acc_stride = std::max(2, (max_cols + 1) & ~1);
+  if (size_t(acc_stride) * sizeof(double) > 200 * 1024)
+    return fail(c, FEC_ERR_UNSUPPORTED, "a node's columns hold %d entries; the gather supports %d", max_cols,
+                int(200 * 1024 / sizeof(double)));
+  // element map and the full-neighbourhood flag
+  if ((rc = ensure(c, c->d_epos, sizeof(uint16_t) * size_t(epos_total > 0 ? epos_total : 1)))) return rc;
+  FEC_CUDA(c, fec::pattern_element_map(PB, conn, nbr_ptr, nbr, rowoff, static_cast<uint16_t*>(c->d_epos.p), s));
+  uint8_t* um2 = static_cast<uint8_t*>(t_um.p);
+  FEC_CUDA(c, fec::pattern_full_neighbourhood(nn, c->nf, nbr_ptr, nbr, um, uint8_t(fec::UMASK_FULL_NBR), um2, s));
+  if (nn > 0) FEC_CUDA(c, cudaMemcpyAsync(c->d_umask.p, um2, size_t(nn), cudaMemcpyDeviceToDevice, s));
+  // host copies for fec_pattern_get and the solver
+  c->nbr_ptr.resize(size_t(nn + 1));
+  c->nbr.resize(size_t(n_nbr));
+  c->col_base.resize(size_t(nn));
+  c->col_len.resize(size_t(nn));
+  FEC_CUDA(c, cudaMemcpyAsync(c->nbr_ptr.data(), nbr_ptr, sizeof(int64_t) * size_t(nn + 1), cudaMemcpyDeviceToHost, s));
+  if (n_nbr > 0)
+    FEC_CUDA(c, cudaMemcpyAsync(c->nbr.data(), nbr, sizeof(int32_t) * size_t(n_nbr), cudaMemcpyDeviceToHost, s));
+  if (nn > 0) {
+    FEC_CUDA(c, cudaMemcpyAsync(c->col_base.data(), col_base, sizeof(int64_t) * size_t(nn), cudaMemcpyDeviceToHost, s));
+    FEC_CUDA(c, cudaMemcpyAsync(c->col_len.data(), col_len, sizeof(int32_t) * size_t(nn), cudaMemcpyDeviceToHost, s));
+  }
+  FEC_CUDA(c, cudaStreamSynchronize(s));
+  c->nnz = nnz;
+  c->acc_stride = acc_stride;
+  c->pattern_ready = true;
+  if (nnz_out) *nnz_out = nnz;
+  return ok(c);
+}
+
+int fec_pattern_get_device(const fec_ctx* cc, int64_t* colptr_dev, int64_t* rowval_dev, void* stream) {
+  fec_ctx* c = const_cast<fec_ctx*>(cc);
+  if (!c) return FEC_ERR_ARG;
+  if (!c->pattern_ready) return fail(c, FEC_ERR_STATE, "fec_pattern_get_device before a pattern build");
+  if (c->device < 0) return fail(c, FEC_ERR_STATE, "host-only context (device -1) cannot run kernels");
+  cudaSetDevice(c->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc;
+  if (!c->d_nbr_ptr.p) {  // a host-built pattern: its neighbour lists go up once
+    if ((rc = upload(c, c->d_nbr_ptr, c->nbr_ptr.data(), sizeof(int64_t) * c->nbr_ptr.size()))) return rc;
+    if ((rc = upload(c, c->d_nbr, c->nbr.data(), sizeof(int32_t) * c->nbr.size()))) return rc;
+  }
+  FEC_CUDA(c, fec::pattern_csc(c->nn, c->nf, static_cast<const uint8_t*>(c->d_umask.p),
+                               static_cast<const int64_t*>(c->d_dtu.p), static_cast<const int64_t*>(c->d_nbr_ptr.p),
+                               static_cast<const int32_t*>(c->d_nbr.p), static_cast<const int64_t*>(c->d_col_base.p),
+                               static_cast<const int32_t*>(c->d_col_len.p), colptr_dev, rowval_dev, s));
   return ok(c);
 }
 

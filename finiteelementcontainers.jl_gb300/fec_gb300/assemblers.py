@@ -55,16 +55,25 @@ class SparseMatrixAssembler:
     (src/assemblers/SparseMatrixAssembler.jl:64-133).
 
     device: CUDA device index, or -1 for a host-only assembler that can build
-    the pattern (colptr/rowval) but not assemble values."""
+    the pattern (colptr/rowval) but not assemble values.
+    symbolic: "host" builds the pattern and its maps on the host threads
+    (fec_pattern_build), "device" with kernels (fec_pattern_build_device); both
+    give the same pattern and maps."""
 
     def __init__(self, var_or_dof, *, sparse_matrix_type: str = "csc", use_condensed: bool = False,
-                 use_inplace_methods: bool = False, device: int = 0, precision: str = "fp64"):
+                 use_inplace_methods: bool = False, device: int = 0, precision: str = "fp64",
+                 symbolic: str = "host"):
         if sparse_matrix_type != "csc":
             raise NotImplementedError(f"sparse_matrix_type={sparse_matrix_type!r}: the accelerated path builds CSC")
         if use_condensed:
             raise NotImplementedError("use_condensed=true is not on the accelerated path")
         if precision not in PRECISIONS:
             raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
+        if symbolic not in ("host", "device"):
+            raise ValueError("symbolic must be 'host' or 'device'")
+        if symbolic == "device" and device < 0:
+            raise ValueError("symbolic='device' needs a CUDA device")
+        self.symbolic = symbolic
         self.dof = var_or_dof if isinstance(var_or_dof, DofManager) else DofManager(var_or_dof)
         self.fspace: FunctionSpace = self.dof.var.fspace
         self.use_inplace_methods = use_inplace_methods
@@ -105,7 +114,13 @@ class SparseMatrixAssembler:
     def _ensure_pattern(self):
         if self._pattern_dirty:
             nnz = C.c_int64()
-            self._call("fec_pattern_build", C.byref(nnz))
+            if self.symbolic == "device":
+                torch = _torch()
+                with torch.cuda.device(self.device):
+                    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+                self._call("fec_pattern_build_device", C.byref(nnz), s)
+            else:
+                self._call("fec_pattern_build", C.byref(nnz))
             self.nnz = int(nnz.value)
             self._pattern_dirty = False
         return self.nnz
@@ -124,6 +139,20 @@ class SparseMatrixAssembler:
             self._call("fec_pattern_get", _lib.ptr(colptr), _lib.ptr(rowval))
             self._csc_host = (colptr, rowval)
         return self._csc_host
+
+    def pattern_device(self):
+        """1-based (colptr, rowval) of the CSC stiffness as int64 device tensors,
+        filled by a kernel (for a CuSparse-style matrix on the device)."""
+        torch = _torch()
+        self._ensure_pattern()
+        n = int(self.dof.unknown_dofs.size)
+        dev = self._torch_device()
+        colptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+        rowval = torch.empty(self.nnz, dtype=torch.int64, device=dev)
+        with torch.cuda.device(self.device):
+            s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        self._call("fec_pattern_get_device", _lib.ptr(colptr), _lib.ptr(rowval), s)
+        return colptr, rowval
 
     def create_field(self):
         return _torch().zeros(len(self.dof), dtype=_torch().float64, device=self._torch_device())

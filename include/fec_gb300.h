@@ -112,6 +112,15 @@ int fec_dofs_set(fec_ctx* ctx, int num_fields, const int64_t* dof_to_unknown, in
 int fec_pattern_build(fec_ctx* ctx, int64_t* nnz_out);
 /* Copies the 1-based colptr (num_unknowns + 1) and rowval (nnz) to host. */
 int fec_pattern_get(const fec_ctx* ctx, int64_t* colptr, int64_t* rowval);
+/* The symbolic phase on the device (SparseMatrixPattern + _update_dofs!,
+ * src/assemblers/SparsityPatterns.jl:53-231): the same pattern, maps and nnz as
+ * fec_pattern_build, formed by kernels on `stream` (the call waits for them).
+ * FEC_ERR_UNSUPPORTED for more than 16 element blocks or a node whose adjacent
+ * elements hold more than 2048 nodes. */
+int fec_pattern_build_device(fec_ctx* ctx, int64_t* nnz_out, void* stream);
+/* 1-based colptr (n_unknowns + 1) and rowval (nnz) written into DEVICE buffers
+ * on `stream` (the colptr/rowval of sparse!, SparsityPatterns.jl:301-308). */
+int fec_pattern_get_device(const fec_ctx* ctx, int64_t* colptr_dev, int64_t* rowval_dev, void* stream);
 
 /* Field update -------------------------------------------------------------- */
 
