@@ -5,6 +5,7 @@ DirichletBC, SparseMatrixAssembler, assemble_vector/assemble_stiffness,
 residual/stiffness) over the C ABI of libfec_gb300.so, whose sm_103a kernels
 do the element quadrature, the gathers and the deterministic scatter."""
 from .meshes import StructuredMesh, UnstructuredMesh, Mesh, ArgumentError
+from .exodus import ExodusFile, ExodusPostProcessor, read_exodus
 from .spaces import FunctionSpace, ScalarFunction, VectorFunction
 from .dofs import DofManager, update_dofs
 from .bcs import DirichletBC, dirichlet_dofs

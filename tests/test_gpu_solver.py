@@ -42,6 +42,36 @@ def test_poisson_gold_through_device_solve(fec, preconditioner):
     assert np.abs(u - g["u_gold"]).max() <= 1e-9 * np.abs(g["u_gold"]).max()
 
 
+def test_poisson_gold_through_exodus_files(fec, tmp_path):
+    """The reference's Poisson regression flow end to end through files: the mesh
+    written to and read from an Exodus file, the device solve, the solution
+    written by the post-processor and read back against poisson.gold
+    (test/poisson/TestPoisson.jl:54-100, which compares with exodiff)."""
+    torch = _torch()
+    g = np.load(GOLD / "poisson_quad4.npz")
+    src = fec.UnstructuredMesh(g["coords"], {"block_1": ("QUAD4", g["conn"])},
+                               nodesets={f"nset_{i}": g[f"nset_{i}"] for i in range(1, 5)})
+    with fec.ExodusPostProcessor(src, tmp_path / "poisson.g", []):
+        pass
+    mesh = fec.read_exodus(tmp_path / "poisson.g")
+    bcs = [fec.DirichletBC("u", lambda X, t: 0.0, nodeset_name=f"nset_{i}") for i in range(1, 5)]
+    asm = fec.SparseMatrixAssembler(fec.ScalarFunction(fec.FunctionSpace(mesh), "u"), device=0)
+    p = fec.create_parameters(mesh, asm, fec.Poisson(2 * np.pi ** 2), dirichlet_bcs=bcs)
+    solver = fec.IterativeLinearSolver(asm, preconditioner="jacobi", rtol=1e-13, max_iter=20000)
+    Uu = torch.zeros(asm.dof.unknown_dofs.size, dtype=torch.float64, device="cuda")
+    solver.solve(Uu, p)
+    torch.cuda.synchronize()
+    u = np.zeros(mesh.num_nodes)
+    u[asm.dof.unknown_dofs - 1] = Uu.cpu().numpy()
+    with fec.ExodusPostProcessor(mesh, tmp_path / "poisson.e", ["u"]) as pp:
+        pp.write_times(1, 0.0)
+        pp.write_field(1, "u", u)
+    with fec.ExodusFile(tmp_path / "poisson.e") as f:
+        assert f.nodal_variable_names() == ["u"]
+        uo = f.nodal_variable("u", 1)
+    assert np.abs(uo - g["u_gold"]).max() <= 1e-9 * np.abs(g["u_gold"]).max()
+
+
 def test_neohookean_newton_update_matches_direct_solve(fec):
     torch = _torch()
     mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (7, 7, 7))
