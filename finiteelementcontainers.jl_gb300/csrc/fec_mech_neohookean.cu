@@ -5,6 +5,7 @@
 #include <type_traits>
 #include "fec_autotune.h"
 #include "fec_launch.h"
+#include "fec_mech_hex27.cuh"
 #include "fec_mech_hex8.cuh"
 
 namespace fec {
@@ -109,6 +110,23 @@ cudaError_t hex8_df64(bool want_r, bool want_k, const ElemArgs& a, cudaStream_t 
   return hex8_df64_1<EPB, false, true>(a, s);
 }
 
+template <bool R, bool K>
+cudaError_t hex27_df64_1(const ElemArgs& a, cudaStream_t s) {
+  constexpr size_t smem = Hex27Df64Smem<NeoHookean>::BYTES;
+  cudaError_t err;
+  if ((err = ensure_smem<mech_hex27_df64_kernel<NeoHookean, R, K>>(smem)) != cudaSuccess) return err;
+  mech_hex27_df64_kernel<NeoHookean, R, K><<<unsigned(a.ne), HEX27_THREADS, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t hex27_df64(bool want_r, bool want_k, const ElemArgs& a, cudaStream_t s, int* launches) {
+  if (a.ne <= 0 || (!want_r && !want_k)) return cudaSuccess;
+  ++*launches;
+  if (want_r && want_k) return hex27_df64_1<true, true>(a, s);
+  if (want_r) return hex27_df64_1<true, false>(a, s);
+  return hex27_df64_1<false, true>(a, s);
+}
+
 // FP64 hex8: the contraction runs in df64 on the FP32 pipes unless
 // FEC_FP64_CONTRACTION=native selects the all-FP64 kernel.
 bool fp64_native() {
@@ -165,6 +183,7 @@ cudaError_t launch_mech_neohookean(int elem_type, int precision, bool want_r, bo
     case 8:
       if (precision == 1 && want_k && !hex27_on_cuda_cores())
         return launch_hex27_tc(2, want_r, want_k, a, s, launches);
+      if (precision == 0 && !fp64_native()) return hex27_df64(want_r, want_k, a, s, launches);
       return tuned<8>(precision, want_r, want_k, a, s, launches);
     default: return cudaErrorNotSupported;
   }

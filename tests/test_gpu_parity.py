@@ -176,6 +176,21 @@ def test_higher_order_and_simplex_elements(fec, orc, kind):
     assert max(rel_err(nz, nzo)) <= TOL64
 
 
+def test_hex27_j2_fp64(fec, orc):
+    """FP64 hex27 J2 (the symmetric double-float hex27 kernel) against the oracle,
+    from a plastic first step."""
+    mesh = fec.meshes.box_hex27((3, 3, 3))
+    phys = fec.J2Plasticity(200.0, 0.3, 0.25, 2.0)
+    U = 3.0 * stretch_field(mesh.nodal_coords, seed=2, noise=1e-4, diag=(1.004, 0.999, 0.999)).ravel()
+    asm, p = _setup(fec, mesh, "vector", phys)
+    R, nz, K = _run(fec, asm, p, U)
+    st = np.zeros(7 * 27 * mesh.num_elements())
+    Ro, colptr, rowval, nzo = _oracle(orc, mesh, "j2", phys.create_properties(), U, asm, st, np.zeros_like(st))
+    assert np.array_equal(K.colptr, colptr) and np.array_equal(K.rowval, rowval)
+    assert max(rel_err(R, Ro)) <= TOL64
+    assert max(rel_err(nz, nzo)) <= TOL64
+
+
 @pytest.mark.parametrize("kind", ["tet4", "tet10", "hex27"])
 @pytest.mark.parametrize("phys_name", ["neohookean", "j2"])
 def test_higher_order_fp32_element(fec, orc, kind, phys_name):
