@@ -92,4 +92,59 @@ __device__ __forceinline__ float2 df64_fma(float2 a, float2 b, float2 c) {
 
 __device__ __forceinline__ float2 df64_neg(float2 a) { return make_float2(-a.x, -a.y); }
 
+// c + a0 b0 + a1 b1 + a2 b2 with one renormalisation: each product's high part
+// and exact error come from one FMA (two-product), the three high parts are
+// added to c.x with TwoSum, and all low-order terms (product errors, cross
+// terms, TwoSum errors, c.y) are summed in FP32 before the final Fast2Sum.
+// 38 FP32 operations against 45 for three chained df64_fma, same ~2^-48
+// relative accuracy for these short sums.
+__device__ __forceinline__ float2 df64_dot3_acc(float2 c, float2 a0, float2 b0, float2 a1, float2 b1, float2 a2,
+                                                float2 b2) {
+  const float p0 = __fmul_rn(a0.x, b0.x), p1 = __fmul_rn(a1.x, b1.x), p2 = __fmul_rn(a2.x, b2.x);
+  float e = __fmaf_rn(a0.x, b0.x, -p0);
+  e = __fmaf_rn(a0.x, b0.y, e);
+  e = __fmaf_rn(a0.y, b0.x, e);
+  e = __fadd_rn(__fmaf_rn(a1.x, b1.x, -p1), e);
+  e = __fmaf_rn(a1.x, b1.y, e);
+  e = __fmaf_rn(a1.y, b1.x, e);
+  e = __fadd_rn(__fmaf_rn(a2.x, b2.x, -p2), e);
+  e = __fmaf_rn(a2.x, b2.y, e);
+  e = __fmaf_rn(a2.y, b2.x, e);
+  float s = c.x, lo = __fadd_rn(c.y, e);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float p = k == 0 ? p0 : (k == 1 ? p1 : p2);
+    const float t = __fadd_rn(s, p);
+    const float v = __fsub_rn(t, s);
+    lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(s, __fsub_rn(t, v)), __fsub_rn(p, v)));
+    s = t;
+  }
+  return df64_fast2sum(s, lo);
+}
+
+// a0 b0 + a1 b1 + a2 b2 (the same without an accumulator: the first high part
+// starts the sum).
+__device__ __forceinline__ float2 df64_dot3(float2 a0, float2 b0, float2 a1, float2 b1, float2 a2, float2 b2) {
+  const float p0 = __fmul_rn(a0.x, b0.x), p1 = __fmul_rn(a1.x, b1.x), p2 = __fmul_rn(a2.x, b2.x);
+  float e = __fmaf_rn(a0.x, b0.x, -p0);
+  e = __fmaf_rn(a0.x, b0.y, e);
+  e = __fmaf_rn(a0.y, b0.x, e);
+  e = __fadd_rn(__fmaf_rn(a1.x, b1.x, -p1), e);
+  e = __fmaf_rn(a1.x, b1.y, e);
+  e = __fmaf_rn(a1.y, b1.x, e);
+  e = __fadd_rn(__fmaf_rn(a2.x, b2.x, -p2), e);
+  e = __fmaf_rn(a2.x, b2.y, e);
+  e = __fmaf_rn(a2.y, b2.x, e);
+  float s = p0, lo = e;
+#pragma unroll
+  for (int k = 1; k < 3; ++k) {
+    const float p = k == 1 ? p1 : p2;
+    const float t = __fadd_rn(s, p);
+    const float v = __fsub_rn(t, s);
+    lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(s, __fsub_rn(t, v)), __fsub_rn(p, v)));
+    s = t;
+  }
+  return df64_fast2sum(s, lo);
+}
+
 }  // namespace fec

@@ -131,15 +131,15 @@ __global__ void __launch_bounds__(HEX27_THREADS, 3) mech_hex27_df64_kernel(ElemA
     const float2 g0 = dNX[a * 3], g1 = dNX[a * 3 + 1], g2 = dNX[a * 3 + 2];
     if (WANT_R && cs == 0) {
       const float2* P = s_P + q * 9 + i * 3;
-      R = df64_fma(g0, P[0], df64_fma(g1, P[1], df64_fma(g2, P[2], R)));
+      R = df64_dot3_acc(R, g0, P[0], g1, P[1], g2, P[2]);
     }
     if (WANT_K) {
       const float2* Aq = s_A + q * 45;
       float2 t[9];
 #pragma unroll
       for (int kl = 0; kl < 9; ++kl)
-        t[kl] = df64_fma(g0, Aq[sym_index(3 * i, kl)],
-                         df64_fma(g1, Aq[sym_index(3 * i + 1, kl)], df64_mul(g2, Aq[sym_index(3 * i + 2, kl)])));
+        t[kl] = df64_dot3(g0, Aq[sym_index(3 * i, kl)], g1, Aq[sym_index(3 * i + 1, kl)], g2,
+                          Aq[sym_index(3 * i + 2, kl)]);
 #pragma unroll
       for (int dd = 0; dd < 7; ++dd) {
         int b = a + 7 * cs + dd;
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(HEX27_THREADS, 3) mech_hex27_df64_kernel(ElemA
         const float2 h0 = dNX[b * 3], h1 = dNX[b * 3 + 1], h2 = dNX[b * 3 + 2];
 #pragma unroll
         for (int k = 0; k < 3; ++k)
-          K[dd * 3 + k] = df64_fma(t[k * 3], h0, df64_fma(t[k * 3 + 1], h1, df64_fma(t[k * 3 + 2], h2, K[dd * 3 + k])));
+          K[dd * 3 + k] = df64_dot3_acc(K[dd * 3 + k], t[k * 3], h0, t[k * 3 + 1], h1, t[k * 3 + 2], h2);
       }
     }
   }

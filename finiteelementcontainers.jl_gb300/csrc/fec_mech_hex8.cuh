@@ -593,15 +593,15 @@ __global__ void __launch_bounds__(EPB * 24, 4) mech_hex8_df64_kernel(ElemArgs g)
       const float2 g0 = dNX[a * 3], g1 = dNX[a * 3 + 1], g2 = dNX[a * 3 + 2];
       if (WANT_R) {
         const float2* P = s_P + q * 9 + i * 3;
-        R = df64_fma(g0, P[0], df64_fma(g1, P[1], df64_fma(g2, P[2], R)));
+        R = df64_dot3_acc(R, g0, P[0], g1, P[1], g2, P[2]);
       }
       if (WANT_K) {
         const float2* Aq = s_A + q * 45;
         float2 t[9];
 #pragma unroll
         for (int kl = 0; kl < 9; ++kl)
-          t[kl] = df64_fma(g0, Aq[sym_index(r1v[0], kl)],
-                           df64_fma(g1, Aq[sym_index(r1v[1], kl)], df64_mul(g2, Aq[sym_index(r1v[2], kl)])));
+          t[kl] = df64_dot3(g0, Aq[sym_index(r1v[0], kl)], g1, Aq[sym_index(r1v[1], kl)], g2,
+                            Aq[sym_index(r1v[2], kl)]);
 #pragma unroll
         for (int d = 0; d < 5; ++d) {
           if (d == 4 && !fifth) break;
@@ -609,7 +609,7 @@ __global__ void __launch_bounds__(EPB * 24, 4) mech_hex8_df64_kernel(ElemArgs g)
           const float2 h0 = dNX[b * 3], h1 = dNX[b * 3 + 1], h2 = dNX[b * 3 + 2];
 #pragma unroll
           for (int k = 0; k < 3; ++k)
-            K[d * 3 + k] = df64_fma(t[k * 3], h0, df64_fma(t[k * 3 + 1], h1, df64_fma(t[k * 3 + 2], h2, K[d * 3 + k])));
+            K[d * 3 + k] = df64_dot3_acc(K[d * 3 + k], t[k * 3], h0, t[k * 3 + 1], h1, t[k * 3 + 2], h2);
         }
       }
     }
