@@ -86,10 +86,12 @@ def test_newton_loop_graph_replays_eager_bits(fec, precision):
 
 
 def test_autotuned_generic_kernels_are_bitwise_identical(fec):
-    """Every launch configuration the autotuner may pick for the tet4/tet10/hex27
-    kernels (elements per CTA, threads per element) gives bitwise the same
-    residual and nzval, in FP64 and FP32-element arithmetic; the tuned run
-    reports its choices."""
+    """Every launch configuration the autotuner may pick for the tet4/tet10
+    kernels (elements per CTA) gives bitwise the same residual and nzval, in FP64
+    and FP32-element arithmetic; the tuned run reports its choices.  (Hex27 has
+    its own kernels in both arithmetics: double-float in FP64, tensor cores in
+    FP32-element; its generic configurations stay tunable behind
+    FEC_HEX27_ON_CUDA_CORES=1 and FEC_FP64_CONTRACTION=native.)"""
     import os
     torch = _torch()
     from fec_gb300 import batching
@@ -119,4 +121,4 @@ def test_autotuned_generic_kernels_are_bitwise_identical(fec):
             assert np.array_equal(results[(precision, cand)][1], ref[1])
     report = fec.autotune_report()
     print("\n".join(report))
-    assert any("hex27" in line for line in report) and any("tet10" in line for line in report)
+    assert any("tet4" in line for line in report) and any("tet10" in line for line in report)
