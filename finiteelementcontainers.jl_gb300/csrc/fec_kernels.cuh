@@ -701,7 +701,7 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
         const float2* Ai = reinterpret_cast<const float2*>(s_A + q * 81 + i * 27);
         float2 t[9];
 #pragma unroll
-        for (int kl = 0; kl < 9; ++kl) t[kl] = df64_fma(g0, Ai[kl], df64_fma(g1, Ai[9 + kl], df64_mul(g2, Ai[18 + kl])));
+        for (int kl = 0; kl < 9; ++kl) t[kl] = df64_dot3(g0, Ai[kl], g1, Ai[9 + kl], g2, Ai[18 + kl]);
 #pragma unroll
         for (int bb = 0; bb < CW; ++bb) {
           const int b = b0 + bb;
@@ -709,8 +709,7 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
             const float2 h0 = dNf[b * 3 + 0], h1 = dNf[b * 3 + 1], h2 = dNf[b * 3 + 2];
 #pragma unroll
             for (int k = 0; k < 3; ++k)
-              Kf[bb * 3 + k] = df64_add(Kf[bb * 3 + k],
-                                        df64_fma(t[k * 3 + 0], h0, df64_fma(t[k * 3 + 1], h1, df64_mul(t[k * 3 + 2], h2))));
+              Kf[bb * 3 + k] = df64_dot3_acc(Kf[bb * 3 + k], t[k * 3 + 0], h0, t[k * 3 + 1], h1, t[k * 3 + 2], h2);
           }
         }
       }
