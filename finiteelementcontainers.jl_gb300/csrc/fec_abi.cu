@@ -87,6 +87,7 @@ struct fec_ctx {
   DevBuf d_colptr0, d_rowval32, d_cg;  // linear solve: 0-based CSC pattern, CG scratch
   DevBuf d_flag;                       // non-finite scan result
   DevBuf d_nbr_ptr, d_nbr;             // neighbour lists on the device (device symbolic phase, CSC fill)
+  bool single_launch = false;          // FP64 mechanics: every element block in one launch
   float cl_tol = 0.f;
   // optional per-launch timing (CUDA events on the caller's stream)
   bool profiling = false;
@@ -124,6 +125,16 @@ int ok(fec_ctx* c) {
     cudaError_t _e = (call);                                                                            \
     if (_e != cudaSuccess) return fail(ctx, FEC_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(_e));    \
   } while (0)
+
+// FEC_FP64_CONTRACTION=native keeps the FP64 mechanics on the all-FP64 kernels
+// (per block).
+bool fp64_native_env() {
+  static const bool v = [] {
+    const char* e = std::getenv("FEC_FP64_CONTRACTION");
+    return e && e[0] == 'n';
+  }();
+  return v;
+}
 
 int upload(fec_ctx* c, DevBuf& b, const void* src, size_t bytes) {
   b.release();
@@ -572,6 +583,12 @@ int fec_pattern_build(fec_ctx* c, int64_t* nnz_out) {
   return ok(c);
 }
 
+int fec_set_single_launch(fec_ctx* c, int on) {
+  if (!c) return FEC_ERR_ARG;
+  c->single_launch = on != 0;
+  return ok(c);
+}
+
 int fec_pattern_build_device(fec_ctx* c, int64_t* nnz_out, void* stream) {
   if (!c) return FEC_ERR_ARG;
   if (c->n_unknowns < 0) return fail(c, FEC_ERR_STATE, "fec_pattern_build_device before fec_dofs_set");
@@ -811,10 +828,20 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
   int rc;
   if (want_k && (rc = ensure(c, c->d_Ke, rsz * size_t(ke_total)))) return rc;
   if (want_r && (rc = ensure(c, c->d_Re, rsz * size_t(re_total)))) return rc;
-  // element kernels, one launch per block
+  // element kernels: one launch per block, or one for all blocks (fec_set_single_launch)
   GatherArgs ga;
   memset(&ga, 0, sizeof ga);
   int64_t ke_off = 0, re_off = 0, st_off = 0;
+  // (a single-block system is one launch already, on its own kernel)
+  bool mixed = c->single_launch && precision == FEC_FP64 && c->blocks.size() >= 2 &&
+               c->blocks.size() <= size_t(fec::MIXED_MAX_BLOCKS) && !fp64_native_env();
+  std::vector<int> mixed_types;
+  std::vector<ElemArgs> mixed_args;
+  for (const Block& B : c->blocks) {
+    mixed = mixed && B.physics == c->blocks[0].physics;
+    mixed_types.push_back(B.elem_type);
+  }
+  mixed = mixed && fec::mixed_launch_supported(c->blocks[0].physics, int(c->blocks.size()), mixed_types.data());
   for (size_t b = 0; b < c->blocks.size(); ++b) {
     const Block& B = c->blocks[b];
     const int ndof = c->nf * B.nnpe;
@@ -834,8 +861,10 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     ea.closure = c->d_cl_args.p;
     if (B.physics == FEC_PHYS_J2_MLP && !ea.closure)
       return fail(c, FEC_ERR_STATE, "block %d uses the learned closure but fec_closure_set was not called", int(b) + 1);
-    cudaError_t e;
-    {
+    cudaError_t e = cudaSuccess;
+    if (mixed) {
+      mixed_args.push_back(ea);
+    } else {
       static const char* kNames[5][9] = {
           {"", "", "", "", "", "", "", "", ""},
           {"", "element_poisson", "element_poisson_quad4", "", "", "", "element_poisson_tet4",
@@ -889,6 +918,15 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     ke_off += pad4(B.ne * ndof * ndof);
     re_off += B.ne * ndof;
     st_off += int64_t(ns) * B.nq * B.ne;
+  }
+  if (mixed) {
+    cudaError_t e;
+    {
+      LaunchTimer timer(c, s, "element_all_blocks");
+      e = fec::launch_mech_mixed(c->blocks[0].physics, int(c->blocks.size()), mixed_types.data(), mixed_args.data(),
+                                 want_r, want_k, s, &c->last_launches);
+    }
+    if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "element kernel launch: %s", cudaGetErrorString(e));
   }
   ga.nn = c->nn;
   ga.nf = c->nf;

@@ -585,15 +585,16 @@ struct J2 {
 // chunk cs:  R_r += sum_J dNX_aJ P'_iJ;  t_kL = sum_J dNX_aJ A'_iJkL;
 // K_r,(b,k) += sum_L t_kL dNX_bL.
 // ---------------------------------------------------------------------------
+// One tile of EPB elements (thread (tx, ty): row/column chunk tx of element ty),
+// shared by the kernel below and the single-launch kernel of mixed blocks.
 template <int ET, class Model, typename Real, int EPB, int CSPLIT, bool WANT_R, bool WANT_K>
-__global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
-    mech_element_kernel(ElemArgs g) {
+__device__ __forceinline__ void mech_element_tile(const ElemArgs& g, unsigned tile, int tx, int ty,
+                                                  unsigned char* smem_raw) {
   using E = Elem<ET>;
   using L = RefLayout<ET>;
   constexpr int D = 3, A = E::NNPE, NQ = E::NQ, NDOF = 3 * A, TPE = NDOF * CSPLIT;
   constexpr int CW = (A + CSPLIT - 1) / CSPLIT;  // nodes b per column chunk
   constexpr int NS = Model::NS, SCR = Model::SCR;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   // carve shared memory
   double* s_ref = reinterpret_cast<double*>(smem_raw);
   double* s_x_all = s_ref + ((L::SIZE + 1) & ~1);
@@ -613,8 +614,7 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
   float* s_reff = reinterpret_cast<float*>(s_conn_all + ((EPB * A + 3) & ~3));
   float* s_xd_all = s_reff + ((L::SIZE + 3) & ~3);
 
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int64_t e = int64_t(blockIdx.x) * EPB + ty;
+  const int64_t e = int64_t(tile) * EPB + ty;
   double* s_x = s_x_all + ty * A * D;
   double* s_u = s_u_all + ty * A * D;
   Real* s_dNX = s_dNX_all + ty * NQ * A * D;
@@ -638,7 +638,7 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
   // (FP64 in the FP64 variant) work has all its lanes busy
   for (int w = ty * TPE + tx; w < EPB * NQ; w += EPB * TPE) {
     const int el = w / NQ, q = w % NQ;
-    const int64_t ee = int64_t(blockIdx.x) * EPB + el;
+    const int64_t ee = int64_t(tile) * EPB + el;
     if (ee >= g.ne) continue;
     const double* px = s_x_all + el * A * D;
     const double* pu = s_u_all + el * A * D;
@@ -764,6 +764,13 @@ __global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
   }
   if (WANT_R && cs == 0) static_cast<typename WS<Real>::T*>(g.Re)[e * NDOF + r] = WS<Real>::from(R);
   }
+}
+
+template <int ET, class Model, typename Real, int EPB, int CSPLIT, bool WANT_R, bool WANT_K>
+__global__ void __launch_bounds__(EPB * 3 * Elem<ET>::NNPE * CSPLIT)
+    mech_element_kernel(ElemArgs g) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  mech_element_tile<ET, Model, Real, EPB, CSPLIT, WANT_R, WANT_K>(g, blockIdx.x, threadIdx.x, threadIdx.y, smem_raw);
 }
 
 template <int ET, class Model, typename Real, int EPB, bool WANT_K>

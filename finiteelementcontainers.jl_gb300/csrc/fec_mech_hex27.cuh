@@ -28,12 +28,14 @@ struct Hex27Df64Smem {
 
 constexpr int HEX27_THREADS = 192;  // 162 contracting threads, padded to whole warps
 
-template <class Model, bool WANT_R, bool WANT_K>
-__global__ void __launch_bounds__(HEX27_THREADS, 3) mech_hex27_df64_kernel(ElemArgs g) {
+// One element by NTHR threads (thread tid), shared by the kernel below and the
+// single-launch kernel of mixed element blocks.
+template <class Model, bool WANT_R, bool WANT_K, int NTHR>
+__device__ __forceinline__ void hex27_df64_tile(const ElemArgs& g, unsigned elem, int tid, unsigned char* smem_raw) {
   constexpr int NQ = 27, A = 27, NDOF = 81, NS = Model::NS, SCR = Model::SCR, SCR2 = Model::SCR2;
+  static_assert(NTHR >= 2 * NDOF, "162 contracting threads");
   using S = Hex27Df64Smem<Model>;
   using L = RefLayout<8>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   double* dbase = reinterpret_cast<double*>(smem_raw);
   double* s_dN = dbase + S::D_DN;
   double* s_w = dbase + S::D_W;
@@ -46,10 +48,9 @@ __global__ void __launch_bounds__(HEX27_THREADS, 3) mech_hex27_df64_kernel(ElemA
   float2* s_A = fb + S::F_A;
   int* s_conn = reinterpret_cast<int*>(fb + S::N_F2);
 
-  const int tid = threadIdx.x;
-  const int64_t e = blockIdx.x;  // one element per CTA; the grid covers the block
-  for (int k = tid; k < NQ * A * 3; k += HEX27_THREADS) s_dN[k] = g.ref[L::DN_OFF + k];
-  for (int k = tid; k < NQ; k += HEX27_THREADS) s_w[k] = g.ref[L::W_OFF + k];
+  const int64_t e = elem;
+  for (int k = tid; k < NQ * A * 3; k += NTHR) s_dN[k] = g.ref[L::DN_OFF + k];
+  for (int k = tid; k < NQ; k += NTHR) s_w[k] = g.ref[L::W_OFF + k];
   if (tid < A) s_conn[tid] = g.conn[e * A + tid];
   __syncthreads();
   if (tid < A * 3) {
@@ -109,7 +110,7 @@ __global__ void __launch_bounds__(HEX27_THREADS, 3) mech_hex27_df64_kernel(ElemA
   }
   __syncthreads();
   if (WANT_K) {
-    for (int w = tid; w < NQ * 45; w += HEX27_THREADS) {
+    for (int w = tid; w < NQ * 45; w += NTHR) {
       const int q = w / 45;
       int r1, r2;
       sym_pair(w - q * 45, r1, r2);
@@ -166,6 +167,12 @@ __global__ void __launch_bounds__(HEX27_THREADS, 3) mech_hex27_df64_kernel(ElemA
       }
     }
   }
+}
+
+template <class Model, bool WANT_R, bool WANT_K>
+__global__ void __launch_bounds__(HEX27_THREADS, 3) mech_hex27_df64_kernel(ElemArgs g) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  hex27_df64_tile<Model, WANT_R, WANT_K, HEX27_THREADS>(g, blockIdx.x, threadIdx.x, smem_raw);
 }
 
 }  // namespace fec

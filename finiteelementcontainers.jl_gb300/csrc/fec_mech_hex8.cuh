@@ -29,9 +29,11 @@ namespace fec {
 // a block that does not start on a 16-byte boundary, or a wait that gives up,
 // falls back to plain loads.  Ends with a barrier.
 __device__ __forceinline__ void stage_hex8_tables(const double* gref, double* s_ref, const int32_t* gconn, int nlive,
-                                                  int* s_conn, uint64_t* bar, int tid, int nthr) {
+                                                  int* s_conn, uint64_t* bar, int tid, int nthr,
+                                                  bool allow_bulk = true) {
   constexpr int NREF = RefLayout<1>::SIZE;
-  const bool bulk = ((reinterpret_cast<uintptr_t>(gref) | reinterpret_cast<uintptr_t>(gconn)) & 15) == 0;
+  const bool bulk =
+      allow_bulk && ((reinterpret_cast<uintptr_t>(gref) | reinterpret_cast<uintptr_t>(gconn)) & 15) == 0;
   bool done = false;
   if (bulk) {
     if (tid == 0) {
@@ -501,19 +503,21 @@ struct Hex8Df64Smem {
 // and holds 15 accumulators, which fits 4 CTAs (24 warps) on an SM: the df64
 // chains are latency-bound, and twice the warps of a 12-thread-per-element
 // layout (rows paired as in mech_hex8_sym_kernel) cut the kernel time by 21%.
-template <class Model, int EPB, bool WANT_R, bool WANT_K>
-__global__ void __launch_bounds__(EPB * 24, 4) mech_hex8_df64_kernel(ElemArgs g) {
+// One CTA-sized tile of EPB elements (thread (tx, ty): row node and component
+// tx, element ty), shared by the kernel below and the single-launch kernel of
+// mixed element blocks (which stages without the bulk copy: BULK = false).
+template <class Model, int EPB, bool WANT_R, bool WANT_K, bool BULK = true>
+__device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile, int tx, int ty,
+                                               unsigned char* smem_raw) {
   constexpr int NQ = 8, TPE = 24, NS = Model::NS, SCR = Model::SCR, SCR2 = Model::SCR2;
   using S = Hex8Df64Smem<Model, EPB>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   double* dbase = reinterpret_cast<double*>(smem_raw);
   double* s_ref = dbase + S::D_REF;
   float2* fb = reinterpret_cast<float2*>(dbase + S::N_DOUBLE);
   int* s_conn_all = reinterpret_cast<int*>(fb + S::N_F2);
 
-  const int tx = threadIdx.x, ty = threadIdx.y;
   const int tid = ty * TPE + tx, nthr = EPB * TPE;
-  const int64_t e0 = int64_t(blockIdx.x) * EPB;
+  const int64_t e0 = int64_t(tile) * EPB;
   const int64_t e = e0 + ty;
   const bool live = e < g.ne;
   double* s_x = dbase + S::D_X + ty * 24;
@@ -527,7 +531,7 @@ __global__ void __launch_bounds__(EPB * 24, 4) mech_hex8_df64_kernel(ElemArgs g)
   {
     const int64_t left = g.ne - e0;
     stage_hex8_tables(g.ref, s_ref, g.conn + e0 * 8, left < EPB ? int(left) : EPB, s_conn_all,
-                      reinterpret_cast<uint64_t*>(s_conn_all + EPB * 8), tid, nthr);
+                      reinterpret_cast<uint64_t*>(s_conn_all + EPB * 8), tid, nthr, BULK);
   }
   if (live) {
     const int a = tx / 3, d = tx % 3;
@@ -641,6 +645,12 @@ __global__ void __launch_bounds__(EPB * 24, 4) mech_hex8_df64_kernel(ElemArgs g)
       dst[idx] = *reinterpret_cast<const double2*>(src + el * S::K_STRIDE + off * 2);
     }
   }
+}
+
+template <class Model, int EPB, bool WANT_R, bool WANT_K>
+__global__ void __launch_bounds__(EPB * 24, 4) mech_hex8_df64_kernel(ElemArgs g) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  hex8_df64_tile<Model, EPB, WANT_R, WANT_K>(g, blockIdx.x, threadIdx.x, threadIdx.y, smem_raw);
 }
 
 }  // namespace fec

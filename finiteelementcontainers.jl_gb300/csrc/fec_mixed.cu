@@ -1,0 +1,132 @@
+// fec_mixed.cu -- all element blocks of an FP64 mechanics system in one
+// persistent launch.
+//
+// Blocks of different element types (hex8, tet4, tet10, hex27) have different
+// kernels; here one kernel of 240-thread CTAs walks a list of work tiles over
+// all blocks (blockIdx-strided) and runs, per tile, the same tile function the
+// per-block kernels use, with a tile shape that fills 240 threads: 10 hex8
+// elements (24 threads each), 20 tet4 (12 threads), 4 tet10 (60 threads) or one
+// hex27 (162 contracting threads).  The arithmetic per element is the per-block
+// kernels', so the workspace -- and the assembled system -- is bitwise the same.
+// (Tile shapes: 10 hex8 x 24 threads, 20 tet4 x 12, 4 tet10 x 60 (two column
+// chunks per row), one hex27 x 240.)
+#include "fec_launch.h"
+#include "fec_mech_hex27.cuh"
+#include "fec_mech_hex8.cuh"
+
+namespace fec {
+namespace {
+
+constexpr int MIX_THREADS = 240;
+constexpr int MIX_HEX8_EPB = 10, MIX_TET4_EPB = 20, MIX_TET10_EPB = 4;  // tet10: 2 column chunks per row
+constexpr int MIX_MAX_BLOCKS = MIXED_MAX_BLOCKS;
+
+struct MixedBlocks {
+  int n;
+  int type[MIX_MAX_BLOCKS];
+  unsigned tile_start[MIX_MAX_BLOCKS + 1];
+  ElemArgs args[MIX_MAX_BLOCKS];
+};
+
+template <class Model, bool R, bool K>
+__device__ __forceinline__ void run_tile(int type, const ElemArgs& g, unsigned tile, int tid, unsigned char* sm) {
+  switch (type) {
+    case 1: hex8_df64_tile<Model, MIX_HEX8_EPB, R, K, false>(g, tile, tid % 24, tid / 24, sm); break;
+    case 6: mech_element_tile<6, Model, double, MIX_TET4_EPB, 1, R, K>(g, tile, tid % 12, tid / 12, sm); break;
+    case 7: mech_element_tile<7, Model, double, MIX_TET10_EPB, 2, R, K>(g, tile, tid % 60, tid / 60, sm); break;
+    default: hex27_df64_tile<Model, R, K, MIX_THREADS>(g, tile, tid, sm); break;
+  }
+}
+
+template <class Model, bool R, bool K>
+__global__ void __launch_bounds__(MIX_THREADS, 2) mixed_df64_kernel(MixedBlocks m) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const unsigned total = m.tile_start[m.n];
+  for (unsigned item = blockIdx.x; item < total; item += gridDim.x) {
+    int b = 0;
+    while (b + 1 < m.n && item >= m.tile_start[b + 1]) ++b;
+    ElemArgs g;  // the block's arguments, read with static indices from the parameter block
+    int type;
+    unsigned start;
+    switch (b) {
+      case 0: g = m.args[0]; type = m.type[0]; start = m.tile_start[0]; break;
+      case 1: g = m.args[1]; type = m.type[1]; start = m.tile_start[1]; break;
+      case 2: g = m.args[2]; type = m.type[2]; start = m.tile_start[2]; break;
+      default: g = m.args[3]; type = m.type[3]; start = m.tile_start[3]; break;
+    }
+    run_tile<Model, R, K>(type, g, item - start, threadIdx.x, smem_raw);
+    __syncthreads();  // the next tile reuses the shared memory
+  }
+}
+
+template <class Model>
+constexpr size_t mixed_smem(bool want_k) {
+  const size_t a = Hex8Df64Smem<Model, MIX_HEX8_EPB>::BYTES;
+  const size_t b = want_k ? mech_smem_bytes<6, Model, double, MIX_TET4_EPB, true>()
+                          : mech_smem_bytes<6, Model, double, MIX_TET4_EPB, false>();
+  const size_t c = want_k ? mech_smem_bytes<7, Model, double, MIX_TET10_EPB, true>()
+                          : mech_smem_bytes<7, Model, double, MIX_TET10_EPB, false>();
+  const size_t d = Hex27Df64Smem<Model>::BYTES;
+  size_t m = a > b ? a : b;
+  m = m > c ? m : c;
+  return m > d ? m : d;
+}
+
+template <class Model, bool R, bool K>
+cudaError_t go(const MixedBlocks& m, cudaStream_t s) {
+  const size_t smem = mixed_smem<Model>(K);
+  cudaError_t e;
+  if ((e = ensure_smem<mixed_df64_kernel<Model, R, K>>(smem)) != cudaSuccess) return e;
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned total = m.tile_start[m.n];
+  const unsigned grid = total < unsigned(2 * sms) ? total : unsigned(2 * sms);
+  mixed_df64_kernel<Model, R, K><<<grid, MIX_THREADS, smem, s>>>(m);
+  return cudaGetLastError();
+}
+
+template <class Model>
+cudaError_t dispatch(bool want_r, bool want_k, const MixedBlocks& m, cudaStream_t s) {
+  if (want_r && want_k) return go<Model, true, true>(m, s);
+  if (want_r) return go<Model, true, false>(m, s);
+  return go<Model, false, true>(m, s);
+}
+
+}  // namespace
+
+bool mixed_launch_supported(int physics, int nblocks, const int* elem_types) {
+  if (physics != 2 && physics != 3) return false;
+  if (nblocks < 1 || nblocks > MIX_MAX_BLOCKS) return false;
+  for (int b = 0; b < nblocks; ++b) {
+    const int t = elem_types[b];
+    if (t != 1 && t != 6 && t != 7 && t != 8) return false;
+  }
+  return true;
+}
+
+cudaError_t launch_mech_mixed(int physics, int nblocks, const int* elem_types, const ElemArgs* args, bool want_r,
+                              bool want_k, cudaStream_t s, int* launches) {
+  if (!mixed_launch_supported(physics, nblocks, elem_types)) return cudaErrorNotSupported;
+  if (!want_r && !want_k) return cudaSuccess;
+  MixedBlocks m{};
+  m.n = nblocks;
+  unsigned start = 0;
+  for (int b = 0; b < nblocks; ++b) {
+    const int t = elem_types[b];
+    const int64_t per = t == 1 ? MIX_HEX8_EPB : (t == 6 ? MIX_TET4_EPB : (t == 7 ? MIX_TET10_EPB : 1));
+    const int64_t tiles = (args[b].ne + per - 1) / per;
+    if (tiles < 0 || int64_t(start) + tiles >= (int64_t(1) << 31)) return cudaErrorNotSupported;
+    m.type[b] = t;
+    m.args[b] = args[b];
+    m.tile_start[b] = start;
+    start += unsigned(tiles);
+  }
+  m.tile_start[nblocks] = start;
+  for (int b = nblocks; b < MIX_MAX_BLOCKS; ++b) m.tile_start[b + 1] = start;
+  if (start == 0) return cudaSuccess;
+  ++*launches;
+  return physics == 2 ? dispatch<NeoHookean>(want_r, want_k, m, s) : dispatch<J2>(want_r, want_k, m, s);
+}
+
+}  // namespace fec

@@ -41,6 +41,7 @@ SIGNATURES = {
     "fec_pattern_build": (C.c_int, [_vp, _i64p]),
     "fec_pattern_get": (C.c_int, [_vp, _vp, _vp]),
     "fec_pattern_build_device": (C.c_int, [_vp, _i64p, _vp]),
+    "fec_set_single_launch": (C.c_int, [_vp, C.c_int]),
     "fec_pattern_get_device": (C.c_int, [_vp, _vp, _vp, _vp]),
     "fec_update_field": (C.c_int, [_vp, _vp, _vp, C.c_int64, _vp, _vp, _vp]),
     "fec_assemble": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_double, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

@@ -140,6 +140,11 @@ class SparseMatrixAssembler:
             self._csc_host = (colptr, rowval)
         return self._csc_host
 
+    def set_single_launch(self, on: bool = True) -> None:
+        """Run every element block of an FP64 Neo-Hookean/J2 system (hex8, tet4,
+        tet10, hex27 blocks) in one persistent launch (fec_set_single_launch)."""
+        self._call("fec_set_single_launch", 1 if on else 0)
+
     def pattern_device(self):
         """1-based (colptr, rowval) of the CSC stiffness as int64 device tensors,
         filled by a kernel (for a CuSparse-style matrix on the device)."""

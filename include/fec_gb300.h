@@ -118,6 +118,12 @@ int fec_pattern_get(const fec_ctx* ctx, int64_t* colptr, int64_t* rowval);
  * FEC_ERR_UNSUPPORTED for more than 16 element blocks or a node whose adjacent
  * elements hold more than 2048 nodes. */
 int fec_pattern_build_device(fec_ctx* ctx, int64_t* nnz_out, void* stream);
+/* FP64 Neo-Hookean / J2 systems of two to four blocks of hex8, tet4, tet10 or
+ * hex27 elements (one physics): on != 0 runs every element block in ONE
+ * persistent launch (a work list of per-type tiles) instead of one launch per
+ * block; the assembled values are bitwise the same.  Other systems keep one
+ * launch per block. */
+int fec_set_single_launch(fec_ctx* ctx, int on);
 /* 1-based colptr (n_unknowns + 1) and rowval (nnz) written into DEVICE buffers
  * on `stream` (the colptr/rowval of sparse!, SparsityPatterns.jl:301-308). */
 int fec_pattern_get_device(const fec_ctx* ctx, int64_t* colptr_dev, int64_t* rowval_dev, void* stream);

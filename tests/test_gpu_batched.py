@@ -122,3 +122,36 @@ def test_autotuned_generic_kernels_are_bitwise_identical(fec):
     report = fec.autotune_report()
     print("\n".join(report))
     assert any("tet4" in line for line in report) and any("tet10" in line for line in report)
+
+
+@pytest.mark.parametrize("physics", ["neohookean", "j2"])
+def test_single_launch_matches_per_block_launches(fec, physics):
+    """hex8 + tet4 + tet10 + hex27 blocks in ONE persistent element launch give
+    bitwise the residual, nzval and state of one launch per block."""
+    torch = _torch()
+    from fec_gb300 import batching
+    from helpers import stretch_field
+    mesh = fec.meshes.merge_meshes(
+        [fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (5, 5, 5)), fec.meshes.box_tet4((3, 3, 3)),
+         fec.meshes.box_tet10((3, 3, 3)), fec.meshes.box_hex27((3, 3, 3))],
+        names=["hex8", "tet4", "tet10", "hex27"])
+    out = []
+    for single in (False, True):
+        asm = fec.SparseMatrixAssembler(fec.VectorFunction(fec.FunctionSpace(mesh), "u"), device=0)
+        asm.set_single_launch(single)
+        if physics == "neohookean":
+            phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+            U = stretch_field(mesh.nodal_coords, seed=2).ravel()
+        else:
+            phys = fec.J2Plasticity(200.0, 0.3, 0.25, 2.0)
+            U = 3.0 * stretch_field(mesh.nodal_coords, seed=2, noise=1e-4, diag=(1.004, 0.999, 0.999)).ravel()
+        p = fec.create_parameters(mesh, asm, phys)
+        Uu = torch.from_numpy(U[asm.dof.unknown_dofs - 1].copy()).cuda()
+        R, K = fec.assemble_residual_and_stiffness(asm, Uu, p)
+        torch.cuda.synchronize()
+        st = p.state_new.clone() if physics == "j2" else None
+        out.append((R.clone(), K.nzval.clone(), asm.last_launch_count(), st))
+    assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
+    if physics == "j2":
+        assert torch.equal(out[0][3], out[1][3])
+    assert out[0][2] == 5 and out[1][2] == 2  # element launches + the gather
