@@ -203,14 +203,18 @@ __device__ __forceinline__ float map_point_mixed(const double* __restrict__ s_re
 }
 
 // Copy the reference tables and gather X (and U) of each element of the CTA
-// into shared memory.  Threads of element slot ty use tx = 0..TPE-1.
-template <int ET, int NF, int EPB, int TPE>
+// into shared memory.  Threads of element slot ty use tx = 0..TPE-1; slots
+// ty >= EPB (threads past EPB * TPE in a CTA of NTHR threads) only take part in
+// the barriers, and the caller passes them an element index e >= g.ne.
+template <int ET, int NF, int EPB, int TPE, int NTHR = EPB * TPE>
 __device__ __forceinline__ void stage_element(const ElemArgs& g, int64_t e, int tx, int ty, double* s_ref, int* s_conn,
                                               double* s_x, double* s_u) {
   using E = Elem<ET>;
   constexpr int D = E::DIM, A = E::NNPE;
+  static_assert(NTHR >= EPB * TPE, "NTHR covers the element slots");
   const int tid = ty * TPE + tx;
-  for (int i = tid; i < RefLayout<ET>::SIZE; i += EPB * TPE) s_ref[i] = g.ref[i];
+  if (NTHR == EPB * TPE || tid < EPB * TPE)
+    for (int i = tid; i < RefLayout<ET>::SIZE; i += EPB * TPE) s_ref[i] = g.ref[i];
   const bool live = e < g.ne;
   if (live)
     for (int a = tx; a < A; a += TPE) s_conn[a] = g.conn[e * A + a];
@@ -586,13 +590,17 @@ struct J2 {
 // K_r,(b,k) += sum_L t_kL dNX_bL.
 // ---------------------------------------------------------------------------
 // One tile of EPB elements (thread (tx, ty): row/column chunk tx of element ty),
-// shared by the kernel below and the single-launch kernel of mixed blocks.
-template <int ET, class Model, typename Real, int EPB, int CSPLIT, bool WANT_R, bool WANT_K>
+// shared by the kernel below and the single-launch kernel of mixed blocks.  In
+// a CTA of NTHR > EPB * TPE threads the slots ty >= EPB are idle: they pass
+// every barrier and touch no memory.
+template <int ET, class Model, typename Real, int EPB, int CSPLIT, bool WANT_R, bool WANT_K,
+          int NTHR = EPB * 3 * Elem<ET>::NNPE * CSPLIT>
 __device__ __forceinline__ void mech_element_tile(const ElemArgs& g, unsigned tile, int tx, int ty,
                                                   unsigned char* smem_raw) {
   using E = Elem<ET>;
   using L = RefLayout<ET>;
   constexpr int D = 3, A = E::NNPE, NQ = E::NQ, NDOF = 3 * A, TPE = NDOF * CSPLIT;
+  constexpr bool HAS_IDLE = NTHR > EPB * TPE;
   constexpr int CW = (A + CSPLIT - 1) / CSPLIT;  // nodes b per column chunk
   constexpr int NS = Model::NS, SCR = Model::SCR;
   // carve shared memory
@@ -614,7 +622,7 @@ __device__ __forceinline__ void mech_element_tile(const ElemArgs& g, unsigned ti
   float* s_reff = reinterpret_cast<float*>(s_conn_all + ((EPB * A + 3) & ~3));
   float* s_xd_all = s_reff + ((L::SIZE + 3) & ~3);
 
-  const int64_t e = int64_t(tile) * EPB + ty;
+  const int64_t e = (HAS_IDLE && ty >= EPB) ? g.ne : int64_t(tile) * EPB + ty;  // idle slot: not live
   double* s_x = s_x_all + ty * A * D;
   double* s_u = s_u_all + ty * A * D;
   Real* s_dNX = s_dNX_all + ty * NQ * A * D;
@@ -623,11 +631,12 @@ __device__ __forceinline__ void mech_element_tile(const ElemArgs& g, unsigned ti
   Real* s_scr = s_scr_all + ty * NQ * SCR;
   Real* s_A = s_A_all + ty * NQ * 81;
   float2* s_dNXf = s_dNXf_all + ty * NQ * A * D;
-  stage_element<ET, 3, EPB, TPE>(g, e, tx, ty, s_ref, s_conn_all + ty * A, s_x, s_u);
+  stage_element<ET, 3, EPB, TPE, NTHR>(g, e, tx, ty, s_ref, s_conn_all + ty * A, s_x, s_u);
   const bool live = e < g.ne;
   float* s_xd = s_xd_all + ty * A * D;
   if constexpr (!DF) {
-    for (int i = ty * TPE + tx; i < L::SIZE; i += EPB * TPE) s_reff[i] = float(s_ref[i]);
+    if (!HAS_IDLE || ty < EPB)
+      for (int i = ty * TPE + tx; i < L::SIZE; i += EPB * TPE) s_reff[i] = float(s_ref[i]);
     if (live)
       for (int i = tx; i < A * D; i += TPE) s_xd[i] = float(s_x[i] - s_x[i % D]);
     __syncthreads();
@@ -636,7 +645,7 @@ __device__ __forceinline__ void mech_element_tile(const ElemArgs& g, unsigned ti
   // quadrature-point kinematics + constitutive update, one thread per point: the
   // CTA's EPB * NQ points go to its first threads so that every warp issuing this
   // (FP64 in the FP64 variant) work has all its lanes busy
-  for (int w = ty * TPE + tx; w < EPB * NQ; w += EPB * TPE) {
+  for (int w = ty * TPE + tx; w < EPB * NQ && (!HAS_IDLE || ty < EPB); w += EPB * TPE) {
     const int el = w / NQ, q = w % NQ;
     const int64_t ee = int64_t(tile) * EPB + el;
     if (ee >= g.ne) continue;
