@@ -155,3 +155,29 @@ def test_single_launch_matches_per_block_launches(fec, physics):
     if physics == "j2":
         assert torch.equal(out[0][3], out[1][3])
     assert out[0][2] == 5 and out[1][2] == 2  # element launches + the gather
+
+
+def test_newton_loop_graph_with_single_launch(fec):
+    """The CUDA-graph Newton loop over the tet4/tet10/hex27 system with all its
+    element blocks in one persistent launch replays the eager loop bitwise, and
+    both equal the loop with one launch per block."""
+    torch = _torch()
+    from fec_gb300 import batching
+    runs = []
+    for single in (False, True):
+        asm, p, _, Uu, _ = _system(fec, batching.mixed_mesh(2, 1, 1))
+        asm.set_single_launch(single)
+        systems = [(asm, p, Uu)]
+        eager = batching.NewtonLoop(systems, iterations=5)
+        eager.run_eager()
+        torch.cuda.synchronize()
+        runs.append((eager.norms.clone(), eager.unknowns(0).clone(), asm.last_launch_count()))
+        if single:
+            graph = batching.NewtonLoop(systems, iterations=5).capture()
+            graph.replay()
+            torch.cuda.synchronize()
+            assert torch.equal(eager.norms, graph.norms)
+            assert torch.equal(eager.unknowns(0), graph.unknowns(0))
+    assert torch.equal(runs[0][0], runs[1][0]) and torch.equal(runs[0][1], runs[1][1])
+    assert bool(torch.isfinite(runs[1][0]).all())
+    assert runs[0][2] == 4 and runs[1][2] == 2  # element launches + the gather
