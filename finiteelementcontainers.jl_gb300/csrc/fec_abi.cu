@@ -87,6 +87,7 @@ struct fec_ctx {
   DevBuf d_colptr0, d_rowval32, d_cg;  // linear solve: 0-based CSC pattern, CG scratch
   DevBuf d_flag;                       // non-finite scan result
   DevBuf d_nbr_ptr, d_nbr;             // neighbour lists on the device (device symbolic phase, CSC fill)
+  DevBuf d_tile_counter;               // single launch of mixed element blocks: next work tile
   bool single_launch = false;          // FP64 mechanics: every element block in one launch
   float cl_tol = 0.f;
   // optional per-launch timing (CUDA events on the caller's stream)
@@ -267,7 +268,7 @@ int fec_ctx_destroy(fec_ctx* c) {
   for (DevBuf* b : {&c->d_coords, &c->d_conn, &c->d_ref, &c->d_nadj_ptr, &c->d_nadj, &c->d_epos, &c->d_umask,
                     &c->d_col_base, &c->d_col_len, &c->d_dtu, &c->d_unknown_dofs, &c->d_Ke, &c->d_Re, &c->d_cl_w,
                     &c->d_cl_norm, &c->d_cl_cnt, &c->d_cl_args, &c->d_cl_img, &c->d_cl_table, &c->d_V, &c->d_colptr0, &c->d_rowval32,
-                    &c->d_cg, &c->d_flag})
+                    &c->d_cg, &c->d_flag, &c->d_nbr_ptr, &c->d_nbr, &c->d_tile_counter})
     b->release();
   delete c;
   return FEC_OK;
@@ -920,11 +921,12 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     st_off += int64_t(ns) * B.nq * B.ne;
   }
   if (mixed) {
+    if (int rc = ensure(c, c->d_tile_counter, sizeof(unsigned))) return rc;
     cudaError_t e;
     {
       LaunchTimer timer(c, s, "element_all_blocks");
       e = fec::launch_mech_mixed(c->blocks[0].physics, int(c->blocks.size()), mixed_types.data(), mixed_args.data(),
-                                 want_r, want_k, s, &c->last_launches);
+                                 want_r, want_k, static_cast<unsigned*>(c->d_tile_counter.p), s, &c->last_launches);
     }
     if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "element kernel launch: %s", cudaGetErrorString(e));
   }

@@ -43,10 +43,12 @@ cudaError_t launch_hex27_tc(int physics, bool want_r, bool want_k, const ElemArg
 bool hex27_on_cuda_cores();
 // FP64 Neo-Hookean (2) or J2 (3) element blocks of types hex8/tet4/tet10/hex27
 // (at most MIXED_MAX_BLOCKS) in one persistent launch; bitwise the per-block result.
+// tile_counter: one unsigned of device memory, zeroed on `stream` by the launch
+// (the CTAs take their work tiles from it).
 constexpr int MIXED_MAX_BLOCKS = 4;
 bool mixed_launch_supported(int physics, int nblocks, const int* elem_types);
 cudaError_t launch_mech_mixed(int physics, int nblocks, const int* elem_types, const ElemArgs* args, bool want_r,
-                              bool want_k, cudaStream_t stream, int* launches);
+                              bool want_k, unsigned* tile_counter, cudaStream_t stream, int* launches);
 
 // Reference-element tables (RefLayout order) for an element type, in double.
 // Returns the number of doubles written (0 for an unknown type).

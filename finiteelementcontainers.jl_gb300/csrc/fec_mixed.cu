@@ -2,9 +2,9 @@
 // persistent launch.
 //
 // Blocks of different element types (hex8, tet4, tet10, hex27) have different
-// kernels; here one kernel of 192-thread CTAs (three per SM) walks a list of
-// work tiles over all blocks (blockIdx-strided) and runs, per tile, the same
-// tile function the per-block kernels use, in a tile shape of 192 threads: 8
+// kernels; here one kernel of 192-thread CTAs (three per SM) takes work tiles
+// from one list over all blocks (dynamically: each CTA fetches its next tile
+// from a device counter) and runs, per tile, the same tile function the per-block kernels use, in a tile shape of 192 threads: 8
 // hex8 elements x 24 threads and one hex27 element x 192 threads (the shapes of
 // their own kernels), 16 tet4 x 12, and 3 tet10 x 60 (two column chunks per
 // row; the last 12 threads idle).  The arithmetic per element is the per-block
@@ -60,15 +60,21 @@ __device__ __forceinline__ void run_tile(int type, const ElemArgs& g, unsigned t
 }
 
 template <class Model, bool R, bool K>
-__global__ void __launch_bounds__(MIX_THREADS, MIX_CTAS_PER_SM) mixed_df64_kernel(const __grid_constant__ MixedBlocks m) {
+__global__ void __launch_bounds__(MIX_THREADS, MIX_CTAS_PER_SM)
+    mixed_df64_kernel(const __grid_constant__ MixedBlocks m, unsigned* next_tile) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned s_item;
   const unsigned total = m.tile_start[m.n];
-  for (unsigned item = blockIdx.x; item < total; item += gridDim.x) {
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(next_tile, 1u);
+    __syncthreads();
+    const unsigned item = s_item;
+    if (item >= total) break;  // the same value in every thread of the CTA
     int b = 0;
     while (b + 1 < m.n && item >= m.tile_start[b + 1]) ++b;
     // the block's arguments are read in place from the (grid-constant) parameter block
     run_tile<Model, R, K>(m.type[b], m.args[b], item - m.tile_start[b], threadIdx.x, smem_raw);
-    __syncthreads();  // the next tile reuses the shared memory
+    __syncthreads();  // the next tile reuses the shared memory and s_item
   }
 }
 
@@ -86,7 +92,7 @@ constexpr size_t mixed_smem(bool want_k) {
 }
 
 template <class Model, bool R, bool K>
-cudaError_t go(const MixedBlocks& m, cudaStream_t s) {
+cudaError_t go(const MixedBlocks& m, unsigned* counter, cudaStream_t s) {
   const size_t smem = mixed_smem<Model>(K);
   cudaError_t e;
   if ((e = ensure_smem<mixed_df64_kernel<Model, R, K>>(smem)) != cudaSuccess) return e;
@@ -96,15 +102,16 @@ cudaError_t go(const MixedBlocks& m, cudaStream_t s) {
   const unsigned total = m.tile_start[m.n];
   const unsigned slots = unsigned(MIX_CTAS_PER_SM * sms);
   const unsigned grid = total < slots ? total : slots;
-  mixed_df64_kernel<Model, R, K><<<grid, MIX_THREADS, smem, s>>>(m);
+  if ((e = cudaMemsetAsync(counter, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
+  mixed_df64_kernel<Model, R, K><<<grid, MIX_THREADS, smem, s>>>(m, counter);
   return cudaGetLastError();
 }
 
 template <class Model>
-cudaError_t dispatch(bool want_r, bool want_k, const MixedBlocks& m, cudaStream_t s) {
-  if (want_r && want_k) return go<Model, true, true>(m, s);
-  if (want_r) return go<Model, true, false>(m, s);
-  return go<Model, false, true>(m, s);
+cudaError_t dispatch(bool want_r, bool want_k, const MixedBlocks& m, unsigned* counter, cudaStream_t s) {
+  if (want_r && want_k) return go<Model, true, true>(m, counter, s);
+  if (want_r) return go<Model, true, false>(m, counter, s);
+  return go<Model, false, true>(m, counter, s);
 }
 
 }  // namespace
@@ -120,8 +127,9 @@ bool mixed_launch_supported(int physics, int nblocks, const int* elem_types) {
 }
 
 cudaError_t launch_mech_mixed(int physics, int nblocks, const int* elem_types, const ElemArgs* args, bool want_r,
-                              bool want_k, cudaStream_t s, int* launches) {
+                              bool want_k, unsigned* tile_counter, cudaStream_t s, int* launches) {
   if (!mixed_launch_supported(physics, nblocks, elem_types)) return cudaErrorNotSupported;
+  if (!tile_counter) return cudaErrorInvalidValue;
   if (!want_r && !want_k) return cudaSuccess;
   // work of one tile ~ elements x (element dofs)^2 x points: hex27 1 x 81^2 x 27,
   // hex8 8 x 24^2 x 8, tet10 3 x 30^2 x 5, tet4 16 x 12^2 x 1
@@ -154,7 +162,8 @@ cudaError_t launch_mech_mixed(int physics, int nblocks, const int* elem_types, c
   for (int b = nblocks; b < MIX_MAX_BLOCKS; ++b) m.tile_start[b + 1] = start;
   if (start == 0) return cudaSuccess;
   ++*launches;
-  return physics == 2 ? dispatch<NeoHookean>(want_r, want_k, m, s) : dispatch<J2>(want_r, want_k, m, s);
+  return physics == 2 ? dispatch<NeoHookean>(want_r, want_k, m, tile_counter, s)
+                      : dispatch<J2>(want_r, want_k, m, tile_counter, s);
 }
 
 }  // namespace fec
