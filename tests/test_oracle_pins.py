@@ -134,3 +134,95 @@ def test_element_tangent_is_residual_jacobian(orc):
         Rp, _, _ = orc.element("HEX8", "neohookean", [0.8333, 0.3846], x, u + du)
         Rm, _, _ = orc.element("HEX8", "neohookean", [0.8333, 0.3846], x, u - du)
         assert np.abs((Rp - Rm) / (2 * h) - K[:, c]).max() < 1e-6 * np.abs(K).max()
+
+
+# ---------------------------------------------------------------------------
+# Shape functions, gradients and quadrature weights of every element type,
+# pinned by identities that hold exactly (to rounding) on an affinely mapped
+# element: partition of unity of the gradients (sum_a dN_a = 0), completeness
+# (sum_a X_a (x) dN_a = I) and exact volume (sum_q JxW = V).  No reference test
+# holds element-level data for these types, so these identities are their pins.
+# ---------------------------------------------------------------------------
+NEO_HOOKEAN = [0.8333333333333334, 0.38461538461538464]  # bulk, shear of E = 1, nu = 0.3
+J2_PROPS = [200.0, 0.3, 0.25, 2.0]
+
+
+def _affine_element(elem, rng):
+    """Node coordinates of the first element of a small generated mesh of the type,
+    mapped by a random affine map, and the element's volume (area for quad4)."""
+    from fec_gb300 import meshes
+    if elem == "HEX8":
+        m = meshes.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (2, 2, 2))
+    elif elem == "QUAD4":
+        m = meshes.StructuredMesh("quad", (0.0, 0.0), (1.0, 1.0), (2, 2))
+    elif elem == "TETRA4":
+        m = meshes.box_tet4((2, 2, 2))
+    elif elem == "TETRA10":
+        m = meshes.box_tet10((2, 2, 2))
+    else:
+        m = meshes.box_hex27((2, 2, 2))
+    b = m.element_block_names[0]
+    x0 = m.nodal_coords[m.element_conns[b][0] - 1]
+    D = x0.shape[1]
+    if elem.startswith("TETRA"):  # straight-sided: the corner tet's volume
+        c = x0[:4]
+        v0 = abs(np.linalg.det((c[1:] - c[0]).T)) / 6.0
+    else:  # axis-aligned box cell
+        v0 = float(np.prod(x0.max(0) - x0.min(0)))
+    A = np.eye(D) + 0.3 * rng.standard_normal((D, D))
+    assert np.linalg.det(A) > 0.2
+    return x0 @ A.T + rng.standard_normal(D), v0 * np.linalg.det(A)
+
+
+@pytest.mark.parametrize("elem", ["QUAD4", "HEX8", "TETRA4", "TETRA10", "HEX27"])
+def test_element_tables_by_linear_fields(orc, elem):
+    """Poisson element (source amplitude 0, so R = K u) under a linear field u = c.X + c0:
+    grad u = c at every point, so sum_a R_a = 0 and sum_a R_a X_a = V c; K is symmetric
+    with zero row sums."""
+    rng = np.random.default_rng(11)
+    x, V = _affine_element(elem, rng)
+    c = rng.standard_normal(x.shape[1])
+    u = x @ c + 0.7
+    R, K, _ = orc.element(elem, "poisson", [0.0], x, u)
+    scale = np.abs(K).max() * np.abs(u).max()
+    assert abs(R.sum()) <= 1e-14 * scale
+    assert np.abs(R @ x - V * c).max() <= 1e-13 * V * np.abs(c).max()
+    assert np.abs(K.sum(axis=1)).max() <= 1e-14 * np.abs(K).max()
+    assert np.array_equal(K, K.T)
+    assert np.abs(R - K @ u).max() <= 1e-13 * scale
+
+
+@pytest.mark.parametrize("elem", ["HEX8", "TETRA4", "TETRA10", "HEX27"])
+def test_mechanics_element_identities(orc, elem):
+    """Mechanics elements (TestMechanicsCommon.jl:140-190):
+    - homogeneous deformation u = H X: sum_a R_a = 0 and sum_a R_a (x) X_a = V P(I + H);
+    - at u = 0 the tangent annihilates translations; for rotations W X it gives W R0_a,
+      the objectivity of the Neo-Hookean energy of TestMechanicsLargeDeformation.jl:17-27,
+      which is not stress-free at F = I (P(I) = -K/2 I from its -ln J term);
+    - small-strain J2 at a zero state: the tangent annihilates all six rigid modes."""
+    rng = np.random.default_rng(12)
+    x, V = _affine_element(elem, rng)
+    n = x.shape[0]
+    H = 0.05 * rng.standard_normal((3, 3))
+    R, _, _ = orc.element(elem, "neohookean", NEO_HOOKEAN, x, (x @ H.T).ravel())
+    P, _ = orc.neohookean_PA(np.eye(3) + H, *NEO_HOOKEAN)
+    P = P.reshape(3, 3, order="F")  # P[i + 3 J] = P_iJ
+    Rn = R.reshape(n, 3)
+    assert np.abs(Rn.sum(axis=0)).max() <= 1e-14 * V * np.abs(P).max() * n
+    assert np.abs(Rn.T @ x - V * P).max() <= 1e-13 * V * np.abs(P).max()
+
+    P0, _ = orc.neohookean_PA(np.eye(3), *NEO_HOOKEAN)
+    assert np.allclose(P0.reshape(3, 3, order="F"), -0.5 * NEO_HOOKEAN[0] * np.eye(3), rtol=0, atol=1e-15)
+    R0, K0, _ = orc.element(elem, "neohookean", NEO_HOOKEAN, x, np.zeros(3 * n))
+    _, Kj, _ = orc.element(elem, "j2", J2_PROPS, x, np.zeros(3 * n))
+    for d in range(3):
+        t = np.zeros((n, 3))
+        t[:, d] = 1.0
+        assert np.abs(K0 @ t.ravel()).max() <= 1e-14 * np.abs(K0).max() * n
+        assert np.abs(Kj @ t.ravel()).max() <= 1e-14 * np.abs(Kj).max() * n
+    for w in rng.standard_normal((3, 3)):
+        W = np.array([[0.0, -w[2], w[1]], [w[2], 0.0, -w[0]], [-w[1], w[0], 0.0]])
+        r = (x @ W.T).ravel()
+        scale = np.abs(K0).max() * np.abs(r).max() * n
+        assert np.abs((K0 @ r).reshape(n, 3) - R0.reshape(n, 3) @ W.T).max() <= 1e-14 * scale
+        assert np.abs(Kj @ r).max() <= 1e-14 * np.abs(Kj).max() * np.abs(r).max() * n
