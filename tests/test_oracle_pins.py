@@ -226,3 +226,32 @@ def test_mechanics_element_identities(orc, elem):
         scale = np.abs(K0).max() * np.abs(r).max() * n
         assert np.abs((K0 @ r).reshape(n, 3) - R0.reshape(n, 3) @ W.T).max() <= 1e-14 * scale
         assert np.abs(Kj @ r).max() <= 1e-14 * np.abs(Kj).max() * np.abs(r).max() * n
+
+
+def test_j2_pure_shear_closed_form(orc):
+    """J2 radial return (Simo & Hughes 1998, Box 3.2) against the closed form of pure
+    shear gamma = du_x/dy from a virgin state: yield at sqrt(3) tau = sigma_y + H eqps with
+    eqps = gamma_p / sqrt(3) gives gamma_p = (3 G gamma - sqrt(3) sigma_y) / (3 G + H),
+    tau = G (gamma - gamma_p), tangent d tau/d gamma = G H / (3 G + H); the same state in
+    three load steps (radial return is exact for monotonic proportional loading with
+    linear hardening); elastic unloading with slope G and the state unchanged."""
+    E, nu, sy, H = J2_PROPS
+    G = E / (2 * (1 + nu))
+    gamma = 0.01  # about 5x the shear yield strain
+    gu = np.zeros((3, 3)); gu[0, 1] = gamma
+    P, A, sn = orc.j2_update(gu, J2_PROPS, np.zeros(7))
+    gp = (3 * G * gamma - np.sqrt(3) * sy) / (3 * G + H)
+    tau = G * (gamma - gp)
+    assert abs(P[3] - tau) <= 1e-14 * tau and abs(P[1] - tau) <= 1e-14 * tau  # sigma_xy = sigma_yx
+    assert np.abs(P[[0, 2, 4, 5, 6, 7, 8]]).max() <= 1e-15 * tau
+    assert abs(sn[6] - gp / np.sqrt(3)) <= 1e-14 * gp and abs(sn[5] - gp / 2) <= 1e-14 * gp
+    assert abs(A[3 + 9 * 3] - G * H / (3 * G + H)) <= 1e-12 * G
+    st = np.zeros(7)
+    for k in (1, 2, 3):
+        gu = np.zeros((3, 3)); gu[0, 1] = gamma * k / 3
+        P3, _, st = orc.j2_update(gu, J2_PROPS, st)
+    assert abs(P3[3] - P[3]) <= 1e-14 * tau and np.abs(st - sn).max() <= 1e-15
+    gu = np.zeros((3, 3)); gu[0, 1] = gamma - 1e-3
+    Pu, Au, su = orc.j2_update(gu, J2_PROPS, sn)
+    assert abs(Pu[3] - (P[3] - G * 1e-3)) <= 1e-13 * tau
+    assert np.array_equal(su, sn) and abs(Au[3 + 9 * 3] - G) <= 1e-13 * G
