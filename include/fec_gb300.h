@@ -122,7 +122,8 @@ int fec_pattern_build_device(fec_ctx* ctx, int64_t* nnz_out, void* stream);
  * hex27 elements (one physics): on != 0 runs every element block in ONE
  * persistent launch (a work list of per-type tiles) instead of one launch per
  * block; the assembled values are bitwise the same.  Other systems keep one
- * launch per block. */
+ * launch per block.  No counterpart in the reference, which launches one
+ * kernel per block from foreach_block (src/Utils.jl:171-189). */
 int fec_set_single_launch(fec_ctx* ctx, int on);
 /* 1-based colptr (n_unknowns + 1) and rowval (nnz) written into DEVICE buffers
  * on `stream` (the colptr/rowval of sparse!, SparsityPatterns.jl:301-308). */
