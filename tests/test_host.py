@@ -117,6 +117,33 @@ def test_pattern_mixed_blocks(fec, orc):
     _pattern_case(fec, orc, m, "vector", [])
 
 
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_pattern_random_shared_blocks_and_dirichlet(fec, orc, seed):
+    """hex8 and tet4 blocks cut from the same node grid (so the blocks share nodes),
+    in either block order, with random per-component Dirichlet node sets: colptr/rowval
+    bit-exact against the oracle's element-ordered COO + sparse!, scalar and vector."""
+    rng = np.random.default_rng(seed)
+    counts = (5, 4, 5)  # counts[0] == counts[2]: the reference's coordinate loop swaps their bounds
+    hexm = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), counts)
+    tets = fec.meshes.box_tet4(counts)
+    assert np.array_equal(tets.nodal_coords, hexm.nodal_coords)
+    h = hexm.element_conns["block_1"]
+    t = tets.element_conns["block_1"]
+    keep_h = rng.random(h.shape[0]) < 0.5
+    keep_t = np.repeat(~keep_h, 6)  # the tets of the other hexes
+    blocks = {"hexes": ("HEX8", h[keep_h]), "tets": ("TETRA4", t[keep_t])}
+    if seed % 2:
+        blocks = dict(reversed(list(blocks.items())))
+    nn = hexm.nodal_coords.shape[0]
+    sets = {f"s{k}": np.sort(rng.choice(np.arange(1, nn + 1), size=int(rng.integers(1, nn // 3)), replace=False))
+            for k in range(3)}
+    mesh = fec.UnstructuredMesh(hexm.nodal_coords, blocks, nodesets=sets)
+    _pattern_case(fec, orc, mesh, "scalar", [fec.DirichletBC("u", lambda X, t: 0.0, nodeset_name="s0")])
+    comps = ["u_x", "u_y", "u_z"]
+    bcs = [fec.DirichletBC(comps[int(rng.integers(0, 3))], lambda X, t: 0.0, nodeset_name=f"s{k}") for k in range(3)]
+    _pattern_case(fec, orc, mesh, "vector", bcs)
+
+
 def test_pattern_quad4_gold_mesh(fec, orc):
     g = np.load(GOLD / "poisson_quad4.npz")
     mesh = fec.UnstructuredMesh(g["coords"], {"block_1": ("QUAD4", g["conn"])},
