@@ -718,6 +718,7 @@ int fec_pattern_get_device(const fec_ctx* cc, int64_t* colptr_dev, int64_t* rowv
   fec_ctx* c = const_cast<fec_ctx*>(cc);
   if (!c) return FEC_ERR_ARG;
   if (!c->pattern_ready) return fail(c, FEC_ERR_STATE, "fec_pattern_get_device before a pattern build");
+  if (!colptr_dev || (!rowval_dev && c->nnz > 0)) return fail(c, FEC_ERR_ARG, "colptr or rowval is NULL");
   if (c->device < 0) return fail(c, FEC_ERR_STATE, "host-only context (device -1) cannot run kernels");
   cudaSetDevice(c->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);

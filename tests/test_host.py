@@ -199,6 +199,12 @@ def test_abi_error_paths_host_only(fec):
         props = np.array([1.0])
         assert lib.fec_physics_set(h, 2, 1, props.ctypes.data, 1) == _lib.FEC_ERR_ARG
         assert lib.fec_physics_set(h, 1, 99, props.ctypes.data, 1) == _lib.FEC_ERR_UNSUPPORTED
+        # device outputs of the pattern: NULL is refused before any device work
+        st = lib.fec_pattern_get_device(h, None, None, None)
+        assert st == _lib.FEC_ERR_ARG and "NULL" in _lib.last_error(lib, h)
+        cp = C.c_void_p(16)  # never dereferenced: a host-only context refuses next
+        assert lib.fec_pattern_get_device(h, cp, cp, None) == _lib.FEC_ERR_STATE
+        assert lib.fec_set_single_launch(h, 1) == 0 and lib.fec_set_single_launch(None, 1) == _lib.FEC_ERR_ARG
     finally:
         lib.fec_ctx_destroy(h)
 
