@@ -255,3 +255,37 @@ def test_j2_pure_shear_closed_form(orc):
     Pu, Au, su = orc.j2_update(gu, J2_PROPS, sn)
     assert abs(Pu[3] - (P[3] - G * 1e-3)) <= 1e-13 * tau
     assert np.array_equal(su, sn) and abs(Au[3 + 9 * 3] - G) <= 1e-13 * G
+
+
+@pytest.mark.parametrize("elem", ["HEX8", "TETRA4", "TETRA10", "HEX27"])
+def test_patch_test_on_assembled_mesh(orc, elem):
+    """Patch test of the whole assembly (element loop, connectivity, local node orders of
+    the generated meshes): under a linear field (Poisson, no source) and a homogeneous
+    deformation (Neo-Hookean) the assembled residual vanishes at every interior node of
+    the unit box, however the mesh is distorted by an affine map."""
+    from fec_gb300 import meshes
+    if elem == "HEX8":
+        m = meshes.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (4, 4, 4))
+    elif elem == "TETRA4":
+        m = meshes.box_tet4((4, 4, 4))
+    elif elem == "TETRA10":
+        m = meshes.box_tet10((3, 3, 3))
+    else:
+        m = meshes.box_hex27((3, 3, 3))
+    blocks = [(m.element_types[b], m.element_conns[b]) for b in m.element_block_names]
+    X0 = m.nodal_coords
+    interior = np.all((X0 > 1e-12) & (X0 < 1 - 1e-12), axis=1)
+    assert interior.sum() >= 8
+    rng = np.random.default_rng(21)
+    A = np.eye(3) + 0.2 * rng.standard_normal((3, 3))
+    X = X0 @ A.T
+    c = rng.standard_normal(3)
+    R, _ = orc.assemble(blocks, X, "poisson", [0.0], X @ c + 0.3)
+    scale = np.abs(c).max() * np.abs(X).max() ** 2
+    assert np.abs(R[interior]).max() <= 1e-13 * scale
+    assert np.abs(R[~interior]).max() > 1e-6 * scale  # the boundary carries the flux
+    H = 0.05 * rng.standard_normal((3, 3))
+    R, _ = orc.assemble(blocks, X, "neohookean", NEO_HOOKEAN, (X @ H.T).ravel())
+    Rn = R.reshape(-1, 3)
+    assert np.abs(Rn[interior]).max() <= 1e-13 * np.abs(Rn).max()
+    assert np.abs(Rn[~interior]).max() > 1e-6
