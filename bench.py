@@ -725,9 +725,13 @@ def run_ours(args) -> None:
                 "residual": float((Rv - ref_R).norm() / ref_R.norm())}
             del ref_R, ref_nz
         R0, K0 = step()
+    stateful_errors = None
+    if stateful and not args.no_variants:
+        stateful_errors = path_errors(fec, asm, p, dev_inputs, args.precision,
+                                      "fp32_element" if args.precision == "fp64" else "fp64")
     if args.no_e2e:
         return finish(args, fec, world, rank, local, wl, mesh, asm, ne, nn, nf, n_u, nnz, t_ms, value, clocks,
-                      per_kernel, launches, None, variants)
+                      per_kernel, launches, None, variants, stateful_errors)
     host_inputs = [(torch.from_numpy(u).pin_memory(), None if b is None else torch.from_numpy(b).pin_memory())
                    for u, b in inputs]
     n_bc = 0 if inputs[0][1] is None else int(inputs[0][1].size)
@@ -777,11 +781,38 @@ def run_ours(args) -> None:
            "d2h_bytes_per_step": 8 * (n_u + nnz),
            "pipelining": "the read-back of step i (copy stream) overlaps the assembly of step i+1"}
     finish(args, fec, world, rank, local, wl, mesh, asm, ne, nn, nf, n_u, nnz, t_ms, value, clocks, per_kernel,
-           launches, e2e, variants)
+           launches, e2e, variants, stateful_errors)
+
+
+def path_errors(fec, asm, p, dev_inputs, main: str, other: str) -> dict:
+    """One clean pass of a stateful load path (state from zero) in both precisions
+    in lockstep, each carrying its own state: the worst relative error (2-norm)
+    of the `other` variant against `main` over the path, per output."""
+    import torch
+    saved = (p.state_old, p.state_new)
+    s_main = [torch.zeros_like(p.state_old), torch.zeros_like(p.state_old)]
+    s_oth = [torch.zeros_like(p.state_old), torch.zeros_like(p.state_old)]
+    worst = {"residual": 0.0, "nzval": 0.0, "state": 0.0}
+    for Uu, bc in dev_inputs:
+        p.bc_vals = bc
+        p.state_old, p.state_new = s_main
+        R, K = fec.assemble_residual_and_stiffness(asm, Uu, p, precision=main)
+        Rr, Kr = R.clone(), K.nzval.clone()
+        p.state_old, p.state_new = s_oth
+        R2, K2 = fec.assemble_residual_and_stiffness(asm, Uu, p, precision=other)
+        for k, a, b in (("residual", R2, Rr), ("nzval", K2.nzval, Kr), ("state", s_oth[1], s_main[1])):
+            nb = float(b.norm())
+            if nb > 0:
+                worst[k] = max(worst[k], float((a - b).norm()) / nb)
+        del Rr, Kr
+        s_main.reverse()
+        s_oth.reverse()
+    p.state_old, p.state_new = saved
+    return {f"{other}_vs_{main}_max_rel_err_over_path": worst}
 
 
 def finish(args, fec, world, rank, local, wl, mesh, asm, ne, nn, nf, n_u, nnz, t_ms, value, clocks, per_kernel,
-           launches, e2e, variants):
+           launches, e2e, variants, stateful_errors=None):
     import torch.distributed as dist
     if rank != 0:
         if world > 1:
@@ -826,6 +857,8 @@ def finish(args, fec, world, rank, local, wl, mesh, asm, ne, nn, nf, n_u, nnz, t
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.workload)
+    if stateful_errors is not None:
+        variants.setdefault("path_errors", stateful_errors)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -845,9 +878,45 @@ def finish(args, fec, world, rank, local, wl, mesh, asm, ne, nn, nf, n_u, nnz, t
         "cpu_baseline": cpu,
         "variants": variants,
     }
+    if world == 1 and args.workload == "neohookean" and not args.no_sub_results:
+        line["sub_results"] = sub_results(args)
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+# The other workloads, each run as its own process after the headline one and
+# reported inside the headline line.  (steps, warmup) are capped so that the
+# whole default run stays within a few minutes; the closure run trains its
+# network first (5M return-map samples, 60 epochs).
+SUB_RESULTS = (
+    ("poisson_hex8_32cubed", ["--workload", "poisson"], None),
+    ("j2_hex8_96cubed_20_step_path", ["--workload", "j2"], None),
+    ("j2_mlp_closure_hex8_96cubed", ["--workload", "j2mlp"], (2, 1)),
+    ("batched_64_hex8_plus_tet4_tet10_hex27", ["--workload", "batched"], (5, 2)),
+    ("matrix_free_action_neohookean_128cubed", ["--workload", "action"], None),
+    ("symbolic_phase_neohookean_128cubed", ["--workload", "symbolic"], (3, 1)),
+)
+
+
+def sub_results(args) -> dict:
+    out = {}
+    for name, extra, cap in SUB_RESULTS:
+        steps, warmup = (min(args.steps, cap[0]), min(args.warmup, cap[1])) if cap else (args.steps, args.warmup)
+        cmd = [sys.executable, os.path.abspath(__file__), *extra, "--steps", str(steps), "--warmup", str(warmup),
+               "--no-sub-results"]
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+            lines = [ln for ln in r.stdout.strip().splitlines() if ln.startswith("{")]
+            if r.returncode == 0 and lines:
+                out[name] = json.loads(lines[-1])
+            else:
+                out[name] = {"error": f"exit {r.returncode}: {(r.stderr or r.stdout)[-400:]}"}
+        except subprocess.TimeoutExpired:
+            out[name] = {"error": "timed out after 900 s"}
+        out[name]["wall_s"] = round(time.perf_counter() - t0, 1)
+    return out
 
 
 def main() -> None:
@@ -862,6 +931,8 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) measurement")
     ap.add_argument("--n", type=int, default=None, help="elements per box side (default: the workload's size)")
     ap.add_argument("--no-variants", action="store_true", help="skip timing the other precision variant")
+    ap.add_argument("--no-sub-results", action="store_true",
+                    help="default workload only: skip running the other workloads as sub-results")
     ap.add_argument("--single-launch", action="store_true",
                     help="batched FP64: every element block of a system in one persistent launch")
     ap.add_argument("--epochs", type=int, default=60, help="closure training epochs (j2mlp workload)")

@@ -2,6 +2,7 @@
 // context, mesh/physics/DOF set-up, the symbolic phase that builds the CSC
 // pattern and the element -> nzval maps, and the assembly driver.
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
@@ -79,6 +80,7 @@ struct fec_ctx {
   DevBuf d_coords, d_conn, d_ref, d_nadj_ptr, d_nadj, d_epos, d_umask, d_col_base, d_col_len, d_dtu, d_unknown_dofs;
   DevBuf d_Ke, d_Re;
   std::vector<int64_t> ref_off;  // per block offset (doubles) into d_ref
+  std::vector<double> ref_host;  // host copy of d_ref (all blocks' tables)
   // learned closure (FEC_PHYS_J2_MLP): BF16 parameters, normalisation, counters, and the
   // ClosureArgs struct the kernels read
   DevBuf d_cl_w, d_cl_norm, d_cl_cnt, d_cl_args;
@@ -371,9 +373,54 @@ int fec_mesh_set(fec_ctx* c, int dim, int64_t nn, const double* coords, int nblo
   c->blocks = std::move(blocks);
   c->conn = std::move(conn0);
   c->ref_off = std::move(ref_off);
+  c->ref_host = std::move(ref);
   c->n_unknowns = -1;
   c->nf = 0;
   invalidate_pattern(c);
+  return ok(c);
+}
+
+int fec_block_reference_set(fec_ctx* c, int block, int num_q, const double* N, const double* dN, const double* w) {
+  if (!c) return FEC_ERR_ARG;
+  if (block < 1 || block > int(c->blocks.size()))
+    return fail(c, FEC_ERR_ARG, "block %d out of range 1..%d", block, int(c->blocks.size()));
+  const Block& B = c->blocks[block - 1];
+  const int A = B.nnpe, D = fec::elem_dim(B.elem_type), NQ = fec::elem_nq(B.elem_type);
+  if (num_q != NQ)
+    return fail(c, FEC_ERR_UNSUPPORTED,
+                "block %d: the kernels of element type %d are built for %d quadrature points (got %d)", block,
+                B.elem_type, NQ, num_q);
+  if (!N || !dN || !w) return fail(c, FEC_ERR_ARG, "block %d: N, dN and w must not be NULL", block);
+  // RefLayout order: N [q][a], dN [q][a][k], w [q]
+  std::vector<double> t(size_t(NQ) * A * (1 + D) + NQ);
+  std::copy(N, N + size_t(NQ) * A, t.begin());
+  std::copy(dN, dN + size_t(NQ) * A * D, t.begin() + size_t(NQ) * A);
+  std::copy(w, w + NQ, t.begin() + size_t(NQ) * A * (1 + D));
+  for (size_t i = 0; i < t.size(); ++i)
+    if (!std::isfinite(t[i])) return fail(c, FEC_ERR_ARG, "block %d: table entry %zu is not finite", block, i);
+  std::copy(t.begin(), t.end(), c->ref_host.begin() + c->ref_off[block - 1]);
+  if (c->device >= 0) {
+    cudaSetDevice(c->device);
+    // other blocks share the buffer: rewrite only this block's slice (kernels read it in stream order,
+    // so the caller must not change tables while an assembly that uses them is in flight)
+    FEC_CUDA(c, cudaMemcpy(static_cast<double*>(c->d_ref.p) + c->ref_off[block - 1], t.data(),
+                           sizeof(double) * t.size(), cudaMemcpyHostToDevice));
+  }
+  return ok(c);
+}
+
+int fec_block_reference_get(const fec_ctx* cc, int block, int* num_q, double* N, double* dN, double* w) {
+  fec_ctx* c = const_cast<fec_ctx*>(cc);
+  if (!c) return FEC_ERR_ARG;
+  if (block < 1 || block > int(c->blocks.size()))
+    return fail(c, FEC_ERR_ARG, "block %d out of range 1..%d", block, int(c->blocks.size()));
+  const Block& B = c->blocks[block - 1];
+  const int A = B.nnpe, D = fec::elem_dim(B.elem_type), NQ = fec::elem_nq(B.elem_type);
+  if (num_q) *num_q = NQ;
+  const double* t = c->ref_host.data() + c->ref_off[block - 1];
+  if (N) std::copy(t, t + size_t(NQ) * A, N);
+  if (dN) std::copy(t + size_t(NQ) * A, t + size_t(NQ) * A * (1 + D), dN);
+  if (w) std::copy(t + size_t(NQ) * A * (1 + D), t + size_t(NQ) * A * (1 + D) + NQ, w);
   return ok(c);
 }
 
@@ -819,6 +866,8 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
   if (any_state && !state_old) return fail(c, FEC_ERR_ARG, "state_old is NULL for a physics with state");
   cudaSetDevice(c->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int* wait_err = nullptr;
+  FEC_CUDA(c, fec::wait_error_flag(&wait_err));
   if (c->n_timed > 1) c->n_timed = 0;  // keep a preceding fec_update_field timing
   const size_t rsz = precision == FEC_FP64 ? sizeof(double) : sizeof(float);
   int64_t ke_total = 0, re_total = 0;
@@ -854,6 +903,7 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     ea.coords = static_cast<const double*>(c->d_coords.p);
     ea.U = U;
     ea.ref = static_cast<const double*>(c->d_ref.p) + c->ref_off[b];
+    ea.wait_err = wait_err;
     for (int i = 0; i < 8; ++i) ea.props[i] = B.props[i];
     const int ns = num_states_of(B.physics);
     ea.state_old = ns ? state_old + st_off : nullptr;
@@ -980,6 +1030,8 @@ int fec_assemble_action(fec_ctx* c, int precision, double t, double dt, const do
   if (any_state && !state_old) return fail(c, FEC_ERR_ARG, "state_old is NULL for a physics with state");
   cudaSetDevice(c->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int* wait_err = nullptr;
+  FEC_CUDA(c, fec::wait_error_flag(&wait_err));
   c->n_timed = 0;
   const size_t rsz = precision == FEC_FP64 ? sizeof(double) : sizeof(float);
   int64_t re_total = 0;
@@ -1010,6 +1062,7 @@ int fec_assemble_action(fec_ctx* c, int precision, double t, double dt, const do
     ea.coords = static_cast<const double*>(c->d_coords.p);
     ea.U = U;
     ea.ref = static_cast<const double*>(c->d_ref.p) + c->ref_off[b];
+    ea.wait_err = wait_err;
     for (int i = 0; i < 8; ++i) ea.props[i] = B.props[i];
     const int ns = num_states_of(B.physics);
     ea.state_old = ns ? state_old + st_off : nullptr;
@@ -1118,6 +1171,15 @@ int fec_check_finite(fec_ctx* c, const double* R_u, const double* nzval, int64_t
   if (first_bad) *first_bad = h[0] != none ? int64_t(h[0]) : (h[1] != none ? int64_t(h[1]) : -1);
   if (h[0] != none) return fail(c, FEC_ERR_NONFINITE, "residual entry %lld is not finite", (long long)h[0]);
   if (h[1] != none) return fail(c, FEC_ERR_NONFINITE, "nzval entry %lld is not finite", (long long)h[1]);
+  // a bounded wait in an element kernel that gave up leaves outputs that may be wrong however finite they are
+  int* wait_err = nullptr;
+  FEC_CUDA(c, fec::wait_error_flag(&wait_err));
+  int werr = 0;
+  FEC_CUDA(c, cudaMemcpy(&werr, wait_err, sizeof werr, cudaMemcpyDeviceToHost));
+  if (werr)
+    return fail(c, FEC_ERR_DEVICE,
+                "an element kernel gave up a bounded wait (tensor-core MMA or bulk table copy); the outputs are "
+                "invalid until fec_tensor_core_status(1) clears the flag");
   return ok(c);
 }
 
@@ -1290,17 +1352,30 @@ constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mutex;
 void* g_noalloc_addr[kMaxDevices] = {nullptr};
 
-// Device address of g_noalloc_scratch on the current device `dev`, looked up
-// once per device (host code cannot use the symbol itself as a pointer).
-int noalloc_scratch_address(fec_ctx* c, int dev, void** out) {
+// Device address of g_noalloc_scratch on the current device `dev` (host code
+// cannot use the symbol itself as a pointer).  Looked up again on every call
+// made outside stream capture: a reset of the device's primary context
+// (cudaDeviceReset, CUDA.jl's device_reset!) unloads the module, and the array
+// can sit at another address once it is loaded again.  Under capture, where
+// the lookup (which may load the module) is not allowed, the address of the
+// last call on this device is used.
+int noalloc_scratch_address(fec_ctx* c, int dev, cudaStream_t s, void** out) {
   if (dev < 0 || dev >= kMaxDevices) return fail(c, FEC_ERR_ARG, "device %d out of range for the static scratch", dev);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+    cudaGetLastError();  // the failed query is not sticky; reset the runtime's last error
+    cs = cudaStreamCaptureStatusActive;
+  }
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_addr[dev]) {
+  if (cs == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p)
       return fail(c, FEC_ERR_CUDA, "cudaGetSymbolAddress(static scratch): %s", cudaGetErrorString(e));
     g_noalloc_addr[dev] = p;
+  } else if (!g_noalloc_addr[dev]) {
+    return fail(c, FEC_ERR_STATE,
+                "fec_assemble_noalloc: the first call on a device must come before any stream capture");
   }
   *out = g_noalloc_addr[dev];
   return FEC_OK;
@@ -1354,12 +1429,15 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
                 "(FEC_NOALLOC_SCRATCH_BYTES); use fec_assemble for this mesh",
                 need, size_t(FEC_NOALLOC_SCRATCH_BYTES));
   if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, FEC_ERR_CUDA, "cudaSetDevice(%d) failed", c->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
   void* scratch = nullptr;
-  int rc = noalloc_scratch_address(c, c->device, &scratch);
+  int rc = noalloc_scratch_address(c, c->device, s, &scratch);
   if (rc) return rc;
   void* Ke = want_k ? scratch : nullptr;
   void* Re = want_r ? static_cast<char*>(scratch) + re_off_bytes : nullptr;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int* wait_err = nullptr;
+  FEC_CUDA(c, fec::wait_error_flag(&wait_err));
+  c->n_timed = 0;  // no launch of this call is timed: the timing query reports none
   GatherArgs ga;
   memset(&ga, 0, sizeof ga);
   int64_t ke_off = 0, re_off = 0, st_off = 0;
@@ -1373,6 +1451,7 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
     ea.coords = static_cast<const double*>(c->d_coords.p);
     ea.U = U;
     ea.ref = static_cast<const double*>(c->d_ref.p) + c->ref_off[b];
+    ea.wait_err = wait_err;
     for (int i = 0; i < 8; ++i) ea.props[i] = B.props[i];
     const int ns = num_states_of(B.physics);
     ea.state_old = ns ? state_old + st_off : nullptr;

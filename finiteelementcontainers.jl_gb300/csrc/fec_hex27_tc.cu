@@ -296,22 +296,25 @@ bool hex27_on_cuda_cores() {
 }
 
 namespace {
-// set by a hex27 tensor-core kernel whose wait on the tensor cores gave up
-__device__ int g_hex27_tc_error = 0;
+// set by an element kernel whose bounded wait gave up: a hex27 tensor-core
+// kernel waiting on its MMAs, or a hex8 kernel waiting on its bulk table copies
+__device__ int g_wait_error = 0;
 }  // namespace
 
-cudaError_t hex27_tc_error_flag(int** flag) {
+cudaError_t wait_error_flag(int** flag) {
   void* p = nullptr;
-  const cudaError_t e = cudaGetSymbolAddress(&p, g_hex27_tc_error);
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_wait_error);
   *flag = static_cast<int*>(p);
   return e;
 }
 
 cudaError_t launch_hex27_tc(int physics, bool want_r, bool want_k, const ElemArgs& a, cudaStream_t s,
                             int* launches) {
-  int* err = nullptr;
-  cudaError_t e = hex27_tc_error_flag(&err);
-  if (e != cudaSuccess) return e;
+  int* err = a.wait_err;
+  if (!err) {
+    const cudaError_t e = wait_error_flag(&err);
+    if (e != cudaSuccess) return e;
+  }
   if (physics == 2) return h27::launch<NeoHookean>(want_r, want_k, a, err, s, launches);
   if (physics == 3) return h27::launch<J2>(want_r, want_k, a, err, s, launches);
   return cudaErrorNotSupported;
@@ -321,7 +324,7 @@ cudaError_t launch_hex27_tc(int physics, bool want_r, bool want_k, const ElemArg
 
 extern "C" int fec_tensor_core_status(int reset) {
   int* flag = nullptr;
-  if (fec::hex27_tc_error_flag(&flag) != cudaSuccess) return FEC_ERR_CUDA;
+  if (fec::wait_error_flag(&flag) != cudaSuccess) return FEC_ERR_CUDA;
   int h = 0;
   if (cudaMemcpy(&h, flag, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess) return FEC_ERR_CUDA;
   if (reset && cudaMemset(flag, 0, sizeof h) != cudaSuccess) return FEC_ERR_CUDA;

@@ -65,6 +65,7 @@ struct ElemArgs {
   void* Ke;                 // block base, Real[ne][NDOF][NDOF]
   void* Re;                 // block base, Real[ne][NDOF]
   const void* closure;      // learned-closure data (ClosureArgs) for the physics that uses one
+  int* wait_err;            // set to 1 by a bounded wait that gave up (device flag; may be null)
 };
 
 // ---------------------------------------------------------------------------

@@ -37,6 +37,9 @@ cudaError_t launch_action(int physics, int elem_type, int precision, const ElemA
 // Hex27 FP32-element mechanics with the element-stiffness contraction on the
 // tensor cores (physics 2 Neo-Hookean, 3 J2); a wait that gives up sets the
 // flag fec_tensor_core_status reads.
+// Device address of that flag on the current device (an int, nonzero once an
+// element kernel's bounded wait gave up; ElemArgs::wait_err points at it).
+cudaError_t wait_error_flag(int** flag);
 cudaError_t launch_hex27_tc(int physics, bool want_r, bool want_k, const ElemArgs& args, cudaStream_t stream,
                             int* launches);
 // FEC_HEX27_ON_CUDA_CORES=1 keeps hex27 FP32-element blocks on the generic kernel.

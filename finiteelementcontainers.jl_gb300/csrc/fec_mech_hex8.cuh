@@ -26,10 +26,12 @@ namespace fec {
 // Stages the hex8 reference tables (shape-function values and gradients, 264
 // doubles) and the connectivity of the CTA's `nlive` elements into shared
 // memory with bulk (TMA) copies that complete on an mbarrier.  Connectivity of
-// a block that does not start on a 16-byte boundary, or a wait that gives up,
-// falls back to plain loads.  Ends with a barrier.
+// a block that does not start on a 16-byte boundary falls back to plain loads.
+// A wait that gives up (about 1 s of SM clocks) sets *err, waits once more
+// (bounded) so that no copy lands after the CTA has moved on, and then loads
+// with plain loads.  Ends with a barrier.
 __device__ __forceinline__ void stage_hex8_tables(const double* gref, double* s_ref, const int32_t* gconn, int nlive,
-                                                  int* s_conn, uint64_t* bar, int tid, int nthr,
+                                                  int* s_conn, uint64_t* bar, int tid, int nthr, int* err,
                                                   bool allow_bulk = true) {
   constexpr int NREF = RefLayout<1>::SIZE;
   const bool bulk =
@@ -46,7 +48,13 @@ __device__ __forceinline__ void stage_hex8_tables(const double* gref, double* s_
       tc::bulk_g2s(s_ref, gref, NREF * 8, bar);
       tc::bulk_g2s(s_conn, gconn, uint32_t(nlive * 32), bar);
     }
-    done = tc::mbar_wait(bar, 0, 2000000000LL);
+    const bool landed = tc::mbar_wait(bar, 0, 2000000000LL);
+    if (__syncthreads_or(!landed)) {
+      if (tid == 0 && err) atomicExch(err, 1);
+      tc::mbar_wait(bar, 0, 2000000000LL);
+    } else {
+      done = true;
+    }
   }
   if (!done) {
     for (int i = tid; i < NREF; i += nthr) s_ref[i] = gref[i];
@@ -354,7 +362,7 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_rows2_kernel(ElemArgs g) {
   {
     const int64_t left = g.ne - e0;
     stage_hex8_tables(g.ref, s_ref, g.conn + e0 * 8, left < EPB ? int(left) : EPB, s_conn_all,
-                      reinterpret_cast<uint64_t*>(s_conn_all + EPB * 8), tid, nthr);
+                      reinterpret_cast<uint64_t*>(s_conn_all + EPB * 8), tid, nthr, g.wait_err);
   }
   for (int i = tid; i < L::SIZE; i += nthr) s_reff[i] = Real(s_ref[i]);
   if (live) {
@@ -531,7 +539,7 @@ __device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile,
   {
     const int64_t left = g.ne - e0;
     stage_hex8_tables(g.ref, s_ref, g.conn + e0 * 8, left < EPB ? int(left) : EPB, s_conn_all,
-                      reinterpret_cast<uint64_t*>(s_conn_all + EPB * 8), tid, nthr, BULK);
+                      reinterpret_cast<uint64_t*>(s_conn_all + EPB * 8), tid, nthr, g.wait_err, BULK);
   }
   if (live) {
     const int a = tx / 3, d = tx % 3;

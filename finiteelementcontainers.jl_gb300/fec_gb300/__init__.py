@@ -7,6 +7,8 @@ do the element quadrature, the gathers and the deterministic scatter."""
 from .meshes import StructuredMesh, UnstructuredMesh, Mesh, ArgumentError
 from .exodus import ExodusFile, ExodusPostProcessor, read_exodus
 from .spaces import FunctionSpace, ScalarFunction, VectorFunction
+from . import quadrature
+from .quadrature import reference_tables
 from .dofs import DofManager, update_dofs
 from .bcs import DirichletBC, dirichlet_dofs
 from .physics import Poisson, NeoHookean, J2Plasticity, num_fields, num_properties, num_states

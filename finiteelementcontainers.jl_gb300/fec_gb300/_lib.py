@@ -37,6 +37,8 @@ SIGNATURES = {
     "fec_last_error": (C.c_int, [_vp, C.c_char_p, C.c_size_t]),
     "fec_mesh_set": (C.c_int, [_vp, C.c_int, C.c_int64, _vp, C.c_int, _vp, _vp, _vp]),
     "fec_physics_set": (C.c_int, [_vp, C.c_int, C.c_int, _vp, C.c_int]),
+    "fec_block_reference_set": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, _vp]),
+    "fec_block_reference_get": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), _vp, _vp, _vp]),
     "fec_dofs_set": (C.c_int, [_vp, C.c_int, _vp, C.c_int64]),
     "fec_pattern_build": (C.c_int, [_vp, _i64p]),
     "fec_pattern_get": (C.c_int, [_vp, _vp, _vp]),

@@ -90,6 +90,7 @@ class SparseMatrixAssembler:
         types = fs.element_type_ids()
         self._call("fec_mesh_set", fs.num_dimensions, fs.num_nodes, _lib.ptr(coords), len(types), _lib.ptr(types),
                    _lib.ptr(fs.block_num_elems), _lib.ptr(fs.conn_data))
+        self.set_reference_tables()
         self._physics_key = None
         self._push_dofs()
 
@@ -139,6 +140,27 @@ class SparseMatrixAssembler:
             self._call("fec_pattern_get", _lib.ptr(colptr), _lib.ptr(rowval))
             self._csc_host = (colptr, rowval)
         return self._csc_host
+
+    def set_reference_tables(self, tables=None) -> None:
+        """Hands each block's quadrature rule and shape-function tables to the
+        library (fec_block_reference_set): the function space's ReferenceFEs, or
+        `tables`, a list of (N, dN, w) per block."""
+        tables = self.fspace.ref_fes if tables is None else tables
+        for b, (N, dN, w) in enumerate(tables, start=1):
+            N = np.ascontiguousarray(N, dtype=np.float64)
+            dN = np.ascontiguousarray(dN, dtype=np.float64)
+            w = np.ascontiguousarray(w, dtype=np.float64)
+            self._call("fec_block_reference_set", b, int(w.size), _lib.ptr(N), _lib.ptr(dN), _lib.ptr(w))
+
+    def reference_tables(self, block: int):
+        """(N, dN, w) block `block` (1-based) is assembled with (fec_block_reference_get)."""
+        fs = self.fspace
+        nq = C.c_int()
+        self._call("fec_block_reference_get", block, C.byref(nq), None, None, None)
+        nnpe, dim = int(fs.nepes[block - 1]), fs.num_dimensions
+        N = np.empty((nq.value, nnpe)); dN = np.empty((nq.value, nnpe, dim)); w = np.empty(nq.value)
+        self._call("fec_block_reference_get", block, C.byref(nq), _lib.ptr(N), _lib.ptr(dN), _lib.ptr(w))
+        return N, dN, w
 
     def set_single_launch(self, on: bool = True) -> None:
         """Run every element block of an FP64 Neo-Hookean/J2 system (hex8, tet4,

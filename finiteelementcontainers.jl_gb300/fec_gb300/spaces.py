@@ -5,10 +5,12 @@ from __future__ import annotations
 import numpy as np
 
 from .meshes import ELEMENT_IDS, NNPE, Mesh
+from .quadrature import KERNEL_NQ, reference_tables
 
-# default interpolation degree and quadrature per element type (src/FunctionSpaces.jl:1-29);
-# quadrature here: 2-point Gauss-Legendre tensor rule for hex8/quad4, 1/4/27 points for tet4/tet10/hex27
-NUM_QP = {"HEX8": 8, "QUAD4": 4, "TETRA4": 1, "TETRA10": 4, "HEX27": 27}
+# quadrature points per element type on the accelerated path (the point counts
+# the kernels are built for): 2-point tensor rules for hex8/quad4, 3-point for
+# hex27, 1/4 points for tet4/tet10
+NUM_QP = dict(KERNEL_NQ)
 
 
 class FunctionSpace:
@@ -18,9 +20,11 @@ class FunctionSpace:
     (src/Fields.jl:129-160): `conn_data` concatenates each block's NNPE x NE
     column-major matrix, `conn_offsets` are 1-based block offsets."""
 
-    def __init__(self, mesh: Mesh, field_type: str = "H1Field", interp: str = "Lagrange"):
+    def __init__(self, mesh: Mesh, field_type: str = "H1Field", interp: str = "Lagrange", *,
+                 q_type: str = "GaussLegendre", q_degree: int | None = None):
         if field_type != "H1Field" or interp != "Lagrange":
             raise NotImplementedError("only H1Field/Lagrange spaces are on the assembly path")
+        self.q_type, self.q_degree = q_type, q_degree
         self.mesh = mesh
         self.coords = mesh.nodal_coords
         self.block_names = list(mesh.element_block_names)
@@ -34,6 +38,12 @@ class FunctionSpace:
             offs.append(o)
             o += c.size
         self.conn_offsets = np.array(offs, dtype=np.int64)
+        # per block (N, dN, w): the ReferenceFE of each block (src/FunctionSpaces.jl:104-126)
+        self.ref_fes = [reference_tables(t, q_type, q_degree) for t in self.elem_types]
+        for t, (N, _, _) in zip(self.elem_types, self.ref_fes):
+            if N.shape[0] != KERNEL_NQ[t]:
+                raise NotImplementedError(f"{t} with {N.shape[0]} quadrature points: the kernels are built for "
+                                          f"{KERNEL_NQ[t]}")
 
     @property
     def num_dimensions(self) -> int:

@@ -91,6 +91,28 @@ int fec_last_error(const fec_ctx* ctx, char* buf, size_t len);
 int fec_mesh_set(fec_ctx* ctx, int dim, int64_t num_nodes, const double* coords, int num_blocks,
                  const int32_t* elem_types, const int64_t* block_num_elems, const int64_t* conn);
 
+/* Replaces: the block's ReferenceFE (src/FunctionSpaces.jl:104-126) -- its
+ * quadrature rule and the shape-function values and reference-coordinate
+ * gradients at the points, the interpolants _cell_interpolants hands to the
+ * physics (src/assemblers/Assemblers.jl:129-131).  The caller passes the tables
+ * its own ReferenceFE holds, so the assembled values follow the caller's rule
+ * (GaussLobattoLegendre, the reference's default q_type at
+ * src/FunctionSpaces.jl:187, or any other).  Host arrays, row-major:
+ *   N  [num_q][nnpe]       shape-function values at the points
+ *   dN [num_q][nnpe][dim]  their gradients in reference coordinates
+ *   w  [num_q]             quadrature weights
+ * num_q must be the point count the block's kernels are built for (HEX8 8,
+ * QUAD4 4, TET4 1, TET10 4, HEX27 27; FEC_ERR_UNSUPPORTED otherwise).  A block
+ * whose tables are never set uses the library's own: the Gauss-Legendre tensor
+ * rule with 2 points per direction (HEX8, QUAD4) or 3 (HEX27), and the 1- and
+ * 4-point rules of TET4 and TET10.  fec_mesh_set resets every block to those.
+ * Synchronous; do not call it while an assembly of this context is in flight. */
+int fec_block_reference_set(fec_ctx* ctx, int block, int num_q, const double* N, const double* dN,
+                            const double* w);
+/* The tables block `block` currently uses (any output may be NULL; num_q gets
+ * the point count, N/dN/w need room for the sizes above). */
+int fec_block_reference_get(const fec_ctx* ctx, int block, int* num_q, double* N, double* dN, double* w);
+
 /* Per-block physics and properties (the (physics, props) pair that
  * foreach_block hands to _assemble_block!, src/Utils.jl:171-189). */
 int fec_physics_set(fec_ctx* ctx, int block, int physics, const double* props, int num_props);
@@ -180,8 +202,10 @@ int fec_cg_solve(fec_ctx* ctx, const double* nzval_dev, const double* b_dev, dou
 
 /* Scans assembled outputs (either may be NULL) for NaN/Inf: FEC_OK, or
  * FEC_ERR_NONFINITE with the first offending index (residual first, then nzval;
- * -1 if none) and a message naming the array.  Synchronises the stream.  The
- * boundary's non-finite check; the reference does not check. */
+ * -1 if none) and a message naming the array; then FEC_ERR_DEVICE if an element
+ * kernel gave up a bounded wait (the flag of fec_tensor_core_status, not
+ * cleared here).  Synchronises the stream.  The boundary's output check; the
+ * reference does not check. */
 int fec_check_finite(fec_ctx* ctx, const double* R_u_dev, const double* nzval_dev, int64_t* first_bad,
                      void* stream);
 
@@ -192,19 +216,29 @@ int fec_check_finite(fec_ctx* ctx, const double* R_u_dev, const double* nzval_de
  * device memory all goes through their own pool (CUDA.jl's pool, PyTorch's
  * caching allocator), where a private cudaMalloc escapes the pool's accounting
  * and a cudaFree synchronizes the device mid-step, or callers with a device
- * memory budget fixed up front -- call this instead.  Same arguments, same
- * results as fec_assemble; the context still has to be set up (mesh, dofs,
- * pattern) beforehand, and the inputs and outputs are the caller's.
+ * memory budget fixed up front -- call this instead.  Same arguments, and the
+ * same kernels as fec_assemble, so bitwise the same results, with one
+ * exception: hex8 blocks of FEC_PHYS_J2_MLP in FEC_FP32_ELEMENT arithmetic
+ * evaluate the learned closure per point on the CUDA cores here (the
+ * tensor-core closure needs a per-point table the size of the mesh), which is
+ * what fec_assemble does with FEC_CLOSURE_ON_CUDA_CORES=1; their outputs and
+ * closure counters then differ from fec_assemble's tensor-core results within
+ * the closure's own tolerance.  The context still has to be set up (mesh,
+ * dofs, pattern) beforehand, and the inputs and outputs are the caller's.
+ * No launch of this call is timed (fec_kernel_times reports none after it).
  *
  * Its workspace is one static device array of FEC_NOALLOC_SCRATCH_BYTES that
  * every GPU which loads the library holds until the process exits.  Meshes
  * whose element workspace (NE * NDOF^2 element-matrix entries plus NE * NDOF
  * element-residual entries, 8 bytes each in FP64, 4 in FP32) exceeds it are
- * rejected with FEC_ERR_ARG.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress); make that first call before any
- * stream capture.  All calls share the array: calls whose work overlaps on the
- * GPU (different streams, different contexts) race on it.  Nothing in it needs
- * clearing, as every element rewrites its entries before they are read. */
+ * rejected with FEC_ERR_ARG.  Every call made outside stream capture looks up
+ * the array's device address (cudaGetSymbolAddress), so a reset of the
+ * device's primary context in between is harmless; a call under capture uses
+ * the address of the last call on that device, so make the first call on a
+ * device (and the first after a reset) before any stream capture.  All calls
+ * share the array: calls whose work overlaps on the GPU (different streams,
+ * different contexts) race on it.  Nothing in it needs clearing, as every
+ * element rewrites its entries before they are read. */
 #define FEC_NOALLOC_SCRATCH_BYTES (64u << 20)
 int fec_assemble_noalloc(fec_ctx* ctx, int want, int precision, double t, double dt, const double* U_dev,
                          const double* U_old_dev, const double* state_old_dev, double* state_new_dev,
@@ -281,9 +315,12 @@ int fec_df64_split_check(const double* x_dev, int64_t n, float* split_dev, doubl
  * outside CUDA-graph capture; FEC_AUTOTUNE=0 keeps the defaults.  No
  * counterpart in the reference. */
 int fec_autotune_report(char* buf, size_t len);
-/* FEC_OK, or FEC_ERR_DEVICE if a tensor-core element kernel (hex27
- * FP32-element) on the current device gave up waiting for its MMAs (its
- * results are then invalid); reset clears the flag.  Synchronous.  No
+/* FEC_OK, or FEC_ERR_DEVICE if an element kernel on the current device gave
+ * up a bounded wait -- a tensor-core kernel (hex27 FP32-element) waiting for
+ * its MMAs, or a hex8 kernel waiting for the bulk copy of its reference tables
+ * and connectivity (it then falls back to plain loads) -- since the flag was
+ * last cleared; the results of that call are then not to be trusted.  reset
+ * clears the flag.  fec_check_finite reports the same flag.  Synchronous.  No
  * counterpart in the reference. */
 int fec_tensor_core_status(int reset);
 int fec_sizes(const fec_ctx* ctx, int64_t* num_nodes, int64_t* num_elems, int64_t* num_unknowns, int64_t* nnz,

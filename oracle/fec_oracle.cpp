@@ -385,6 +385,21 @@ RefFE make_ref(int et) {
   return r;
 }
 
+// Caller-supplied tables (the ReferenceFE a caller builds with its own
+// quadrature rule, src/FunctionSpaces.jl:104-126), set by orc_set_reference;
+// otherwise the element type's default tables above.  Not for concurrent use
+// with a change of tables.
+RefFE g_override[9];
+bool g_has_override[9] = {false};
+
+const RefFE& ref_of(int et) {
+  static thread_local RefFE defaults[9];
+  if (et < 1 || et > 8) return defaults[0];
+  if (g_has_override[et]) return g_override[et];
+  if (defaults[et].nnpe == 0) defaults[et] = make_ref(et);
+  return defaults[et];
+}
+
 struct Mapped {
   double JxW;
   double Xq[3];
@@ -563,10 +578,8 @@ extern "C" {
 // Ke[r + NDOF*c] = dR_r / du_c.  Either output may be null.
 int orc_element(int et, int phys, const double* props, const double* xel, const double* uel,
                 const double* st_old, double* st_new, double* Re, double* Ke) {
-  static thread_local RefFE cache[9];
   if (et < 1 || et > 8) return -1;
-  RefFE& r = cache[et];
-  if (r.nnpe == 0) r = make_ref(et);
+  const RefFE& r = ref_of(et);
   if (r.nnpe == 0) return -1;
   const int D = r.dim, A = r.nnpe;
   const int NF = phys == PHYS_POISSON ? 1 : 3;
@@ -653,7 +666,7 @@ int orc_assemble(int nblocks, const int* elem_types, const i64* ne, const i64* c
   i64 coff = 0, koff = 0, soff = 0;
   int err = 0;
   for (int b = 0; b < nblocks; ++b) {
-    RefFE r = make_ref(elem_types[b]);
+    const RefFE& r = ref_of(elem_types[b]);
     if (r.nnpe == 0 || r.dim != dim) return -1;
     const int A = r.nnpe, NDOF = NF * A;
     const i64 NEb = ne[b];
@@ -698,7 +711,30 @@ int orc_assemble(int nblocks, const int* elem_types, const i64* ne, const i64* c
 }
 
 // Quadrature-point count of an element type (0 if unknown).
-int orc_num_qp(int et) { return make_ref(et).nq; }
+int orc_num_qp(int et) { return ref_of(et).nq; }
+
+// Installs caller tables for element type et (N [nq][nnpe], dN [nq][nnpe][dim],
+// w [nq]); nq may be 1..27.  orc_clear_reference(et) restores the
+// defaults.  Returns 0 or -1 for an unknown element type.
+int orc_set_reference(int et, int nq, const double* N, const double* dN, const double* w) {
+  if (et < 1 || et > 8 || nq <= 0 || nq > 27) return -1;
+  const RefFE d = make_ref(et);
+  if (d.nnpe == 0) return -1;
+  RefFE r;
+  r.dim = d.dim;
+  r.nnpe = d.nnpe;
+  r.nq = nq;
+  r.N.assign(N, N + size_t(nq) * d.nnpe);
+  r.dN.assign(dN, dN + size_t(nq) * d.nnpe * d.dim);
+  r.w.assign(w, w + nq);
+  g_override[et] = r;
+  g_has_override[et] = true;
+  return 0;
+}
+
+void orc_clear_reference(int et) {
+  if (et >= 1 && et <= 8) g_has_override[et] = false;
+}
 
 // Neo-Hookean P and A at one deformation gradient (F row-major [i][J]).
 void orc_neohookean_PA(const double* F9, double Kb, double Gs, double* P9, double* A81) {

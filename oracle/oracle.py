@@ -50,6 +50,8 @@ def lib():
             "orc_neohookean_PA": (None, [vp, C.c_double, C.c_double, vp, vp]),
             "orc_j2_update": (None, [vp, vp, vp, vp, vp, vp]),
             "orc_max_threads": (C.c_int, []),
+            "orc_set_reference": (C.c_int, [C.c_int, C.c_int, vp, vp, vp]),
+            "orc_clear_reference": (None, [C.c_int]),
         }
         for k, (r, a) in sig.items():
             f = getattr(_lib, k)
@@ -190,6 +192,29 @@ def j2_update(gradu, props, st_old):
     pr = np.ascontiguousarray(props, dtype=np.float64)
     lib().orc_j2_update(_p(g), _p(pr), _p(so), _p(sn), _p(P), _p(A))
     return P, A, sn
+
+
+class reference_tables:
+    """with reference_tables("HEX8", N, dN, w): the oracle integrates that element
+    type with the caller's tables (a ReferenceFE built with another quadrature
+    rule, src/FunctionSpaces.jl:104-126) inside the block."""
+
+    def __init__(self, elem: str, N, dN, w):
+        self.et = ELEM[elem]
+        self.N = np.ascontiguousarray(N, dtype=np.float64)
+        self.dN = np.ascontiguousarray(dN, dtype=np.float64)
+        self.w = np.ascontiguousarray(w, dtype=np.float64)
+
+    def __enter__(self):
+        if lib().orc_set_reference(self.et, int(self.w.size), _p(self.N), _p(self.dN), _p(self.w)):
+            raise ValueError("orc_set_reference rejected the tables")
+        NQ[self.et] = int(self.w.size)
+        return self
+
+    def __exit__(self, *exc):
+        lib().orc_clear_reference(self.et)
+        NQ[self.et] = {1: 8, 2: 4, 6: 1, 7: 4, 8: 27}[self.et]
+        return False
 
 
 def max_threads() -> int:

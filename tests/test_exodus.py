@@ -8,7 +8,8 @@ import numpy as np
 import pytest
 
 GOLD = Path(__file__).resolve().parent / "golden"
-REF = Path(os.environ.get("FEC_REFERENCE_DIR", "/root/reference"))
+# the reference checkout, when FEC_REFERENCE_DIR names one (its files are read only by the test below)
+REF = Path(os.environ["FEC_REFERENCE_DIR"]) if os.environ.get("FEC_REFERENCE_DIR") else None
 
 
 def test_round_trip_mesh_sets_and_fields(fec, tmp_path):
@@ -41,6 +42,8 @@ def test_round_trip_mesh_sets_and_fields(fec, tmp_path):
 
 
 def _ref(rel: str) -> Path:
+    if REF is None:
+        pytest.skip("FEC_REFERENCE_DIR does not name a reference checkout")
     p = REF / rel
     if not p.exists():
         pytest.skip("reference checkout not present")
