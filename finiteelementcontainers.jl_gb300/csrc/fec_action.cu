@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(EPB * Elem<ET>::NQ) action_kernel(ElemArgs g, 
     if (ee >= g.ne) continue;
     Real sum = 0;
     for (int qq = 0; qq < NQ; ++qq) sum += s_kq[(le * NQ + qq) * NDOF + c];
-    static_cast<typename WS<Real>::T*>(g.Re)[ee * NDOF + c] = WS<Real>::from(sum);
+    static_cast<Real*>(g.Re)[ee * NDOF + c] = sum;
   }
 }
 

@@ -80,6 +80,19 @@ int elem_nnpe(int et) {
   switch (et) { case 1: return 8; case 2: return 4; case 6: return 4; case 7: return 10; case 8: return 27; }
   return 0;
 }
+int num_sms() {
+  static int count[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+  if (!count[dev]) cudaDeviceGetAttribute(&count[dev], cudaDevAttrMultiProcessorCount, dev);
+  return count[dev] > 0 ? count[dev] : 148;
+}
+
+bool hex8_df64_tile_kernel() {
+  const char* v = std::getenv("FEC_HEX8_DF64");
+  return v && v[0] == 't';
+}
+
 int elem_dim(int et) {
   switch (et) { case 1: case 6: case 7: case 8: return 3; case 2: return 2; }
   return 0;

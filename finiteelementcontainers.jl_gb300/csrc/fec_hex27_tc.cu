@@ -173,12 +173,14 @@ __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err)
     for (int c = 0; c < NCHUNK; ++c) {
       const int buf = c & 1;
       if (c >= 2) {
+        // the phase flips only when every thread saw it complete, so that after a
+        // timeout ph[] still names the phases whose MMAs may be in flight
         const bool ok = mbar_wait(&bar[buf], ph[buf], WAIT_BUDGET);
-        ph[buf] ^= 1u;
         if (__syncthreads_or(!ok)) {
           failed = true;
           break;
         }
+        ph[buf] ^= 1u;
       }
       if (row < 3 * ND) {
         float v[8];
@@ -222,14 +224,14 @@ __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err)
     if (failed) break;
     // the last two chunks' barriers (chunk 12 on buffer 0, chunk 13 on buffer 1)
     {
-      bool ok = mbar_wait(&bar[0], ph[0], WAIT_BUDGET);
-      ph[0] ^= 1u;
-      ok = mbar_wait(&bar[1], ph[1], WAIT_BUDGET) && ok;
-      ph[1] ^= 1u;
-      if (__syncthreads_or(!ok)) {
+      const bool ok0 = mbar_wait(&bar[0], ph[0], WAIT_BUDGET);
+      const bool ok1 = mbar_wait(&bar[1], ph[1], WAIT_BUDGET);
+      if (__syncthreads_or(!(ok0 && ok1))) {
         failed = true;
         break;
       }
+      ph[0] ^= 1u;
+      ph[1] ^= 1u;
     }
     tc_fence_after();
     // ---- read D back: warp w holds rows 128 (w / 4) + 32 (w % 4) + lane ----
@@ -249,6 +251,8 @@ __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err)
     __syncthreads();
   }
   if (failed) {
+    // one more bounded wait on each barrier's pending phase (a phase that already
+    // completed returns at once), so that no MMA is left writing TMEM below
     if (tid == 0) atomicExch(err, 1);
     mbar_wait(&bar[0], ph[0], WAIT_BUDGET);
     mbar_wait(&bar[1], ph[1], WAIT_BUDGET);

@@ -85,6 +85,13 @@ template <> struct WS<float> {
   using T = float;
   __device__ static T from(float v) { return v; }
 };
+// Element residuals are stored in the arithmetic's own type: double in the FP64
+// variant (formed in native FP64 and summed in FP64 by the node gather, so the
+// residual keeps FP64 accuracy), float in the FP32-element variant.  RE<W> maps
+// the gather's matrix-entry type to it.
+template <typename W> struct RE;
+template <> struct RE<float2> { using T = double; };
+template <> struct RE<float> { using T = float; };
 
 // ---------------------------------------------------------------------------
 // small helpers
@@ -309,7 +316,7 @@ __global__ void __launch_bounds__(EPB * Elem<ET>::NNPE) poisson_element_kernel(E
 #pragma unroll
     for (int b = 0; b < A; ++b) Ke[b] = WS<Real>::from(Krow[b]);
   }
-  if (WANT_R) static_cast<typename WS<Real>::T*>(g.Re)[e * A + a] = WS<Real>::from(R);
+  if (WANT_R) static_cast<Real*>(g.Re)[e * A + a] = R;
 }
 
 // ---------------------------------------------------------------------------
@@ -735,7 +742,7 @@ __device__ __forceinline__ void mech_element_tile(const ElemArgs& g, unsigned ti
         const double* P = s_P + q * 9 + i * 3;
         R = fma(dNX[a * 3], P[0], fma(dNX[a * 3 + 1], P[1], fma(dNX[a * 3 + 2], P[2], R)));
       }
-      static_cast<float2*>(g.Re)[e * NDOF + r] = df64_split(R);
+      static_cast<double*>(g.Re)[e * NDOF + r] = R;
     }
   } else {
   Real Krow[CW * 3];
@@ -772,7 +779,7 @@ __device__ __forceinline__ void mech_element_tile(const ElemArgs& g, unsigned ti
     for (int c = 0; c < CW * 3; ++c)
       if (b0 * 3 + c < NDOF) Ke[c] = WS<Real>::from(Krow[c]);
   }
-  if (WANT_R && cs == 0) static_cast<typename WS<Real>::T*>(g.Re)[e * NDOF + r] = WS<Real>::from(R);
+  if (WANT_R && cs == 0) static_cast<Real*>(g.Re)[e * NDOF + r] = R;
   }
 }
 
@@ -906,14 +913,15 @@ struct GatherAcc {
 // flight per lane instead of a dependent load chain per element.
 template <typename Real, int NF, int A, int BUDGET>
 __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo& B, int64_t p, int64_t pend, unsigned um,
-                                           bool fast, int Ln, float* acc, float2& racc, int lane, bool wantK,
+                                           bool fast, int Ln, float* acc, double& racc, int lane, bool wantK,
                                            bool wantR) {
   constexpr int NDOF = NF * A;
   constexpr int TOTAL = NF * NDOF;                         // values of one element's rows for this node
   constexpr int VPL = (TOTAL + 31) / 32;                   // values per lane per element
   constexpr int CH = VPL >= BUDGET ? 1 : (BUDGET / VPL > 8 ? 8 : BUDGET / VPL);
+  using RT = typename RE<Real>::T;
   const Real* Ke = static_cast<const Real*>(g.Ke) + B.ke_off;
-  const Real* Re = static_cast<const Real*>(g.Re) + B.re_off;
+  const RT* Re = static_cast<const RT*>(g.Re) + B.re_off;
   for (; p < pend; p += 32) {
     const int64_t left32 = pend - p;
     const int n32 = left32 < 32 ? int(left32) : 32;
@@ -922,11 +930,11 @@ __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo&
       const int nh = (n32 - c0) < CH ? (n32 - c0) : CH;
       Real v[CH][VPL];
       int pos[CH][VPL];
-      Real rv[CH];
+      RT rv[CH];
 #pragma unroll
       for (int c = 0; c < CH; ++c) {
         const uint32_t packed = __shfl_sync(0xffffffffu, mine, (c0 + c) & 31);
-        rv[c] = Real{};
+        rv[c] = RT(0);
 #pragma unroll
         for (int j = 0; j < VPL; ++j) pos[c][j] = -1;
         if (c < nh) {
@@ -959,7 +967,7 @@ __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo&
 #pragma unroll
       for (int c = 0; c < CH; ++c) {
         if (c < nh) {
-          racc = GatherAcc::plus(racc, rv[c]);
+          racc += double(rv[c]);
           if (wantK) {
             // one element's values of this lane go to distinct positions: loads,
             // additions and stores are batched
@@ -983,17 +991,18 @@ __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo&
 // blocks have different element sizes).
 template <typename Real, int NF>
 __device__ __forceinline__ void gather_run_generic(const GatherArgs& g, const BlockInfo& B, int64_t p, int64_t pend,
-                                                   unsigned um, bool fast, int Ln, float* acc, float2& racc, int lane,
+                                                   unsigned um, bool fast, int Ln, float* acc, double& racc, int lane,
                                                    bool wantK, bool wantR) {
+  using RT = typename RE<Real>::T;
   const int A = B.nnpe, NDOF = B.ndof;
   const bool node_rows = B.layout == KE_NODE_ROWS;
   const Real* Ke = static_cast<const Real*>(g.Ke) + B.ke_off;
-  const Real* Re = static_cast<const Real*>(g.Re) + B.re_off;
+  const RT* Re = static_cast<const RT*>(g.Re) + B.re_off;
   for (; p < pend; ++p) {
     const uint32_t packed = g.nadj[p];
     const int64_t le = int64_t(packed >> 5) - B.elem_start;
     const int a = int(packed & 31u);
-    if (wantR) racc = GatherAcc::plus(racc, Re[le * NDOF + a * NF + lane]);
+    if (wantR) racc += double(Re[le * NDOF + a * NF + lane]);
     if (wantK) {
       const Real* Krows = Ke + (le * NDOF + int64_t(a) * NF) * NDOF;
       const uint16_t* ep = g.epos + B.epos_off + (le * A + a) * A;
@@ -1034,11 +1043,12 @@ struct alignas(32) F2x4 {
 // value.
 template <typename Real>
 __device__ __forceinline__ void gather_run_hex8v(const GatherArgs& g, const BlockInfo& B, int64_t p, int64_t pend,
-                                                 int Ln, float* acc, float2& racc, int lane, bool wantK, bool wantR) {
+                                                 int Ln, float* acc, double& racc, int lane, bool wantK, bool wantR) {
   constexpr int CH = sizeof(Real) == 8 ? 4 : 6;
   using V4 = typename std::conditional<sizeof(Real) == 4, float4, F2x4>::type;
+  using RT = typename RE<Real>::T;
   const Real* Ke = static_cast<const Real*>(g.Ke) + B.ke_off;
-  const Real* Re = static_cast<const Real*>(g.Re) + B.re_off;
+  const RT* Re = static_cast<const RT*>(g.Re) + B.re_off;
   const bool kl = lane < 18;
   const int ki = lane >> 1, bh = lane & 1;
   const int base = (ki / 3) * Ln + (ki % 3);
@@ -1050,11 +1060,11 @@ __device__ __forceinline__ void gather_run_hex8v(const GatherArgs& g, const Bloc
       const int nh = (n32 - c0) < CH ? (n32 - c0) : CH;
       V4 v[CH];
       uint2 ep[CH];
-      Real rv[CH];
+      RT rv[CH];
 #pragma unroll
       for (int c = 0; c < CH; ++c) {
         const uint32_t packed = __shfl_sync(0xffffffffu, mine, (c0 + c) & 31);
-        rv[c] = Real{};
+        rv[c] = RT(0);
         if (c < nh) {
           const uint32_t le = (packed >> 5) - uint32_t(B.elem_start);
           const uint32_t a = packed & 31u;
@@ -1070,7 +1080,7 @@ __device__ __forceinline__ void gather_run_hex8v(const GatherArgs& g, const Bloc
 #pragma unroll
       for (int c = 0; c < CH; ++c) {
         if (c < nh) {
-          racc = GatherAcc::plus(racc, rv[c]);
+          racc += double(rv[c]);
           if (wantK) {
             if (kl) {
               // the four columns of one element go to four distinct positions, so
@@ -1115,7 +1125,7 @@ __global__ void __launch_bounds__(WPB * 32, MINB) node_gather_kernel(GatherArgs 
   const bool wantR = g.R_u != nullptr && lane < NF && ((um >> lane) & 1u);
   if (wantK)
     for (int j = lane; j < ncols * Ln; j += 32) GatherAcc::zero(acc, j);
-  float2 racc = make_float2(0.f, 0.f);
+  double racc = 0.0;  // the residual is summed in FP64, in increasing element order
   __syncwarp();
   int64_t p = g.nadj_ptr[n];
   const int64_t p1 = g.nadj_ptr[n + 1];
@@ -1147,7 +1157,7 @@ __global__ void __launch_bounds__(WPB * 32, MINB) node_gather_kernel(GatherArgs 
     double* out = g.nzval + g.col_base[n];
     for (int j = lane; j < ncols * Ln; j += 32) out[j] = GatherAcc::value(acc, j);
   }
-  if (wantR) g.R_u[g.dof_to_unknown[n * NF + lane]] = GatherAcc::value(racc);
+  if (wantR) g.R_u[g.dof_to_unknown[n * NF + lane]] = racc;
 }
 
 }  // namespace fec

@@ -53,6 +53,12 @@ bool mixed_launch_supported(int physics, int nblocks, const int* elem_types);
 cudaError_t launch_mech_mixed(int physics, int nblocks, const int* elem_types, const ElemArgs* args, bool want_r,
                               bool want_k, unsigned* tile_counter, cudaStream_t stream, int* launches);
 
+// Streaming multiprocessors of the current device (cached per device).
+int num_sms();
+// FEC_HEX8_DF64=tile selects the one-tile-per-CTA FP64 hex8 kernel instead of
+// the warp-specialised persistent one.
+bool hex8_df64_tile_kernel();
+
 // Reference-element tables (RefLayout order) for an element type, in double.
 // Returns the number of doubles written (0 for an unknown type).
 int ref_tables(int elem_type, double* out, int cap);

@@ -8,7 +8,9 @@
 // diagonal block), so the 351 off-diagonal node blocks are formed once and
 // written to both triangles.  Each thread keeps 21 double-float accumulators.
 // The per-point map streams each node's spatial gradient into shared memory
-// as it is formed (the 81 gradients of a point are never live together).
+// as it is formed (the 81 gradients of a point are never live together), as a
+// double-float for the contraction and in FP64 for the residual, which is
+// formed in native FP64.
 #pragma once
 #include "fec_kernels.cuh"
 #include "fec_mech_hex8.cuh"
@@ -19,8 +21,10 @@ template <class Model>
 struct Hex27Df64Smem {
   static constexpr int NQ = 27, A = 27, SCR2 = Model::SCR2;
   static constexpr int D_DN = 0, D_W = D_DN + NQ * A * 3, D_X = D_W + NQ, D_U = D_X + A * 3;
-  static constexpr int N_DOUBLE = D_U + A * 3;  // even
-  static constexpr int F_DNX = 0, F_P = F_DNX + NQ * A * 3, F_SCR = F_P + NQ * 9, F_A = F_SCR + NQ * SCR2;
+  // FP64 spatial gradients and JxW P of every point, read by the FP64 residual rows
+  static constexpr int D_DNX = D_U + A * 3, D_P = D_DNX + NQ * A * 3;
+  static constexpr int N_DOUBLE = D_P + NQ * 9;  // even
+  static constexpr int F_DNX = 0, F_SCR = F_DNX + NQ * A * 3, F_A = F_SCR + NQ * SCR2;
   static constexpr int N_F2 = F_A + NQ * 45;
   static constexpr size_t BYTES = sizeof(double) * N_DOUBLE + sizeof(float2) * N_F2 + sizeof(int) * 32;
   static_assert(N_DOUBLE % 2 == 0, "float2 region alignment");
@@ -41,9 +45,10 @@ __device__ __forceinline__ void hex27_df64_tile(const ElemArgs& g, unsigned elem
   double* s_w = dbase + S::D_W;
   double* s_x = dbase + S::D_X;
   double* s_u = dbase + S::D_U;
+  double* s_dNX64 = dbase + S::D_DNX;
+  double* s_P64 = dbase + S::D_P;
   float2* fb = reinterpret_cast<float2*>(dbase + S::N_DOUBLE);
   float2* s_dNX = fb + S::F_DNX;
-  float2* s_P = fb + S::F_P;
   float2* s_scr = fb + S::F_SCR;
   float2* s_A = fb + S::F_A;
   int* s_conn = reinterpret_cast<int*>(fb + S::N_F2);
@@ -93,6 +98,7 @@ __device__ __forceinline__ void hex27_df64_tile(const ElemArgs& g, unsigned elem
         for (int k = 0; k < 3; ++k) s = fma(dN[a * 3 + k], Ji[k][d], s);
         gx[d] = s;
         pdNX[a * 3 + d] = df64_split(s);
+        if (WANT_R) s_dNX64[(q * A + a) * 3 + d] = s;
       }
 #pragma unroll
       for (int i = 0; i < 3; ++i)
@@ -104,8 +110,9 @@ __device__ __forceinline__ void hex27_df64_tile(const ElemArgs& g, unsigned elem
     double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
     double P9[9], scr[SCR];
     Model::point(g.props, gu, jxw, so, sn, P9, scr);
+    if (WANT_R)
 #pragma unroll
-    for (int m = 0; m < 9; ++m) s_P[q * 9 + m] = df64_split(P9[m]);
+      for (int m = 0; m < 9; ++m) s_P64[q * 9 + m] = P9[m];
     Model::split_scratch(scr, s_scr + q * SCR2);
   }
   __syncthreads();
@@ -122,18 +129,22 @@ __device__ __forceinline__ void hex27_df64_tile(const ElemArgs& g, unsigned elem
   const int r = tid >> 1, cs = tid & 1;
   const int a = r / 3, i = r % 3;
   const float2 z = make_float2(0.f, 0.f);
+  if (WANT_R && cs == 0) {  // residual row (a, i) in native FP64, points in order
+    double R = 0.0;
+    for (int q = 0; q < NQ; ++q) {
+      const double* gx = s_dNX64 + (q * A + a) * 3;
+      const double* P = s_P64 + q * 9 + i * 3;
+      R = fma(gx[0], P[0], fma(gx[1], P[1], fma(gx[2], P[2], R)));
+    }
+    static_cast<double*>(g.Re)[e * NDOF + r] = R;
+  }
   float2 K[21];
 #pragma unroll
   for (int c = 0; c < 21; ++c) K[c] = z;
-  float2 R = z;
 #pragma unroll 1
   for (int q = 0; q < NQ; ++q) {
     const float2* dNX = s_dNX + q * A * 3;
     const float2 g0 = dNX[a * 3], g1 = dNX[a * 3 + 1], g2 = dNX[a * 3 + 2];
-    if (WANT_R && cs == 0) {
-      const float2* P = s_P + q * 9 + i * 3;
-      R = df64_dot3_acc(R, g0, P[0], g1, P[1], g2, P[2]);
-    }
     if (WANT_K) {
       const float2* Aq = s_A + q * 45;
       float2 t[9];
@@ -152,7 +163,6 @@ __device__ __forceinline__ void hex27_df64_tile(const ElemArgs& g, unsigned elem
       }
     }
   }
-  if (WANT_R && cs == 0) static_cast<float2*>(g.Re)[e * NDOF + r] = R;
   if (WANT_K) {
     float2* Ke = static_cast<float2*>(g.Ke) + e * (NDOF * NDOF);
 #pragma unroll

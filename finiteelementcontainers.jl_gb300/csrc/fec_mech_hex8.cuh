@@ -294,9 +294,9 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_sym_kernel(ElemArgs g) {
     }
   }
   if (WANT_R && live) {
-    typename WS<Real>::T* Re = static_cast<typename WS<Real>::T*>(g.Re) + e * 24;
-    Re[a1 * 3 + i] = WS<Real>::from(R1);
-    Re[a2 * 3 + i] = WS<Real>::from(R2);
+    Real* Re = static_cast<Real*>(g.Re) + e * 24;
+    Re[a1 * 3 + i] = R1;
+    Re[a2 * 3 + i] = R2;
   }
   if (WANT_K) {
     __syncthreads();
@@ -480,6 +480,41 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_rows2_kernel(ElemArgs g) {
   }
 }
 
+// Element residual of a hex8 element in native FP64, from its 8 point threads:
+// 8 consecutive lanes (q = lane & 7) holding their point's spatial gradients
+// dNX[a][J] and JxW P[i][J].  Each lane forms its point's 24 terms
+// R_q[a][i] = sum_J dNX[a][J] P[i][J]; a reduce-scatter over the 8 lanes
+// (partners lane ^ 4, ^ 2, ^ 1; each pair sum taken with the lower lane's
+// operand first, so every value is summed in one fixed order) leaves lane q
+// with R_e[3q .. 3q+2], which it writes to Re_e.  `mask` holds the 8 lanes.
+__device__ __forceinline__ void hex8_residual_fp64(const double* dNX, const double* P9, int q, unsigned mask,
+                                                   double* Re_e) {
+  double v[24];
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      v[a * 3 + i] = fma(dNX[a * 3], P9[i * 3], fma(dNX[a * 3 + 1], P9[i * 3 + 1], dNX[a * 3 + 2] * P9[i * 3 + 2]));
+  const bool b2 = (q & 4) != 0, b1 = (q & 2) != 0, b0 = (q & 1) != 0;
+  double w12[12];
+#pragma unroll
+  for (int m = 0; m < 12; ++m) {
+    const double recv = __shfl_xor_sync(mask, b2 ? v[m] : v[12 + m], 4);
+    w12[m] = b2 ? recv + v[12 + m] : v[m] + recv;
+  }
+  double w6[6];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const double recv = __shfl_xor_sync(mask, b1 ? w12[m] : w12[6 + m], 2);
+    w6[m] = b1 ? recv + w12[6 + m] : w12[m] + recv;
+  }
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    const double recv = __shfl_xor_sync(mask, b0 ? w6[m] : w6[3 + m], 1);
+    Re_e[3 * q + m] = b0 ? recv + w6[3 + m] : w6[m] + recv;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // FP64 variant with the contraction on the FP32 pipes.  Kinematics and the
 // constitutive update stay in FP64; the shape-function gradients, the stress and
@@ -494,8 +529,7 @@ struct Hex8Df64Smem {
   static constexpr int D_REF = 0, D_X = REF, D_U = D_X + EPB * 24;
   static constexpr int N_DOUBLE = D_U + EPB * 24;
   static constexpr int F_DNX = 0;                       // float2 entries, after the doubles
-  static constexpr int F_P = F_DNX + EPB * NQ * 24;
-  static constexpr int F_SCR = F_P + EPB * NQ * 9;
+  static constexpr int F_SCR = F_DNX + EPB * NQ * 24;
   static constexpr int F_A = (F_SCR + EPB * NQ * SCR2 + 1) & ~1;  // 45 unique tangent entries per point
   static constexpr int A_STRIDE = NQ * 45;
   static constexpr int K_STRIDE = 576;                  // K staging per element, over the whole float2 region
@@ -531,7 +565,6 @@ __device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile,
   double* s_x = dbase + S::D_X + ty * 24;
   double* s_u = dbase + S::D_U + ty * 24;
   const float2* s_dNX = fb + S::F_DNX + ty * NQ * 24;
-  const float2* s_P = fb + S::F_P + ty * NQ * 9;
   const float2* s_scr = fb + S::F_SCR + ty * NQ * SCR2;
   float2* s_A = fb + S::F_A + ty * S::A_STRIDE;
   int* s_conn = s_conn_all + ty * 8;
@@ -550,7 +583,7 @@ __device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile,
   if (tid < EPB * NQ) {  // per-point map and constitutive update, native FP64, full warps
     const int el = tid / NQ, q = tid % NQ;
     const int64_t ep = e0 + el;
-    if (ep < g.ne) {
+    if (ep < g.ne) {  // uniform over the element's 8 lanes
       const double* px = dbase + S::D_X + el * 24;
       const double* pu = dbase + S::D_U + el * 24;
       double dNX[24];
@@ -567,15 +600,14 @@ __device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile,
         }
       float2* pdNX = fb + S::F_DNX + el * NQ * 24;
 #pragma unroll
-      for (int m = 0; m < 24; ++m) pdNX[q * 24 + m] = df64_split(dNX[m]);  // dNX dies before the model
+      for (int m = 0; m < 24; ++m) pdNX[q * 24 + m] = df64_split(dNX[m]);
       const double* so = NS ? g.state_old + (ep * NQ + q) * NS : nullptr;
       double* sn = (NS && g.state_new) ? g.state_new + (ep * NQ + q) * NS : nullptr;
       double P9[9], scr[SCR];
       Model::point(g.props, gu, jxw, so, sn, P9, scr);
-      float2* pP = fb + S::F_P + el * NQ * 9;
+      if (WANT_R)
+        hex8_residual_fp64(dNX, P9, q, 0xffu << ((tid & 31) & ~7), static_cast<double*>(g.Re) + ep * 24);
       float2* pscr = fb + S::F_SCR + el * NQ * SCR2;
-#pragma unroll
-      for (int m = 0; m < 9; ++m) pP[q * 9 + m] = df64_split(P9[m]);
       Model::split_scratch(scr, pscr + q * SCR2);
     }
   }
@@ -597,17 +629,12 @@ __device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile,
   float2 K[15];
 #pragma unroll
   for (int c = 0; c < 15; ++c) K[c] = z;
-  float2 R = z;
-  if (live) {
+  if (WANT_K && live) {
 #pragma unroll 1
     for (int q = 0; q < NQ; ++q) {
       const float2* dNX = s_dNX + q * 24;
       const float2 g0 = dNX[a * 3], g1 = dNX[a * 3 + 1], g2 = dNX[a * 3 + 2];
-      if (WANT_R) {
-        const float2* P = s_P + q * 9 + i * 3;
-        R = df64_dot3_acc(R, g0, P[0], g1, P[1], g2, P[2]);
-      }
-      if (WANT_K) {
+      {
         const float2* Aq = s_A + q * 45;
         float2 t[9];
 #pragma unroll
@@ -640,7 +667,6 @@ __device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile,
       }
     }
   }
-  if (WANT_R && live) static_cast<float2*>(g.Re)[e * 24 + tx] = R;
   if (WANT_K) {
     __syncthreads();
     constexpr int PER = 576 / 2;
@@ -659,6 +685,194 @@ template <class Model, int EPB, bool WANT_R, bool WANT_K>
 __global__ void __launch_bounds__(EPB * 24, 4) mech_hex8_df64_kernel(ElemArgs g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   hex8_df64_tile<Model, EPB, WANT_R, WANT_K>(g, blockIdx.x, threadIdx.x, threadIdx.y, smem_raw);
+}
+
+// ---------------------------------------------------------------------------
+// Warp-specialised, persistent form of the FP64 hex8 kernel (the default).
+//
+// The per-point phase (isoparametric map, constitutive update, the element
+// residual and the 45 unique tangent entries, native FP64 plus double-float
+// splits) and the
+// double-float contraction of K_e run on different warps of one CTA and on
+// different tiles of 16 elements at a time: while 12 consumer warps contract
+// tile t, 4 producer warps (one per SM sub-partition, so that every FP64 unit
+// of the SM carries a share of the point phase) prepare tile t+1 in the other
+// half of a double-buffered shared-memory stage.  One CTA per SM takes the
+// tiles blockIdx.x, blockIdx.x + gridDim.x, ...  The hand-over uses named
+// barriers: FULL[b] (producers arrive, consumers wait) and EMPTY[b] (consumers
+// arrive after their last read of stage b, producers wait before refilling it).
+// Every warp of a role runs the same tile sequence and reaches every barrier,
+// so each barrier generation completes with exactly NTHR threads.  The
+// arithmetic is that of hex8_df64_tile, operation for operation, so both give
+// bitwise the same workspace.
+// ---------------------------------------------------------------------------
+namespace ws {
+constexpr int EPB = 16, NQ = 8;
+constexpr int PROD_WARPS = 4, CONS_WARPS = 12;
+constexpr int NPROD = 32 * PROD_WARPS;  // one thread per quadrature point of the tile
+constexpr int NCONS = 32 * CONS_WARPS;  // one thread per row of K_e of the tile
+constexpr int NTHR = NPROD + NCONS;
+static_assert(NPROD == EPB * NQ && NCONS == EPB * 24, "tile shape");
+// named barrier ids (0 is __syncthreads)
+constexpr int BAR_FULL = 1;   // 1, 2: stage b filled
+constexpr int BAR_EMPTY = 3;  // 3, 4: stage b consumed
+constexpr int BAR_PROD = 5;   // producers only
+constexpr int BAR_CONS = 6;   // consumers only
+// shared memory (bytes): reference tables, then two stages
+constexpr int REF_BYTES = ((RefLayout<1>::SIZE * 8 + 15) / 16) * 16;
+constexpr int ST_X = 0;                          // double [EPB][24] coordinates
+constexpr int ST_U = ST_X + EPB * 24 * 8;        // double [EPB][24] displacements
+constexpr int ST_DNX = ST_U + EPB * 24 * 8;      // float2 [EPB][NQ][24] spatial gradients
+constexpr int ST_A = ST_DNX + EPB * NQ * 24 * 8; // float2 [EPB][NQ][45] JxW A, unique entries
+constexpr int ST_BYTES = ST_A + EPB * NQ * 45 * 8;
+constexpr int K_BYTES = EPB * 576 * 8;           // K_e staging over a consumed stage
+static_assert(K_BYTES <= ST_BYTES && ST_BYTES % 16 == 0, "stage layout");
+constexpr int SMEM = REF_BYTES + 2 * ST_BYTES;
+
+__device__ __forceinline__ void named_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+__device__ __forceinline__ void named_arrive(int id, int n) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+}  // namespace ws
+
+template <class Model, bool WANT_R, bool WANT_K>
+__global__ void __launch_bounds__(ws::NTHR, 1) mech_hex8_df64_ws_kernel(ElemArgs g) {
+  using namespace ws;
+  constexpr int NS = Model::NS, SCR = Model::SCR, SCR2 = Model::SCR2;
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* s_ref = reinterpret_cast<double*>(smem);
+  const int tid = threadIdx.x;
+  for (int i = tid; i < RefLayout<1>::SIZE; i += NTHR) s_ref[i] = g.ref[i];
+  __syncthreads();
+  const int64_t ntiles = (g.ne + EPB - 1) / EPB;
+
+  if (tid < NPROD) {
+    // ---- producers: thread (el, q) owns quadrature point q of element el ----
+    const int el = tid >> 3, q = tid & 7;
+    for (int k = 0;; ++k) {
+      const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
+      if (tile >= ntiles) break;
+      const int buf = k & 1;
+      unsigned char* st = smem + REF_BYTES + buf * ST_BYTES;
+      if (k >= 2) named_sync(BAR_EMPTY + buf, NTHR);  // the consumers are done with tile k-2
+      const int64_t e = tile * EPB + el;
+      const bool live = e < g.ne;
+      double* s_x = reinterpret_cast<double*>(st + ST_X) + el * 24;
+      double* s_u = reinterpret_cast<double*>(st + ST_U) + el * 24;
+      if (live) {
+        const int64_t node = g.conn[e * 8 + q];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          s_x[q * 3 + d] = __ldg(&g.coords[node * 3 + d]);
+          s_u[q * 3 + d] = __ldg(&g.U[node * 3 + d]);
+        }
+      }
+      named_sync(BAR_PROD, NPROD);
+      if (live) {
+        double dNX[24];
+        const double jxw = map_point<1, double>(s_ref, q, s_x, dNX, nullptr);
+        double gu[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            double sum = 0;
+#pragma unroll
+            for (int a = 0; a < 8; ++a) sum = fma(s_u[a * 3 + i], dNX[a * 3 + j], sum);
+            gu[i][j] = sum;
+          }
+        float2* pdNX = reinterpret_cast<float2*>(st + ST_DNX) + (el * NQ + q) * 24;
+#pragma unroll
+        for (int m = 0; m < 24; ++m) pdNX[m] = df64_split(dNX[m]);
+        const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
+        double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
+        double P9[9], scr[SCR];
+        Model::point(g.props, gu, jxw, so, sn, P9, scr);
+        if (WANT_R) hex8_residual_fp64(dNX, P9, q, 0xffu << ((tid & 31) & ~7), static_cast<double*>(g.Re) + e * 24);
+        if (WANT_K) {
+          float2 s2[SCR2];
+          Model::split_scratch(scr, s2);
+          float2* pA = reinterpret_cast<float2*>(st + ST_A) + (el * NQ + q) * 45;
+#pragma unroll
+          for (int m = 0; m < 45; ++m) {
+            int r1, r2;
+            sym_pair(m, r1, r2);
+            pA[m] = Model::aentry_df64(s2, r1 / 3, r1 % 3, r2 / 3, r2 % 3);
+          }
+        }
+      }
+      named_arrive(BAR_FULL + buf, NTHR);
+    }
+    return;
+  }
+
+  // ---- consumers: thread (el, tx) owns row tx = (a, i) of element el's K_e ----
+  const int c = tid - NPROD, el = c / 24, tx = c - el * 24;
+  const int a = tx / 3, i = tx % 3;
+  const bool fifth = a < 4;
+  const int r1v[3] = {3 * i, 3 * i + 1, 3 * i + 2};
+  const float2 z = make_float2(0.f, 0.f);
+  for (int k = 0;; ++k) {
+    const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
+    if (tile >= ntiles) break;
+    const int buf = k & 1;
+    unsigned char* st = smem + REF_BYTES + buf * ST_BYTES;
+    named_sync(BAR_FULL + buf, NTHR);  // tile k is in stage buf
+    const int64_t e0 = tile * EPB, e = e0 + el;
+    const bool live = e < g.ne;
+    const float2* s_dNX = reinterpret_cast<const float2*>(st + ST_DNX) + el * NQ * 24;
+    const float2* s_A = reinterpret_cast<const float2*>(st + ST_A) + el * NQ * 45;
+    float2 K[15];
+#pragma unroll
+    for (int cc = 0; cc < 15; ++cc) K[cc] = z;
+    if (WANT_K && live) {
+#pragma unroll 1
+      for (int q = 0; q < NQ; ++q) {
+        const float2* dNX = s_dNX + q * 24;
+        const float2 g0 = dNX[a * 3], g1 = dNX[a * 3 + 1], g2 = dNX[a * 3 + 2];
+        {
+          const float2* Aq = s_A + q * 45;
+          float2 t[9];
+#pragma unroll
+          for (int kl = 0; kl < 9; ++kl)
+            t[kl] = df64_dot3(g0, Aq[sym_index(r1v[0], kl)], g1, Aq[sym_index(r1v[1], kl)], g2,
+                              Aq[sym_index(r1v[2], kl)]);
+#pragma unroll
+          for (int d = 0; d < 5; ++d) {
+            if (d == 4 && !fifth) break;
+            const int b = (a + d) & 7;
+            const float2 h0 = dNX[b * 3], h1 = dNX[b * 3 + 1], h2 = dNX[b * 3 + 2];
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk)
+              K[d * 3 + kk] = df64_dot3_acc(K[d * 3 + kk], t[kk * 3], h0, t[kk * 3 + 1], h1, t[kk * 3 + 2], h2);
+          }
+        }
+      }
+    }
+    if (WANT_K) {
+      named_sync(BAR_CONS, NCONS);  // every consumer is done reading stage buf: stage K_e over it
+      if (live) {
+        float2* Ks = reinterpret_cast<float2*>(st) + el * 576;  // KE_NODE_ROWS layout
+#pragma unroll
+        for (int d = 0; d < 5; ++d) {
+          if (d == 4 && !fifth) break;
+          const int b = (a + d) & 7;
+#pragma unroll
+          for (int kk = 0; kk < 3; ++kk) {
+            Ks[((a * 3 + i) * 3 + kk) * 8 + b] = K[d * 3 + kk];
+            if (d) Ks[((b * 3 + kk) * 3 + i) * 8 + a] = K[d * 3 + kk];
+          }
+        }
+      }
+      named_sync(BAR_CONS, NCONS);
+      const int64_t left = g.ne - e0;
+      const int nlive = left < EPB ? int(left) : EPB;
+      double2* dst = reinterpret_cast<double2*>(static_cast<double*>(g.Ke) + e0 * 576);
+      const double2* src = reinterpret_cast<const double2*>(st);
+      for (int idx = c; idx < nlive * 288; idx += NCONS) dst[idx] = src[idx];
+    }
+    named_arrive(BAR_EMPTY + buf, NTHR);  // stage buf may be refilled
+  }
 }
 
 }  // namespace fec

@@ -101,10 +101,28 @@ cudaError_t hex8_df64_1(const ElemArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+template <bool R, bool K>
+cudaError_t hex8_df64_ws_1(const ElemArgs& a, cudaStream_t s) {
+  cudaError_t err;
+  if ((err = ensure_smem<mech_hex8_df64_ws_kernel<NeoHookean, R, K>>(ws::SMEM)) != cudaSuccess) return err;
+  const int64_t tiles = (a.ne + ws::EPB - 1) / ws::EPB;
+  const int64_t sms = num_sms();
+  const unsigned grid = unsigned(tiles < sms ? tiles : sms);
+  mech_hex8_df64_ws_kernel<NeoHookean, R, K><<<grid, ws::NTHR, ws::SMEM, s>>>(a);
+  return cudaGetLastError();
+}
+
+// FP64 hex8: the warp-specialised persistent kernel, or with FEC_HEX8_DF64=tile
+// the one-tile-per-CTA kernel (bitwise the same results)
 template <int EPB>
 cudaError_t hex8_df64(bool want_r, bool want_k, const ElemArgs& a, cudaStream_t s, int* launches) {
   if (a.ne <= 0 || (!want_r && !want_k)) return cudaSuccess;
   ++*launches;
+  if (!hex8_df64_tile_kernel()) {
+    if (want_r && want_k) return hex8_df64_ws_1<true, true>(a, s);
+    if (want_r) return hex8_df64_ws_1<true, false>(a, s);
+    return hex8_df64_ws_1<false, true>(a, s);
+  }
   if (want_r && want_k) return hex8_df64_1<EPB, true, true>(a, s);
   if (want_r) return hex8_df64_1<EPB, true, false>(a, s);
   return hex8_df64_1<EPB, false, true>(a, s);

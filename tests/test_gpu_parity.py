@@ -231,7 +231,7 @@ def test_higher_order_fp32_element(fec, orc, kind, phys_name):
             del os.environ["FEC_HEX27_ON_CUDA_CORES"]
         print("hex27 tensor cores vs CUDA cores: residual", rel_err(R, R2), "nzval", rel_err(nz, nz2, FLOOR32))
         assert np.array_equal(R, R2)  # the residual is formed on the CUDA cores either way
-        assert max(rel_err(nz, nz2, FLOOR32)) <= 2e-6
+        assert max(rel_err(nz, nz2, FLOOR32)) <= 5e-6   # two FP32-element paths, entry-wise
 
 
 def test_j2_one_load_step_with_state(fec, orc):
@@ -301,3 +301,41 @@ def test_nonfinite_outputs_are_reported(fec):
     with pytest.raises(fec.FECError) as info:
         fec.assemble_residual_and_stiffness(asm, Uu, p, check_finite=True)
     assert info.value.status == -5 and "residual" in str(info.value)
+
+
+@pytest.mark.parametrize("phys_name", ["neohookean", "j2"])
+@pytest.mark.parametrize("n", [3, 17, 40])
+def test_fp64_hex8_warp_specialised_kernel_matches_tile_kernel(fec, n, phys_name):
+    """The persistent warp-specialised FP64 hex8 kernel (default) against the
+    one-tile-per-CTA kernel (FEC_HEX8_DF64=tile): bitwise the same residual,
+    stiffness and new state, for a single partial tile (27 elements), a few
+    tiles per CTA (4,913) and many (64,000); fused and separate R / K calls."""
+    import os
+    torch = _torch()
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n + 1,) * 3)
+    if phys_name == "neohookean":
+        phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+        U = stretch_field(mesh.nodal_coords, seed=1).ravel()
+    else:
+        phys = fec.J2Plasticity(200.0, 0.3, 0.25, 2.0)
+        U = 3.0 * stretch_field(mesh.nodal_coords, seed=2, noise=1e-4, diag=(1.004, 0.999, 0.999)).ravel()
+    asm, p = _setup(fec, mesh, "vector", phys)
+    Uu = torch.from_numpy(U[asm.dof.unknown_dofs - 1].copy()).cuda()
+    out = {}
+    for kernel in ("ws", "tile"):
+        if kernel == "tile":
+            os.environ["FEC_HEX8_DF64"] = "tile"
+        try:
+            R, K = fec.assemble_residual_and_stiffness(asm, Uu, p)
+            torch.cuda.synchronize()
+            res = [R.cpu().numpy().copy(), K.nzval.cpu().numpy().copy(), p.state_new.cpu().numpy().copy()]
+            fec.assemble_vector(asm, fec.residual, Uu, p)
+            fec.assemble_stiffness(asm, fec.stiffness, Uu, p)
+            torch.cuda.synchronize()
+            res += [fec.residual(asm).cpu().numpy().copy(), fec.stiffness(asm).nzval.cpu().numpy().copy()]
+            out[kernel] = res
+        finally:
+            os.environ.pop("FEC_HEX8_DF64", None)
+    for a, b in zip(out["ws"], out["tile"]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(out["ws"][0], out["ws"][3]) and np.array_equal(out["ws"][1], out["ws"][4])

@@ -88,7 +88,9 @@ def test_poisson_hex8_lobatto_with_dirichlet(fec, orc):
 
 
 def test_poisson_quad4_lobatto(fec, orc):
-    mesh = fec.StructuredMesh("quad", (0.0, 0.0), (1.0, 2.0), (11, 13))
+    # square node counts: the reference's structured quad generator (and so its
+    # mirror) indexes x-coordinates with the y counter (StructuredMesh.jl:472-483)
+    mesh = fec.StructuredMesh("quad", (0.0, 0.0), (1.0, 2.0), (12, 12))
     U = np.random.default_rng(4).uniform(-1, 1, mesh.num_nodes)
     asm, p, R, nz, K = _assemble(fec, mesh, "scalar", fec.Poisson(2.0), "GaussLobattoLegendre", U=U)
     Ro, colptr, rowval, nzo = _oracle(orc, mesh, asm, "poisson", [2.0], U, asm.reference_tables(1))
