@@ -1160,4 +1160,190 @@ __global__ void __launch_bounds__(WPB * 32, MINB) node_gather_kernel(GatherArgs 
   if (wantR) g.R_u[g.dof_to_unknown[n * NF + lane]] = racc;
 }
 
+// ---------------------------------------------------------------------------
+// Software-pipelined node gather for meshes of one hex8 mechanics block (the
+// KE_NODE_ROWS layout).  Each warp walks the nodes gw, gw + GW, ... (GW =
+// warps in the grid).  While it accumulates node i from shared memory, the
+// rows its elements hold for node i+1 (8 x 72 entries), their element-map
+// entries and residual values are already on their way into the warp's other
+// stage buffer by cp.async, and node i+2's adjacency entries are in
+// registers, so the three dependent loads of a node (adjacency, element rows,
+// accumulate) no longer serialise per node.  The accumulation is the one of
+// gather_run_hex8v, value for value and in the same element order, so the
+// results are bitwise those of node_gather_kernel.  Nodes outside the fast
+// path (a Dirichlet dof in the neighbourhood, or more than 8 adjacent
+// elements) are gathered in place by the general routine.
+// ---------------------------------------------------------------------------
+namespace gp {
+constexpr int WPB = 8;
+constexpr int MAXE = 8;  // elements staged per node
+template <typename Real>
+struct Stage {
+  static constexpr int K_BYTES = MAXE * 72 * int(sizeof(Real));  // node a's 72 entries of each element
+  static constexpr int EP_OFF = K_BYTES;                         // uint16 [MAXE][8] element-map entries
+  static constexpr int R_OFF = EP_OFF + MAXE * 16;               // RE<Real> [MAXE][3] residual values
+  static constexpr int BYTES = (R_OFF + MAXE * 3 * int(sizeof(typename RE<Real>::T)) + 15) / 16 * 16;
+  static constexpr int CHUNKS = 72 * int(sizeof(Real)) / 16;     // 16-byte copies per element row block
+};
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void cp16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+template <int BYTES>
+__device__ __forceinline__ void cp_small(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_addr(dst)), "l"(src), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+struct NodeMeta {
+  int64_t n;        // node, or -1 past the end
+  int64_t p0;       // first adjacency entry
+  int cnt;          // adjacency entries
+  unsigned um;      // umask with the full-neighbourhood bit
+  int Ln;           // rows per column
+  uint32_t adj;     // this lane's adjacency entry (lane < cnt)
+  bool pipe;        // staged through shared memory
+};
+
+__device__ __forceinline__ NodeMeta load_meta(const GatherArgs& g, int64_t n, int lane) {
+  NodeMeta m;
+  m.n = n < g.nn ? n : -1;
+  m.p0 = 0;
+  m.cnt = 0;
+  m.um = 0;
+  m.Ln = 0;
+  m.adj = 0;
+  m.pipe = false;
+  if (m.n < 0) return m;
+  m.um = g.umask[n];
+  m.Ln = g.col_len[n];
+  m.p0 = g.nadj_ptr[n];
+  m.cnt = int(g.nadj_ptr[n + 1] - m.p0);
+  m.pipe = (m.um & UMASK_FULL_NBR) != 0 && m.cnt >= 1 && m.cnt <= MAXE;
+  if (m.pipe && lane < m.cnt) m.adj = g.nadj[m.p0 + lane];
+  return m;
+}
+
+// cp.async of node m's staged data into `st` (all 32 lanes; a commit group always follows)
+template <typename Real>
+__device__ __forceinline__ void issue(const GatherArgs& g, const NodeMeta& m, unsigned char* st, int lane) {
+  using S = Stage<Real>;
+  using RT = typename RE<Real>::T;
+  if (!m.pipe) return;
+  const BlockInfo& B = g.blk[0];
+  const unsigned char* Ke = reinterpret_cast<const unsigned char*>(static_cast<const Real*>(g.Ke) + B.ke_off);
+  const uint16_t* ep = g.epos + B.epos_off;
+  const RT* Re = static_cast<const RT*>(g.Re) + B.re_off;
+  // element rows: chunk t = lane + 32 j; every lane takes part in every shuffle (the
+  // trip count is fixed), copies only for t < cnt * CHUNKS
+  const int total = m.cnt * S::CHUNKS;
+  constexpr int TRIPS = (MAXE * S::CHUNKS + 31) / 32;
+#pragma unroll
+  for (int j = 0; j < TRIPS; ++j) {
+    const int t = lane + 32 * j;
+    const int c = t / S::CHUNKS < MAXE ? t / S::CHUNKS : MAXE - 1, w = t - c * S::CHUNKS;
+    const uint32_t packed = __shfl_sync(0xffffffffu, m.adj, c);
+    const uint64_t le = (packed >> 5) - uint32_t(B.elem_start), a = packed & 31u;
+    if (t < total) cp16(st + (c * 72) * sizeof(Real) + w * 16, Ke + ((le * 576u + a * 72u) * sizeof(Real)) + w * 16);
+  }
+  if (lane < m.cnt) {  // element-map row of node a: 8 uint16, 16-byte aligned
+    const uint64_t le = (m.adj >> 5) - uint32_t(B.elem_start), a = m.adj & 31u;
+    cp16(st + S::EP_OFF + lane * 16, ep + le * 64u + a * 8u);
+  }
+  {  // residual values: lane t = 3 c + i < 3 cnt (at most 24)
+    const int c = lane / 3 < MAXE ? lane / 3 : MAXE - 1, i = lane - 3 * c;
+    const uint32_t packed = __shfl_sync(0xffffffffu, m.adj, c);
+    const uint64_t le = (packed >> 5) - uint32_t(B.elem_start), a = packed & 31u;
+    if (g.R_u && lane < 3 * m.cnt)
+      cp_small<sizeof(RT)>(st + S::R_OFF + lane * sizeof(RT), Re + le * 24u + a * 3u + i);
+  }
+}
+}  // namespace gp
+
+template <typename Real, int MINB>
+__global__ void __launch_bounds__(gp::WPB * 32, MINB) node_gather_hex8_pipe_kernel(GatherArgs g) {
+  using namespace gp;
+  using S = Stage<Real>;
+  using RT = typename RE<Real>::T;
+  using V4 = typename std::conditional<sizeof(Real) == 4, float4, F2x4>::type;
+  extern __shared__ __align__(16) unsigned char smem_g[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t acc_bytes = (size_t(g.acc_stride) * GatherAcc::WORDS * sizeof(float) + 15) / 16 * 16;
+  unsigned char* wbase = smem_g + warp * (acc_bytes + 2 * S::BYTES);
+  float* acc = reinterpret_cast<float*>(wbase);
+  unsigned char* stage[2] = {wbase + acc_bytes, wbase + acc_bytes + S::BYTES};
+  const int64_t GW = int64_t(gridDim.x) * WPB;
+  const bool wantK = g.nzval != nullptr;
+  const BlockInfo& B = g.blk[0];
+  const bool kl = lane < 18;
+  const int ki = lane >> 1, bh = lane & 1;
+
+  NodeMeta cur = load_meta(g, int64_t(blockIdx.x) * WPB + warp, lane);
+  issue<Real>(g, cur, stage[0], lane);
+  commit();
+  NodeMeta nxt = load_meta(g, cur.n < 0 ? g.nn : cur.n + GW, lane);
+  for (int it = 0; cur.n >= 0; ++it) {
+    const int s = it & 1;
+    issue<Real>(g, nxt, stage[s ^ 1], lane);  // node i+1 into the other stage
+    commit();
+    const NodeMeta nn2 = load_meta(g, nxt.n < 0 ? g.nn : nxt.n + GW, lane);  // node i+2's adjacency
+    wait_prev();                              // node i's copies (this lane's) have landed
+    __syncwarp();                             // ... and every lane's
+    const int64_t n = cur.n;
+    const unsigned um = cur.um & ~UMASK_FULL_NBR;
+    if (um != 0) {
+      const int Ln = cur.Ln, ncols = __popc(um);
+      const bool wantR = g.R_u != nullptr && lane < 3 && ((um >> lane) & 1u);
+      if (wantK)
+        for (int j = lane; j < ncols * Ln; j += 32) GatherAcc::zero(acc, j);
+      double racc = 0.0;
+      __syncwarp();
+      if (cur.pipe) {
+        const unsigned char* st = stage[s];
+        const int base = (ki / 3) * Ln + (ki % 3);
+        for (int c = 0; c < cur.cnt; ++c) {
+          if (wantR) racc += double(reinterpret_cast<const RT*>(st + S::R_OFF)[c * 3 + lane]);
+          if (wantK) {
+            if (kl) {
+              const V4 v = *reinterpret_cast<const V4*>(st + (c * 72 + ki * 8 + bh * 4) * sizeof(Real));
+              const uint2 ep = *reinterpret_cast<const uint2*>(st + S::EP_OFF + c * 16 + bh * 8);
+              float2* A2 = reinterpret_cast<float2*>(acc);
+              const int p0 = base + int(ep.x & 0xffffu), p1 = base + int(ep.x >> 16);
+              const int p2 = base + int(ep.y & 0xffffu), p3 = base + int(ep.y >> 16);
+              float2 s0 = A2[p0], s1 = A2[p1], s2 = A2[p2], s3 = A2[p3];
+              s0 = GatherAcc::plus(s0, v.x);
+              s1 = GatherAcc::plus(s1, v.y);
+              s2 = GatherAcc::plus(s2, v.z);
+              s3 = GatherAcc::plus(s3, v.w);
+              A2[p0] = s0;
+              A2[p1] = s1;
+              A2[p2] = s2;
+              A2[p3] = s3;
+            }
+            __syncwarp();
+          }
+        }
+      } else {
+        const bool fast = (cur.um & UMASK_FULL_NBR) != 0;
+        const int64_t p1 = cur.p0 + cur.cnt;
+        if (fast)
+          gather_run_hex8v<Real>(g, B, cur.p0, p1, Ln, acc, racc, lane, wantK, wantR);
+        else
+          gather_run_generic<Real, 3>(g, B, cur.p0, p1, um, fast, Ln, acc, racc, lane, wantK, wantR);
+      }
+      __syncwarp();
+      if (wantK) {
+        double* out = g.nzval + g.col_base[n];
+        for (int j = lane; j < ncols * Ln; j += 32) out[j] = GatherAcc::value(acc, j);
+      }
+      if (wantR) g.R_u[g.dof_to_unknown[n * 3 + lane]] = racc;
+      __syncwarp();
+    }
+    cur = nxt;
+    nxt = nn2;
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 }  // namespace fec

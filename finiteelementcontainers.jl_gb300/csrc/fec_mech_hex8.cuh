@@ -480,41 +480,6 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_rows2_kernel(ElemArgs g) {
   }
 }
 
-// Element residual of a hex8 element in native FP64, from its 8 point threads:
-// 8 consecutive lanes (q = lane & 7) holding their point's spatial gradients
-// dNX[a][J] and JxW P[i][J].  Each lane forms its point's 24 terms
-// R_q[a][i] = sum_J dNX[a][J] P[i][J]; a reduce-scatter over the 8 lanes
-// (partners lane ^ 4, ^ 2, ^ 1; each pair sum taken with the lower lane's
-// operand first, so every value is summed in one fixed order) leaves lane q
-// with R_e[3q .. 3q+2], which it writes to Re_e.  `mask` holds the 8 lanes.
-__device__ __forceinline__ void hex8_residual_fp64(const double* dNX, const double* P9, int q, unsigned mask,
-                                                   double* Re_e) {
-  double v[24];
-#pragma unroll
-  for (int a = 0; a < 8; ++a)
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-      v[a * 3 + i] = fma(dNX[a * 3], P9[i * 3], fma(dNX[a * 3 + 1], P9[i * 3 + 1], dNX[a * 3 + 2] * P9[i * 3 + 2]));
-  const bool b2 = (q & 4) != 0, b1 = (q & 2) != 0, b0 = (q & 1) != 0;
-  double w12[12];
-#pragma unroll
-  for (int m = 0; m < 12; ++m) {
-    const double recv = __shfl_xor_sync(mask, b2 ? v[m] : v[12 + m], 4);
-    w12[m] = b2 ? recv + v[12 + m] : v[m] + recv;
-  }
-  double w6[6];
-#pragma unroll
-  for (int m = 0; m < 6; ++m) {
-    const double recv = __shfl_xor_sync(mask, b1 ? w12[m] : w12[6 + m], 2);
-    w6[m] = b1 ? recv + w12[6 + m] : w12[m] + recv;
-  }
-#pragma unroll
-  for (int m = 0; m < 3; ++m) {
-    const double recv = __shfl_xor_sync(mask, b0 ? w6[m] : w6[3 + m], 1);
-    Re_e[3 * q + m] = b0 ? recv + w6[3 + m] : w6[m] + recv;
-  }
-}
-
 // ---------------------------------------------------------------------------
 // FP64 variant with the contraction on the FP32 pipes.  Kinematics and the
 // constitutive update stay in FP64; the shape-function gradients, the stress and
@@ -529,7 +494,8 @@ struct Hex8Df64Smem {
   static constexpr int D_REF = 0, D_X = REF, D_U = D_X + EPB * 24;
   static constexpr int N_DOUBLE = D_U + EPB * 24;
   static constexpr int F_DNX = 0;                       // float2 entries, after the doubles
-  static constexpr int F_SCR = F_DNX + EPB * NQ * 24;
+  static constexpr int F_P = F_DNX + EPB * NQ * 24;
+  static constexpr int F_SCR = F_P + EPB * NQ * 9;
   static constexpr int F_A = (F_SCR + EPB * NQ * SCR2 + 1) & ~1;  // 45 unique tangent entries per point
   static constexpr int A_STRIDE = NQ * 45;
   static constexpr int K_STRIDE = 576;                  // K staging per element, over the whole float2 region
@@ -565,6 +531,7 @@ __device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile,
   double* s_x = dbase + S::D_X + ty * 24;
   double* s_u = dbase + S::D_U + ty * 24;
   const float2* s_dNX = fb + S::F_DNX + ty * NQ * 24;
+  const float2* s_P = fb + S::F_P + ty * NQ * 9;
   const float2* s_scr = fb + S::F_SCR + ty * NQ * SCR2;
   float2* s_A = fb + S::F_A + ty * S::A_STRIDE;
   int* s_conn = s_conn_all + ty * 8;
@@ -583,7 +550,7 @@ __device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile,
   if (tid < EPB * NQ) {  // per-point map and constitutive update, native FP64, full warps
     const int el = tid / NQ, q = tid % NQ;
     const int64_t ep = e0 + el;
-    if (ep < g.ne) {  // uniform over the element's 8 lanes
+    if (ep < g.ne) {
       const double* px = dbase + S::D_X + el * 24;
       const double* pu = dbase + S::D_U + el * 24;
       double dNX[24];
@@ -600,14 +567,15 @@ __device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile,
         }
       float2* pdNX = fb + S::F_DNX + el * NQ * 24;
 #pragma unroll
-      for (int m = 0; m < 24; ++m) pdNX[q * 24 + m] = df64_split(dNX[m]);
+      for (int m = 0; m < 24; ++m) pdNX[q * 24 + m] = df64_split(dNX[m]);  // dNX dies before the model
       const double* so = NS ? g.state_old + (ep * NQ + q) * NS : nullptr;
       double* sn = (NS && g.state_new) ? g.state_new + (ep * NQ + q) * NS : nullptr;
       double P9[9], scr[SCR];
       Model::point(g.props, gu, jxw, so, sn, P9, scr);
-      if (WANT_R)
-        hex8_residual_fp64(dNX, P9, q, 0xffu << ((tid & 31) & ~7), static_cast<double*>(g.Re) + ep * 24);
+      float2* pP = fb + S::F_P + el * NQ * 9;
       float2* pscr = fb + S::F_SCR + el * NQ * SCR2;
+#pragma unroll
+      for (int m = 0; m < 9; ++m) pP[q * 9 + m] = df64_split(P9[m]);
       Model::split_scratch(scr, pscr + q * SCR2);
     }
   }
@@ -629,12 +597,17 @@ __device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile,
   float2 K[15];
 #pragma unroll
   for (int c = 0; c < 15; ++c) K[c] = z;
-  if (WANT_K && live) {
+  float2 R = z;
+  if (live) {
 #pragma unroll 1
     for (int q = 0; q < NQ; ++q) {
       const float2* dNX = s_dNX + q * 24;
       const float2 g0 = dNX[a * 3], g1 = dNX[a * 3 + 1], g2 = dNX[a * 3 + 2];
-      {
+      if (WANT_R) {
+        const float2* P = s_P + q * 9 + i * 3;
+        R = df64_dot3_acc(R, g0, P[0], g1, P[1], g2, P[2]);
+      }
+      if (WANT_K) {
         const float2* Aq = s_A + q * 45;
         float2 t[9];
 #pragma unroll
@@ -653,6 +626,8 @@ __device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile,
       }
     }
   }
+  // the residual leaves as one double: hi + lo of a normalised pair is exact in FP64
+  if (WANT_R && live) static_cast<double*>(g.Re)[e * 24 + tx] = widen(R.x) + widen(R.y);
   __syncthreads();  // the whole float2 region is reused for the K staging below
   if (WANT_K && live) {
     float2* Ks = fb + ty * S::K_STRIDE;  // 576 double-float entries, KE_NODE_ROWS layout
@@ -690,11 +665,11 @@ __global__ void __launch_bounds__(EPB * 24, 4) mech_hex8_df64_kernel(ElemArgs g)
 // ---------------------------------------------------------------------------
 // Warp-specialised, persistent form of the FP64 hex8 kernel (the default).
 //
-// The per-point phase (isoparametric map, constitutive update, the element
-// residual and the 45 unique tangent entries, native FP64 plus double-float
-// splits) and the
-// double-float contraction of K_e run on different warps of one CTA and on
-// different tiles of 16 elements at a time: while 12 consumer warps contract
+// The per-point phase (isoparametric map and constitutive update in native
+// FP64, then the double-float splits of the gradients, the stress and the
+// tangent scratch) and the double-float work of K_e and R_e (the 45 unique
+// tangent entries per point, the contraction) run on different warps of one
+// CTA and on different tiles of 16 elements: while 12 consumer warps work on
 // tile t, 4 producer warps (one per SM sub-partition, so that every FP64 unit
 // of the SM carries a share of the point phase) prepare tile t+1 in the other
 // half of a double-buffered shared-memory stage.  One CTA per SM takes the
@@ -718,16 +693,22 @@ constexpr int BAR_FULL = 1;   // 1, 2: stage b filled
 constexpr int BAR_EMPTY = 3;  // 3, 4: stage b consumed
 constexpr int BAR_PROD = 5;   // producers only
 constexpr int BAR_CONS = 6;   // consumers only
-// shared memory (bytes): reference tables, then two stages
 constexpr int REF_BYTES = ((RefLayout<1>::SIZE * 8 + 15) / 16) * 16;
-constexpr int ST_X = 0;                          // double [EPB][24] coordinates
-constexpr int ST_U = ST_X + EPB * 24 * 8;        // double [EPB][24] displacements
-constexpr int ST_DNX = ST_U + EPB * 24 * 8;      // float2 [EPB][NQ][24] spatial gradients
-constexpr int ST_A = ST_DNX + EPB * NQ * 24 * 8; // float2 [EPB][NQ][45] JxW A, unique entries
-constexpr int ST_BYTES = ST_A + EPB * NQ * 45 * 8;
-constexpr int K_BYTES = EPB * 576 * 8;           // K_e staging over a consumed stage
-static_assert(K_BYTES <= ST_BYTES && ST_BYTES % 16 == 0, "stage layout");
-constexpr int SMEM = REF_BYTES + 2 * ST_BYTES;
+
+// shared memory (bytes): reference tables, then two stages of
+template <class Model>
+struct Layout {
+  static constexpr int X = 0;                           // double [EPB][24] coordinates
+  static constexpr int U = X + EPB * 24 * 8;            // double [EPB][24] displacements
+  static constexpr int DNX = U + EPB * 24 * 8;          // float2 [EPB][NQ][24] spatial gradients
+  static constexpr int P = DNX + EPB * NQ * 24 * 8;     // float2 [EPB][NQ][9] JxW P
+  static constexpr int SCR = P + EPB * NQ * 9 * 8;      // float2 [EPB][NQ][SCR2] tangent scratch
+  static constexpr int A = SCR + EPB * NQ * Model::SCR2 * 8;  // float2 [EPB][NQ][45] JxW A, unique entries
+  static constexpr int STAGE = ((A + EPB * NQ * 45 * 8) + 15) / 16 * 16;
+  static constexpr int K_BYTES = EPB * 576 * 8;         // K_e staging over a consumed stage
+  static_assert(K_BYTES <= STAGE, "stage layout");
+  static constexpr int SMEM = REF_BYTES + 2 * STAGE;
+};
 
 __device__ __forceinline__ void named_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
 __device__ __forceinline__ void named_arrive(int id, int n) {
@@ -738,6 +719,7 @@ __device__ __forceinline__ void named_arrive(int id, int n) {
 template <class Model, bool WANT_R, bool WANT_K>
 __global__ void __launch_bounds__(ws::NTHR, 1) mech_hex8_df64_ws_kernel(ElemArgs g) {
   using namespace ws;
+  using Lay = Layout<Model>;
   constexpr int NS = Model::NS, SCR = Model::SCR, SCR2 = Model::SCR2;
   extern __shared__ __align__(16) unsigned char smem[];
   double* s_ref = reinterpret_cast<double*>(smem);
@@ -753,12 +735,12 @@ __global__ void __launch_bounds__(ws::NTHR, 1) mech_hex8_df64_ws_kernel(ElemArgs
       const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
       if (tile >= ntiles) break;
       const int buf = k & 1;
-      unsigned char* st = smem + REF_BYTES + buf * ST_BYTES;
+      unsigned char* st = smem + REF_BYTES + buf * Lay::STAGE;
       if (k >= 2) named_sync(BAR_EMPTY + buf, NTHR);  // the consumers are done with tile k-2
       const int64_t e = tile * EPB + el;
       const bool live = e < g.ne;
-      double* s_x = reinterpret_cast<double*>(st + ST_X) + el * 24;
-      double* s_u = reinterpret_cast<double*>(st + ST_U) + el * 24;
+      double* s_x = reinterpret_cast<double*>(st + Lay::X) + el * 24;
+      double* s_u = reinterpret_cast<double*>(st + Lay::U) + el * 24;
       if (live) {
         const int64_t node = g.conn[e * 8 + q];
 #pragma unroll
@@ -781,25 +763,18 @@ __global__ void __launch_bounds__(ws::NTHR, 1) mech_hex8_df64_ws_kernel(ElemArgs
             for (int a = 0; a < 8; ++a) sum = fma(s_u[a * 3 + i], dNX[a * 3 + j], sum);
             gu[i][j] = sum;
           }
-        float2* pdNX = reinterpret_cast<float2*>(st + ST_DNX) + (el * NQ + q) * 24;
+        const int pt = el * NQ + q;
+        float2* pdNX = reinterpret_cast<float2*>(st + Lay::DNX) + pt * 24;
 #pragma unroll
-        for (int m = 0; m < 24; ++m) pdNX[m] = df64_split(dNX[m]);
+        for (int m = 0; m < 24; ++m) pdNX[m] = df64_split(dNX[m]);  // dNX dies before the model
         const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
         double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
         double P9[9], scr[SCR];
         Model::point(g.props, gu, jxw, so, sn, P9, scr);
-        if (WANT_R) hex8_residual_fp64(dNX, P9, q, 0xffu << ((tid & 31) & ~7), static_cast<double*>(g.Re) + e * 24);
-        if (WANT_K) {
-          float2 s2[SCR2];
-          Model::split_scratch(scr, s2);
-          float2* pA = reinterpret_cast<float2*>(st + ST_A) + (el * NQ + q) * 45;
+        float2* pP = reinterpret_cast<float2*>(st + Lay::P) + pt * 9;
 #pragma unroll
-          for (int m = 0; m < 45; ++m) {
-            int r1, r2;
-            sym_pair(m, r1, r2);
-            pA[m] = Model::aentry_df64(s2, r1 / 3, r1 % 3, r2 / 3, r2 % 3);
-          }
-        }
+        for (int m = 0; m < 9; ++m) pP[m] = df64_split(P9[m]);
+        Model::split_scratch(scr, reinterpret_cast<float2*>(st + Lay::SCR) + pt * SCR2);
       }
       named_arrive(BAR_FULL + buf, NTHR);
     }
@@ -816,21 +791,38 @@ __global__ void __launch_bounds__(ws::NTHR, 1) mech_hex8_df64_ws_kernel(ElemArgs
     const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
     if (tile >= ntiles) break;
     const int buf = k & 1;
-    unsigned char* st = smem + REF_BYTES + buf * ST_BYTES;
+    unsigned char* st = smem + REF_BYTES + buf * Lay::STAGE;
     named_sync(BAR_FULL + buf, NTHR);  // tile k is in stage buf
     const int64_t e0 = tile * EPB, e = e0 + el;
     const bool live = e < g.ne;
-    const float2* s_dNX = reinterpret_cast<const float2*>(st + ST_DNX) + el * NQ * 24;
-    const float2* s_A = reinterpret_cast<const float2*>(st + ST_A) + el * NQ * 45;
+    const float2* s_dNX = reinterpret_cast<const float2*>(st + Lay::DNX) + el * NQ * 24;
+    const float2* s_P = reinterpret_cast<const float2*>(st + Lay::P) + el * NQ * 9;
+    const float2* s_scr = reinterpret_cast<const float2*>(st + Lay::SCR) + el * NQ * SCR2;
+    float2* s_A = reinterpret_cast<float2*>(st + Lay::A) + el * NQ * 45;
+    if (WANT_K) {
+      if (live)
+        for (int w = tx; w < NQ * 45; w += 24) {
+          const int q = w / 45;
+          int r1, r2;
+          sym_pair(w - q * 45, r1, r2);
+          s_A[w] = Model::aentry_df64(s_scr + q * SCR2, r1 / 3, r1 % 3, r2 / 3, r2 % 3);
+        }
+      named_sync(BAR_CONS, NCONS);
+    }
     float2 K[15];
 #pragma unroll
     for (int cc = 0; cc < 15; ++cc) K[cc] = z;
-    if (WANT_K && live) {
+    float2 R = z;
+    if (live) {
 #pragma unroll 1
       for (int q = 0; q < NQ; ++q) {
         const float2* dNX = s_dNX + q * 24;
         const float2 g0 = dNX[a * 3], g1 = dNX[a * 3 + 1], g2 = dNX[a * 3 + 2];
-        {
+        if (WANT_R) {
+          const float2* P = s_P + q * 9 + i * 3;
+          R = df64_dot3_acc(R, g0, P[0], g1, P[1], g2, P[2]);
+        }
+        if (WANT_K) {
           const float2* Aq = s_A + q * 45;
           float2 t[9];
 #pragma unroll
@@ -849,6 +841,7 @@ __global__ void __launch_bounds__(ws::NTHR, 1) mech_hex8_df64_ws_kernel(ElemArgs
         }
       }
     }
+    if (WANT_R && live) static_cast<double*>(g.Re)[e * 24 + tx] = widen(R.x) + widen(R.y);
     if (WANT_K) {
       named_sync(BAR_CONS, NCONS);  // every consumer is done reading stage buf: stage K_e over it
       if (live) {

@@ -104,11 +104,11 @@ cudaError_t hex8_df64_1(const ElemArgs& a, cudaStream_t s) {
 template <bool R, bool K>
 cudaError_t hex8_df64_ws_1(const ElemArgs& a, cudaStream_t s) {
   cudaError_t err;
-  if ((err = ensure_smem<mech_hex8_df64_ws_kernel<NeoHookean, R, K>>(ws::SMEM)) != cudaSuccess) return err;
+  if ((err = ensure_smem<mech_hex8_df64_ws_kernel<NeoHookean, R, K>>(ws::Layout<NeoHookean>::SMEM)) != cudaSuccess) return err;
   const int64_t tiles = (a.ne + ws::EPB - 1) / ws::EPB;
   const int64_t sms = num_sms();
   const unsigned grid = unsigned(tiles < sms ? tiles : sms);
-  mech_hex8_df64_ws_kernel<NeoHookean, R, K><<<grid, ws::NTHR, ws::SMEM, s>>>(a);
+  mech_hex8_df64_ws_kernel<NeoHookean, R, K><<<grid, ws::NTHR, ws::Layout<NeoHookean>::SMEM, s>>>(a);
   return cudaGetLastError();
 }
 

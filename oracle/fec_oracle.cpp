@@ -576,6 +576,13 @@ extern "C" {
 // (Assemblers.jl:418-431).  xel [a][d], uel [a][f], state arrays [q][s].
 // Re[NDOF]; Ke[NDOF*NDOF] column-major like StaticArrays' K_el.data:
 // Ke[r + NDOF*c] = dR_r / du_c.  Either output may be null.
+// When set (per thread, by orc_assemble), orc_element also accumulates into it,
+// per element dof, the magnitude of the terms its residual entry sums:
+// sum_q JxW |grad N_a| (|grad u| + |N_a f|) for Poisson, sum_q JxW |grad N_a|_1 |P|_F
+// for mechanics -- a bound on every product the entry is formed from, so
+// that c eps times it bounds the rounding of any FP64 evaluation of the entry.
+thread_local double* tl_elem_abs = nullptr;
+
 int orc_element(int et, int phys, const double* props, const double* xel, const double* uel,
                 const double* st_old, double* st_new, double* Re, double* Ke) {
   if (et < 1 || et > 8) return -1;
@@ -601,6 +608,11 @@ int orc_element(int et, int phys, const double* props, const double* xel, const 
           double s = 0;
           for (int d = 0; d < D; ++d) s += gu[d] * m.dNX[a][d];
           Re[a] += m.JxW * (s - r.N[q * A + a] * f);
+          if (tl_elem_abs) {
+            double sa = 0;
+            for (int d = 0; d < D; ++d) sa += std::fabs(gu[d] * m.dNX[a][d]);
+            tl_elem_abs[a] += std::fabs(m.JxW) * (sa + std::fabs(r.N[q * A + a] * f));
+          }
         }
       if (Ke)
         for (int b = 0; b < A; ++b)
@@ -633,6 +645,15 @@ int orc_element(int et, int phys, const double* props, const double* xel, const 
             for (int J = 0; J < 3; ++J) s += m.dNX[a][J] * P9[i + 3 * J];
             Re[a * 3 + i] += m.JxW * s;
           }
+      if (Re && tl_elem_abs) {
+        double pn = 0;
+        for (int k = 0; k < 9; ++k) pn += P9[k] * P9[k];
+        pn = std::sqrt(pn);
+        for (int a = 0; a < A; ++a) {
+          const double g1 = std::fabs(m.dNX[a][0]) + std::fabs(m.dNX[a][1]) + std::fabs(m.dNX[a][2]);
+          for (int i = 0; i < 3; ++i) tl_elem_abs[a * 3 + i] += std::fabs(m.JxW) * g1 * pn;
+        }
+      }
       if (Ke)
         for (int b = 0; b < A; ++b)
           for (int k = 0; k < 3; ++k)
@@ -647,6 +668,8 @@ int orc_element(int et, int phys, const double* props, const double* xel, const 
   }
   return 0;
 }
+
+double* g_abs_out = nullptr;  // optional per-dof sums of |R_e| (orc_set_abs_output)
 
 // The block loop of assemble_vector!/assemble_matrix! (Assemblers.jl:402-432).
 //   R_full: length NF*NN, zeroed here, filled by scatter-add in element order
@@ -665,6 +688,9 @@ int orc_assemble(int nblocks, const int* elem_types, const i64* ne, const i64* c
     for (i64 i = 0; i < NF * nn; ++i) R_full[i] = 0;
   i64 coff = 0, koff = 0, soff = 0;
   int err = 0;
+  double* R_abs = R_full ? g_abs_out : nullptr;
+  if (R_abs)
+    for (i64 i = 0; i < NF * nn; ++i) R_abs[i] = 0;
   for (int b = 0; b < nblocks; ++b) {
     const RefFE& r = ref_of(elem_types[b]);
     if (r.nnpe == 0 || r.dim != dim) return -1;
@@ -683,8 +709,11 @@ int orc_assemble(int nblocks, const int* elem_types, const i64* ne, const i64* c
       const double* so = NS ? st_old + soff + e * NS * r.nq : nullptr;
       double* sn = (NS && st_new) ? st_new + soff + e * NS * r.nq : nullptr;
       double so_zero[7 * 27] = {0};
+      double Rabs[81] = {0};
+      tl_elem_abs = R_abs ? Rabs : nullptr;
       int rc = orc_element(elem_types[b], phys, props, xel, uel, so ? so : so_zero, sn, R_full ? Re : nullptr,
                            Kstore ? Ke : nullptr);
+      tl_elem_abs = nullptr;
       if (rc) err = rc;
       if (R_full) {
         for (int f = 0; f < NF; ++f)
@@ -699,6 +728,13 @@ int orc_assemble(int nblocks, const int* elem_types, const i64* ne, const i64* c
             } else {
               *dst += v;
             }
+            if (R_abs) {
+              double* da = &R_abs[NF * (c[a] - 1) + f];
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+              *da += Rabs[NF * a + f];
+            }
           }
       }
       if (Kstore) std::memcpy(Kstore + koff + e * NDOF * NDOF, Ke, sizeof(double) * NDOF * NDOF);
@@ -709,6 +745,14 @@ int orc_assemble(int nblocks, const int* elem_types, const i64* ne, const i64* c
   }
   return err;
 }
+
+// With a non-null `out` (NF * NN doubles), the next orc_assemble calls with a
+// residual also write out[dof] = the sum over the dof's elements of the
+// magnitudes of the terms its residual entry sums (see tl_elem_abs): the scale
+// against which the rounding of an assembled residual entry is measured, whose
+// value results from cancelling sums (of element forces near equilibrium, and
+// inside the stress itself).  NULL turns it off.
+void orc_set_abs_output(double* out) { g_abs_out = out; }
 
 // Quadrature-point count of an element type (0 if unknown).
 int orc_num_qp(int et) { return ref_of(et).nq; }

@@ -52,6 +52,7 @@ def lib():
             "orc_max_threads": (C.c_int, []),
             "orc_set_reference": (C.c_int, [C.c_int, C.c_int, vp, vp, vp]),
             "orc_clear_reference": (None, [C.c_int]),
+            "orc_set_abs_output": (None, [vp]),
         }
         for k, (r, a) in sig.items():
             f = getattr(_lib, k)
@@ -144,10 +145,13 @@ def element(elem: str, phys: str, props, xel, uel, st_old=None, want_state=False
 
 
 def assemble(blocks, coords, phys: str, props, U, st_old=None, st_new=None, *, want_r=True, want_k=True,
-             threads: int = 1):
+             threads: int = 1, abs_out=None):
     """The block loop of assemble_vector!/assemble_matrix! (Assemblers.jl:402-432).
     Returns (R_full, Kstore) with Kstore in the reference's element slot order
-    (K_el.data, column-major per element)."""
+    (K_el.data, column-major per element).  abs_out (NF * NN doubles), if given,
+    receives per dof the summed magnitudes of the terms its residual entry is
+    formed from (sum over elements and points of JxW |grad N_a| |P| for
+    mechanics), the scale that bounds the rounding of the entry."""
     types = np.array([ELEM[t] for t, _ in blocks], dtype=np.int32)
     ne = np.array([c.shape[0] for _, c in blocks], dtype=np.int64)
     conn = np.ascontiguousarray(np.concatenate([c.ravel() for _, c in blocks]), dtype=np.int64)
@@ -159,8 +163,14 @@ def assemble(blocks, coords, phys: str, props, U, st_old=None, st_new=None, *, w
     nk = int(sum(n * (nf * NNPE[t]) ** 2 for t, n in zip(types, ne)))
     K = np.empty(nk) if want_k else None
     props = np.ascontiguousarray(props, dtype=np.float64)
-    rc = lib().orc_assemble(len(blocks), _p(types), _p(ne), _p(conn), dim, _p(coords), PHYS[phys], _p(props), _p(U),
-                            _p(st_old), _p(st_new), nn, _p(R), _p(K), threads)
+    if abs_out is not None:
+        assert abs_out.dtype == np.float64 and abs_out.size == nf * nn and abs_out.flags.c_contiguous
+    lib().orc_set_abs_output(_p(abs_out))
+    try:
+        rc = lib().orc_assemble(len(blocks), _p(types), _p(ne), _p(conn), dim, _p(coords), PHYS[phys], _p(props),
+                                _p(U), _p(st_old), _p(st_new), nn, _p(R), _p(K), threads)
+    finally:
+        lib().orc_set_abs_output(None)
     if rc:
         raise RuntimeError(f"orc_assemble failed ({rc})")
     return R, K

@@ -166,3 +166,63 @@ def test_training_gains_over_untrained_network(fec):
     errs_cc, plast_cc, fb_cc = runs["trained_loose_cuda_cores"]
     assert plast_cc == plast
     assert max(e[0] for e in errs) <= 1.5 * max(e[0] for e in errs_cc) + 1e-4
+
+
+def test_closure_at_configured_operating_point(fec):
+    """The learned closure at its configured operating point: trained on 5M
+    return-map samples (250k strain paths x 20 steps, seed 4, 60 epochs), BF16
+    weights on the tensor cores, fallback to the exact return map where the
+    consistency residual exceeds 1e-4 sigma_y.  Along the 20-step uniaxial path
+    to 1% strain (state carried, FP32-element arithmetic) the stress-derived
+    outputs -- residual and tangent -- stay within 1e-3 of exact FP64 assembly
+    at every step, the configuration's stress bar, as does the network's
+    held-out stress error; the plastic state, which integrates the network's
+    plastic-strain increments over the path, within 1e-2.  The fallback rate is
+    recorded: most plastic points fall back at this tolerance, since the BF16
+    network's stress error (~2e-4) is above it."""
+    torch = _torch()
+    from fec_gb300 import closure
+    from fec_gb300.workloads import uniaxial_bcs, uniaxial_inputs
+    X, Y, plastic = closure.generate_samples(PROPS, n_paths=250_000, steps=20, seed=4)
+    assert X.shape[0] == 5_000_000
+    X, Y = X[plastic], Y[plastic]
+    ntr = int(0.95 * X.shape[0])
+    trained = closure.train(X[:ntr], Y[:ntr], epochs=60, batch=4096, lr=5e-3)
+    val = closure.validation_errors(trained, PROPS, X[ntr:], Y[ntr:])
+    n = 24
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n + 1,) * 3)
+
+    def system(physics, precision):
+        asm = fec.SparseMatrixAssembler(fec.VectorFunction(fec.FunctionSpace(mesh), "u"), device=0,
+                                        precision=precision)
+        p = fec.create_parameters(mesh, asm, physics, dirichlet_bcs=uniaxial_bcs())
+        return asm, p
+
+    cl = closure.J2Closure(*PROPS, closure.TrainedClosure(trained.params, trained.normalisation, [], 1e-4))
+    a_cl, p_cl = system(cl, "fp32_element")
+    a_x, p_x = system(fec.J2Plasticity(*PROPS), "fp64")
+    inputs = uniaxial_inputs(mesh.nodal_coords, a_x.dof.unknown_dofs, p_x.bc_dofs.cpu().numpy(), 20)
+    worst = {"residual": 0.0, "nzval": 0.0, "state": 0.0}
+    for Uu, bc in inputs:
+        Uu_d, bc_d = torch.from_numpy(Uu).cuda(), torch.from_numpy(bc).cuda()
+        p_x.bc_vals = bc_d
+        p_cl.bc_vals = bc_d
+        Rx, Kx = fec.assemble_residual_and_stiffness(a_x, Uu_d, p_x)
+        Rx, nzx, sx = Rx.clone(), Kx.nzval.clone(), p_x.state_new.clone()
+        Rc, Kc = fec.assemble_residual_and_stiffness(a_cl, Uu_d, p_cl)
+        for k, a, b in (("residual", Rc, Rx), ("nzval", Kc.nzval, nzx), ("state", p_cl.state_new, sx)):
+            nb = float(b.norm())
+            if nb > 0:
+                worst[k] = max(worst[k], float((a - b).norm()) / nb)
+        p_x.swap_states()
+        p_cl.swap_states()
+    torch.cuda.synchronize()
+    plast, fb = closure.J2Closure.stats(a_cl)
+    rate = fb / max(plast, 1)
+    print("held-out validation:", val, "path error vs exact FP64:", worst, "plastic points", plast,
+          "fallback rate", rate)
+    assert plast > 0 and 0.0 <= rate < 1.0          # some plastic points are served by the network
+    assert val["bf16_params"]["stress"] <= 1e-3, val    # the 1e-3 stress bar of the configuration
+    assert worst["residual"] <= 1e-3 and worst["nzval"] <= 1e-3, worst
+    assert worst["state"] <= 1e-2, worst
+    assert fec.load_library().fec_tensor_core_status(0) == 0
