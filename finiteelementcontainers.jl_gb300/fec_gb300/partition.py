@@ -134,16 +134,8 @@ class PartitionedAssembler:
             gvals[d - 1] = [bc.func(mesh.nodal_coords[n - 1], 0.0) for n in nodes]
         self.local = []
         for part in self.parts:
-            asm = SparseMatrixAssembler(_var(part.mesh, nf), device=device, precision=precision)
-            p = create_parameters(part.mesh, asm, physics)
-            ldd = np.nonzero(part.dof_to_unknown < 0)[0] + 1
-            update_dofs(asm.dof, ldd)
-            asm._push_dofs()
-            gdofs = (nf * (part.nodes[:, None] - 1) + np.arange(nf)[None, :]).ravel()
-            p.bc_dofs = torch.as_tensor(ldd, dtype=torch.int64).to(dev)
-            p.bc_vals = torch.as_tensor(gvals[gdofs[ldd - 1]], dtype=torch.float64).to(dev)
-            lcp, lrv = asm.pattern()
-            part.kmap = local_pattern_map(part, lcp, lrv, self.colptr, self.rowval)
+            asm, p = local_assembler(part, physics, gvals, self.colptr, self.rowval, device=device,
+                                     precision=precision)
             self.local.append((asm, p, torch.from_numpy(part.unknown_l2g).to(dev),
                                torch.from_numpy(part.kmap).to(dev)))
         self.R = torch.zeros(self.dof.unknown_dofs.size, dtype=torch.float64, device=dev)
@@ -159,6 +151,29 @@ class PartitionedAssembler:
             self.R.index_add_(0, l2g, R_l)
             self.nzval.index_add_(0, kmap, K_l.nzval)
         return self.R, self.nzval
+
+
+def local_assembler(part: Part, physics, dirichlet_values: np.ndarray, colptr: np.ndarray, rowval: np.ndarray, *,
+                    device: int = 0, precision: str = "fp64"):
+    """A part's own assembler and parameters on `device`: its elements over its
+    local numbering, its local unknowns (the global Dirichlet dofs among its
+    nodes stay Dirichlet, with their global values), and part.kmap set from its
+    pattern.  Its assemblies take the part's unknowns,
+    Uu_global[part.unknown_l2g]."""
+    import torch
+    nf = part.dof_to_unknown.size // part.nodes.size
+    asm = SparseMatrixAssembler(_var(part.mesh, nf), device=device, precision=precision)
+    p = create_parameters(part.mesh, asm, physics)
+    ldd = np.nonzero(part.dof_to_unknown < 0)[0] + 1
+    update_dofs(asm.dof, ldd)
+    asm._push_dofs()
+    gdofs = (nf * (part.nodes[:, None] - 1) + np.arange(nf)[None, :]).ravel()
+    dev = f"cuda:{device}"
+    p.bc_dofs = torch.as_tensor(ldd, dtype=torch.int64).to(dev)
+    p.bc_vals = torch.as_tensor(dirichlet_values[gdofs[ldd - 1]], dtype=torch.float64).to(dev)
+    lcp, lrv = asm.pattern()
+    part.kmap = local_pattern_map(part, lcp, lrv, colptr, rowval)
+    return asm, p
 
 
 def owned_positions(part: Part, colptr: np.ndarray) -> tuple[np.ndarray, np.ndarray]:

@@ -1,6 +1,7 @@
 """Partitioned assembly: the part/ghost bookkeeping on the host, the multi-rank
-exchange with 2 gloo ranks on CPU (local values from the oracle), and the
-one-GPU partitioned assembler against the single-part assembly."""
+exchange with 2 gloo ranks (on CPU with the oracle's part values, the exchange
+logic alone; and with each rank assembling its part through the library on the
+GPU), and the one-GPU partitioned assembler against the single-part assembly."""
 import os
 import socket
 
@@ -137,3 +138,63 @@ def test_partitioned_assembler_on_one_gpu(fec, orc, nparts):
     assert np.array_equal(K1.colptr, pa.colptr) and np.array_equal(K1.rowval, pa.rowval)
     assert max(rel_err(R2.cpu().numpy(), R1.cpu().numpy())) <= 1e-12
     assert max(rel_err(nz2.cpu().numpy(), K1.nzval.cpu().numpy())) <= 1e-12
+
+
+def _gpu_worker(rank, world, port, out_path):
+    """One rank: its part assembled through the product path on the GPU (each
+    rank its own process and context on device 0, no kernel waits on another
+    rank), then the host exchange to the owners over gloo."""
+    import sys
+    sys.path[:0] = [os.path.join(ROOT, "finiteelementcontainers.jl_gb300"), ROOT, os.path.join(ROOT, "tests")]
+    import torch
+    import torch.distributed as dist
+    import fec_gb300 as fec
+    from fec_gb300 import partition
+    from oracle import oracle as orc
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        mesh, unknown, dtu, colptr, rowval, parts, U = _problem(fec, orc, world)
+        part = parts[rank]
+        asm, p = partition.local_assembler(part, fec.NeoHookean.from_youngs(1.0, 0.3), np.zeros(U.size), colptr,
+                                           rowval, device=0)
+        Uu = torch.from_numpy(U[unknown - 1][part.unknown_l2g].copy()).cuda()
+        R_l, K_l = fec.assemble_residual_and_stiffness(asm, Uu, p)
+        torch.cuda.synchronize()
+        cols, Rown, pos, nzown = partition.exchange_to_owners(part, R_l.cpu().numpy(), K_l.nzval.cpu().numpy(),
+                                                              rank, world, colptr)
+        R = torch.zeros(unknown.size, dtype=torch.float64)
+        nz = torch.zeros(rowval.size, dtype=torch.float64)
+        R[torch.from_numpy(cols)] = torch.from_numpy(Rown)
+        nz[torch.from_numpy(pos)] = torch.from_numpy(nzown)
+        dist.reduce(R, 0)
+        dist.reduce(nz, 0)
+        if rank == 0:
+            np.savez(out_path, R=R.numpy(), nz=nz.numpy())
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+def test_two_rank_exchange_of_gpu_assembled_parts(fec, orc, tmp_path):
+    """2 gloo ranks, each assembling its part with the library on the GPU: the
+    exchanged global residual and CSC values against the oracle's single-part
+    assembly (<= 1e-12), and bitwise the one-GPU partitioned assembler's."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import torch.multiprocessing as mp
+    from fec_gb300 import partition
+    out = str(tmp_path / "r0.npz")
+    mp.start_processes(_gpu_worker, args=(2, _free_port(), out), nprocs=2, join=True, start_method="spawn")
+    got = np.load(out)
+    mesh, unknown, dtu, colptr, rowval, parts, U = _problem(fec, orc, 2)
+    props = fec.NeoHookean.from_youngs(1.0, 0.3).create_properties()
+    Ro, _, _, nzo = orc.assembled_system(blocks_of(mesh), mesh.nodal_coords, "neohookean", props, U, dtu, unknown)
+    assert max(rel_err(got["R"], Ro)) <= 1e-12 and max(rel_err(got["nz"], nzo)) <= 1e-12
+    bcs = [fec.DirichletBC("u_x", lambda X, t: 0.0, nodeset_name="left")]
+    pa = partition.PartitionedAssembler(mesh, fec.NeoHookean.from_youngs(1.0, 0.3), 2, dirichlet_bcs=bcs)
+    assert np.array_equal(pa.dof.dof_to_unknown, dtu)
+    R2, nz2 = pa.assemble(torch.from_numpy(U[unknown - 1].copy()).cuda())
+    assert np.array_equal(got["R"], R2.cpu().numpy()) and np.array_equal(got["nz"], nz2.cpu().numpy())
