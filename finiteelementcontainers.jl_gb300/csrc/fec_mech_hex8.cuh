@@ -140,7 +140,10 @@ struct Hex8Smem {
   static constexpr int R_XD = R_REFF + REF;
   static constexpr int R_U = R_XD + EPB * 24;
   static constexpr int R_DNX = R_U + EPB * 24;
-  static constexpr int R_JXW = R_DNX + EPB * NQ * 24;
+  // per-element stride of the spatial gradients, padded by 8 words: a warp spans
+  // up to 3 elements reading the same offset, which then fall in distinct banks
+  static constexpr int DNX_STRIDE = NQ * 24 + (sizeof(Real) == 4 ? 8 : 4);
+  static constexpr int R_JXW = R_DNX + EPB * DNX_STRIDE;
   static constexpr int R_P = R_JXW + EPB * NQ;
   static constexpr int R_SCR = R_P + EPB * NQ * 9;
   static constexpr int R_A = (R_SCR + EPB * NQ * SCR + 3) & ~3;     // 16-byte aligned for the vector copy-out
@@ -170,7 +173,7 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_sym_kernel(ElemArgs g) {
   double* s_x = s_x_all + ty * 24;
   Real* s_xd = rb + S::R_XD + ty * 24;
   Real* s_u = rb + S::R_U + ty * 24;
-  Real* s_dNX = rb + S::R_DNX + ty * NQ * 24;
+  Real* s_dNX = rb + S::R_DNX + ty * S::DNX_STRIDE;
   Real* s_jxw = rb + S::R_JXW + ty * NQ;
   Real* s_P = rb + S::R_P + ty * NQ * 9;
   Real* s_scr = rb + S::R_SCR + ty * NQ * SCR;
@@ -353,7 +356,7 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_rows2_kernel(ElemArgs g) {
   double* s_x = s_x_all + ty * 24;
   Real* s_xd = rb + S::R_XD + ty * 24;
   Real* s_u = rb + S::R_U + ty * 24;
-  Real* s_dNX = rb + S::R_DNX + ty * NQ * 24;
+  Real* s_dNX = rb + S::R_DNX + ty * S::DNX_STRIDE;
   Real* s_P = rb + S::R_P + ty * NQ * 9;
   Real* s_scr = rb + S::R_SCR + ty * NQ * SCR;
   Real* s_A = rb + S::R_A + ty * S::A_STRIDE;
@@ -494,7 +497,8 @@ struct Hex8Df64Smem {
   static constexpr int D_REF = 0, D_X = REF, D_U = D_X + EPB * 24;
   static constexpr int N_DOUBLE = D_U + EPB * 24;
   static constexpr int F_DNX = 0;                       // float2 entries, after the doubles
-  static constexpr int F_P = F_DNX + EPB * NQ * 24;
+  static constexpr int DNXS = NQ * 24 + 4;              // per element, padded (distinct banks across elements)
+  static constexpr int F_P = F_DNX + EPB * DNXS;
   static constexpr int F_SCR = F_P + EPB * NQ * 9;
   static constexpr int F_A = (F_SCR + EPB * NQ * SCR2 + 1) & ~1;  // 45 unique tangent entries per point
   static constexpr int A_STRIDE = NQ * 45;
@@ -530,7 +534,7 @@ __device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile,
   const bool live = e < g.ne;
   double* s_x = dbase + S::D_X + ty * 24;
   double* s_u = dbase + S::D_U + ty * 24;
-  const float2* s_dNX = fb + S::F_DNX + ty * NQ * 24;
+  const float2* s_dNX = fb + S::F_DNX + ty * S::DNXS;
   const float2* s_P = fb + S::F_P + ty * NQ * 9;
   const float2* s_scr = fb + S::F_SCR + ty * NQ * SCR2;
   float2* s_A = fb + S::F_A + ty * S::A_STRIDE;
@@ -565,7 +569,7 @@ __device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile,
           for (int a = 0; a < 8; ++a) s = fma(pu[a * 3 + i], dNX[a * 3 + j], s);
           gu[i][j] = s;
         }
-      float2* pdNX = fb + S::F_DNX + el * NQ * 24;
+      float2* pdNX = fb + S::F_DNX + el * S::DNXS;
 #pragma unroll
       for (int m = 0; m < 24; ++m) pdNX[q * 24 + m] = df64_split(dNX[m]);  // dNX dies before the model
       const double* so = NS ? g.state_old + (ep * NQ + q) * NS : nullptr;
@@ -700,8 +704,11 @@ template <class Model>
 struct Layout {
   static constexpr int X = 0;                           // double [EPB][24] coordinates
   static constexpr int U = X + EPB * 24 * 8;            // double [EPB][24] displacements
-  static constexpr int DNX = U + EPB * 24 * 8;          // float2 [EPB][NQ][24] spatial gradients
-  static constexpr int P = DNX + EPB * NQ * 24 * 8;     // float2 [EPB][NQ][9] JxW P
+  // float2 [EPB][DNXS] spatial gradients ([NQ][24] per element, padded by 4 float2 so
+  // that the two elements of a consumer warp read the same offset from distinct banks)
+  static constexpr int DNXS = NQ * 24 + 4;
+  static constexpr int DNX = U + EPB * 24 * 8;
+  static constexpr int P = DNX + EPB * DNXS * 8;        // float2 [EPB][NQ][9] JxW P
   static constexpr int SCR = P + EPB * NQ * 9 * 8;      // float2 [EPB][NQ][SCR2] tangent scratch
   static constexpr int A = SCR + EPB * NQ * Model::SCR2 * 8;  // float2 [EPB][NQ][45] JxW A, unique entries
   static constexpr int STAGE = ((A + EPB * NQ * 45 * 8) + 15) / 16 * 16;
@@ -764,7 +771,7 @@ __global__ void __launch_bounds__(ws::NTHR, 1) mech_hex8_df64_ws_kernel(ElemArgs
             gu[i][j] = sum;
           }
         const int pt = el * NQ + q;
-        float2* pdNX = reinterpret_cast<float2*>(st + Lay::DNX) + pt * 24;
+        float2* pdNX = reinterpret_cast<float2*>(st + Lay::DNX) + el * Lay::DNXS + q * 24;
 #pragma unroll
         for (int m = 0; m < 24; ++m) pdNX[m] = df64_split(dNX[m]);  // dNX dies before the model
         const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
@@ -795,7 +802,7 @@ __global__ void __launch_bounds__(ws::NTHR, 1) mech_hex8_df64_ws_kernel(ElemArgs
     named_sync(BAR_FULL + buf, NTHR);  // tile k is in stage buf
     const int64_t e0 = tile * EPB, e = e0 + el;
     const bool live = e < g.ne;
-    const float2* s_dNX = reinterpret_cast<const float2*>(st + Lay::DNX) + el * NQ * 24;
+    const float2* s_dNX = reinterpret_cast<const float2*>(st + Lay::DNX) + el * Lay::DNXS;
     const float2* s_P = reinterpret_cast<const float2*>(st + Lay::P) + el * NQ * 9;
     const float2* s_scr = reinterpret_cast<const float2*>(st + Lay::SCR) + el * NQ * SCR2;
     float2* s_A = reinterpret_cast<float2*>(st + Lay::A) + el * NQ * 45;
