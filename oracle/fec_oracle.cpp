@@ -577,10 +577,11 @@ extern "C" {
 // Re[NDOF]; Ke[NDOF*NDOF] column-major like StaticArrays' K_el.data:
 // Ke[r + NDOF*c] = dR_r / du_c.  Either output may be null.
 // When set (per thread, by orc_assemble), orc_element also accumulates into it,
-// per element dof, the magnitude of the terms its residual entry sums:
-// sum_q JxW |grad N_a| (|grad u| + |N_a f|) for Poisson, sum_q JxW |grad N_a|_1 |P|_F
-// for mechanics -- a bound on every product the entry is formed from, so
-// that c eps times it bounds the rounding of any FP64 evaluation of the entry.
+// per element dof, the magnitude of the terms its residual entry is formed
+// from, down to the nodal values: sum_q JxW |grad N_a| (|grad u| + sum_b |u_b
+// grad N_b|) + |N_a f| for Poisson, sum_q JxW |grad N_a|_1 (|P|_F + |A|_F |sum_b
+// u_b (x) grad N_b|_F) for mechanics -- so that c eps times it bounds the
+// rounding of any FP64 evaluation of the entry from the same nodal values.
 thread_local double* tl_elem_abs = nullptr;
 
 int orc_element(int et, int phys, const double* props, const double* xel, const double* uel,
@@ -608,9 +609,13 @@ int orc_element(int et, int phys, const double* props, const double* xel, const 
           double s = 0;
           for (int d = 0; d < D; ++d) s += gu[d] * m.dNX[a][d];
           Re[a] += m.JxW * (s - r.N[q * A + a] * f);
-          if (tl_elem_abs) {
+          if (tl_elem_abs) {  // |grad u| and the sum of nodal terms it is formed from
             double sa = 0;
-            for (int d = 0; d < D; ++d) sa += std::fabs(gu[d] * m.dNX[a][d]);
+            for (int d = 0; d < D; ++d) {
+              double g = 0;
+              for (int b = 0; b < A; ++b) g += std::fabs(uel[b] * m.dNX[b][d]);
+              sa += std::fabs(m.dNX[a][d]) * (std::fabs(gu[d]) + g);
+            }
             tl_elem_abs[a] += std::fabs(m.JxW) * (sa + std::fabs(r.N[q * A + a] * f));
           }
         }
@@ -631,9 +636,10 @@ int orc_element(int et, int phys, const double* props, const double* xel, const 
         double F[3][3];
         for (int i = 0; i < 3; ++i)
           for (int j = 0; j < 3; ++j) F[i][j] = gu[i][j] + (i == j ? 1.0 : 0.0);
-        neohookean_PA(F, props[0], props[1], P9, Ke ? A81 : nullptr);
+        neohookean_PA(F, props[0], props[1], P9, (Ke || tl_elem_abs) ? A81 : nullptr);
       } else if (phys == PHYS_J2) {
-        j2_update(gu, props, st_old + 7 * q, st_new ? st_new + 7 * q : nullptr, P9, Ke ? A81 : nullptr);
+        j2_update(gu, props, st_old + 7 * q, st_new ? st_new + 7 * q : nullptr, P9,
+                  (Ke || tl_elem_abs) ? A81 : nullptr);
       } else {
         return -3;
       }
@@ -646,9 +652,20 @@ int orc_element(int et, int phys, const double* props, const double* xel, const 
             Re[a * 3 + i] += m.JxW * s;
           }
       if (Re && tl_elem_abs) {
-        double pn = 0;
+        // |P| plus the stress the rounding of grad u can move: grad u is a sum of
+        // nodal terms u_a (x) grad N_a much larger than itself where u is large
+        // against its variation over an element (u ~ eps x cancels by ~x/h), and
+        // |A| |that sum| bounds the resulting change of P
+        double pn = 0, an = 0, gn = 0;
         for (int k = 0; k < 9; ++k) pn += P9[k] * P9[k];
-        pn = std::sqrt(pn);
+        for (int k = 0; k < 81; ++k) an += A81[k] * A81[k];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            double g = 0;
+            for (int a = 0; a < A; ++a) g += std::fabs(uel[a * 3 + i] * m.dNX[a][j]);
+            gn += g * g;
+          }
+        pn = std::sqrt(pn) + std::sqrt(an) * std::sqrt(gn);
         for (int a = 0; a < A; ++a) {
           const double g1 = std::fabs(m.dNX[a][0]) + std::fabs(m.dNX[a][1]) + std::fabs(m.dNX[a][2]);
           for (int i = 0; i < 3; ++i) tl_elem_abs[a * 3 + i] += std::fabs(m.JxW) * g1 * pn;

@@ -38,12 +38,14 @@ def rel_err(a, b, floor: float = FLOOR64) -> tuple[float, float, float]:
 
 def residual_err(a, b, abs_sum, floor: float = FLOOR64) -> tuple[float, float, float]:
     """rel_err for an assembled residual.  Its entries come out of cancelling
-    sums -- element forces near equilibrium, and stress components that vanish
-    (uniaxial stress) -- so the entry-wise term holds entry i to the bar
-    relative to max(|b_i|, floor * abs_sum_i), with abs_sum_i the summed
-    magnitude of every term the entry is formed from (the oracle's abs_out):
-    relative to the entry itself, with an absolute floor of bar * floor
-    (1e-14 for FP64) times the terms it sums."""
+    sums -- element forces near equilibrium, stress components that vanish
+    (uniaxial stress), and displacement gradients formed from nodal
+    displacements much larger than their differences -- so the entry-wise term
+    holds entry i to the bar relative to max(|b_i|, floor * abs_sum_i), with
+    abs_sum_i the summed magnitude of every term the entry is formed from,
+    down to the nodal values (the oracle's abs_out): relative to the entry
+    itself, with an absolute floor of bar * floor (1e-14 for FP64) times the
+    terms it sums."""
     a = np.asarray(a, dtype=np.float64); b = np.asarray(b, dtype=np.float64)
     m, n2, _ = rel_err(a, b)
     if not b.size:

@@ -356,7 +356,9 @@ def test_pipelined_gather_matches_node_gather(fec, case):
     if case == "batch":
         mesh = batching.box_batch([3, 1, 5, 2, 7]).mesh
     else:
-        mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (13, 11, 9))
+        # a cube: the reference's structured hex generator (and so its mirror) is only
+        # consistent for equal counts (StructuredMesh.jl:433-449)
+        mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 2.0, 1.5), (11, 11, 11))
     if case.startswith("j2"):
         phys = fec.J2Plasticity(200.0, 0.3, 0.25, 2.0)
         U = 3.0 * stretch_field(mesh.nodal_coords, seed=2, noise=1e-4, diag=(1.004, 0.999, 0.999)).ravel()
