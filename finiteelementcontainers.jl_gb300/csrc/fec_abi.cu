@@ -30,6 +30,8 @@ using fec::GatherArgs;
 namespace {
 
 thread_local int g_create_status = FEC_OK;
+// SM clocks the element kernels' bounded waits allow (0: their default, about 1 s)
+long long g_wait_budget = 0;
 thread_local char g_create_msg[256] = "";
 
 struct DevBuf {
@@ -904,6 +906,7 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     ea.U = U;
     ea.ref = static_cast<const double*>(c->d_ref.p) + c->ref_off[b];
     ea.wait_err = wait_err;
+    ea.wait_budget = g_wait_budget;
     for (int i = 0; i < 8; ++i) ea.props[i] = B.props[i];
     const int ns = num_states_of(B.physics);
     ea.state_old = ns ? state_old + st_off : nullptr;
@@ -1063,6 +1066,7 @@ int fec_assemble_action(fec_ctx* c, int precision, double t, double dt, const do
     ea.U = U;
     ea.ref = static_cast<const double*>(c->d_ref.p) + c->ref_off[b];
     ea.wait_err = wait_err;
+    ea.wait_budget = g_wait_budget;
     for (int i = 0; i < 8; ++i) ea.props[i] = B.props[i];
     const int ns = num_states_of(B.physics);
     ea.state_old = ns ? state_old + st_off : nullptr;
@@ -1169,9 +1173,8 @@ int fec_check_finite(fec_ctx* c, const double* R_u, const double* nzval, int64_t
   FEC_CUDA(c, cudaStreamSynchronize(s));
   const unsigned long long none = ~0ull;
   if (first_bad) *first_bad = h[0] != none ? int64_t(h[0]) : (h[1] != none ? int64_t(h[1]) : -1);
-  if (h[0] != none) return fail(c, FEC_ERR_NONFINITE, "residual entry %lld is not finite", (long long)h[0]);
-  if (h[1] != none) return fail(c, FEC_ERR_NONFINITE, "nzval entry %lld is not finite", (long long)h[1]);
-  // a bounded wait in an element kernel that gave up leaves outputs that may be wrong however finite they are
+  // a bounded wait in an element kernel that gave up leaves outputs that may be wrong however finite
+  // they are: reported first, as the cause
   int* wait_err = nullptr;
   FEC_CUDA(c, fec::wait_error_flag(&wait_err));
   int werr = 0;
@@ -1180,6 +1183,8 @@ int fec_check_finite(fec_ctx* c, const double* R_u, const double* nzval, int64_t
     return fail(c, FEC_ERR_DEVICE,
                 "an element kernel gave up a bounded wait (tensor-core MMA or bulk table copy); the outputs are "
                 "invalid until fec_tensor_core_status(1) clears the flag");
+  if (h[0] != none) return fail(c, FEC_ERR_NONFINITE, "residual entry %lld is not finite", (long long)h[0]);
+  if (h[1] != none) return fail(c, FEC_ERR_NONFINITE, "nzval entry %lld is not finite", (long long)h[1]);
   return ok(c);
 }
 
@@ -1223,6 +1228,12 @@ int fec_closure_stats(fec_ctx* c, int64_t* plastic, int64_t* fallbacks, int rese
   if (h[2]) return fail(c, FEC_ERR_DEVICE, "closure kernel: a wait on the tensor cores gave up (results invalid)");
   if (reset) FEC_CUDA(c, cudaMemset(c->d_cl_cnt.p, 0, 2 * sizeof(unsigned long long)));
   return ok(c);
+}
+
+int fec_set_wait_budget(long long clocks) {
+  if (clocks < 0) return FEC_ERR_ARG;
+  g_wait_budget = clocks;
+  return FEC_OK;
 }
 
 int fec_set_profiling(fec_ctx* c, int on) {
@@ -1452,6 +1463,7 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
     ea.U = U;
     ea.ref = static_cast<const double*>(c->d_ref.p) + c->ref_off[b];
     ea.wait_err = wait_err;
+    ea.wait_budget = g_wait_budget;
     for (int i = 0; i < 8; ++i) ea.props[i] = B.props[i];
     const int ns = num_states_of(B.physics);
     ea.state_old = ns ? state_old + st_off : nullptr;

@@ -103,6 +103,9 @@ __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err)
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + S_TSLOT);
   uint32_t ph[2] = {0u, 0u};
   bool failed = false;
+  // the main waits' budget (settable, fec_set_wait_budget); the drain after a
+  // timeout always allows the full WAIT_BUDGET
+  const long long budget = g.wait_budget > 0 ? g.wait_budget : WAIT_BUDGET;
   // this thread's row of C: (i, b, k)
   const int row = tid, ri = row / ND, rb = (row % ND) / 3, rk = row % 3;
 
@@ -175,7 +178,7 @@ __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err)
       if (c >= 2) {
         // the phase flips only when every thread saw it complete, so that after a
         // timeout ph[] still names the phases whose MMAs may be in flight
-        const bool ok = mbar_wait(&bar[buf], ph[buf], WAIT_BUDGET);
+        const bool ok = mbar_wait(&bar[buf], ph[buf], budget);
         if (__syncthreads_or(!ok)) {
           failed = true;
           break;
@@ -224,8 +227,8 @@ __global__ void __launch_bounds__(NTHR, 2) hex27_tc_kernel(ElemArgs g, int* err)
     if (failed) break;
     // the last two chunks' barriers (chunk 12 on buffer 0, chunk 13 on buffer 1)
     {
-      const bool ok0 = mbar_wait(&bar[0], ph[0], WAIT_BUDGET);
-      const bool ok1 = mbar_wait(&bar[1], ph[1], WAIT_BUDGET);
+      const bool ok0 = mbar_wait(&bar[0], ph[0], budget);
+      const bool ok1 = mbar_wait(&bar[1], ph[1], budget);
       if (__syncthreads_or(!(ok0 && ok1))) {
         failed = true;
         break;

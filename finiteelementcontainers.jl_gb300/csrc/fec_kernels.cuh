@@ -66,6 +66,7 @@ struct ElemArgs {
   void* Re;                 // block base, Real[ne][NDOF]
   const void* closure;      // learned-closure data (ClosureArgs) for the physics that uses one
   int* wait_err;            // set to 1 by a bounded wait that gave up (device flag; may be null)
+  long long wait_budget;    // SM clocks a bounded wait allows before giving up (0: the default, ~1 s)
 };
 
 // ---------------------------------------------------------------------------

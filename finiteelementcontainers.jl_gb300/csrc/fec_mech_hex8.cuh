@@ -27,12 +27,12 @@ namespace fec {
 // doubles) and the connectivity of the CTA's `nlive` elements into shared
 // memory with bulk (TMA) copies that complete on an mbarrier.  Connectivity of
 // a block that does not start on a 16-byte boundary falls back to plain loads.
-// A wait that gives up (about 1 s of SM clocks) sets *err, waits once more
-// (bounded) so that no copy lands after the CTA has moved on, and then loads
-// with plain loads.  Ends with a barrier.
+// A wait that gives up (after `budget` SM clocks, 0: about 1 s) sets *err,
+// waits once more (about 1 s) so that no copy lands after the CTA has moved
+// on, and then loads with plain loads.  Ends with a barrier.
 __device__ __forceinline__ void stage_hex8_tables(const double* gref, double* s_ref, const int32_t* gconn, int nlive,
                                                   int* s_conn, uint64_t* bar, int tid, int nthr, int* err,
-                                                  bool allow_bulk = true) {
+                                                  long long budget, bool allow_bulk = true) {
   constexpr int NREF = RefLayout<1>::SIZE;
   const bool bulk =
       allow_bulk && ((reinterpret_cast<uintptr_t>(gref) | reinterpret_cast<uintptr_t>(gconn)) & 15) == 0;
@@ -48,7 +48,7 @@ __device__ __forceinline__ void stage_hex8_tables(const double* gref, double* s_
       tc::bulk_g2s(s_ref, gref, NREF * 8, bar);
       tc::bulk_g2s(s_conn, gconn, uint32_t(nlive * 32), bar);
     }
-    const bool landed = tc::mbar_wait(bar, 0, 2000000000LL);
+    const bool landed = tc::mbar_wait(bar, 0, budget > 0 ? budget : 2000000000LL);
     if (__syncthreads_or(!landed)) {
       if (tid == 0 && err) atomicExch(err, 1);
       tc::mbar_wait(bar, 0, 2000000000LL);
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(EPB * 12) mech_hex8_rows2_kernel(ElemArgs g) {
   {
     const int64_t left = g.ne - e0;
     stage_hex8_tables(g.ref, s_ref, g.conn + e0 * 8, left < EPB ? int(left) : EPB, s_conn_all,
-                      reinterpret_cast<uint64_t*>(s_conn_all + EPB * 8), tid, nthr, g.wait_err);
+                      reinterpret_cast<uint64_t*>(s_conn_all + EPB * 8), tid, nthr, g.wait_err, g.wait_budget);
   }
   for (int i = tid; i < L::SIZE; i += nthr) s_reff[i] = Real(s_ref[i]);
   if (live) {
@@ -543,7 +543,8 @@ __device__ __forceinline__ void hex8_df64_tile(const ElemArgs& g, unsigned tile,
   {
     const int64_t left = g.ne - e0;
     stage_hex8_tables(g.ref, s_ref, g.conn + e0 * 8, left < EPB ? int(left) : EPB, s_conn_all,
-                      reinterpret_cast<uint64_t*>(s_conn_all + EPB * 8), tid, nthr, g.wait_err, BULK);
+                      reinterpret_cast<uint64_t*>(s_conn_all + EPB * 8), tid, nthr, g.wait_err, g.wait_budget,
+                      BULK);
   }
   if (live) {
     const int a = tx / 3, d = tx % 3;

@@ -62,6 +62,7 @@ SIGNATURES = {
     "fec_cg_solve": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int),
                                C.POINTER(C.c_double), _vp]),
     "fec_tensor_core_status": (C.c_int, [C.c_int]),
+    "fec_set_wait_budget": (C.c_int, [C.c_longlong]),
     "fec_mlp_gradient": (C.c_int, [_vp, _vp, _vp, C.c_int64, _vp, C.c_int64, _vp, _vp, _vp]),
     "fec_mlp_adam_step": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int64, C.c_int64, C.c_float, _vp, C.c_int64, _vp,
                                     _vp]),

@@ -200,12 +200,13 @@ int fec_assemble_action(fec_ctx* ctx, int precision, double t, double dt, const 
 int fec_cg_solve(fec_ctx* ctx, const double* nzval_dev, const double* b_dev, double* x_dev, int max_iter,
                  double rtol, int preconditioner, int* iterations, double* rel_residual, void* stream);
 
-/* Scans assembled outputs (either may be NULL) for NaN/Inf: FEC_OK, or
- * FEC_ERR_NONFINITE with the first offending index (residual first, then nzval;
- * -1 if none) and a message naming the array; then FEC_ERR_DEVICE if an element
+/* Checks assembled outputs (either may be NULL): FEC_ERR_DEVICE if an element
  * kernel gave up a bounded wait (the flag of fec_tensor_core_status, not
- * cleared here).  Synchronises the stream.  The boundary's output check; the
- * reference does not check. */
+ * cleared here; the outputs are then not to be trusted), else FEC_ERR_NONFINITE
+ * if they hold NaN/Inf, with the first offending index (residual first, then
+ * nzval; -1 if none) and a message naming the array, else FEC_OK.
+ * Synchronises the stream.  The boundary's output check; the reference does
+ * not check. */
 int fec_check_finite(fec_ctx* ctx, const double* R_u_dev, const double* nzval_dev, int64_t* first_bad,
                      void* stream);
 
@@ -323,6 +324,14 @@ int fec_autotune_report(char* buf, size_t len);
  * clears the flag.  fec_check_finite reports the same flag.  Synchronous.  No
  * counterpart in the reference. */
 int fec_tensor_core_status(int reset);
+/* SM clocks the element kernels' bounded waits allow before they give up:
+ * the main waits of the hex27 tensor-core kernel (hex27 FP32-element) and the
+ * hex8 kernels' wait on their bulk table copy (FEC_HEX8_DF64=tile and the
+ * FP32-element hex8 kernel).  0 (the default) is about one second.  The drain
+ * that follows a timeout always allows the full second.  Process-wide; for
+ * testing the timeout path on operations that complete anyway.  No
+ * counterpart in the reference. */
+int fec_set_wait_budget(long long clocks);
 int fec_sizes(const fec_ctx* ctx, int64_t* num_nodes, int64_t* num_elems, int64_t* num_unknowns, int64_t* nnz,
               int64_t* state_len);
 

@@ -382,3 +382,58 @@ def test_pipelined_gather_matches_node_gather(fec, case):
         finally:
             del os.environ["FEC_GATHER_PIPE"]
     assert np.array_equal(out["1"][0], out["0"][0]) and np.array_equal(out["1"][1], out["0"][1])
+
+
+def test_bounded_waits_report_and_drain(fec):
+    """The element kernels' bounded waits, made to give up on operations that
+    complete anyway (a budget of 200 SM clocks, fec_set_wait_budget): the hex8
+    kernel's wait on its bulk table copy reports through the device flag, waits
+    again and falls back to plain loads (the results stay bitwise exact); the
+    hex27 tensor-core kernel reports, drains its MMAs and frees its tensor
+    memory (its results are invalid, but the context stays usable: the next
+    call is exact and the flag stays clear)."""
+    import os
+    torch = _torch()
+    lib = fec.load_library()
+    from fec_gb300 import _lib
+    assert lib.fec_tensor_core_status(1) == 0
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (7, 7, 7))
+    phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+    asm, p = _setup(fec, mesh, "vector", phys)
+    U = stretch_field(mesh.nodal_coords, seed=1).ravel()
+    os.environ["FEC_HEX8_DF64"] = "tile"   # the hex8 kernel that stages by bulk copy
+    try:
+        R0, nz0, _ = _run(fec, asm, p, U)
+        assert lib.fec_tensor_core_status(0) == 0
+        assert lib.fec_set_wait_budget(200) == 0
+        R1, nz1, _ = _run(fec, asm, p, U)
+    finally:
+        lib.fec_set_wait_budget(0)
+        del os.environ["FEC_HEX8_DF64"]
+    assert lib.fec_tensor_core_status(1) == _lib.FEC_ERR_DEVICE    # the waits gave up, and said so
+    assert np.array_equal(R0, R1) and np.array_equal(nz0, nz1)      # ... and the plain loads took over
+    # hex27 FP32-element on the tensor cores
+    mesh27 = fec.meshes.box_hex27((3, 3, 3))
+    asm27, p27 = _setup(fec, mesh27, "vector", phys, precision="fp32_element")
+    U27 = stretch_field(mesh27.nodal_coords, seed=2).ravel()
+    Ra, nza, _ = _run(fec, asm27, p27, U27)
+    assert lib.fec_tensor_core_status(0) == 0
+    assert lib.fec_set_wait_budget(200) == 0
+    try:
+        _run(fec, asm27, p27, U27)
+    finally:
+        lib.fec_set_wait_budget(0)
+    assert lib.fec_tensor_core_status(1) == _lib.FEC_ERR_DEVICE
+    with pytest.raises(fec.FECError) as info:   # the boundary's output check reports it too
+        lib2 = fec.load_library()
+        lib2.fec_set_wait_budget(200)
+        try:
+            fec.assemble_residual_and_stiffness(asm27, torch.from_numpy(U27[asm27.dof.unknown_dofs - 1].copy()).cuda(),
+                                                p27, check_finite=True)
+        finally:
+            lib2.fec_set_wait_budget(0)
+    assert info.value.status == _lib.FEC_ERR_DEVICE
+    assert lib.fec_tensor_core_status(1) == _lib.FEC_ERR_DEVICE
+    Rb, nzb, _ = _run(fec, asm27, p27, U27)
+    assert lib.fec_tensor_core_status(0) == 0
+    assert np.array_equal(Ra, Rb) and np.array_equal(nza, nzb)
