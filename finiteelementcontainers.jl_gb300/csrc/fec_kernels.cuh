@@ -1267,7 +1267,6 @@ __global__ void __launch_bounds__(gp::WPB * 32, MINB) node_gather_hex8_pipe_kern
   using namespace gp;
   using S = Stage<Real>;
   using RT = typename RE<Real>::T;
-  using V4 = typename std::conditional<sizeof(Real) == 4, float4, F2x4>::type;
   extern __shared__ __align__(16) unsigned char smem_g[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t acc_bytes = (size_t(g.acc_stride) * GatherAcc::WORDS * sizeof(float) + 15) / 16 * 16;
@@ -1277,8 +1276,9 @@ __global__ void __launch_bounds__(gp::WPB * 32, MINB) node_gather_hex8_pipe_kern
   const int64_t GW = int64_t(gridDim.x) * WPB;
   const bool wantK = g.nzval != nullptr;
   const BlockInfo& B = g.blk[0];
-  const bool kl = lane < 18;
-  const int ki = lane >> 1, bh = lane & 1;
+  // lane (k, b) < 24 adds column node b's three entries of row component k
+  const bool kl = lane < 24;
+  const int lk = lane >> 3, lb = lane & 7;
 
   NodeMeta cur = load_meta(g, int64_t(blockIdx.x) * WPB + warp, lane);
   issue<Real>(g, cur, stage[0], lane);
@@ -1302,25 +1302,24 @@ __global__ void __launch_bounds__(gp::WPB * 32, MINB) node_gather_hex8_pipe_kern
       __syncwarp();
       if (cur.pipe) {
         const unsigned char* st = stage[s];
-        const int base = (ki / 3) * Ln + (ki % 3);
+        const int base = lk * Ln;
         for (int c = 0; c < cur.cnt; ++c) {
           if (wantR) racc += double(reinterpret_cast<const RT*>(st + S::R_OFF)[c * 3 + lane]);
           if (wantK) {
             if (kl) {
-              const V4 v = *reinterpret_cast<const V4*>(st + (c * 72 + ki * 8 + bh * 4) * sizeof(Real));
-              const uint2 ep = *reinterpret_cast<const uint2*>(st + S::EP_OFF + c * 16 + bh * 8);
-              float2* A2 = reinterpret_cast<float2*>(acc);
-              const int p0 = base + int(ep.x & 0xffffu), p1 = base + int(ep.x >> 16);
-              const int p2 = base + int(ep.y & 0xffffu), p3 = base + int(ep.y >> 16);
-              float2 s0 = A2[p0], s1 = A2[p1], s2 = A2[p2], s3 = A2[p3];
-              s0 = GatherAcc::plus(s0, v.x);
-              s1 = GatherAcc::plus(s1, v.y);
-              s2 = GatherAcc::plus(s2, v.z);
-              s3 = GatherAcc::plus(s3, v.w);
-              A2[p0] = s0;
-              A2[p1] = s1;
-              A2[p2] = s2;
-              A2[p3] = s3;
+              // entries ((k*3 + i)*8 + b) of the element's rows for this node, i = 0..2, go to
+              // the three adjacent positions k*Ln + epos[b] + i
+              const Real* row = reinterpret_cast<const Real*>(st) + c * 72 + lk * 24 + lb;
+              const Real v0 = row[0], v1 = row[8], v2 = row[16];
+              const int p = base + int(reinterpret_cast<const uint16_t*>(st + S::EP_OFF + c * 16)[lb]);
+              float2* A2 = reinterpret_cast<float2*>(acc) + p;
+              float2 s0 = A2[0], s1 = A2[1], s2 = A2[2];
+              s0 = GatherAcc::plus(s0, v0);
+              s1 = GatherAcc::plus(s1, v1);
+              s2 = GatherAcc::plus(s2, v2);
+              A2[0] = s0;
+              A2[1] = s1;
+              A2[2] = s2;
             }
             __syncwarp();
           }
