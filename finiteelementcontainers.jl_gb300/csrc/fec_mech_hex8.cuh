@@ -724,41 +724,6 @@ __device__ __forceinline__ void named_arrive(int id, int n) {
 }
 }  // namespace ws
 
-// One consumer thread's contraction over a tile's points: row (a, I) of its
-// element, I a compile-time constant so that every tangent-entry offset is too.
-template <int I, bool WANT_R, bool WANT_K>
-__device__ __forceinline__ void ws_contract(const float2* __restrict__ s_dNX, const float2* __restrict__ s_P,
-                                            const float2* __restrict__ s_A, int a, float2 (&K)[15], float2& R) {
-  constexpr int NQ = 8;
-  const bool fifth = a < 4;
-#pragma unroll 1
-  for (int q = 0; q < NQ; ++q) {
-    const float2* dNX = s_dNX + q * 24;
-    const float2 g0 = dNX[a * 3], g1 = dNX[a * 3 + 1], g2 = dNX[a * 3 + 2];
-    if (WANT_R) {
-      const float2* P = s_P + q * 9 + I * 3;
-      R = df64_dot3_acc(R, g0, P[0], g1, P[1], g2, P[2]);
-    }
-    if (WANT_K) {
-      const float2* Aq = s_A + q * 45;
-      float2 t[9];
-#pragma unroll
-      for (int kl = 0; kl < 9; ++kl)
-        t[kl] = df64_dot3(g0, Aq[sym_index(3 * I, kl)], g1, Aq[sym_index(3 * I + 1, kl)], g2,
-                          Aq[sym_index(3 * I + 2, kl)]);
-#pragma unroll
-      for (int d = 0; d < 5; ++d) {
-        if (d == 4 && !fifth) break;
-        const int b = (a + d) & 7;
-        const float2 h0 = dNX[b * 3], h1 = dNX[b * 3 + 1], h2 = dNX[b * 3 + 2];
-#pragma unroll
-        for (int kk = 0; kk < 3; ++kk)
-          K[d * 3 + kk] = df64_dot3_acc(K[d * 3 + kk], t[kk * 3], h0, t[kk * 3 + 1], h1, t[kk * 3 + 2], h2);
-      }
-    }
-  }
-}
-
 template <class Model, bool WANT_R, bool WANT_K>
 __global__ void __launch_bounds__(ws::NTHR, 1) mech_hex8_df64_ws_kernel(ElemArgs g) {
   using namespace ws;
@@ -824,12 +789,12 @@ __global__ void __launch_bounds__(ws::NTHR, 1) mech_hex8_df64_ws_kernel(ElemArgs
     return;
   }
 
-  // ---- consumers: thread (i, el, a) owns row tx = (a, i) of element el's K_e; the
-  // row component i is the same across a warp (128 consumers per component), so
-  // the contraction runs specialised on it ----
-  const int c = tid - NPROD, i = c >> 7, el = (c & 127) >> 3, a = c & 7;
-  const int tx = a * 3 + i;
+  // ---- consumers: thread (el, tx) owns row tx = (a, i) of element el's K_e (a warp
+  // spans fewer than two elements, so its gradient loads touch few distinct addresses) ----
+  const int c = tid - NPROD, el = c / 24, tx = c - el * 24;
+  const int a = tx / 3, i = tx % 3;
   const bool fifth = a < 4;
+  const int r1v[3] = {3 * i, 3 * i + 1, 3 * i + 2};
   const float2 z = make_float2(0.f, 0.f);
   for (int k = 0;; ++k) {
     const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
@@ -857,13 +822,33 @@ __global__ void __launch_bounds__(ws::NTHR, 1) mech_hex8_df64_ws_kernel(ElemArgs
 #pragma unroll
     for (int cc = 0; cc < 15; ++cc) K[cc] = z;
     float2 R = z;
-    if (live) {  // warp-uniform branch on the row component
-      if (i == 0)
-        ws_contract<0, WANT_R, WANT_K>(s_dNX, s_P, s_A, a, K, R);
-      else if (i == 1)
-        ws_contract<1, WANT_R, WANT_K>(s_dNX, s_P, s_A, a, K, R);
-      else
-        ws_contract<2, WANT_R, WANT_K>(s_dNX, s_P, s_A, a, K, R);
+    if (live) {
+#pragma unroll 1
+      for (int q = 0; q < NQ; ++q) {
+        const float2* dNX = s_dNX + q * 24;
+        const float2 g0 = dNX[a * 3], g1 = dNX[a * 3 + 1], g2 = dNX[a * 3 + 2];
+        if (WANT_R) {
+          const float2* P = s_P + q * 9 + i * 3;
+          R = df64_dot3_acc(R, g0, P[0], g1, P[1], g2, P[2]);
+        }
+        if (WANT_K) {
+          const float2* Aq = s_A + q * 45;
+          float2 t[9];
+#pragma unroll
+          for (int kl = 0; kl < 9; ++kl)
+            t[kl] = df64_dot3(g0, Aq[sym_index(r1v[0], kl)], g1, Aq[sym_index(r1v[1], kl)], g2,
+                              Aq[sym_index(r1v[2], kl)]);
+#pragma unroll
+          for (int d = 0; d < 5; ++d) {
+            if (d == 4 && !fifth) break;
+            const int b = (a + d) & 7;
+            const float2 h0 = dNX[b * 3], h1 = dNX[b * 3 + 1], h2 = dNX[b * 3 + 2];
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk)
+              K[d * 3 + kk] = df64_dot3_acc(K[d * 3 + kk], t[kk * 3], h0, t[kk * 3 + 1], h1, t[kk * 3 + 2], h2);
+          }
+        }
+      }
     }
     if (WANT_R && live) static_cast<double*>(g.Re)[e * 24 + tx] = widen(R.x) + widen(R.y);
     if (WANT_K) {
