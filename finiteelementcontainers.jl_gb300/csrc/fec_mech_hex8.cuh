@@ -705,9 +705,7 @@ template <class Model>
 struct Layout {
   static constexpr int X = 0;                           // double [EPB][24] coordinates
   static constexpr int U = X + EPB * 24 * 8;            // double [EPB][24] displacements
-  // float2 [EPB][DNXS] spatial gradients ([NQ][24] per element, padded by 4 float2 so
-  // that the two elements of a consumer warp read the same offset from distinct banks)
-  static constexpr int DNXS = NQ * 24 + 4;
+  static constexpr int DNXS = NQ * 24;                  // float2 [EPB][NQ][24] spatial gradients
   static constexpr int DNX = U + EPB * 24 * 8;
   static constexpr int P = DNX + EPB * DNXS * 8;        // float2 [EPB][NQ][9] JxW P
   static constexpr int SCR = P + EPB * NQ * 9 * 8;      // float2 [EPB][NQ][SCR2] tangent scratch

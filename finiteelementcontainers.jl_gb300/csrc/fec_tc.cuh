@@ -43,27 +43,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// try_wait with an explicit suspend-time limit (nanoseconds) in place of the
-// system-dependent one, so that a short budget can run out
-__device__ __forceinline__ bool mbar_try_wait_hint(uint64_t* bar, uint32_t parity, uint32_t hint_ns) {
+// Non-blocking probe of the phase with the given parity.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+      : "r"(smem_u32(bar)), "r"(parity)
       : "memory");
   return ok != 0;
 }
 // Waits for the phase with the given parity to complete; false after about
 // `budget` SM clocks without completion.  Budgets under a million clocks (a
-// test setting) suspend at most 32 ns per try, as try_wait may otherwise
-// suspend until the phase completes.
+// test setting) poll with the non-blocking test_wait, as try_wait may suspend
+// until the phase completes.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long budget) {
   const long long t0 = clock64();
   if (budget < 1000000LL) {
-    while (!mbar_try_wait_hint(bar, parity, 32u)) {
+    while (!mbar_test_wait(bar, parity)) {
       if (clock64() - t0 > budget) return false;
     }
     return true;
