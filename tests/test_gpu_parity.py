@@ -386,7 +386,8 @@ def test_pipelined_gather_matches_node_gather(fec, case):
 
 def test_bounded_waits_report_and_drain(fec):
     """The element kernels' bounded waits, made to give up on operations that
-    complete anyway (a budget of 200 SM clocks, fec_set_wait_budget): the hex8
+    complete anyway (a budget of one SM clock, fec_set_wait_budget: a wait that
+    starts right after its copy or MMAs were issued gives up): the hex8
     kernel's wait on its bulk table copy reports through the device flag, waits
     again and falls back to plain loads (the results stay bitwise exact); the
     hex27 tensor-core kernel reports, drains its MMAs and frees its tensor
@@ -405,7 +406,7 @@ def test_bounded_waits_report_and_drain(fec):
     try:
         R0, nz0, _ = _run(fec, asm, p, U)
         assert lib.fec_tensor_core_status(0) == 0
-        assert lib.fec_set_wait_budget(200) == 0
+        assert lib.fec_set_wait_budget(1) == 0
         R1, nz1, _ = _run(fec, asm, p, U)
     finally:
         lib.fec_set_wait_budget(0)
@@ -418,7 +419,7 @@ def test_bounded_waits_report_and_drain(fec):
     U27 = stretch_field(mesh27.nodal_coords, seed=2).ravel()
     Ra, nza, _ = _run(fec, asm27, p27, U27)
     assert lib.fec_tensor_core_status(0) == 0
-    assert lib.fec_set_wait_budget(200) == 0
+    assert lib.fec_set_wait_budget(1) == 0
     try:
         _run(fec, asm27, p27, U27)
     finally:
@@ -426,7 +427,7 @@ def test_bounded_waits_report_and_drain(fec):
     assert lib.fec_tensor_core_status(1) == _lib.FEC_ERR_DEVICE
     with pytest.raises(fec.FECError) as info:   # the boundary's output check reports it too
         lib2 = fec.load_library()
-        lib2.fec_set_wait_budget(200)
+        lib2.fec_set_wait_budget(1)
         try:
             fec.assemble_residual_and_stiffness(asm27, torch.from_numpy(U27[asm27.dof.unknown_dofs - 1].copy()).cuda(),
                                                 p27, check_finite=True)
