@@ -51,6 +51,10 @@ struct Block {
   int physics = 0;
   double props[8] = {0};
   int nprops = 0;
+  // hex8 block whose elements are translates of the first one (node offsets
+  // within 1e-13 of the element size): x0 = the first element's coordinates
+  bool congruent = false;
+  double x0[24] = {0};
 };
 
 }  // namespace
@@ -92,6 +96,7 @@ struct fec_ctx {
   DevBuf d_flag;                       // non-finite scan result
   DevBuf d_nbr_ptr, d_nbr;             // neighbour lists on the device (device symbolic phase, CSC fill)
   DevBuf d_tile_counter;               // single launch of mixed element blocks: next work tile
+  std::vector<DevBuf> d_affine;        // per block: the tensor-core operand table of a congruent hex8 block
   bool single_launch = false;          // FP64 mechanics: every element block in one launch
   float cl_tol = 0.f;
   // optional per-launch timing (CUDA events on the caller's stream)
@@ -148,6 +153,28 @@ int upload(fec_ctx* c, DevBuf& b, const void* src, size_t bytes) {
   b.bytes = bytes;
   FEC_CUDA(c, cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice));
   return FEC_OK;
+}
+
+// The tensor-core operand table of block b (hex8, elements translates of the
+// first), from its current reference tables; none for other blocks, on a
+// host-only context, or for a degenerate first element.
+int build_affine(fec_ctx* c, size_t b) {
+  if (c->d_affine.size() != c->blocks.size()) c->d_affine.resize(c->blocks.size());
+  DevBuf& d = c->d_affine[b];
+  d.release();
+  const Block& B = c->blocks[b];
+  if (!B.congruent || c->device < 0) return FEC_OK;
+  std::vector<unsigned char> tab;
+  if (!fec::hex8_affine_table(B.x0, c->ref_host.data() + c->ref_off[b], tab)) return FEC_OK;
+  return upload(c, d, tab.data(), tab.size());
+}
+
+// The table a launch of block b may use: FP64 assemblies of congruent hex8
+// blocks on their own launch (the single launch across blocks keeps the
+// per-element kernels), unless FEC_HEX8_AFFINE=0.
+const void* affine_table(const fec_ctx* c, size_t b, int precision, bool mixed) {
+  if (precision != FEC_FP64 || mixed || b >= c->d_affine.size() || !fec::hex8_affine_enabled()) return nullptr;
+  return c->d_affine[b].p;
 }
 
 int ensure(fec_ctx* c, DevBuf& b, size_t bytes) {
@@ -274,6 +301,7 @@ int fec_ctx_destroy(fec_ctx* c) {
                     &c->d_cl_norm, &c->d_cl_cnt, &c->d_cl_args, &c->d_cl_img, &c->d_cl_table, &c->d_V, &c->d_colptr0, &c->d_rowval32,
                     &c->d_cg, &c->d_flag, &c->d_nbr_ptr, &c->d_nbr, &c->d_tile_counter})
     b->release();
+  for (DevBuf& b : c->d_affine) b.release();
   delete c;
   return FEC_OK;
 }
@@ -355,6 +383,29 @@ int fec_mesh_set(fec_ctx* c, int dim, int64_t nn, const double* coords, int nblo
     }
     if (dup >= 0) return fail(c, FEC_ERR_ARG, "element %lld repeats a node", (long long)(B.elem_start + dup + 1));
   }
+  // hex8 blocks whose elements are all translates of the first one
+  for (Block& B : blocks) {
+    if (B.elem_type != 1 || dim != 3 || B.ne < 1) continue;
+    const int32_t* c0 = conn0.data() + B.conn_off;
+    double d0[24], h = 0.0;
+    for (int a = 0; a < 8; ++a)
+      for (int d = 0; d < 3; ++d) {
+        B.x0[a * 3 + d] = coords[int64_t(c0[a]) * 3 + d];
+        d0[a * 3 + d] = coords[int64_t(c0[a]) * 3 + d] - coords[int64_t(c0[0]) * 3 + d];
+        h = std::max(h, std::fabs(d0[a * 3 + d]));
+      }
+    double dev = 0.0;
+#pragma omp parallel for schedule(static) reduction(max : dev)
+    for (int64_t e = 0; e < B.ne; ++e) {
+      const int32_t* ce = conn0.data() + B.conn_off + e * 8;
+      for (int a = 1; a < 8; ++a)
+        for (int d = 0; d < 3; ++d) {
+          const double off = coords[int64_t(ce[a]) * 3 + d] - coords[int64_t(ce[0]) * 3 + d];
+          dev = std::max(dev, std::fabs(off - d0[a * 3 + d]));
+        }
+    }
+    B.congruent = h > 0.0 && dev <= 1e-13 * h;
+  }
   // reference tables
   std::vector<double> ref;
   std::vector<int64_t> ref_off(nblocks);
@@ -376,6 +427,10 @@ int fec_mesh_set(fec_ctx* c, int dim, int64_t nn, const double* coords, int nblo
   c->conn = std::move(conn0);
   c->ref_off = std::move(ref_off);
   c->ref_host = std::move(ref);
+  for (DevBuf& d : c->d_affine) d.release();
+  c->d_affine.assign(c->blocks.size(), DevBuf());
+  for (size_t b = 0; b < c->blocks.size(); ++b)
+    if ((rc = build_affine(c, b))) return rc;
   c->n_unknowns = -1;
   c->nf = 0;
   invalidate_pattern(c);
@@ -408,6 +463,8 @@ int fec_block_reference_set(fec_ctx* c, int block, int num_q, const double* N, c
     FEC_CUDA(c, cudaMemcpy(static_cast<double*>(c->d_ref.p) + c->ref_off[block - 1], t.data(),
                            sizeof(double) * t.size(), cudaMemcpyHostToDevice));
   }
+  int rc;
+  if ((rc = build_affine(c, size_t(block - 1)))) return rc;
   return ok(c);
 }
 
@@ -914,6 +971,7 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     ea.Ke = want_k ? static_cast<char*>(c->d_Ke.p) + rsz * size_t(ke_off) : nullptr;
     ea.Re = want_r ? static_cast<char*>(c->d_Re.p) + rsz * size_t(re_off) : nullptr;
     ea.closure = c->d_cl_args.p;
+    ea.affine = affine_table(c, b, precision, mixed);
     if (B.physics == FEC_PHYS_J2_MLP && !ea.closure)
       return fail(c, FEC_ERR_STATE, "block %d uses the learned closure but fec_closure_set was not called", int(b) + 1);
     cudaError_t e = cudaSuccess;
@@ -1471,6 +1529,7 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
     ea.Ke = want_k ? static_cast<char*>(Ke) + rsz * size_t(ke_off) : nullptr;
     ea.Re = want_r ? static_cast<char*>(Re) + rsz * size_t(re_off) : nullptr;
     ea.closure = c->d_cl_args.p;
+    ea.affine = affine_table(c, b, precision, false);
     if (B.physics == FEC_PHYS_J2_MLP && !ea.closure)
       return fail(c, FEC_ERR_STATE, "block %d uses the learned closure but fec_closure_set was not called", int(b) + 1);
     cudaError_t e;

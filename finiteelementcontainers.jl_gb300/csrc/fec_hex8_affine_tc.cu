@@ -1,0 +1,605 @@
+// fec_hex8_affine_tc.cu -- FP64-accurate hex8 element stiffness on the tensor
+// cores for blocks whose elements are translates of one another (structured
+// meshes), by exact integer slicing of both operands (the Ozaki scheme: Ozaki,
+// Ogita, Oishi and Rump, Numer. Algorithms 59 (2012) 95-118, restated here for
+// BF16 digits and FP32 accumulation).
+//
+// The tangent of element e is (src/Formulations.jl:462-576)
+//     K_(a,i),(b,k) = sum_q sum_(J,L) dNX_qaJ * JxW A_q,iJkL * dNX_qbL .
+// With every element a translate of the first, dNX_q and JxW_q are the same for
+// all elements, so with r = (q, J, L) (72 values) and the node pair n = (a, b),
+// a <= b (36 pairs: the rest follow from K = K^T),
+//     D[(e, i, k), n] = sum_r A_e[(e, i, k), r] * W[n, r],   W[n, r] = dNX_qaJ dNX_qbL,
+// one GEMM over all elements with a constant right operand.  Each A row (one
+// element, scaled by a power of two 2^tau_e over the element's largest entry)
+// and each W row (2^sigma_n) is written as seven signed 8-bit digits,
+//     x = 2^tau * sum_t d_t 2^(-7-8t),  |d_t| <= 256,
+// every digit exact in BF16.  A digit product is an integer below 2^16 and a
+// 72-term dot product of digits below 2^23, so the sums over r of all digit
+// pairs with s + t = L (at most seven pairs, each with |d| <= 256 in one digit
+// position per value at most) stay below 2^24: each level L = 0..6 accumulates
+// exactly in its own FP32 TMEM accumulator.  Levels above 6 are dropped
+// (contributions below 2^-56 of the scales); the epilogue sums the seven levels
+// in double-float and scales by 2^(tau_e + sigma_n - 14).
+//
+// One persistent CTA per SM, tiles of 14 elements (126 of the 128 MMA rows):
+//   warps 0-3   FP64 point phase (displacement gradient, constitutive update),
+//               one thread per quadrature point, into a staging area;
+//   warps 4-10  tangent entries (45 unique per point, double-float), the element
+//               scale, the digits into the seven A slices; one thread then
+//               issues the 140 MMAs (28 digit pairs x 5 K steps of 16);
+//   warp 11     the residual R = sum_q dNX P in double-float;
+//   warps 12-15 the epilogue: TMEM -> double-float K_e entries, staged in shared
+//               memory over the consumed A slices, written out coalesced in the
+//               node-rows layout the node gather reads.
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <cmath>
+#include <vector>
+
+#include "fec_df64.cuh"
+#include "fec_kernels.cuh"
+#include "fec_launch.h"
+#include "fec_tc.cuh"
+
+namespace fec {
+namespace aff {
+
+constexpr int EPT = 14;              // elements per tile
+constexpr int NQ = 8;
+constexpr int NPT = EPT * NQ;        // quadrature points per tile (112)
+constexpr int KR = 72, KP = 80;      // reduction length r = (q, J, L), padded to 5 K steps
+constexpr int NPAIR = 36, NPAD = 48; // node pairs a <= b, padded N
+constexpr int ND = 7;                // digits per operand
+constexpr int NLEV = 7;              // accumulated levels s + t = 0..6
+constexpr int SBO = KP * 16;         // bytes between 8-row groups of an operand tile
+constexpr int A_SLICE = 128 * KP * 2;
+constexpr int W_SLICE = NPAD * KP * 2;
+// table built on the host (hex8_affine_table): W digits, sigma, dNX, JxW
+constexpr int T_W = 0;
+constexpr int T_SIG = ND * W_SLICE;
+constexpr int T_G = T_SIG + NPAD * 4;
+constexpr int T_JXW = T_G + NQ * 24 * 8;
+constexpr int T_BYTES = T_JXW + NQ * 8;
+static_assert(T_BYTES % 16 == 0 && T_G % 8 == 0, "table layout");
+// output staging over the A slices: each 8-row group of a slice holds 1152 bytes
+// of K columns 0..71 and 128 bytes of the (always zero) padding columns 72..79;
+// element el's K_e (72 node rows of 9 float2, the ninth a bank-spreading pad)
+// takes five groups' first 1152 bytes
+constexpr int ST_ROW = 9;
+constexpr int ST_PER_GROUP = 1152 / 8;  // float2 per group
+constexpr int ST_GROUPS = 5;
+static_assert(72 * ST_ROW <= ST_GROUPS * ST_PER_GROUP && EPT * ST_GROUPS <= ND * 16, "output staging");
+constexpr int TMEM_COLS = 512;
+constexpr long long WAIT_BUDGET = 2000000000LL;
+
+constexpr int PROD_W = 4, SL_W = 7, R_W = 1, EP_W = 4;
+constexpr int NTHR = 32 * (PROD_W + SL_W + R_W + EP_W);
+constexpr int T_SL = 32 * PROD_W, T_R = T_SL + 32 * SL_W, T_EP = T_R + 32 * R_W;
+constexpr int NSL = 32 * SL_W;
+static_assert(NSL == 2 * NPT && T_EP / 32 == 12, "roles");
+// named barriers (0 is __syncthreads)
+constexpr int BAR_FULL = 1;   // producers arrive, slicers + residual warp sync
+constexpr int BAR_EMPTY = 2;  // slicers + residual warp arrive, producers sync
+constexpr int BAR_AFREE = 3;  // epilogue arrives (slices consumed, staging written out), slicers sync
+constexpr int BAR_SL = 4;     // slicers
+constexpr int BAR_EP = 5;     // epilogue
+constexpr int N_FULL = 32 * (PROD_W + SL_W + R_W);
+constexpr int N_AFREE = 32 * (SL_W + EP_W);
+
+template <class Model>
+struct Layout {
+  static constexpr int W = 0;
+  static constexpr int A = W + ND * W_SLICE;
+  static constexpr int P = A + ND * A_SLICE;                      // float2 [112][9]
+  static constexpr int SCR = P + NPT * 9 * 8;                     // float2 [112][SCR2]
+  static constexpr int G = (SCR + NPT * Model::SCR2 * 8 + 15) / 16 * 16;  // double [8][24]
+  static constexpr int G2 = G + NQ * 24 * 8;                      // float2 [8][24]
+  static constexpr int JXW = G2 + NQ * 24 * 8;                    // double [8]
+  static constexpr int SIG = JXW + NQ * 8;                        // int [48]
+  static constexpr int TAU = SIG + NPAD * 4;                      // int [14] (+pad)
+  static constexpr int CODE = TAU + 16 * 4;                       // uint32 [45] entry codes (+pad)
+  static constexpr int PAIR = CODE + 48 * 4;                      // uint8 [48] node pair a*8+b
+  static constexpr int BAR = (PAIR + 48 + 15) / 16 * 16;          // mbarriers: slices done, MMAs done
+  static constexpr int TSLOT = BAR + 16;
+  static constexpr int SMEM = TSLOT + 16;
+  static_assert(SMEM <= 232448, "shared memory");
+};
+
+__device__ __forceinline__ void named_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+__device__ __forceinline__ void named_arrive(int id, int n) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
+}
+// 2^k as a float for k in [-126, 127]
+__device__ __forceinline__ float pow2f(int k) { return __uint_as_float(uint32_t(k + 127) << 23); }
+
+// byte offset of element (row, col) in a K-major operand tile with K = 80
+__host__ __device__ __forceinline__ uint32_t op_off(int row, int col) {
+  return uint32_t(row >> 3) * SBO + uint32_t(col >> 3) * 128 + uint32_t(row & 7) * 16 + uint32_t(col & 7) * 2;
+}
+// byte offset (within the A slices) of float2 f of element el's output staging
+__device__ __forceinline__ uint32_t st_off(int el, int f) {
+  const int grp = el * ST_GROUPS + f / ST_PER_GROUP;  // 0 .. 69
+  return uint32_t(grp >> 4) * A_SLICE + uint32_t(grp & 15) * SBO + uint32_t(f % ST_PER_GROUP) * 8;
+}
+
+// Seven 8-column loads (the seven levels of one column chunk) under one wait.
+__device__ __forceinline__ void tmem_ld8x7(uint32_t taddr, float (*v)[8]) {
+  uint32_t r[56];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%56];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8, %9, %10, %11, %12, %13, %14, %15}, [%57];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16, %17, %18, %19, %20, %21, %22, %23}, [%58];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%24, %25, %26, %27, %28, %29, %30, %31}, [%59];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%32, %33, %34, %35, %36, %37, %38, %39}, [%60];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%40, %41, %42, %43, %44, %45, %46, %47}, [%61];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%48, %49, %50, %51, %52, %53, %54, %55}, [%62];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
+        "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
+        "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
+        "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55])
+      : "r"(taddr), "r"(taddr + 48u), "r"(taddr + 96u), "r"(taddr + 144u), "r"(taddr + 192u), "r"(taddr + 240u),
+        "r"(taddr + 288u)
+      : "memory");
+#pragma unroll
+  for (int L = 0; L < NLEV; ++L)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[L][j] = __uint_as_float(r[L * 8 + j]);
+}
+
+// kind::f16 (BF16 operands), FP32 accumulate, M = 128, N = 48, both K-major
+constexpr uint32_t IDESC = tc::idesc_bf16(128, NPAD);
+
+// Point phase of quadrature point q of element e (FP64): the eight lanes of an
+// element (consecutive, aligned to 8) each load one node's displacement and
+// share it; gu = sum_a u_a (x) dNX_qa; the constitutive update.  Every lane of
+// the warp calls it (the shuffles); `live` lanes get P9 and scr.
+template <class Model>
+__device__ __forceinline__ void point_phase(const ElemArgs& g, const double* s_g, const double* s_jxw, int64_t e, int q,
+                                            bool live, double* P9, double* scr) {
+  const int lane = threadIdx.x & 31;
+  double uo[3] = {0.0, 0.0, 0.0};
+  if (live) {
+    const int64_t node = g.conn[e * 8 + q];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) uo[d] = __ldg(&g.U[node * 3 + d]);
+  }
+  double gu[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  const double* gq = s_g + q * 24;
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    const int src = (lane & ~7) | a;
+    const double u0 = __shfl_sync(0xffffffffu, uo[0], src), u1 = __shfl_sync(0xffffffffu, uo[1], src),
+                 u2 = __shfl_sync(0xffffffffu, uo[2], src);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const double gj = gq[a * 3 + j];
+      gu[0][j] = fma(u0, gj, gu[0][j]);
+      gu[1][j] = fma(u1, gj, gu[1][j]);
+      gu[2][j] = fma(u2, gj, gu[2][j]);
+    }
+  }
+  if (live) {
+    const double* so = Model::NS ? g.state_old + (e * NQ + q) * Model::NS : nullptr;
+    double* sn = (Model::NS && g.state_new) ? g.state_new + (e * NQ + q) * Model::NS : nullptr;
+    Model::point(g.props, gu, s_jxw[q], so, sn, P9, scr);
+  }
+}
+
+// R_(a,i) of one element from its points' split JxW P [8][9] (double-float, q in order)
+__device__ __forceinline__ double residual_entry(const float2* s_g2, const float2* P8, int a, int i) {
+  float2 R = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    const float2* gq = s_g2 + q * 24 + a * 3;
+    const float2* P = P8 + q * 9 + i * 3;
+    R = df64_dot3_acc(R, gq[0], P[0], gq[1], P[1], gq[2], P[2]);
+  }
+  return widen(R.x) + widen(R.y);
+}
+
+template <class Model, bool WANT_R>
+__global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, const unsigned char* __restrict__ tab) {
+  using namespace tc;
+  using Lay = Layout<Model>;
+  constexpr int SCR2 = Model::SCR2;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t s0 = smem_u32(sm);
+  double* s_g = reinterpret_cast<double*>(sm + Lay::G);
+  float2* s_g2 = reinterpret_cast<float2*>(sm + Lay::G2);
+  double* s_jxw = reinterpret_cast<double*>(sm + Lay::JXW);
+  int* s_sig = reinterpret_cast<int*>(sm + Lay::SIG);
+  int* s_tau = reinterpret_cast<int*>(sm + Lay::TAU);
+  uint32_t* s_code = reinterpret_cast<uint32_t*>(sm + Lay::CODE);
+  uint8_t* s_pair = sm + Lay::PAIR;
+  uint64_t* bar_sl = reinterpret_cast<uint64_t*>(sm + Lay::BAR);
+  uint64_t* bar_mma = bar_sl + 1;
+  float2* s_P = reinterpret_cast<float2*>(sm + Lay::P);
+  float2* s_scr = reinterpret_cast<float2*>(sm + Lay::SCR);
+
+  // ---- setup: A slices zero (their padding columns stay zero), W digits, tables ----
+  for (int i = tid; i < ND * A_SLICE / 16; i += NTHR)
+    reinterpret_cast<uint4*>(sm + Lay::A)[i] = make_uint4(0u, 0u, 0u, 0u);
+  for (int i = tid; i < ND * W_SLICE / 16; i += NTHR)
+    reinterpret_cast<uint4*>(sm + Lay::W)[i] = __ldg(reinterpret_cast<const uint4*>(tab + T_W) + i);
+  for (int i = tid; i < NQ * 24; i += NTHR) {
+    const double v = __ldg(reinterpret_cast<const double*>(tab + T_G) + i);
+    s_g[i] = v;
+    s_g2[i] = df64_split(v);
+  }
+  if (tid < NQ) s_jxw[tid] = __ldg(reinterpret_cast<const double*>(tab + T_JXW) + tid);
+  if (tid < NPAD) s_sig[tid] = __ldg(reinterpret_cast<const int*>(tab + T_SIG) + tid);
+  if (tid < 45) {
+    // unique entry w = (r1, r2), r1 <= r2, r1 = 3i + J, r2 = 3k + L: i, J, k, L and
+    // the operand positions (row i*3+k, column J*3+L) and (row k*3+i, column L*3+J)
+    int m = tid, r = 0;
+    for (int c = 0; c < 9; ++c)
+      if (m >= 9 - r) { m -= 9 - r; ++r; }
+    const int r1 = r, r2 = r + m;
+    const int i = r1 / 3, J = r1 % 3, k = r2 / 3, L = r2 % 3;
+    s_code[tid] = uint32_t(i) | uint32_t(J) << 4 | uint32_t(k) << 8 | uint32_t(L) << 12 |
+                  uint32_t(i * 3 + k) << 16 | uint32_t(J * 3 + L) << 20 | uint32_t(k * 3 + i) << 24 |
+                  uint32_t(L * 3 + J) << 28;
+  }
+  if (tid < NPAD) {
+    int a = 0, b = 0, n = tid;
+    if (n < NPAIR) {
+      while (n >= 8 - a) { n -= 8 - a; ++a; }
+      b = a + n;
+    }
+    s_pair[tid] = uint8_t(a * 8 + b);
+  }
+  if (tid == 0) {
+    mbar_init(bar_sl, NSL);
+    mbar_init(bar_mma, 1);
+    mbar_fence_init();
+  }
+  if (warp == T_EP / 32) tmem_alloc(reinterpret_cast<uint32_t*>(sm + Lay::TSLOT), TMEM_COLS);
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + Lay::TSLOT);
+  const int64_t ntiles = (g.ne + EPT - 1) / EPT;
+  const long long budget = g.wait_budget > 0 ? g.wait_budget : WAIT_BUDGET;
+
+  if (tid < T_SL) {
+    // ---------------- producers: thread (el, q) ----------------
+    const int el = tid >> 3, q = tid & 7;
+    const bool active = tid < NPT;
+    for (int k = 0;; ++k) {
+      const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
+      if (tile >= ntiles) break;
+      const int64_t e = tile * EPT + el;
+      const bool live = active && e < g.ne;
+      double P9[9], scr[Model::SCR];
+      point_phase<Model>(g, s_g, s_jxw, e, q, live, P9, scr);
+      if (k >= 1) named_sync(BAR_EMPTY, N_FULL);  // tile k-1's staging has been read
+      if (live) {
+        float2* pP = s_P + tid * 9;
+#pragma unroll
+        for (int m = 0; m < 9; ++m) pP[m] = df64_split(P9[m]);
+        Model::split_scratch(scr, s_scr + tid * SCR2);
+      }
+      named_arrive(BAR_FULL, N_FULL);
+    }
+  } else if (tid < T_R) {
+    // ---------------- slicers: thread (point p, half h) ----------------
+    const int ts = tid - T_SL, p = ts >> 1, h = ts & 1, el = p >> 3, q = p & 7;
+    const int w0 = h ? 23 : 0, cnt = h ? 22 : 23;
+    for (int k = 0;; ++k) {
+      const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
+      if (tile >= ntiles) break;
+      const bool live = tile * EPT + el < g.ne;
+      named_sync(BAR_FULL, N_FULL);
+      float2 av[23];
+      float mx = 0.f;
+      const float2* sc = s_scr + p * SCR2;
+#pragma unroll
+      for (int c = 0; c < 23; ++c) {
+        av[c] = make_float2(0.f, 0.f);
+        if (c < cnt && live) {
+          const uint32_t code = s_code[w0 + c];
+          av[c] = Model::aentry_df64(sc, code & 15, (code >> 4) & 15, (code >> 8) & 15, (code >> 12) & 15);
+          mx = fmaxf(mx, fabsf(av[c].x));
+        }
+      }
+      named_arrive(BAR_EMPTY, N_FULL);  // the staging may be refilled
+      // the element's scale: its 16 threads are lanes 16*(el%2) .. +15 of this warp
+#pragma unroll
+      for (int o = 1; o < 16; o <<= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      int tau = 0;
+      if (mx > 0.f) frexpf(mx, &tau);  // |entry| < 2^tau
+      tau = tau < -119 ? -119 : (tau > 126 ? 126 : tau);
+      const float fs = pow2f(7 - tau);  // entries scaled to |x| < 128
+      if (k >= 1) named_sync(BAR_AFREE, N_AFREE);  // the epilogue is done with the slices
+      if ((ts & 15) == 0) s_tau[el] = tau;
+      unsigned char* As = sm + Lay::A;
+#pragma unroll
+      for (int c = 0; c < 23; ++c) {
+        if (c >= cnt) break;
+        const uint32_t code = s_code[w0 + c];
+        const int row = el * 9 + int((code >> 16) & 15), col = q * 9 + int((code >> 20) & 15);
+        const int row2 = el * 9 + int((code >> 24) & 15), col2 = q * 9 + int(code >> 28);
+        const bool twin = row != row2 || col != col2;
+        const uint32_t o1 = op_off(row, col), o2 = op_off(row2, col2);
+        float xh = av[c].x * fs, xl = av[c].y * fs;
+#pragma unroll
+        for (int s = 0; s < ND; ++s) {
+          const float dh = rintf(xh), dl = rintf(xl);
+          xh = (xh - dh) * 256.f;
+          xl = (xl - dl) * 256.f;
+          const unsigned short bits = static_cast<unsigned short>(__float_as_uint(dh + dl) >> 16);
+          *reinterpret_cast<unsigned short*>(As + s * A_SLICE + o1) = bits;
+          if (twin) *reinterpret_cast<unsigned short*>(As + s * A_SLICE + o2) = bits;
+        }
+      }
+      fence_async_smem();
+      mbar_arrive(bar_sl);
+      named_sync(BAR_SL, NSL);
+      if (ts == 0) {
+        tc_fence_after();
+        const uint32_t aB = s0 + Lay::A, wB = s0 + Lay::W;
+#pragma unroll 1
+        for (int L = 0; L < NLEV; ++L) {
+          uint32_t acc = 0;
+#pragma unroll 1
+          for (int t = 0; t <= L; ++t) {
+            const int s = L - t;
+#pragma unroll
+            for (int kk = 0; kk < KP / 16; ++kk) {
+              mma_bf16(tmem + uint32_t(L * NPAD), smem_desc(aB + t * A_SLICE + kk * 256, 128, SBO),
+                       smem_desc(wB + s * W_SLICE + kk * 256, 128, SBO), IDESC, acc);
+              acc = 1;
+            }
+          }
+        }
+        mma_commit(bar_mma);
+      }
+    }
+  } else if (tid < T_EP) {
+    // ---------------- residual warp ----------------
+    for (int k = 0;; ++k) {
+      const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
+      if (tile >= ntiles) break;
+      named_sync(BAR_FULL, N_FULL);
+      if (WANT_R) {
+        for (int idx = lane; idx < EPT * 24; idx += 32) {
+          const int el = idx / 24, ai = idx % 24, a = ai / 3, i = ai % 3;
+          const int64_t e = tile * EPT + el;
+          if (e >= g.ne) continue;
+          static_cast<double*>(g.Re)[e * 24 + ai] = residual_entry(s_g2, s_P + el * NQ * 9, a, i);
+        }
+      }
+      named_arrive(BAR_EMPTY, N_FULL);
+    }
+  } else {
+    // ---------------- epilogue: thread = TMEM lane = row (el, i, k) ----------------
+    const int te = tid - T_EP, qw = warp & 3, m = qw * 32 + lane;
+    const int el = m / 9, ik = m % 9, i = ik / 3, kc = ik % 3;
+    const uint32_t lane_addr = tmem + (uint32_t(qw * 32) << 16);
+    for (int k = 0;; ++k) {
+      const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
+      if (tile >= ntiles) break;
+      const uint32_t par = uint32_t(k & 1);
+      bool ok = mbar_wait(bar_sl, par, budget);
+      ok = mbar_wait(bar_mma, par, budget) && ok;
+      if (!ok) {
+        // report, then wait out the MMAs so the accumulators are not reused or
+        // freed under them (the outputs of this call are invalid)
+        if (g.wait_err && lane == 0) atomicExch(g.wait_err, 1);
+        mbar_wait(bar_sl, par, WAIT_BUDGET);
+        mbar_wait(bar_mma, par, WAIT_BUDGET);
+      }
+      tc_fence_after();
+      const int64_t e0 = tile * EPT;
+      const bool live = m < EPT * 9 && e0 + el < g.ne;
+      const int tau = live ? s_tau[el] : 0;
+#pragma unroll 1
+      for (int c = 0; c < 5; ++c) {
+        float v[NLEV][8];
+        tmem_ld8x7(lane_addr + uint32_t(c * 8), v);
+        if (!live) continue;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int n = c * 8 + j;
+          if (n >= NPAIR) break;
+          // sum_L v_L 2^(-8L) in double-float, from the smallest level up
+          float hi = v[NLEV - 1][j], lo = 0.f;
+#pragma unroll
+          for (int L = NLEV - 2; L >= 0; --L) {
+            const float a = v[L][j], b = hi * 0.00390625f;
+            lo *= 0.00390625f;
+            const float s = a + b, bb = s - a;
+            lo += (a - (s - bb)) + (b - bb);
+            hi = s + lo;
+            lo = lo - (hi - s);
+          }
+          const float f1 = pow2f(tau - 7), f2 = pow2f(s_sig[n] - 7);
+          const float2 val = make_float2(hi * f1 * f2, lo * f1 * f2);
+          const int ab = s_pair[n], a = ab >> 3, b = ab & 7;
+          *reinterpret_cast<float2*>(sm + Lay::A + st_off(el, ((a * 3 + i) * 3 + kc) * ST_ROW + b)) = val;
+          if (a != b) *reinterpret_cast<float2*>(sm + Lay::A + st_off(el, ((b * 3 + kc) * 3 + i) * ST_ROW + a)) = val;
+        }
+      }
+      tc_fence_before();
+      named_sync(BAR_EP, 32 * EP_W);
+      // write K_e out: 576 float2 per element in the node-rows layout, two per thread and step
+      const int64_t left = g.ne - e0;
+      const int nlive = left < EPT ? int(left) : EPT;
+      float4* dst = reinterpret_cast<float4*>(static_cast<float2*>(g.Ke) + e0 * 576);
+      for (int idx = te; idx < nlive * 288; idx += 32 * EP_W) {
+        const int ee = idx / 288, w = (idx % 288) * 2, f = (w >> 3) * ST_ROW + (w & 7);
+        const float2 x0 = *reinterpret_cast<const float2*>(sm + Lay::A + st_off(ee, f));
+        const float2 x1 = *reinterpret_cast<const float2*>(sm + Lay::A + st_off(ee, f + 1));
+        dst[idx] = make_float4(x0.x, x0.y, x1.x, x1.y);
+      }
+      named_arrive(BAR_AFREE, N_AFREE);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == T_EP / 32) {
+    tc_fence_after();
+    tmem_dealloc(tmem, TMEM_COLS);
+  }
+}
+
+// Residual only (no tangent): the same point phase and residual arithmetic as
+// the tensor-core kernel, so both give bitwise the same R and state.  16
+// elements per CTA, one thread per point.
+constexpr int R_EPB = 16;
+template <class Model>
+__global__ void __launch_bounds__(R_EPB * NQ) hex8_affine_r_kernel(ElemArgs g, const unsigned char* __restrict__ tab) {
+  __shared__ double s_g[NQ * 24], s_jxw[NQ];
+  __shared__ float2 s_g2[NQ * 24], s_P[R_EPB * NQ * 9];
+  const int tid = threadIdx.x, el = tid >> 3, q = tid & 7;
+  for (int i = tid; i < NQ * 24; i += blockDim.x) {
+    const double v = __ldg(reinterpret_cast<const double*>(tab + T_G) + i);
+    s_g[i] = v;
+    s_g2[i] = df64_split(v);
+  }
+  if (tid < NQ) s_jxw[tid] = __ldg(reinterpret_cast<const double*>(tab + T_JXW) + tid);
+  __syncthreads();
+  const int64_t e0 = int64_t(blockIdx.x) * R_EPB, e = e0 + el;
+  const bool live = e < g.ne;
+  double P9[9], scr[Model::SCR];
+  point_phase<Model>(g, s_g, s_jxw, e, q, live, P9, scr);
+  if (live) {
+#pragma unroll
+    for (int m = 0; m < 9; ++m) s_P[tid * 9 + m] = df64_split(P9[m]);
+  }
+  __syncthreads();
+  for (int idx = tid; idx < R_EPB * 24; idx += blockDim.x) {
+    const int ee = idx / 24, ai = idx % 24;
+    if (e0 + ee < g.ne)
+      static_cast<double*>(g.Re)[(e0 + ee) * 24 + ai] = residual_entry(s_g2, s_P + ee * NQ * 9, ai / 3, ai % 3);
+  }
+}
+
+template <class Model, bool WANT_R>
+cudaError_t launch1(const ElemArgs& a, cudaStream_t s, int* launches) {
+  constexpr int SMEM = Layout<Model>::SMEM;
+  const cudaError_t e = ensure_smem<hex8_affine_tc_kernel<Model, WANT_R>>(SMEM);
+  if (e != cudaSuccess) return e;
+  const int64_t ntiles = (a.ne + EPT - 1) / EPT;
+  if (ntiles == 0) return cudaSuccess;
+  const int grid = int(ntiles < num_sms() ? ntiles : num_sms());
+  hex8_affine_tc_kernel<Model, WANT_R><<<grid, NTHR, SMEM, s>>>(a, static_cast<const unsigned char*>(a.affine));
+  if (launches) ++*launches;
+  return cudaGetLastError();
+}
+
+template <class Model>
+cudaError_t launch_r(const ElemArgs& a, cudaStream_t s, int* launches) {
+  const int64_t nb = (a.ne + R_EPB - 1) / R_EPB;
+  if (nb == 0) return cudaSuccess;
+  hex8_affine_r_kernel<Model><<<unsigned(nb), R_EPB * NQ, 0, s>>>(a, static_cast<const unsigned char*>(a.affine));
+  if (launches) ++*launches;
+  return cudaGetLastError();
+}
+
+}  // namespace aff
+
+bool hex8_affine_enabled() {
+  const char* v = std::getenv("FEC_HEX8_AFFINE");
+  return !(v && v[0] == '0');
+}
+
+cudaError_t launch_hex8_affine_tc(int physics, bool want_r, bool want_k, const ElemArgs& a, cudaStream_t s,
+                                  int* launches) {
+  if (!a.affine || (want_k && !a.Ke) || (want_r && !a.Re)) return cudaErrorInvalidValue;
+  if (!want_k) {
+    if (!want_r) return cudaSuccess;
+    if (physics == 2) return aff::launch_r<NeoHookean>(a, s, launches);
+    if (physics == 3) return aff::launch_r<J2>(a, s, launches);
+    return cudaErrorNotSupported;
+  }
+  if (physics == 2)
+    return want_r ? aff::launch1<NeoHookean, true>(a, s, launches) : aff::launch1<NeoHookean, false>(a, s, launches);
+  if (physics == 3) return want_r ? aff::launch1<J2, true>(a, s, launches) : aff::launch1<J2, false>(a, s, launches);
+  return cudaErrorNotSupported;
+}
+
+// Host: the constant operand of a block whose elements are translates of its
+// first one.  x0: the first element's node coordinates [8][3]; ref: the block's
+// reference tables (RefLayout<1>: N, dN/dxi [q][a][3], weights).  Returns false
+// for a degenerate element (det J <= 0 at a point) or gradient products outside
+// the range the FP32 epilogue scales (2^-126 .. 2^127).
+bool hex8_affine_table(const double* x0, const double* ref, std::vector<unsigned char>& out) {
+  using L = RefLayout<1>;
+  out.assign(aff::T_BYTES, 0);
+  double dNX[8][8][3], jxw[8];
+  for (int q = 0; q < 8; ++q) {
+    const double* dN = ref + L::DN_OFF + q * 24;
+    double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int a = 0; a < 8; ++a)
+      for (int d = 0; d < 3; ++d)
+        for (int k = 0; k < 3; ++k) J[d][k] = std::fma(x0[a * 3 + d], dN[a * 3 + k], J[d][k]);
+    const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1], c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2],
+                 c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+    if (!(det > 0.0)) return false;
+    const double r = 1.0 / det;
+    double Ji[3][3];
+    Ji[0][0] = c00 * r;
+    Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
+    Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+    Ji[1][0] = c01 * r;
+    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+    Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
+    Ji[2][0] = c02 * r;
+    Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * r;
+    Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+    for (int a = 0; a < 8; ++a)
+      for (int d = 0; d < 3; ++d) {
+        double s = 0.0;
+        for (int k = 0; k < 3; ++k) s = std::fma(dN[a * 3 + k], Ji[k][d], s);
+        dNX[q][a][d] = s;
+      }
+    jxw[q] = det * ref[L::W_OFF + q];
+  }
+  int n = 0;
+  int32_t sig[aff::NPAD] = {0};
+  for (int a = 0; a < 8; ++a)
+    for (int b = a; b < 8; ++b, ++n) {
+      double w[aff::KR], mx = 0.0;
+      for (int q = 0; q < 8; ++q)
+        for (int J = 0; J < 3; ++J)
+          for (int Lc = 0; Lc < 3; ++Lc) {
+            w[q * 9 + J * 3 + Lc] = dNX[q][a][J] * dNX[q][b][Lc];
+            mx = std::fmax(mx, std::fabs(w[q * 9 + J * 3 + Lc]));
+          }
+      int e = 0;
+      if (mx > 0.0) std::frexp(mx, &e);  // |w| < 2^e
+      if (e < -119 || e > 134) return false;  // the epilogue scales by 2^(e - 7) in FP32
+      sig[n] = e;
+      for (int r = 0; r < aff::KR; ++r) {
+        double y = std::ldexp(w[r], 7 - e);  // |y| < 128, exact
+        for (int s = 0; s < aff::ND; ++s) {
+          const double d = std::nearbyint(y);
+          y = (y - d) * 256.0;
+          const float fd = float(d);
+          uint32_t u;
+          std::memcpy(&u, &fd, 4);
+          const uint16_t bits = uint16_t(u >> 16);
+          std::memcpy(out.data() + aff::T_W + s * aff::W_SLICE + aff::op_off(n, r), &bits, 2);
+        }
+      }
+    }
+  std::memcpy(out.data() + aff::T_SIG, sig, sizeof sig);
+  std::memcpy(out.data() + aff::T_G, dNX, sizeof dNX);
+  std::memcpy(out.data() + aff::T_JXW, jxw, sizeof jxw);
+  return true;
+}
+
+}  // namespace fec

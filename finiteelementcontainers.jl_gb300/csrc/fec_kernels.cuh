@@ -65,6 +65,7 @@ struct ElemArgs {
   void* Ke;                 // block base, Real[ne][NDOF][NDOF]
   void* Re;                 // block base, Real[ne][NDOF]
   const void* closure;      // learned-closure data (ClosureArgs) for the physics that uses one
+  const void* affine;       // hex8 blocks of translated elements: the constant operand table (or null)
   int* wait_err;            // set to 1 by a bounded wait that gave up (device flag; may be null)
   long long wait_budget;    // SM clocks a bounded wait allows before giving up (0: the default, ~1 s)
 };

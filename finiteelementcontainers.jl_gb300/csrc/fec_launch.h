@@ -2,6 +2,7 @@
 // Each physics family is instantiated in its own translation unit so the
 // library builds in parallel.
 #pragma once
+#include <vector>
 #include <cuda_runtime.h>
 #include "fec_kernels.cuh"
 
@@ -55,6 +56,17 @@ cudaError_t launch_mech_mixed(int physics, int nblocks, const int* elem_types, c
 
 // Streaming multiprocessors of the current device (cached per device).
 int num_sms();
+// FP64 hex8 Neo-Hookean (2) or J2 (3) for a block whose elements are
+// translates of its first one (args.affine: the table hex8_affine_table built):
+// with the tangent, its contraction on the tensor cores in exact 8-bit digit
+// slices; residual-only calls run the same point phase and residual arithmetic.
+cudaError_t launch_hex8_affine_tc(int physics, bool want_r, bool want_k, const ElemArgs& args, cudaStream_t stream,
+                                  int* launches);
+// Host: that table from the first element's node coordinates x0[8][3] and the
+// block's reference tables (RefLayout<1>); false for a degenerate element.
+bool hex8_affine_table(const double* x0, const double* ref, std::vector<unsigned char>& out);
+// FEC_HEX8_AFFINE=0 keeps such blocks on the per-element kernels.
+bool hex8_affine_enabled();
 // FEC_HEX8_DF64=tile selects the one-tile-per-CTA FP64 hex8 kernel instead of
 // the warp-specialised persistent one.
 bool hex8_df64_tile_kernel();

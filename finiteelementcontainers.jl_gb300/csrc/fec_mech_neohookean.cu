@@ -191,6 +191,10 @@ cudaError_t launch_mech_neohookean(int elem_type, int precision, bool want_r, bo
                            cudaStream_t s, int* launches) {
   switch (elem_type) {
     case 1:
+      if (precision == 0 && a.affine && !fp64_native() && hex8_affine_enabled()) {
+        if (a.ne <= 0 || (!want_r && !want_k)) return cudaSuccess;
+        return launch_hex8_affine_tc(2, want_r, want_k, a, s, launches);
+      }
       if (precision == 0)
         return fp64_native() ? hex8<double, 8>(want_r, want_k, a, s, launches)
                              : hex8_df64<8>(want_r, want_k, a, s, launches);

@@ -127,7 +127,10 @@ def test_autotuned_generic_kernels_are_bitwise_identical(fec):
 @pytest.mark.parametrize("physics", ["neohookean", "j2"])
 def test_single_launch_matches_per_block_launches(fec, physics):
     """hex8 + tet4 + tet10 + hex27 blocks in ONE persistent element launch give
-    bitwise the residual, nzval and state of one launch per block."""
+    bitwise the residual, nzval and state of one launch per block.  The single
+    launch runs the per-element hex8 kernel, so the per-block launches do too
+    (FEC_HEX8_AFFINE=0: the structured hex8 block would take the affine path)."""
+    import os
     torch = _torch()
     from fec_gb300 import batching
     from helpers import stretch_field
@@ -136,6 +139,18 @@ def test_single_launch_matches_per_block_launches(fec, physics):
          fec.meshes.box_tet10((3, 3, 3)), fec.meshes.box_hex27((3, 3, 3))],
         names=["hex8", "tet4", "tet10", "hex27"])
     out = []
+    os.environ["FEC_HEX8_AFFINE"] = "0"
+    try:
+        _single_vs_per_block(fec, torch, mesh, physics, stretch_field, out)
+    finally:
+        os.environ.pop("FEC_HEX8_AFFINE", None)
+    assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
+    if physics == "j2":
+        assert torch.equal(out[0][3], out[1][3])
+    assert out[0][2] == 5 and out[1][2] == 2  # element launches + the gather
+
+
+def _single_vs_per_block(fec, torch, mesh, physics, stretch_field, out):
     for single in (False, True):
         asm = fec.SparseMatrixAssembler(fec.VectorFunction(fec.FunctionSpace(mesh), "u"), device=0)
         asm.set_single_launch(single)
@@ -151,10 +166,6 @@ def test_single_launch_matches_per_block_launches(fec, physics):
         torch.cuda.synchronize()
         st = p.state_new.clone() if physics == "j2" else None
         out.append((R.clone(), K.nzval.clone(), asm.last_launch_count(), st))
-    assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
-    if physics == "j2":
-        assert torch.equal(out[0][3], out[1][3])
-    assert out[0][2] == 5 and out[1][2] == 2  # element launches + the gather
 
 
 def test_newton_loop_graph_with_single_launch(fec):

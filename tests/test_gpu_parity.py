@@ -309,7 +309,9 @@ def test_fp64_hex8_warp_specialised_kernel_matches_tile_kernel(fec, n, phys_name
     """The persistent warp-specialised FP64 hex8 kernel (default) against the
     one-tile-per-CTA kernel (FEC_HEX8_DF64=tile): bitwise the same residual,
     stiffness and new state, for a single partial tile (27 elements), a few
-    tiles per CTA (4,913) and many (64,000); fused and separate R / K calls."""
+    tiles per CTA (4,913) and many (64,000); fused and separate R / K calls.
+    These structured meshes would take the affine tensor-core path: both runs
+    keep the per-element kernels (FEC_HEX8_AFFINE=0)."""
     import os
     torch = _torch()
     mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n + 1,) * 3)
@@ -323,6 +325,7 @@ def test_fp64_hex8_warp_specialised_kernel_matches_tile_kernel(fec, n, phys_name
     Uu = torch.from_numpy(U[asm.dof.unknown_dofs - 1].copy()).cuda()
     out = {}
     for kernel in ("ws", "tile"):
+        os.environ["FEC_HEX8_AFFINE"] = "0"
         if kernel == "tile":
             os.environ["FEC_HEX8_DF64"] = "tile"
         try:
@@ -336,6 +339,7 @@ def test_fp64_hex8_warp_specialised_kernel_matches_tile_kernel(fec, n, phys_name
             out[kernel] = res
         finally:
             os.environ.pop("FEC_HEX8_DF64", None)
+            os.environ.pop("FEC_HEX8_AFFINE", None)
     for a, b in zip(out["ws"], out["tile"]):
         assert np.array_equal(a, b)
     assert np.array_equal(out["ws"][0], out["ws"][3]) and np.array_equal(out["ws"][1], out["ws"][4])
@@ -390,7 +394,8 @@ def test_bounded_waits_report_and_drain(fec):
     starts right after its copy or MMAs were issued gives up): the hex8
     kernel's wait on its bulk table copy reports through the device flag, waits
     again and falls back to plain loads (the results stay bitwise exact); the
-    hex27 tensor-core kernel reports, drains its MMAs and frees its tensor
+    affine hex8 tensor-core kernel reports, waits its MMAs out and carries on
+    (bitwise exact); the hex27 tensor-core kernel reports, drains its MMAs and frees its tensor
     memory (its results are invalid, but the context stays usable: the next
     call is exact and the flag stays clear)."""
     import os
@@ -403,6 +408,7 @@ def test_bounded_waits_report_and_drain(fec):
     asm, p = _setup(fec, mesh, "vector", phys)
     U = stretch_field(mesh.nodal_coords, seed=1).ravel()
     os.environ["FEC_HEX8_DF64"] = "tile"   # the hex8 kernel that stages by bulk copy
+    os.environ["FEC_HEX8_AFFINE"] = "0"    # (not the affine path this structured mesh would take)
     try:
         R0, nz0, _ = _run(fec, asm, p, U)
         assert lib.fec_tensor_core_status(0) == 0
@@ -411,8 +417,21 @@ def test_bounded_waits_report_and_drain(fec):
     finally:
         lib.fec_set_wait_budget(0)
         del os.environ["FEC_HEX8_DF64"]
+        del os.environ["FEC_HEX8_AFFINE"]
     assert lib.fec_tensor_core_status(1) == _lib.FEC_ERR_DEVICE    # the waits gave up, and said so
     assert np.array_equal(R0, R1) and np.array_equal(nz0, nz1)      # ... and the plain loads took over
+    # the affine tensor-core kernel (this structured mesh, FP64): its epilogue's
+    # waits give up, report, wait the MMAs out and carry on, so the results stay exact
+    R2, nz2, _ = _run(fec, asm, p, U)
+    assert lib.fec_tensor_core_status(0) == 0
+    assert lib.fec_set_wait_budget(1) == 0
+    try:
+        R3, nz3, _ = _run(fec, asm, p, U)
+    finally:
+        lib.fec_set_wait_budget(0)
+    assert lib.fec_tensor_core_status(1) == _lib.FEC_ERR_DEVICE
+    assert np.array_equal(R2, R3) and np.array_equal(nz2, nz3)
+    assert not np.array_equal(nz0, nz2)  # (the affine path, not the per-element kernel, ran)
     # hex27 FP32-element on the tensor cores
     mesh27 = fec.meshes.box_hex27((3, 3, 3))
     asm27, p27 = _setup(fec, mesh27, "vector", phys, precision="fp32_element")
