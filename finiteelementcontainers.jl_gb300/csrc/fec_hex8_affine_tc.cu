@@ -22,16 +22,22 @@
 // (contributions below 2^-56 of the scales); the epilogue sums the seven levels
 // in double-float and scales by 2^(tau_e + sigma_n - 14).
 //
-// One persistent CTA per SM, tiles of 14 elements (126 of the 128 MMA rows):
-//   warps 0-3   FP64 point phase (displacement gradient, constitutive update),
+// One persistent CTA per SM, tiles of 12 elements.  MMA row m = 32 w + 9 j + ik
+// holds (element 3 w + j, ik = 3 i + k): every element's nine rows lie in one
+// warp's TMEM lanes, lanes 27-31 of each warp are padding rows.
+//   warps 0-2   FP64 point phase (displacement gradient, constitutive update),
 //               one thread per quadrature point, into a staging area;
-//   warps 4-10  tangent entries (45 unique per point, double-float), the element
+//   warps 3-8   tangent entries (45 unique per point, double-float), the element
 //               scale, the digits into the seven A slices; one thread then
 //               issues the 140 MMAs (28 digit pairs x 5 K steps of 16);
-//   warp 11     the residual R = sum_q dNX P in double-float;
-//   warps 12-15 the epilogue: TMEM -> double-float K_e entries, staged in shared
-//               memory over the consumed A slices, written out coalesced in the
-//               node-rows layout the node gather reads.
+//   warp 9      the residual R = sum_q dNX P in double-float;
+//   warps 10-13 the epilogue: TMEM -> double-float values (row (e, i, k) holds
+//               K_(a,i),(b,k) for a <= b); each row thread takes the other
+//               half of its node rows from the transposed row (e, k, i) of the
+//               same warp by shuffles and stores whole 64-byte node rows of
+//               K_e to global memory in the layout the node gather reads.
+// The A slices are rewritten as soon as the MMAs that read them completed; the
+// next MMAs wait only for the epilogue's reads of the accumulators.
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -46,9 +52,9 @@
 namespace fec {
 namespace aff {
 
-constexpr int EPT = 14;              // elements per tile
+constexpr int EPT = 12;              // elements per tile (three per 32-row quarter)
 constexpr int NQ = 8;
-constexpr int NPT = EPT * NQ;        // quadrature points per tile (112)
+constexpr int NPT = EPT * NQ;        // quadrature points per tile (96)
 constexpr int KR = 72, KP = 80;      // reduction length r = (q, J, L), padded to 5 K steps
 constexpr int NPAIR = 36, NPAD = 48; // node pairs a <= b, padded N
 constexpr int ND = 7;                // digits per operand
@@ -63,46 +69,37 @@ constexpr int T_G = T_SIG + NPAD * 4;
 constexpr int T_JXW = T_G + NQ * 24 * 8;
 constexpr int T_BYTES = T_JXW + NQ * 8;
 static_assert(T_BYTES % 16 == 0 && T_G % 8 == 0, "table layout");
-// output staging over the A slices: each 8-row group of a slice holds 1152 bytes
-// of K columns 0..71 and 128 bytes of the (always zero) padding columns 72..79;
-// element el's K_e (72 node rows of 9 float2, the ninth a bank-spreading pad)
-// takes five groups' first 1152 bytes
-constexpr int ST_ROW = 9;
-constexpr int ST_PER_GROUP = 1152 / 8;  // float2 per group
-constexpr int ST_GROUPS = 5;
-static_assert(72 * ST_ROW <= ST_GROUPS * ST_PER_GROUP && EPT * ST_GROUPS <= ND * 16, "output staging");
 constexpr int TMEM_COLS = 512;
 constexpr long long WAIT_BUDGET = 2000000000LL;
 
-constexpr int PROD_W = 4, SL_W = 7, R_W = 1, EP_W = 4;
+constexpr int PROD_W = 3, SL_W = 6, R_W = 1, EP_W = 4;
 constexpr int NTHR = 32 * (PROD_W + SL_W + R_W + EP_W);
 constexpr int T_SL = 32 * PROD_W, T_R = T_SL + 32 * SL_W, T_EP = T_R + 32 * R_W;
 constexpr int NSL = 32 * SL_W;
-static_assert(NSL == 2 * NPT && T_EP / 32 == 12, "roles");
+static_assert(32 * PROD_W == NPT && NSL == 2 * NPT && (T_EP / 32) % 4 == 2, "roles");
 // named barriers (0 is __syncthreads)
 constexpr int BAR_FULL = 1;   // producers arrive, slicers + residual warp sync
 constexpr int BAR_EMPTY = 2;  // slicers + residual warp arrive, producers sync
-constexpr int BAR_AFREE = 3;  // epilogue arrives (slices consumed, staging written out), slicers sync
-constexpr int BAR_SL = 4;     // slicers
-constexpr int BAR_EP = 5;     // epilogue
+constexpr int BAR_SL = 3;     // slicers
 constexpr int N_FULL = 32 * (PROD_W + SL_W + R_W);
-constexpr int N_AFREE = 32 * (SL_W + EP_W);
+
+// MMA row of (element el of the tile, ik = 3 i + k)
+__host__ __device__ __forceinline__ int row_of(int el, int ik) { return 32 * (el / 3) + 9 * (el % 3) + ik; }
 
 template <class Model>
 struct Layout {
   static constexpr int W = 0;
   static constexpr int A = W + ND * W_SLICE;
-  static constexpr int P = A + ND * A_SLICE;                      // float2 [112][9]
-  static constexpr int SCR = P + NPT * 9 * 8;                     // float2 [112][SCR2]
+  static constexpr int P = A + ND * A_SLICE;                      // float2 [96][9]
+  static constexpr int SCR = P + NPT * 9 * 8;                     // float2 [96][SCR2]
   static constexpr int G = (SCR + NPT * Model::SCR2 * 8 + 15) / 16 * 16;  // double [8][24]
   static constexpr int G2 = G + NQ * 24 * 8;                      // float2 [8][24]
   static constexpr int JXW = G2 + NQ * 24 * 8;                    // double [8]
   static constexpr int SIG = JXW + NQ * 8;                        // int [48]
-  static constexpr int TAU = SIG + NPAD * 4;                      // int [14] (+pad)
-  static constexpr int CODE = TAU + 16 * 4;                       // uint32 [45] entry codes (+pad)
-  static constexpr int PAIR = CODE + 48 * 4;                      // uint8 [48] node pair a*8+b
-  static constexpr int BAR = (PAIR + 48 + 15) / 16 * 16;          // mbarriers: slices done, MMAs done
-  static constexpr int TSLOT = BAR + 16;
+  static constexpr int TAU = SIG + NPAD * 4;                      // int [2][12]: per tile parity
+  static constexpr int CODE = TAU + 2 * 16 * 4;                   // uint32 [45] entry codes (+pad)
+  static constexpr int BAR = (CODE + 48 * 4 + 15) / 16 * 16;      // mbarriers: slices, MMAs, TMEM read
+  static constexpr int TSLOT = BAR + 32;
   static constexpr int SMEM = TSLOT + 16;
   static_assert(SMEM <= 232448, "shared memory");
 };
@@ -121,38 +118,29 @@ __device__ __forceinline__ float pow2f(int k) { return __uint_as_float(uint32_t(
 __host__ __device__ __forceinline__ uint32_t op_off(int row, int col) {
   return uint32_t(row >> 3) * SBO + uint32_t(col >> 3) * 128 + uint32_t(row & 7) * 16 + uint32_t(col & 7) * 2;
 }
-// byte offset (within the A slices) of float2 f of element el's output staging
-__device__ __forceinline__ uint32_t st_off(int el, int f) {
-  const int grp = el * ST_GROUPS + f / ST_PER_GROUP;  // 0 .. 69
-  return uint32_t(grp >> 4) * A_SLICE + uint32_t(grp & 15) * SBO + uint32_t(f % ST_PER_GROUP) * 8;
-}
-
-// Seven 8-column loads (the seven levels of one column chunk) under one wait.
-__device__ __forceinline__ void tmem_ld8x7(uint32_t taddr, float (*v)[8]) {
-  uint32_t r[56];
+// Seven 4-column loads (the seven levels of one column chunk) under one wait.
+__device__ __forceinline__ void tmem_ld4x7(uint32_t taddr, float (*v)[4]) {
+  uint32_t r[28];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%56];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8, %9, %10, %11, %12, %13, %14, %15}, [%57];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16, %17, %18, %19, %20, %21, %22, %23}, [%58];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%24, %25, %26, %27, %28, %29, %30, %31}, [%59];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%32, %33, %34, %35, %36, %37, %38, %39}, [%60];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%40, %41, %42, %43, %44, %45, %46, %47}, [%61];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%48, %49, %50, %51, %52, %53, %54, %55}, [%62];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%28];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%4, %5, %6, %7}, [%29];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%8, %9, %10, %11}, [%30];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%12, %13, %14, %15}, [%31];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%16, %17, %18, %19}, [%32];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%20, %21, %22, %23}, [%33];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%24, %25, %26, %27}, [%34];\n\t"
       "tcgen05.wait::ld.sync.aligned;"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
         "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
         "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
-        "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
-        "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
-        "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55])
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27])
       : "r"(taddr), "r"(taddr + 48u), "r"(taddr + 96u), "r"(taddr + 144u), "r"(taddr + 192u), "r"(taddr + 240u),
         "r"(taddr + 288u)
       : "memory");
 #pragma unroll
   for (int L = 0; L < NLEV; ++L)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) v[L][j] = __uint_as_float(r[L * 8 + j]);
+    for (int j = 0; j < 4; ++j) v[L][j] = __uint_as_float(r[L * 4 + j]);
 }
 
 // kind::f16 (BF16 operands), FP32 accumulate, M = 128, N = 48, both K-major
@@ -220,13 +208,13 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
   int* s_sig = reinterpret_cast<int*>(sm + Lay::SIG);
   int* s_tau = reinterpret_cast<int*>(sm + Lay::TAU);
   uint32_t* s_code = reinterpret_cast<uint32_t*>(sm + Lay::CODE);
-  uint8_t* s_pair = sm + Lay::PAIR;
-  uint64_t* bar_sl = reinterpret_cast<uint64_t*>(sm + Lay::BAR);
-  uint64_t* bar_mma = bar_sl + 1;
+  uint64_t* bar_sl = reinterpret_cast<uint64_t*>(sm + Lay::BAR);  // slices of a tile written
+  uint64_t* bar_mma = bar_sl + 1;                                  // a tile's MMAs complete
+  uint64_t* bar_tfree = bar_sl + 2;                                // the epilogue read a tile's accumulators
   float2* s_P = reinterpret_cast<float2*>(sm + Lay::P);
   float2* s_scr = reinterpret_cast<float2*>(sm + Lay::SCR);
 
-  // ---- setup: A slices zero (their padding columns stay zero), W digits, tables ----
+  // ---- setup: A slices zero (padding rows and columns stay zero), W digits, tables ----
   for (int i = tid; i < ND * A_SLICE / 16; i += NTHR)
     reinterpret_cast<uint4*>(sm + Lay::A)[i] = make_uint4(0u, 0u, 0u, 0u);
   for (int i = tid; i < ND * W_SLICE / 16; i += NTHR)
@@ -240,7 +228,7 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
   if (tid < NPAD) s_sig[tid] = __ldg(reinterpret_cast<const int*>(tab + T_SIG) + tid);
   if (tid < 45) {
     // unique entry w = (r1, r2), r1 <= r2, r1 = 3i + J, r2 = 3k + L: i, J, k, L and
-    // the operand positions (row i*3+k, column J*3+L) and (row k*3+i, column L*3+J)
+    // the operand positions (row ik = 3i + k, column 3J + L) and (row 3k + i, column 3L + J)
     int m = tid, r = 0;
     for (int c = 0; c < 9; ++c)
       if (m >= 9 - r) { m -= 9 - r; ++r; }
@@ -250,17 +238,10 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
                   uint32_t(i * 3 + k) << 16 | uint32_t(J * 3 + L) << 20 | uint32_t(k * 3 + i) << 24 |
                   uint32_t(L * 3 + J) << 28;
   }
-  if (tid < NPAD) {
-    int a = 0, b = 0, n = tid;
-    if (n < NPAIR) {
-      while (n >= 8 - a) { n -= 8 - a; ++a; }
-      b = a + n;
-    }
-    s_pair[tid] = uint8_t(a * 8 + b);
-  }
   if (tid == 0) {
     mbar_init(bar_sl, NSL);
     mbar_init(bar_mma, 1);
+    mbar_init(bar_tfree, 32 * EP_W);
     mbar_fence_init();
   }
   if (warp == T_EP / 32) tmem_alloc(reinterpret_cast<uint32_t*>(sm + Lay::TSLOT), TMEM_COLS);
@@ -271,16 +252,23 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + Lay::TSLOT);
   const int64_t ntiles = (g.ne + EPT - 1) / EPT;
   const long long budget = g.wait_budget > 0 ? g.wait_budget : WAIT_BUDGET;
+  // a wait that gave up reports through the flag and waits again (the long
+  // budget) so that no buffer is reused under an operation in flight
+  auto wait_or_report = [&](uint64_t* bar, uint32_t par) {
+    if (!mbar_wait(bar, par, budget)) {
+      if (g.wait_err) atomicExch(g.wait_err, 1);
+      mbar_wait(bar, par, WAIT_BUDGET);
+    }
+  };
 
   if (tid < T_SL) {
     // ---------------- producers: thread (el, q) ----------------
     const int el = tid >> 3, q = tid & 7;
-    const bool active = tid < NPT;
     for (int k = 0;; ++k) {
       const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
       if (tile >= ntiles) break;
       const int64_t e = tile * EPT + el;
-      const bool live = active && e < g.ne;
+      const bool live = e < g.ne;
       double P9[9], scr[Model::SCR];
       point_phase<Model>(g, s_g, s_jxw, e, q, live, P9, scr);
       if (k >= 1) named_sync(BAR_EMPTY, N_FULL);  // tile k-1's staging has been read
@@ -296,6 +284,7 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
     // ---------------- slicers: thread (point p, half h) ----------------
     const int ts = tid - T_SL, p = ts >> 1, h = ts & 1, el = p >> 3, q = p & 7;
     const int w0 = h ? 23 : 0, cnt = h ? 22 : 23;
+    const int rbase = row_of(el, 0);
     for (int k = 0;; ++k) {
       const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
       if (tile >= ntiles) break;
@@ -321,15 +310,15 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
       if (mx > 0.f) frexpf(mx, &tau);  // |entry| < 2^tau
       tau = tau < -119 ? -119 : (tau > 126 ? 126 : tau);
       const float fs = pow2f(7 - tau);  // entries scaled to |x| < 128
-      if (k >= 1) named_sync(BAR_AFREE, N_AFREE);  // the epilogue is done with the slices
-      if ((ts & 15) == 0) s_tau[el] = tau;
+      if (k >= 1) wait_or_report(bar_mma, uint32_t((k - 1) & 1));  // tile k-1's MMAs read the slices
+      if ((ts & 15) == 0) s_tau[(k & 1) * 16 + el] = tau;
       unsigned char* As = sm + Lay::A;
 #pragma unroll
       for (int c = 0; c < 23; ++c) {
         if (c >= cnt) break;
         const uint32_t code = s_code[w0 + c];
-        const int row = el * 9 + int((code >> 16) & 15), col = q * 9 + int((code >> 20) & 15);
-        const int row2 = el * 9 + int((code >> 24) & 15), col2 = q * 9 + int(code >> 28);
+        const int row = rbase + int((code >> 16) & 15), col = q * 9 + int((code >> 20) & 15);
+        const int row2 = rbase + int((code >> 24) & 15), col2 = q * 9 + int(code >> 28);
         const bool twin = row != row2 || col != col2;
         const uint32_t o1 = op_off(row, col), o2 = op_off(row2, col2);
         float xh = av[c].x * fs, xl = av[c].y * fs;
@@ -347,6 +336,7 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
       mbar_arrive(bar_sl);
       named_sync(BAR_SL, NSL);
       if (ts == 0) {
+        if (k >= 1) wait_or_report(bar_tfree, uint32_t((k - 1) & 1));  // the accumulators are free
         tc_fence_after();
         const uint32_t aB = s0 + Lay::A, wB = s0 + Lay::W;
 #pragma unroll 1
@@ -374,49 +364,43 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
       named_sync(BAR_FULL, N_FULL);
       if (WANT_R) {
         for (int idx = lane; idx < EPT * 24; idx += 32) {
-          const int el = idx / 24, ai = idx % 24, a = ai / 3, i = ai % 3;
+          const int el = idx / 24, ai = idx % 24;
           const int64_t e = tile * EPT + el;
-          if (e >= g.ne) continue;
-          static_cast<double*>(g.Re)[e * 24 + ai] = residual_entry(s_g2, s_P + el * NQ * 9, a, i);
+          if (e < g.ne) static_cast<double*>(g.Re)[e * 24 + ai] = residual_entry(s_g2, s_P + el * NQ * 9, ai / 3, ai % 3);
         }
       }
       named_arrive(BAR_EMPTY, N_FULL);
     }
   } else {
     // ---------------- epilogue: thread = TMEM lane = row (el, i, k) ----------------
-    const int te = tid - T_EP, qw = warp & 3, m = qw * 32 + lane;
-    const int el = m / 9, ik = m % 9, i = ik / 3, kc = ik % 3;
+    const int qw = warp & 3;
+    const int el = qw * 3 + (lane < 27 ? lane / 9 : 0), ik = lane % 9, i = ik / 3, kc = ik % 3;
+    const int partner = (lane < 27 ? lane - ik : lane) + (lane < 27 ? kc * 3 + i : 0);  // row (el, k, i)
     const uint32_t lane_addr = tmem + (uint32_t(qw * 32) << 16);
     for (int k = 0;; ++k) {
       const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
       if (tile >= ntiles) break;
       const uint32_t par = uint32_t(k & 1);
-      bool ok = mbar_wait(bar_sl, par, budget);
-      ok = mbar_wait(bar_mma, par, budget) && ok;
-      if (!ok) {
-        // report, then wait out the MMAs so the accumulators are not reused or
-        // freed under them (the outputs of this call are invalid)
-        if (g.wait_err && lane == 0) atomicExch(g.wait_err, 1);
-        mbar_wait(bar_sl, par, WAIT_BUDGET);
-        mbar_wait(bar_mma, par, WAIT_BUDGET);
-      }
+      wait_or_report(bar_sl, par);
+      wait_or_report(bar_mma, par);
       tc_fence_after();
       const int64_t e0 = tile * EPT;
-      const bool live = m < EPT * 9 && e0 + el < g.ne;
-      const int tau = live ? s_tau[el] : 0;
-#pragma unroll 1
-      for (int c = 0; c < 5; ++c) {
-        float v[NLEV][8];
-        tmem_ld8x7(lane_addr + uint32_t(c * 8), v);
-        if (!live) continue;
+      const bool live = lane < 27 && e0 + el < g.ne;
+      const int tau = s_tau[(k & 1) * 16 + el];
+      const float f1 = pow2f(tau - 7);
+      float2 own[NPAIR];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int n = c * 8 + j;
-          if (n >= NPAIR) break;
-          // sum_L v_L 2^(-8L) in double-float, from the smallest level up
-          float hi = v[NLEV - 1][j], lo = 0.f;
+      for (int c = 0; c < NPAIR / 4; ++c) {
+        float v[NLEV][4];
+        tmem_ld4x7(lane_addr + uint32_t(c * 4), v);
 #pragma unroll
-          for (int L = NLEV - 2; L >= 0; --L) {
+        for (int j = 0; j < 4; ++j) {
+          const int n = c * 4 + j;
+          // sum_L v_L 2^(-8L): levels 6..4 in FP32 (their rounding is below 2^-55
+          // of level 0), then 3..0 in double-float
+          float hi = fmaf(fmaf(v[6][j], 0.00390625f, v[5][j]), 0.00390625f, v[4][j]), lo = 0.f;
+#pragma unroll
+          for (int L = 3; L >= 0; --L) {
             const float a = v[L][j], b = hi * 0.00390625f;
             lo *= 0.00390625f;
             const float s = a + b, bb = s - a;
@@ -424,26 +408,33 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
             hi = s + lo;
             lo = lo - (hi - s);
           }
-          const float f1 = pow2f(tau - 7), f2 = pow2f(s_sig[n] - 7);
-          const float2 val = make_float2(hi * f1 * f2, lo * f1 * f2);
-          const int ab = s_pair[n], a = ab >> 3, b = ab & 7;
-          *reinterpret_cast<float2*>(sm + Lay::A + st_off(el, ((a * 3 + i) * 3 + kc) * ST_ROW + b)) = val;
-          if (a != b) *reinterpret_cast<float2*>(sm + Lay::A + st_off(el, ((b * 3 + kc) * 3 + i) * ST_ROW + a)) = val;
+          const float f = f1 * pow2f(s_sig[n] - 7);
+          own[n] = make_float2(hi * f, lo * f);
         }
       }
       tc_fence_before();
-      named_sync(BAR_EP, 32 * EP_W);
-      // write K_e out: 576 float2 per element in the node-rows layout, two per thread and step
-      const int64_t left = g.ne - e0;
-      const int nlive = left < EPT ? int(left) : EPT;
-      float4* dst = reinterpret_cast<float4*>(static_cast<float2*>(g.Ke) + e0 * 576);
-      for (int idx = te; idx < nlive * 288; idx += 32 * EP_W) {
-        const int ee = idx / 288, w = (idx % 288) * 2, f = (w >> 3) * ST_ROW + (w & 7);
-        const float2 x0 = *reinterpret_cast<const float2*>(sm + Lay::A + st_off(ee, f));
-        const float2 x1 = *reinterpret_cast<const float2*>(sm + Lay::A + st_off(ee, f + 1));
-        dst[idx] = make_float4(x0.x, x0.y, x1.x, x1.y);
+      mbar_arrive(bar_tfree);  // the accumulators may be overwritten
+      // node row (c, i, k) of K_e: K_(c,i),(b,k) = own pair (c, b) for b >= c, the
+      // partner row's pair (b, c) for b < c
+      float4* dst = reinterpret_cast<float4*>(static_cast<float2*>(g.Ke) + (e0 + el) * 576);
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        float2 row[8];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+          if (b >= c) {
+            row[b] = own[(c * (15 - c)) / 2 + b];   // pair index of (c, b), c <= b
+          } else {
+            const float2 t = own[(b * (15 - b)) / 2 + c];  // this thread's (b, c); the partner's is wanted
+            row[b] = make_float2(__shfl_sync(0xffffffffu, t.x, partner), __shfl_sync(0xffffffffu, t.y, partner));
+          }
+        }
+        if (live) {
+          float4* d = dst + ((c * 3 + i) * 3 + kc) * 4;
+#pragma unroll
+          for (int b = 0; b < 8; b += 2) d[b / 2] = make_float4(row[b].x, row[b].y, row[b + 1].x, row[b + 1].y);
+        }
       }
-      named_arrive(BAR_AFREE, N_AFREE);
     }
   }
   tc_fence_before();
