@@ -70,6 +70,7 @@ constexpr int T_JXW = T_G + NQ * 24 * 8;
 constexpr int T_BYTES = T_JXW + NQ * 8;
 static_assert(T_BYTES % 16 == 0 && T_G % 8 == 0, "table layout");
 constexpr int TMEM_COLS = 512;
+constexpr int TM_OWN = NLEV * NPAD;  // 72 columns after the accumulators: the epilogue's (hi, lo) per pair
 constexpr long long WAIT_BUDGET = 2000000000LL;
 
 constexpr int PROD_W = 3, SL_W = 6, R_W = 1, EP_W = 4;
@@ -141,6 +142,36 @@ __device__ __forceinline__ void tmem_ld4x7(uint32_t taddr, float (*v)[4]) {
   for (int L = 0; L < NLEV; ++L)
 #pragma unroll
     for (int j = 0; j < 4; ++j) v[L][j] = __uint_as_float(r[L * 4 + j]);
+}
+
+// 8 consecutive 32-bit columns of this thread's lane from registers.
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float* v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
+               "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+               "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+               "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+// Eight 2-column loads (addresses a[0..7]) under one wait.
+__device__ __forceinline__ void tmem_ld2x8(const uint32_t* a, float2* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%16];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%2, %3}, [%17];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%4, %5}, [%18];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%6, %7}, [%19];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%8, %9}, [%20];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%10, %11}, [%21];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%12, %13}, [%22];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%14, %15}, [%23];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7])
+      : "memory");
+#pragma unroll
+  for (int j = 0; j < 8; ++j) v[j] = make_float2(__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1]));
 }
 
 // kind::f16 (BF16 operands), FP32 accumulate, M = 128, N = 48, both K-major
@@ -290,20 +321,10 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
       if (tile >= ntiles) break;
       const bool live = tile * EPT + el < g.ne;
       named_sync(BAR_FULL, N_FULL);
-      float2 av[23];
-      float mx = 0.f;
+      // the element's scale from a bound of its points' tangent entries (the
+      // element's 16 threads are lanes 16*(el%2) .. +15 of this warp)
       const float2* sc = s_scr + p * SCR2;
-#pragma unroll
-      for (int c = 0; c < 23; ++c) {
-        av[c] = make_float2(0.f, 0.f);
-        if (c < cnt && live) {
-          const uint32_t code = s_code[w0 + c];
-          av[c] = Model::aentry_df64(sc, code & 15, (code >> 4) & 15, (code >> 8) & 15, (code >> 12) & 15);
-          mx = fmaxf(mx, fabsf(av[c].x));
-        }
-      }
-      named_arrive(BAR_EMPTY, N_FULL);  // the staging may be refilled
-      // the element's scale: its 16 threads are lanes 16*(el%2) .. +15 of this warp
+      float mx = live ? Model::abound(sc) * 1.0001f : 0.f;
 #pragma unroll
       for (int o = 1; o < 16; o <<= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
       int tau = 0;
@@ -313,25 +334,28 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
       if (k >= 1) wait_or_report(bar_mma, uint32_t((k - 1) & 1));  // tile k-1's MMAs read the slices
       if ((ts & 15) == 0) s_tau[(k & 1) * 16 + el] = tau;
       unsigned char* As = sm + Lay::A;
-#pragma unroll
-      for (int c = 0; c < 23; ++c) {
-        if (c >= cnt) break;
+#pragma unroll 1
+      for (int c = 0; c < cnt; ++c) {
         const uint32_t code = s_code[w0 + c];
+        float2 av = make_float2(0.f, 0.f);
+        if (live) av = Model::aentry_df64(sc, code & 15, (code >> 4) & 15, (code >> 8) & 15, (code >> 12) & 15);
         const int row = rbase + int((code >> 16) & 15), col = q * 9 + int((code >> 20) & 15);
         const int row2 = rbase + int((code >> 24) & 15), col2 = q * 9 + int(code >> 28);
         const bool twin = row != row2 || col != col2;
-        const uint32_t o1 = op_off(row, col), o2 = op_off(row2, col2);
-        float xh = av[c].x * fs, xl = av[c].y * fs;
+        unsigned char* p1 = As + op_off(row, col);
+        unsigned char* p2 = As + op_off(row2, col2);
+        float xh = av.x * fs, xl = av.y * fs;
 #pragma unroll
         for (int s = 0; s < ND; ++s) {
           const float dh = rintf(xh), dl = rintf(xl);
           xh = (xh - dh) * 256.f;
           xl = (xl - dl) * 256.f;
           const unsigned short bits = static_cast<unsigned short>(__float_as_uint(dh + dl) >> 16);
-          *reinterpret_cast<unsigned short*>(As + s * A_SLICE + o1) = bits;
-          if (twin) *reinterpret_cast<unsigned short*>(As + s * A_SLICE + o2) = bits;
+          *reinterpret_cast<unsigned short*>(p1 + s * A_SLICE) = bits;
+          if (twin) *reinterpret_cast<unsigned short*>(p2 + s * A_SLICE) = bits;
         }
       }
+      named_arrive(BAR_EMPTY, N_FULL);  // the staging may be refilled
       fence_async_smem();
       mbar_arrive(bar_sl);
       named_sync(BAR_SL, NSL);
@@ -388,14 +412,15 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
       const bool live = lane < 27 && e0 + el < g.ne;
       const int tau = s_tau[(k & 1) * 16 + el];
       const float f1 = pow2f(tau - 7);
-      float2 own[NPAIR];
-#pragma unroll
+      // levels -> double-float values of the 36 pairs, staged in this lane's TMEM
+      // columns TM_OWN + 2n (hi), + 2n + 1 (lo)
+#pragma unroll 1
       for (int c = 0; c < NPAIR / 4; ++c) {
         float v[NLEV][4];
         tmem_ld4x7(lane_addr + uint32_t(c * 4), v);
+        float out[8];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          const int n = c * 4 + j;
           // sum_L v_L 2^(-8L): levels 6..4 in FP32 (their rounding is below 2^-55
           // of level 0), then 3..0 in double-float
           float hi = fmaf(fmaf(v[6][j], 0.00390625f, v[5][j]), 0.00390625f, v[4][j]), lo = 0.f;
@@ -408,26 +433,32 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
             hi = s + lo;
             lo = lo - (hi - s);
           }
-          const float f = f1 * pow2f(s_sig[n] - 7);
-          own[n] = make_float2(hi * f, lo * f);
+          const float f = f1 * pow2f(s_sig[c * 4 + j] - 7);
+          out[2 * j] = hi * f;
+          out[2 * j + 1] = lo * f;
         }
+        tmem_st8(lane_addr + uint32_t(TM_OWN + c * 8), out);
       }
+      tmem_wait_st();
       tc_fence_before();
       mbar_arrive(bar_tfree);  // the accumulators may be overwritten
-      // node row (c, i, k) of K_e: K_(c,i),(b,k) = own pair (c, b) for b >= c, the
-      // partner row's pair (b, c) for b < c
+      // node row (c, i, k) of K_e: K_(c,i),(b,k) = this row's pair (c, b) for b >= c,
+      // the partner row's pair (b, c) for b < c
       float4* dst = reinterpret_cast<float4*>(static_cast<float2*>(g.Ke) + (e0 + el) * 576);
-#pragma unroll
+#pragma unroll 1
       for (int c = 0; c < 8; ++c) {
-        float2 row[8];
+        uint32_t addr[8];
 #pragma unroll
         for (int b = 0; b < 8; ++b) {
-          if (b >= c) {
-            row[b] = own[(c * (15 - c)) / 2 + b];   // pair index of (c, b), c <= b
-          } else {
-            const float2 t = own[(b * (15 - b)) / 2 + c];  // this thread's (b, c); the partner's is wanted
-            row[b] = make_float2(__shfl_sync(0xffffffffu, t.x, partner), __shfl_sync(0xffffffffu, t.y, partner));
-          }
+          const int n = b >= c ? (c * (15 - c)) / 2 + b : (b * (15 - b)) / 2 + c;
+          addr[b] = lane_addr + uint32_t(TM_OWN + 2 * n);
+        }
+        float2 row[8];
+        tmem_ld2x8(addr, row);
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+          const float x = __shfl_sync(0xffffffffu, row[b].x, partner), y = __shfl_sync(0xffffffffu, row[b].y, partner);
+          if (b < c) row[b] = make_float2(x, y);
         }
         if (live) {
           float4* d = dst + ((c * 3 + i) * 3 + kc) * 4;

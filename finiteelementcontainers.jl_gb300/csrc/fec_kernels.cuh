@@ -426,6 +426,17 @@ struct NeoHookean {
     for (int m = 0; m < 21; ++m) out[m] = df64_split(scr[m]);
     out[21] = df64_split(-2.0 / 3.0 * scr[20]);
   }
+  // An upper bound of max |JxW A_iJkL| from the df64 scratch (hi parts, FP32):
+  // (|a1| + |a2|) max|H|^2 + 2 |2/3 c2| max|H| max|F| + |c2|.
+  __device__ static float abound(const float2* s) {
+    float hm = 0.f, fm = 0.f;
+#pragma unroll
+    for (int m = 0; m < 9; ++m) {
+      fm = fmaxf(fm, fabsf(s[m].x));
+      hm = fmaxf(hm, fabsf(s[9 + m].x));
+    }
+    return (fabsf(s[18].x) + fabsf(s[19].x)) * hm * hm + 2.f * fabsf(s[21].x) * hm * fm + fabsf(s[20].x);
+  }
   // JxW A_iJkL in df64
   __device__ static float2 aentry_df64(const float2* s, int i, int J, int k, int L) {
     const float2* F = s;
@@ -566,6 +577,13 @@ struct J2 {
     out[9] = df64_split(scr[9] - scr[10] / 3.0);
     out[10] = df64_split(0.5 * scr[10]);
     out[11] = df64_split(scr[11]);
+  }
+  // An upper bound of max |C_iJkL| from the df64 scratch: |mb'| max|n|^2 + |c_a| + 2 |c_b|.
+  __device__ static float abound(const float2* s) {
+    float nm = 0.f;
+#pragma unroll
+    for (int m = 0; m < 9; ++m) nm = fmaxf(nm, fabsf(s[m].x));
+    return fabsf(s[11].x) * nm * nm + fabsf(s[9].x) + 2.f * fabsf(s[10].x);
   }
   __device__ static float2 aentry_df64(const float2* s, int i, int J, int k, int L) {
     float2 v = df64_neg(df64_mul(s[11], df64_mul(s[i * 3 + J], s[k * 3 + L])));
