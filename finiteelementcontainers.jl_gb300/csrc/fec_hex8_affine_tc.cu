@@ -98,7 +98,8 @@ struct Layout {
   static constexpr int JXW = G2 + NQ * 24 * 8;                    // double [8]
   static constexpr int SIG = JXW + NQ * 8;                        // int [48]
   static constexpr int TAU = SIG + NPAD * 4;                      // int [2][12]: per tile parity
-  static constexpr int CODE = TAU + 2 * 16 * 4;                   // uint32 [45] entry codes (+pad)
+  static constexpr int TAUST = TAU + 2 * 16 * 4;                  // int [12]: the staged tile's scales
+  static constexpr int CODE = TAUST + 16 * 4;                     // uint32 [45] entry codes (+pad)
   static constexpr int BAR = (CODE + 48 * 4 + 15) / 16 * 16;      // mbarriers: slices, MMAs, TMEM read
   static constexpr int TSLOT = BAR + 32;
   static constexpr int SMEM = TSLOT + 16;
@@ -238,6 +239,7 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
   double* s_jxw = reinterpret_cast<double*>(sm + Lay::JXW);
   int* s_sig = reinterpret_cast<int*>(sm + Lay::SIG);
   int* s_tau = reinterpret_cast<int*>(sm + Lay::TAU);
+  int* s_taust = reinterpret_cast<int*>(sm + Lay::TAUST);
   uint32_t* s_code = reinterpret_cast<uint32_t*>(sm + Lay::CODE);
   uint64_t* bar_sl = reinterpret_cast<uint64_t*>(sm + Lay::BAR);  // slices of a tile written
   uint64_t* bar_mma = bar_sl + 1;                                  // a tile's MMAs complete
@@ -303,11 +305,22 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
       double P9[9], scr[Model::SCR];
       point_phase<Model>(g, s_g, s_jxw, e, q, live, P9, scr);
       if (k >= 1) named_sync(BAR_EMPTY, N_FULL);  // tile k-1's staging has been read
+      float bnd = 0.f;
       if (live) {
         float2* pP = s_P + tid * 9;
 #pragma unroll
         for (int m = 0; m < 9; ++m) pP[m] = df64_split(P9[m]);
         Model::split_scratch(scr, s_scr + tid * SCR2);
+        bnd = Model::abound(s_scr + tid * SCR2) * 1.0001f;
+      }
+      // the element's scale 2^tau > |every tangent entry| (its eight points are
+      // lanes 8j .. 8j+7 of this warp)
+#pragma unroll
+      for (int o = 1; o < 8; o <<= 1) bnd = fmaxf(bnd, __shfl_xor_sync(0xffffffffu, bnd, o));
+      if (q == 0) {
+        int tau = 0;
+        if (bnd > 0.f) frexpf(bnd, &tau);
+        s_taust[el] = tau < -119 ? -119 : (tau > 126 ? 126 : tau);
       }
       named_arrive(BAR_FULL, N_FULL);
     }
@@ -321,38 +334,41 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
       if (tile >= ntiles) break;
       const bool live = tile * EPT + el < g.ne;
       named_sync(BAR_FULL, N_FULL);
-      // the element's scale from a bound of its points' tangent entries (the
-      // element's 16 threads are lanes 16*(el%2) .. +15 of this warp)
       const float2* sc = s_scr + p * SCR2;
-      float mx = live ? Model::abound(sc) * 1.0001f : 0.f;
-#pragma unroll
-      for (int o = 1; o < 16; o <<= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-      int tau = 0;
-      if (mx > 0.f) frexpf(mx, &tau);  // |entry| < 2^tau
-      tau = tau < -119 ? -119 : (tau > 126 ? 126 : tau);
+      const int tau = s_taust[el];
       const float fs = pow2f(7 - tau);  // entries scaled to |x| < 128
       if (k >= 1) wait_or_report(bar_mma, uint32_t((k - 1) & 1));  // tile k-1's MMAs read the slices
       if ((ts & 15) == 0) s_tau[(k & 1) * 16 + el] = tau;
       unsigned char* As = sm + Lay::A;
+      // two entries per step (independent chains)
 #pragma unroll 1
-      for (int c = 0; c < cnt; ++c) {
-        const uint32_t code = s_code[w0 + c];
-        float2 av = make_float2(0.f, 0.f);
-        if (live) av = Model::aentry_df64(sc, code & 15, (code >> 4) & 15, (code >> 8) & 15, (code >> 12) & 15);
-        const int row = rbase + int((code >> 16) & 15), col = q * 9 + int((code >> 20) & 15);
-        const int row2 = rbase + int((code >> 24) & 15), col2 = q * 9 + int(code >> 28);
-        const bool twin = row != row2 || col != col2;
-        unsigned char* p1 = As + op_off(row, col);
-        unsigned char* p2 = As + op_off(row2, col2);
-        float xh = av.x * fs, xl = av.y * fs;
+      for (int c = 0; c < cnt; c += 2) {
+        const bool two = c + 1 < cnt;
+        const uint32_t code0 = s_code[w0 + c], code1 = s_code[w0 + c + (two ? 1 : 0)];
+        float2 a0 = make_float2(0.f, 0.f), a1 = a0;
+        if (live) {
+          a0 = Model::aentry_df64(sc, code0 & 15, (code0 >> 4) & 15, (code0 >> 8) & 15, (code0 >> 12) & 15);
+          a1 = Model::aentry_df64(sc, code1 & 15, (code1 >> 4) & 15, (code1 >> 8) & 15, (code1 >> 12) & 15);
+        }
+        unsigned char* p10 = As + op_off(rbase + int((code0 >> 16) & 15), q * 9 + int((code0 >> 20) & 15));
+        unsigned char* p20 = As + op_off(rbase + int((code0 >> 24) & 15), q * 9 + int(code0 >> 28));
+        unsigned char* p11 = As + op_off(rbase + int((code1 >> 16) & 15), q * 9 + int((code1 >> 20) & 15));
+        unsigned char* p21 = As + op_off(rbase + int((code1 >> 24) & 15), q * 9 + int(code1 >> 28));
+        const bool twin0 = p10 != p20, twin1 = two && p11 != p21;
+        float xh0 = a0.x * fs, xl0 = a0.y * fs, xh1 = a1.x * fs, xl1 = a1.y * fs;
 #pragma unroll
         for (int s = 0; s < ND; ++s) {
-          const float dh = rintf(xh), dl = rintf(xl);
-          xh = (xh - dh) * 256.f;
-          xl = (xl - dl) * 256.f;
-          const unsigned short bits = static_cast<unsigned short>(__float_as_uint(dh + dl) >> 16);
-          *reinterpret_cast<unsigned short*>(p1 + s * A_SLICE) = bits;
-          if (twin) *reinterpret_cast<unsigned short*>(p2 + s * A_SLICE) = bits;
+          const float dh0 = rintf(xh0), dl0 = rintf(xl0), dh1 = rintf(xh1), dl1 = rintf(xl1);
+          xh0 = (xh0 - dh0) * 256.f;
+          xl0 = (xl0 - dl0) * 256.f;
+          xh1 = (xh1 - dh1) * 256.f;
+          xl1 = (xl1 - dl1) * 256.f;
+          const unsigned short b0 = static_cast<unsigned short>(__float_as_uint(dh0 + dl0) >> 16);
+          const unsigned short b1 = static_cast<unsigned short>(__float_as_uint(dh1 + dl1) >> 16);
+          *reinterpret_cast<unsigned short*>(p10 + s * A_SLICE) = b0;
+          if (twin0) *reinterpret_cast<unsigned short*>(p20 + s * A_SLICE) = b0;
+          if (two) *reinterpret_cast<unsigned short*>(p11 + s * A_SLICE) = b1;
+          if (twin1) *reinterpret_cast<unsigned short*>(p21 + s * A_SLICE) = b1;
         }
       }
       named_arrive(BAR_EMPTY, N_FULL);  // the staging may be refilled
@@ -387,10 +403,13 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
       if (tile >= ntiles) break;
       named_sync(BAR_FULL, N_FULL);
       if (WANT_R) {
-        for (int idx = lane; idx < EPT * 24; idx += 32) {
-          const int el = idx / 24, ai = idx % 24;
+        static_assert(EPT * 24 % 32 == 0, "residual entries per lane");
+#pragma unroll 3
+        for (int j = 0; j < EPT * 24 / 32; ++j) {
+          const int idx = lane + 32 * j, el = idx / 24, ai = idx % 24;
           const int64_t e = tile * EPT + el;
-          if (e < g.ne) static_cast<double*>(g.Re)[e * 24 + ai] = residual_entry(s_g2, s_P + el * NQ * 9, ai / 3, ai % 3);
+          const double r = residual_entry(s_g2, s_P + el * NQ * 9, ai / 3, ai % 3);
+          if (e < g.ne) static_cast<double*>(g.Re)[e * 24 + ai] = r;
         }
       }
       named_arrive(BAR_EMPTY, N_FULL);
