@@ -71,6 +71,8 @@ constexpr int T_BYTES = T_JXW + NQ * 8;
 static_assert(T_BYTES % 16 == 0 && T_G % 8 == 0, "table layout");
 constexpr int TMEM_COLS = 512;
 constexpr int TM_OWN = NLEV * NPAD;  // 72 columns after the accumulators: the epilogue's (hi, lo) per pair
+constexpr int TM_ENT = TM_OWN + 2 * NPAIR;  // 2 x 48 columns: the slicers' scaled tangent entries (hi, lo)
+static_assert(TM_ENT + 2 * 48 <= TMEM_COLS, "tensor memory columns");
 constexpr long long WAIT_BUDGET = 2000000000LL;
 
 constexpr int PROD_W = 3, SL_W = 6, R_W = 1, EP_W = 4;
@@ -152,6 +154,22 @@ __device__ __forceinline__ void tmem_st8(uint32_t taddr, const float* v) {
                "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
                "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
                : "memory");
+}
+__device__ __forceinline__ void tmem_st2(uint32_t taddr, float a, float b) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1, %2};" ::"r"(taddr), "r"(__float_as_uint(a)),
+               "r"(__float_as_uint(b))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
 }
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 // Eight 2-column loads (addresses a[0..7]) under one wait.
@@ -329,6 +347,8 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
     const int ts = tid - T_SL, p = ts >> 1, h = ts & 1, el = p >> 3, q = p & 7;
     const int w0 = h ? 23 : 0, cnt = h ? 22 : 23;
     const int rbase = row_of(el, 0);
+    // this warp's TMEM lanes (quarter warp % 4) and entry columns (two slicer warps share quarters 0 and 3)
+    const uint32_t ent = tmem + (uint32_t((warp & 3) * 32) << 16) + uint32_t(TM_ENT + (warp >= 7 ? 48 : 0));
     for (int k = 0;; ++k) {
       const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
       if (tile >= ntiles) break;
@@ -337,41 +357,51 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
       const float2* sc = s_scr + p * SCR2;
       const int tau = s_taust[el];
       const float fs = pow2f(7 - tau);  // entries scaled to |x| < 128
-      if (k >= 1) wait_or_report(bar_mma, uint32_t((k - 1) & 1));  // tile k-1's MMAs read the slices
+      // pass 1 (overlaps the previous tile's MMAs): the scaled entries into this
+      // lane's TMEM columns ent + 2c (hi), + 2c + 1 (lo); 23 steps on every lane
+      // (the .sync.aligned stores), the 23rd a zero on the half with 22
+#pragma unroll 1
+      for (int c = 0; c < 23; c += 2) {
+        const int c1 = c + 1 < 23 ? c + 1 : c;
+        const uint32_t code0 = s_code[w0 + (c < cnt ? c : 0)], code1 = s_code[w0 + (c1 < cnt ? c1 : 0)];
+        float2 a0 = make_float2(0.f, 0.f), a1 = a0;
+        if (live && c < cnt)
+          a0 = Model::aentry_df64(sc, code0 & 15, (code0 >> 4) & 15, (code0 >> 8) & 15, (code0 >> 12) & 15);
+        if (live && c1 < cnt)
+          a1 = Model::aentry_df64(sc, code1 & 15, (code1 >> 4) & 15, (code1 >> 8) & 15, (code1 >> 12) & 15);
+        tmem_st2(ent + uint32_t(2 * c), a0.x * fs, a0.y * fs);
+        if (c + 1 < 23) tmem_st2(ent + uint32_t(2 * c + 2), a1.x * fs, a1.y * fs);
+      }
+      tmem_wait_st();
+      named_arrive(BAR_EMPTY, N_FULL);  // the staging may be refilled
+      // pass 2: the digits, once tile k-1's MMAs have read the slices
+      if (k >= 1) wait_or_report(bar_mma, uint32_t((k - 1) & 1));
       if ((ts & 15) == 0) s_tau[(k & 1) * 16 + el] = tau;
       unsigned char* As = sm + Lay::A;
-      // two entries per step (independent chains)
 #pragma unroll 1
-      for (int c = 0; c < cnt; c += 2) {
-        const bool two = c + 1 < cnt;
-        const uint32_t code0 = s_code[w0 + c], code1 = s_code[w0 + c + (two ? 1 : 0)];
-        float2 a0 = make_float2(0.f, 0.f), a1 = a0;
-        if (live) {
-          a0 = Model::aentry_df64(sc, code0 & 15, (code0 >> 4) & 15, (code0 >> 8) & 15, (code0 >> 12) & 15);
-          a1 = Model::aentry_df64(sc, code1 & 15, (code1 >> 4) & 15, (code1 >> 8) & 15, (code1 >> 12) & 15);
-        }
-        unsigned char* p10 = As + op_off(rbase + int((code0 >> 16) & 15), q * 9 + int((code0 >> 20) & 15));
-        unsigned char* p20 = As + op_off(rbase + int((code0 >> 24) & 15), q * 9 + int(code0 >> 28));
-        unsigned char* p11 = As + op_off(rbase + int((code1 >> 16) & 15), q * 9 + int((code1 >> 20) & 15));
-        unsigned char* p21 = As + op_off(rbase + int((code1 >> 24) & 15), q * 9 + int(code1 >> 28));
-        const bool twin0 = p10 != p20, twin1 = two && p11 != p21;
-        float xh0 = a0.x * fs, xl0 = a0.y * fs, xh1 = a1.x * fs, xl1 = a1.y * fs;
+      for (int c0 = 0; c0 < 24; c0 += 4) {
+        float x[8];
+        tmem_ld8(ent + uint32_t(2 * c0), x);
 #pragma unroll
-        for (int s = 0; s < ND; ++s) {
-          const float dh0 = rintf(xh0), dl0 = rintf(xl0), dh1 = rintf(xh1), dl1 = rintf(xl1);
-          xh0 = (xh0 - dh0) * 256.f;
-          xl0 = (xl0 - dl0) * 256.f;
-          xh1 = (xh1 - dh1) * 256.f;
-          xl1 = (xl1 - dl1) * 256.f;
-          const unsigned short b0 = static_cast<unsigned short>(__float_as_uint(dh0 + dl0) >> 16);
-          const unsigned short b1 = static_cast<unsigned short>(__float_as_uint(dh1 + dl1) >> 16);
-          *reinterpret_cast<unsigned short*>(p10 + s * A_SLICE) = b0;
-          if (twin0) *reinterpret_cast<unsigned short*>(p20 + s * A_SLICE) = b0;
-          if (two) *reinterpret_cast<unsigned short*>(p11 + s * A_SLICE) = b1;
-          if (twin1) *reinterpret_cast<unsigned short*>(p21 + s * A_SLICE) = b1;
+        for (int j = 0; j < 4; ++j) {
+          const int c = c0 + j;
+          if (c >= cnt) break;
+          const uint32_t code = s_code[w0 + c];
+          unsigned char* p1 = As + op_off(rbase + int((code >> 16) & 15), q * 9 + int((code >> 20) & 15));
+          unsigned char* p2 = As + op_off(rbase + int((code >> 24) & 15), q * 9 + int(code >> 28));
+          const bool twin = p1 != p2;
+          float xh = x[2 * j], xl = x[2 * j + 1];
+#pragma unroll
+          for (int s = 0; s < ND; ++s) {
+            const float dh = rintf(xh), dl = rintf(xl);
+            xh = (xh - dh) * 256.f;
+            xl = (xl - dl) * 256.f;
+            const unsigned short bits = static_cast<unsigned short>(__float_as_uint(dh + dl) >> 16);
+            *reinterpret_cast<unsigned short*>(p1 + s * A_SLICE) = bits;
+            if (twin) *reinterpret_cast<unsigned short*>(p2 + s * A_SLICE) = bits;
+          }
         }
       }
-      named_arrive(BAR_EMPTY, N_FULL);  // the staging may be refilled
       fence_async_smem();
       mbar_arrive(bar_sl);
       named_sync(BAR_SL, NSL);
