@@ -27,15 +27,16 @@
 // warp's TMEM lanes, lanes 27-31 of each warp are padding rows.
 //   warps 0-2   FP64 point phase (displacement gradient, constitutive update),
 //               one thread per quadrature point, into a staging area;
-//   warps 3-8   tangent entries (45 unique per point, double-float), the element
-//               scale, the digits into the seven A slices; one thread then
-//               issues the 140 MMAs (28 digit pairs x 5 K steps of 16);
+//   warps 3-8   tangent entries (45 unique per point, double-float), parked in
+//               TMEM, then (once the previous tile's MMAs read the slices) their
+//               digits into the seven A slices;
 //   warp 9      the residual R = sum_q dNX P in double-float;
 //   warps 10-13 the epilogue: TMEM -> double-float values (row (e, i, k) holds
 //               K_(a,i),(b,k) for a <= b); each row thread takes the other
 //               half of its node rows from the transposed row (e, k, i) of the
 //               same warp by shuffles and stores whole 64-byte node rows of
-//               K_e to global memory in the layout the node gather reads.
+//               K_e to global memory in the layout the node gather reads;
+//   warp 14     issues the tile's 50 MMAs (10 groups of digit pairs x 5 K steps).
 // The A slices are rewritten as soon as the MMAs that read them completed; the
 // next MMAs wait only for the epilogue's reads of the accumulators.
 #include <cstdint>
@@ -75,16 +76,23 @@ constexpr int TM_ENT = TM_OWN + 2 * NPAIR;  // 2 x 48 columns: the slicers' scal
 static_assert(TM_ENT + 2 * 48 <= TMEM_COLS, "tensor memory columns");
 constexpr long long WAIT_BUDGET = 2000000000LL;
 
-constexpr int PROD_W = 3, SL_W = 6, R_W = 1, EP_W = 4;
-constexpr int NTHR = 32 * (PROD_W + SL_W + R_W + EP_W);
-constexpr int T_SL = 32 * PROD_W, T_R = T_SL + 32 * SL_W, T_EP = T_R + 32 * R_W;
+constexpr int PROD_W = 3, SL_W = 6, R_W = 1, EP_W = 4, MMA_W = 1;
+constexpr int NTHR = 32 * (PROD_W + SL_W + R_W + EP_W + MMA_W);
+constexpr int T_SL = 32 * PROD_W, T_R = T_SL + 32 * SL_W, T_EP = T_R + 32 * R_W, T_MMA = T_EP + 32 * EP_W;
 constexpr int NSL = 32 * SL_W;
 static_assert(32 * PROD_W == NPT && NSL == 2 * NPT && (T_EP / 32) % 4 == 2, "roles");
 // named barriers (0 is __syncthreads)
 constexpr int BAR_FULL = 1;   // producers arrive, slicers + residual warp sync
 constexpr int BAR_EMPTY = 2;  // slicers + residual warp arrive, producers sync
-constexpr int BAR_SL = 3;     // slicers
 constexpr int N_FULL = 32 * (PROD_W + SL_W + R_W);
+
+// The MMAs of a tile: A slice t against W slices s0 .. s0+ns-1 at once (consecutive
+// W slices are consecutive 48-row blocks, one N = 48 ns operand), accumulating
+// into levels s0+t .. s0+t+ns-1 (consecutive 48-column blocks).  Every pair
+// s + t <= 6 once; the t = 0 groups write each level first.
+constexpr int NGROUP = 10;
+__device__ __constant__ int8_t kGroups[NGROUP][3] = {{0, 0, 4}, {0, 4, 3}, {1, 0, 4}, {1, 4, 2}, {2, 0, 4},
+                                                      {2, 4, 1}, {3, 0, 4}, {4, 0, 3}, {5, 0, 2}, {6, 0, 1}};
 
 // MMA row of (element el of the tile, ik = 3 i + k)
 __host__ __device__ __forceinline__ int row_of(int el, int ik) { return 32 * (el / 3) + 9 * (el % 3) + ik; }
@@ -193,8 +201,6 @@ __device__ __forceinline__ void tmem_ld2x8(const uint32_t* a, float2* v) {
   for (int j = 0; j < 8; ++j) v[j] = make_float2(__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1]));
 }
 
-// kind::f16 (BF16 operands), FP32 accumulate, M = 128, N = 48, both K-major
-constexpr uint32_t IDESC = tc::idesc_bf16(128, NPAD);
 
 // Point phase of quadrature point q of element e (FP64): the eight lanes of an
 // element (consecutive, aligned to 8) each load one node's displacement and
@@ -404,27 +410,6 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
       }
       fence_async_smem();
       mbar_arrive(bar_sl);
-      named_sync(BAR_SL, NSL);
-      if (ts == 0) {
-        if (k >= 1) wait_or_report(bar_tfree, uint32_t((k - 1) & 1));  // the accumulators are free
-        tc_fence_after();
-        const uint32_t aB = s0 + Lay::A, wB = s0 + Lay::W;
-#pragma unroll 1
-        for (int L = 0; L < NLEV; ++L) {
-          uint32_t acc = 0;
-#pragma unroll 1
-          for (int t = 0; t <= L; ++t) {
-            const int s = L - t;
-#pragma unroll
-            for (int kk = 0; kk < KP / 16; ++kk) {
-              mma_bf16(tmem + uint32_t(L * NPAD), smem_desc(aB + t * A_SLICE + kk * 256, 128, SBO),
-                       smem_desc(wB + s * W_SLICE + kk * 256, 128, SBO), IDESC, acc);
-              acc = 1;
-            }
-          }
-        }
-        mma_commit(bar_mma);
-      }
     }
   } else if (tid < T_EP) {
     // ---------------- residual warp ----------------
@@ -444,7 +429,7 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
       }
       named_arrive(BAR_EMPTY, N_FULL);
     }
-  } else {
+  } else if (tid < T_MMA) {
     // ---------------- epilogue: thread = TMEM lane = row (el, i, k) ----------------
     const int qw = warp & 3;
     const int el = qw * 3 + (lane < 27 ? lane / 9 : 0), ik = lane % 9, i = ik / 3, kc = ik % 3;
@@ -515,6 +500,30 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
           for (int b = 0; b < 8; b += 2) d[b / 2] = make_float4(row[b].x, row[b].y, row[b + 1].x, row[b + 1].y);
         }
       }
+    }
+  } else {
+    // ---------------- MMA warp: lane 0 issues, the warp waits together ----------------
+    const uint32_t aB = s0 + Lay::A, wB = s0 + Lay::W;
+    const uint64_t dA = smem_desc(aB, 128, SBO), dW = smem_desc(wB, 128, SBO);
+    for (int k = 0;; ++k) {
+      const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
+      if (tile >= ntiles) break;
+      if (k >= 1) wait_or_report(bar_tfree, uint32_t((k - 1) & 1));  // the accumulators are free
+      wait_or_report(bar_sl, uint32_t(k & 1));                       // the tile's slices are written
+      tc_fence_after();
+      if (lane == 0) {
+#pragma unroll 1
+        for (int gi = 0; gi < NGROUP; ++gi) {
+          const int t = kGroups[gi][0], s0g = kGroups[gi][1], ns = kGroups[gi][2];
+          const uint32_t idesc = tc::idesc_bf16(128, NPAD * ns), d = tmem + uint32_t((s0g + t) * NPAD);
+          const uint64_t a0 = dA + uint64_t((t * A_SLICE) >> 4), w0d = dW + uint64_t((s0g * W_SLICE) >> 4);
+#pragma unroll
+          for (int kk = 0; kk < KP / 16; ++kk)
+            mma_bf16(d, a0 + uint64_t(kk * 16), w0d + uint64_t(kk * 16), idesc, (t == 0 && kk == 0) ? 0u : 1u);
+        }
+        mma_commit(bar_mma);
+      }
+      __syncwarp();
     }
   }
   tc_fence_before();
