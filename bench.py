@@ -653,14 +653,14 @@ def run_ours(args) -> None:
             dist.barrier()
         torch.cuda.synchronize()
 
-    def step(precision=None, feed=None):
+    def step(precision=None, feed=None, out=None):
         """One load step: Dirichlet values and unknowns of step i, fused R+K, state swap."""
         i = counter[0] % len(inputs)
         counter[0] += 1
         Uu, bc = (feed or dev_inputs)[i]
         if bc is not None:
             p.bc_vals = bc if bc.is_cuda else bc.to(asm._torch_device(), non_blocking=True)
-        R, K = fec.assemble_residual_and_stiffness(asm, Uu, p, precision=precision)
+        R, K = fec.assemble_residual_and_stiffness(asm, Uu, p, precision=precision, out=out)
         if stateful:
             p.swap_states()
         return R, K
@@ -737,38 +737,43 @@ def run_ours(args) -> None:
     n_bc = 0 if inputs[0][1] is None else int(inputs[0][1].size)
     R_h = torch.empty(n_u, dtype=torch.float64).pin_memory()
     nz_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
-    # Pipelined read-back: each step's outputs are copied to a device staging pair and read
-    # back on a copy stream while the next step assembles; every step's read-back is inside
-    # the timed region (the region ends after the last one).
+    # Pipelined read-back: the steps write two output pairs in turn (the public call's
+    # out= buffers) and each pair is read back on a copy stream while the next step
+    # assembles into the other; every step's read-back is inside the timed region (the
+    # region ends after the last one).
     copy_stream = torch.cuda.Stream()
-    R_s = torch.empty(n_u, dtype=torch.float64, device=stream.device)
-    nz_s = torch.empty(nnz, dtype=torch.float64, device=stream.device)
-    read_done = torch.cuda.Event()
-    read_done.record(copy_stream)
+    pairs = [(torch.empty(n_u, dtype=torch.float64, device=stream.device),
+              torch.empty(nnz, dtype=torch.float64, device=stream.device)) for _ in range(2)]
+    read_done = [torch.cuda.Event(), torch.cuda.Event()]
+    for ev in read_done:
+        ev.record(copy_stream)
+    turn = [0]
 
     def e2e_step():
-        R, K = step(feed=host_inputs)
-        stream.wait_event(read_done)          # the previous read-back has left the staging pair
-        R_s.copy_(R, non_blocking=True)
-        nz_s.copy_(K.nzval, non_blocking=True)
-        staged = torch.cuda.Event()
-        staged.record(stream)
-        copy_stream.wait_event(staged)
+        j = turn[0] & 1
+        turn[0] += 1
+        stream.wait_event(read_done[j])          # the read-back two steps ago has left pair j
+        R, K = step(feed=host_inputs, out=pairs[j])
+        done = torch.cuda.Event()
+        done.record(stream)
+        copy_stream.wait_event(done)
         with torch.cuda.stream(copy_stream):
-            R_h.copy_(R_s, non_blocking=True)
-            nz_h.copy_(nz_s, non_blocking=True)
-        read_done.record(copy_stream)
+            R_h.copy_(R, non_blocking=True)
+            nz_h.copy_(K.nzval, non_blocking=True)
+        read_done[j].record(copy_stream)
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
-    stream.wait_event(read_done)
+    for ev in read_done:
+        stream.wait_event(ev)
     barrier()
     f0 = torch.cuda.Event(enable_timing=True)
     f1 = torch.cuda.Event(enable_timing=True)
     f0.record(stream)
     for _ in range(args.steps):
         e2e_step()
-    stream.wait_event(read_done)
+    for ev in read_done:
+        stream.wait_event(ev)
     f1.record(stream)
     barrier()
     t_e2e = f0.elapsed_time(f1)
@@ -779,7 +784,8 @@ def run_ours(args) -> None:
     e2e_value = world * ne * args.steps / (t_e2e * 1e-3) / 1e6
     e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * (n_u + n_bc),
            "d2h_bytes_per_step": 8 * (n_u + nnz),
-           "pipelining": "the read-back of step i (copy stream) overlaps the assembly of step i+1"}
+           "pipelining": "two output pairs in turn: the read-back of step i (copy stream) overlaps the assembly "
+                         "of step i+1 into the other pair"}
     finish(args, fec, world, rank, local, wl, mesh, asm, ne, nn, nf, n_u, nnz, t_ms, value, clocks, per_kernel,
            launches, e2e, variants, stateful_errors)
 

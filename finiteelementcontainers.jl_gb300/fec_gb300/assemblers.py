@@ -336,10 +336,23 @@ def _prepare(asm: SparseMatrixAssembler, Uu, p: Parameters):
     return stream
 
 
-def _assemble(asm: SparseMatrixAssembler, want: int, Uu, p: Parameters, precision: str | None):
+def _check_out(asm: SparseMatrixAssembler, t, n: int, name: str):
+    torch = _torch()
+    if not (isinstance(t, torch.Tensor) and t.dtype == torch.float64 and t.is_contiguous() and t.numel() == n
+            and t.device == torch.device(asm._torch_device())):
+        raise ValueError(f"out {name} must be a contiguous float64 tensor of {n} entries on {asm._torch_device()}")
+    return t
+
+
+def _assemble(asm: SparseMatrixAssembler, want: int, Uu, p: Parameters, precision: str | None, out=None):
     stream = _prepare(asm, Uu, p)
-    R = residual(asm) if want & _lib.FEC_WANT_RESIDUAL else None
-    K = stiffness(asm) if want & _lib.FEC_WANT_STIFFNESS else None
+    if out is None:
+        R = residual(asm) if want & _lib.FEC_WANT_RESIDUAL else None
+        K = stiffness(asm) if want & _lib.FEC_WANT_STIFFNESS else None
+    else:
+        colptr, rowval = asm.pattern()
+        R = _check_out(asm, out[0], int(asm.dof.unknown_dofs.size), "residual")
+        K = CSCMatrix(int(asm.dof.unknown_dofs.size), colptr, rowval, _check_out(asm, out[1], asm.nnz, "nzval"))
     has_state = any(ph.NS for ph in p.physics)
     asm._call("fec_assemble", want, PRECISIONS[precision or asm.precision], p.t, p.dt, _lib.ptr(p.field),
               _lib.ptr(p.field_old), _lib.ptr(p.state_old) if has_state else None,
@@ -365,11 +378,14 @@ assemble_matrix = assemble_stiffness
 
 
 def assemble_residual_and_stiffness(asm: SparseMatrixAssembler, Uu, p: Parameters, *, precision: str | None = None,
-                                    check_finite: bool = False):
+                                    check_finite: bool = False, out=None):
     """One fused pass producing both residual(asm) and stiffness(asm), the pair a
     Newton iteration assembles (src/Solvers.jl:128-153).  check_finite raises
-    FECError (FEC_ERR_NONFINITE) when an output holds NaN/Inf (synchronises)."""
-    R, K = _assemble(asm, _lib.FEC_WANT_RESIDUAL | _lib.FEC_WANT_STIFFNESS, Uu, p, precision)
+    FECError (FEC_ERR_NONFINITE) when an output holds NaN/Inf (synchronises).
+    out = (R, nzval): device float64 tensors (unknowns, nnz) the pass writes
+    instead of the assembler's own arrays -- a caller that reads one pair back
+    while the next pass writes the other alternates two."""
+    R, K = _assemble(asm, _lib.FEC_WANT_RESIDUAL | _lib.FEC_WANT_STIFFNESS, Uu, p, precision, out)
     if check_finite:
         check_finite_outputs(asm, R, K)
     return R, K

@@ -92,6 +92,27 @@ def test_poisson_vector_and_matrix_entry_points_agree(fec, orc):
     assert np.array_equal(fec.residual(asm).cpu().numpy(), R)
 
 
+def test_fused_pass_into_caller_buffers(fec):
+    """assemble_residual_and_stiffness(..., out=(R, nzval)) writes the caller's
+    device arrays, bitwise what the assembler's own arrays receive; wrong
+    shapes are refused."""
+    torch = _torch()
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (6, 6, 6))
+    phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+    asm, p = _setup(fec, mesh, "vector", phys)
+    U = stretch_field(mesh.nodal_coords, seed=3).ravel()
+    R, nz, _ = _run(fec, asm, p, U)
+    Uu = torch.from_numpy(U[asm.dof.unknown_dofs - 1].copy()).cuda()
+    out = (torch.full((asm.dof.unknown_dofs.size,), np.nan, dtype=torch.float64, device="cuda"),
+           torch.full((asm.nnz,), np.nan, dtype=torch.float64, device="cuda"))
+    R2, K2 = fec.assemble_residual_and_stiffness(asm, Uu, p, out=out)
+    torch.cuda.synchronize()
+    assert R2.data_ptr() == out[0].data_ptr() and K2.nzval.data_ptr() == out[1].data_ptr()
+    assert np.array_equal(out[0].cpu().numpy(), R) and np.array_equal(out[1].cpu().numpy(), nz)
+    with pytest.raises(ValueError):
+        fec.assemble_residual_and_stiffness(asm, Uu, p, out=(out[0][:-1], out[1]))
+
+
 def test_poisson_quad4_gold_through_gpu(fec):
     """test/poisson/TestPoisson.jl:54-100: GPU-assembled residual and CSC stiffness
     on poisson.g, one linear solve, compared with poisson.gold."""
