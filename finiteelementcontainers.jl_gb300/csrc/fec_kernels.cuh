@@ -901,6 +901,11 @@ __device__ __forceinline__ double widen(float f) {
   return __hiloint2double(int(hiw), int(u << 29));
 }
 
+// A residual contribution as a double: doubles as they are, floats widened
+// exactly on the integer pipes (a conversion would issue on the FP64 pipe).
+__device__ __forceinline__ double to_double(double x) { return x; }
+__device__ __forceinline__ double to_double(float x) { return widen(x); }
+
 // Accumulator of the node gather: a compensated FP32 pair (hi, lo).  Adding a
 // float recovers its rounding error exactly with TwoSum (Knuth); adding a
 // double-float pair is a df64 addition.  Either keeps the sum to about 2^-48
@@ -987,7 +992,7 @@ __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo&
 #pragma unroll
       for (int c = 0; c < CH; ++c) {
         if (c < nh) {
-          racc += double(rv[c]);
+          racc += to_double(rv[c]);
           if (wantK) {
             // one element's values of this lane go to distinct positions: loads,
             // additions and stores are batched
@@ -1022,7 +1027,7 @@ __device__ __forceinline__ void gather_run_generic(const GatherArgs& g, const Bl
     const uint32_t packed = g.nadj[p];
     const int64_t le = int64_t(packed >> 5) - B.elem_start;
     const int a = int(packed & 31u);
-    if (wantR) racc += double(Re[le * NDOF + a * NF + lane]);
+    if (wantR) racc += to_double(Re[le * NDOF + a * NF + lane]);
     if (wantK) {
       const Real* Krows = Ke + (le * NDOF + int64_t(a) * NF) * NDOF;
       const uint16_t* ep = g.epos + B.epos_off + (le * A + a) * A;
@@ -1100,7 +1105,7 @@ __device__ __forceinline__ void gather_run_hex8v(const GatherArgs& g, const Bloc
 #pragma unroll
       for (int c = 0; c < CH; ++c) {
         if (c < nh) {
-          racc += double(rv[c]);
+          racc += to_double(rv[c]);
           if (wantK) {
             if (kl) {
               // the four columns of one element go to four distinct positions, so
@@ -1323,7 +1328,7 @@ __global__ void __launch_bounds__(gp::WPB * 32, MINB) node_gather_hex8_pipe_kern
         const unsigned char* st = stage[s];
         const int base = lk * Ln;
         for (int c = 0; c < cur.cnt; ++c) {
-          if (wantR) racc += double(reinterpret_cast<const RT*>(st + S::R_OFF)[c * 3 + lane]);
+          if (wantR) racc += to_double(reinterpret_cast<const RT*>(st + S::R_OFF)[c * 3 + lane]);
           if (wantK) {
             if (kl) {
               // entries ((k*3 + i)*8 + b) of the element's rows for this node, i = 0..2, go to
