@@ -55,6 +55,10 @@ struct Block {
   // within 1e-13 of the element size): x0 = the first element's coordinates
   bool congruent = false;
   double x0[24] = {0};
+  // tet10/hex27 block whose element e is a translate of element e mod nclass
+  // (nclass <= 8, 0: none): xc = the first nclass elements' node coordinates
+  int nclass = 0;
+  std::vector<double> xc;
 };
 
 }  // namespace
@@ -97,6 +101,7 @@ struct fec_ctx {
   DevBuf d_nbr_ptr, d_nbr;             // neighbour lists on the device (device symbolic phase, CSC fill)
   DevBuf d_tile_counter;               // single launch of mixed element blocks: next work tile
   std::vector<DevBuf> d_affine;        // per block: the tensor-core operand table of a congruent hex8 block
+                                       // or of a tet10/hex27 block of translation classes
   bool single_launch = false;          // FP64 mechanics: every element block in one launch
   float cl_tol = 0.f;
   // optional per-launch timing (CUDA events on the caller's stream)
@@ -163,18 +168,28 @@ int build_affine(fec_ctx* c, size_t b) {
   DevBuf& d = c->d_affine[b];
   d.release();
   const Block& B = c->blocks[b];
-  if (!B.congruent || c->device < 0) return FEC_OK;
+  if (c->device < 0) return FEC_OK;
   std::vector<unsigned char> tab;
-  if (!fec::hex8_affine_table(B.x0, c->ref_host.data() + c->ref_off[b], tab)) return FEC_OK;
+  if (B.congruent) {
+    if (!fec::hex8_affine_table(B.x0, c->ref_host.data() + c->ref_off[b], tab)) return FEC_OK;
+  } else if (B.nclass > 0) {
+    if (!fec::class_tc_table(B.elem_type, B.nclass, B.xc.data(), c->ref_host.data() + c->ref_off[b], tab))
+      return FEC_OK;
+  } else {
+    return FEC_OK;
+  }
   return upload(c, d, tab.data(), tab.size());
 }
 
 // The table a launch of block b may use: FP64 assemblies of congruent hex8
 // blocks on their own launch (the single launch across blocks keeps the
 // per-element kernels), unless FEC_HEX8_AFFINE=0.
+// FP32-element assemblies of tet10/hex27 blocks of translation classes get theirs.
 const void* affine_table(const fec_ctx* c, size_t b, int precision, bool mixed) {
-  if (precision != FEC_FP64 || mixed || b >= c->d_affine.size() || !fec::hex8_affine_enabled()) return nullptr;
-  return c->d_affine[b].p;
+  if (mixed || b >= c->d_affine.size()) return nullptr;
+  if (c->blocks[b].elem_type == FEC_HEX8)
+    return precision == FEC_FP64 && fec::hex8_affine_enabled() ? c->d_affine[b].p : nullptr;
+  return precision == FEC_FP32_ELEMENT ? c->d_affine[b].p : nullptr;
 }
 
 int ensure(fec_ctx* c, DevBuf& b, size_t bytes) {
@@ -187,6 +202,16 @@ int ensure(fec_ctx* c, DevBuf& b, size_t bytes) {
 
 // element-matrix blocks start on 16-byte boundaries (vectorised copy-out)
 inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3); }
+
+// Workspace entries of block b's element matrices: the class tensor-core kernel
+// writes the symmetric half (KE_PAIRS), every other kernel the whole K_e.
+int64_t ke_entries(const fec_ctx* c, size_t b, int precision, bool want_k, bool mixed) {
+  const Block& B = c->blocks[b];
+  if (fec::class_tc_runs(B.physics, B.elem_type, precision, want_k, affine_table(c, b, precision, mixed) != nullptr))
+    return pad4(B.ne * (int64_t(B.nnpe) * (B.nnpe + 1) / 2 * 9));
+  const int ndof = c->nf * B.nnpe;
+  return pad4(B.ne * ndof * ndof);
+}
 
 // FEC_CLOSURE_ON_CUDA_CORES=1 selects the per-thread network evaluation (the
 // generic element kernel) instead of the tensor-core closure kernel.
@@ -405,6 +430,46 @@ int fec_mesh_set(fec_ctx* c, int dim, int64_t nn, const double* coords, int nblo
         }
     }
     B.congruent = h > 0.0 && dev <= 1e-13 * h;
+  }
+  // tet10/hex27 blocks of translation classes: the smallest period P <= 8 such that
+  // every element's node offsets X_e[a] - X_e[0] match element (e mod P)'s to within
+  // 1e-13 of that element's size
+  for (Block& B : blocks) {
+    if ((B.elem_type != 7 && B.elem_type != 8) || dim != 3 || B.ne < 1) continue;
+    const int A = B.nnpe;
+    for (int P = 1; P <= 8 && P <= B.ne; ++P) {
+      std::vector<double> d0(size_t(P) * A * 3), hc(P, 0.0);
+      for (int cl = 0; cl < P; ++cl) {
+        const int32_t* ce = conn0.data() + B.conn_off + int64_t(cl) * A;
+        for (int a = 0; a < A; ++a)
+          for (int d = 0; d < 3; ++d) {
+            const double off = coords[int64_t(ce[a]) * 3 + d] - coords[int64_t(ce[0]) * 3 + d];
+            d0[(size_t(cl) * A + a) * 3 + d] = off;
+            hc[cl] = std::max(hc[cl], std::fabs(off));
+          }
+      }
+      int bad = 0;  // (a bitwise-or reduction: each thread's copy starts at 0)
+#pragma omp parallel for schedule(static) reduction(| : bad)
+      for (int64_t e = 0; e < B.ne; ++e) {
+        if (bad) continue;
+        const int cl = int(e % P);
+        const int32_t* ce = conn0.data() + B.conn_off + e * A;
+        for (int a = 1; a < A && !bad; ++a)
+          for (int d = 0; d < 3; ++d) {
+            const double off = coords[int64_t(ce[a]) * 3 + d] - coords[int64_t(ce[0]) * 3 + d];
+            if (!(std::fabs(off - d0[(size_t(cl) * A + a) * 3 + d]) <= 1e-13 * hc[cl])) bad = 1;
+          }
+      }
+      if (bad) continue;
+      B.nclass = P;
+      B.xc.resize(size_t(P) * A * 3);
+      for (int cl = 0; cl < P; ++cl) {
+        const int32_t* ce = conn0.data() + B.conn_off + int64_t(cl) * A;
+        for (int a = 0; a < A; ++a)
+          for (int d = 0; d < 3; ++d) B.xc[(size_t(cl) * A + a) * 3 + d] = coords[int64_t(ce[a]) * 3 + d];
+      }
+      break;
+    }
   }
   // reference tables
   std::vector<double> ref;
@@ -930,10 +995,9 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
   if (c->n_timed > 1) c->n_timed = 0;  // keep a preceding fec_update_field timing
   const size_t rsz = precision == FEC_FP64 ? sizeof(double) : sizeof(float);
   int64_t ke_total = 0, re_total = 0;
-  for (const Block& B : c->blocks) {
-    const int ndof = c->nf * B.nnpe;
-    ke_total += pad4(B.ne * ndof * ndof);
-    re_total += B.ne * ndof;
+  for (size_t b = 0; b < c->blocks.size(); ++b) {
+    ke_total += ke_entries(c, b, precision, want_k, false);
+    re_total += c->blocks[b].ne * c->nf * c->blocks[b].nnpe;
   }
   int rc;
   if (want_k && (rc = ensure(c, c->d_Ke, rsz * size_t(ke_total)))) return rc;
@@ -1023,12 +1087,14 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     bi.epos_off = B.epos_off;
     bi.nnpe = B.nnpe;
     bi.ndof = ndof;
-    // the hex8 mechanics kernels write the node-rows layout
+    // the hex8 mechanics kernels write the node-rows layout, the class tensor-core
+    // kernel the symmetric half
+    const bool pairs = fec::class_tc_runs(B.physics, B.elem_type, precision, want_k, ea.affine != nullptr);
     bi.layout = (B.elem_type == FEC_HEX8 && (B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2 ||
                                              tc_closure(B, precision)))
                     ? fec::KE_NODE_ROWS
-                    : fec::KE_ROW_MAJOR;
-    ke_off += pad4(B.ne * ndof * ndof);
+                    : (pairs ? fec::KE_PAIRS : fec::KE_ROW_MAJOR);
+    ke_off += ke_entries(c, b, precision, want_k, false);
     re_off += B.ne * ndof;
     st_off += int64_t(ns) * B.nq * B.ne;
   }
@@ -1484,10 +1550,9 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
   // workspace: element matrices, then (256-byte aligned) element residuals
   const size_t rsz = precision == FEC_FP64 ? sizeof(double) : sizeof(float);
   int64_t ke_total = 0, re_total = 0;
-  for (const Block& B : c->blocks) {
-    const int ndof = c->nf * B.nnpe;
-    ke_total += pad4(B.ne * ndof * ndof);
-    re_total += B.ne * ndof;
+  for (size_t b = 0; b < c->blocks.size(); ++b) {
+    ke_total += ke_entries(c, b, precision, want_k, false);
+    re_total += c->blocks[b].ne * c->nf * c->blocks[b].nnpe;
   }
   const size_t ke_bytes = want_k ? rsz * size_t(ke_total) : 0;
   const size_t re_off_bytes = (ke_bytes + 255) & ~size_t(255);
@@ -1549,11 +1614,13 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
     bi.epos_off = B.epos_off;
     bi.nnpe = B.nnpe;
     bi.ndof = ndof;
-    // the hex8 mechanics kernels write the node-rows layout
+    // the hex8 mechanics kernels write the node-rows layout, the class tensor-core
+    // kernel the symmetric half
+    const bool pairs = fec::class_tc_runs(B.physics, B.elem_type, precision, want_k, ea.affine != nullptr);
     bi.layout = (B.elem_type == FEC_HEX8 && (B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2))
                     ? fec::KE_NODE_ROWS
-                    : fec::KE_ROW_MAJOR;
-    ke_off += pad4(B.ne * ndof * ndof);
+                    : (pairs ? fec::KE_PAIRS : fec::KE_ROW_MAJOR);
+    ke_off += ke_entries(c, b, precision, want_k, false);
     re_off += B.ne * ndof;
     st_off += int64_t(ns) * B.nq * B.ne;
   }

@@ -846,7 +846,19 @@ constexpr int MAX_BLOCKS = 16;
 //                   the hex8 mechanics kernels so that the gather reads, per row
 //                   component and column component, the 8 column nodes as two
 //                   16-byte vectors)
-enum { KE_ROW_MAJOR = 0, KE_NODE_ROWS = 1 };
+//   KE_PAIRS:       the symmetric half only (NF = 3): node pair (x, y), x <= y,
+//                   p = x*(2A - x + 1)/2 + y - x, holds K_(x,k'),(y,i') at
+//                   p*9 + 3k' + i'; an entry with a > b is read from pair (b, a)
+//                   transposed (K = K^T).  A(A+1)/2 * 9 entries per element; written
+//                   by the class tensor-core kernel (fec_class_tc.cu)
+enum { KE_ROW_MAJOR = 0, KE_NODE_ROWS = 1, KE_PAIRS = 2 };
+
+// Offset of entry (row (a,k), column (b,i)) of one element in the KE_PAIRS layout.
+__host__ __device__ __forceinline__ int pair_entry(int A, int a, int k, int b, int i) {
+  const bool own = a <= b;
+  const int x = own ? a : b, y = own ? b : a;
+  return (x * (2 * A - x + 1) / 2 + (y - x)) * 9 + (own ? k * 3 + i : i * 3 + k);
+}
 
 struct GatherArgs {
   int64_t nn;                  // nodes
@@ -947,6 +959,8 @@ __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo&
   using RT = typename RE<Real>::T;
   const Real* Ke = static_cast<const Real*>(g.Ke) + B.ke_off;
   const RT* Re = static_cast<const RT*>(g.Re) + B.re_off;
+  const bool pairs = B.layout == KE_PAIRS;
+  constexpr int NPW = A * (A + 1) / 2 * 9;  // KE_PAIRS entries per element
   for (; p < pend; p += 32) {
     const int64_t left32 = pend - p;
     const int n32 = left32 < 32 ? int(left32) : 32;
@@ -969,6 +983,7 @@ __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo&
           if (wantR) rv[c] = Re[row0 + lane];
           if (wantK) {
             const Real* Krows = Ke + row0 * NDOF;
+            const Real* Kel = Ke + uint64_t(uint32_t(le)) * NPW;
             const uint16_t* ep = g.epos + B.epos_off + (uint64_t(uint32_t(le)) * A + a) * A;
 #pragma unroll
             for (int j = 0; j < VPL; ++j) {
@@ -976,7 +991,7 @@ __device__ __forceinline__ void gather_run(const GatherArgs& g, const BlockInfo&
               if (t < TOTAL) {
                 const int k = t / NDOF, rem = t % NDOF;
                 const int b = rem / NF, i = rem % NF;
-                v[c][j] = Krows[t];
+                v[c][j] = pairs ? Kel[pair_entry(A, a, k, b, i)] : Krows[t];
                 if (fast) {
                   pos[c][j] = k * Ln + ep[b] + i;
                 } else if ((um >> k) & 1u) {
@@ -1020,7 +1035,8 @@ __device__ __forceinline__ void gather_run_generic(const GatherArgs& g, const Bl
                                                    bool wantK, bool wantR) {
   using RT = typename RE<Real>::T;
   const int A = B.nnpe, NDOF = B.ndof;
-  const bool node_rows = B.layout == KE_NODE_ROWS;
+  const bool node_rows = B.layout == KE_NODE_ROWS, pairs = B.layout == KE_PAIRS;
+  const int64_t npw = int64_t(A) * (A + 1) / 2 * 9;  // KE_PAIRS entries per element
   const Real* Ke = static_cast<const Real*>(g.Ke) + B.ke_off;
   const RT* Re = static_cast<const RT*>(g.Re) + B.re_off;
   for (; p < pend; ++p) {
@@ -1030,6 +1046,7 @@ __device__ __forceinline__ void gather_run_generic(const GatherArgs& g, const Bl
     if (wantR) racc += to_double(Re[le * NDOF + a * NF + lane]);
     if (wantK) {
       const Real* Krows = Ke + (le * NDOF + int64_t(a) * NF) * NDOF;
+      const Real* Kel = Ke + le * npw;
       const uint16_t* ep = g.epos + B.epos_off + (le * A + a) * A;
       const int32_t* cn = g.conn + B.conn_off + le * A;
 #pragma unroll
@@ -1047,7 +1064,8 @@ __device__ __forceinline__ void gather_run_generic(const GatherArgs& g, const Bl
             if (!((umm >> i) & 1u)) continue;
             pos = kb + ep[b] + __popc(umm & ((1u << i) - 1u));
           }
-          GatherAcc::add(acc, pos, Krows[node_rows ? (k * NF + i) * A + b : k * NDOF + rem]);
+          GatherAcc::add(acc, pos,
+                         pairs ? Kel[pair_entry(A, a, k, b, i)] : Krows[node_rows ? (k * NF + i) * A + b : k * NDOF + rem]);
         }
       }
       __syncwarp();

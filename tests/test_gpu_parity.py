@@ -219,9 +219,11 @@ def test_hex27_j2_fp64(fec, orc):
 @pytest.mark.parametrize("kind", ["tet4", "tet10", "hex27"])
 @pytest.mark.parametrize("phys_name", ["neohookean", "j2"])
 def test_higher_order_fp32_element(fec, orc, kind, phys_name):
-    """FP32-element tet4/tet10/hex27 against the FP64 oracle.  Hex27 runs its
-    element-stiffness contraction on the tensor cores (tcgen05 kind::tf32 with a
-    two-term split); it is also checked against the CUDA-core kernel."""
+    """FP32-element tet4/tet10/hex27 against the FP64 oracle.  These box meshes
+    are blocks of translation classes, so tet10 and hex27 run the class
+    tensor-core kernel; with it switched off (FEC_CLASS_TC=0) hex27 runs the
+    per-element tensor-core kernel (tcgen05 kind::tf32 with a two-term split),
+    which is also checked against the CUDA-core kernel."""
     import os
     gen = {"tet4": fec.meshes.box_tet4, "tet10": fec.meshes.box_tet10, "hex27": fec.meshes.box_hex27}[kind]
     mesh = gen((4, 4, 4))
@@ -244,15 +246,22 @@ def test_higher_order_fp32_element(fec, orc, kind, phys_name):
     assert max(e_r) <= TOL32 and max(e_k) <= TOL32
     if kind == "hex27":
         assert fec.load_library().fec_tensor_core_status(1) == 0
-        os.environ["FEC_HEX27_ON_CUDA_CORES"] = "1"
-        try:
-            asm2, p2 = _setup(fec, mesh, "vector", phys, precision="fp32_element")
-            R2, nz2, _ = _run(fec, asm2, p2, U)
-        finally:
-            del os.environ["FEC_HEX27_ON_CUDA_CORES"]
-        print("hex27 tensor cores vs CUDA cores: residual", rel_err(R, R2), "nzval", rel_err(nz, nz2, FLOOR32))
-        assert np.array_equal(R, R2)  # the residual is formed on the CUDA cores either way
-        assert max(rel_err(nz, nz2, FLOOR32)) <= 5e-6   # two FP32-element paths, entry-wise
+        out = {}
+        for flags in (("FEC_CLASS_TC",), ("FEC_CLASS_TC", "FEC_HEX27_ON_CUDA_CORES")):
+            for f in flags:
+                os.environ[f] = "0" if f == "FEC_CLASS_TC" else "1"
+            try:
+                asm2, p2 = _setup(fec, mesh, "vector", phys, precision="fp32_element")
+                out[len(flags)] = _run(fec, asm2, p2, U)[:2]
+            finally:
+                for f in flags:
+                    del os.environ[f]
+        (R1, nz1), (R2, nz2) = out[1], out[2]
+        print("hex27 per-element tensor cores vs CUDA cores: residual", rel_err(R1, R2), "nzval",
+              rel_err(nz1, nz2, FLOOR32))
+        assert np.array_equal(R1, R2)  # the per-element kernels form the residual alike
+        assert max(rel_err(nz1, nz2, FLOOR32)) <= 5e-6   # two FP32-element paths, entry-wise
+        assert max(rel_err(nz, nz1, FLOOR32)) <= TOL32 and max(rel_err(R, R1, FLOOR32)) <= TOL32
 
 
 def test_j2_one_load_step_with_state(fec, orc):
