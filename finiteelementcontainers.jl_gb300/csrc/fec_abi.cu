@@ -100,6 +100,11 @@ struct fec_ctx {
   DevBuf d_flag;                       // non-finite scan result
   DevBuf d_nbr_ptr, d_nbr;             // neighbour lists on the device (device symbolic phase, CSC fill)
   DevBuf d_tile_counter;               // single launch of mixed element blocks: next work tile
+  // node gather of a mesh of mixed element sizes: the nodes grouped by the element
+  // size of their adjacent elements (built on first use, per pattern)
+  DevBuf d_node_groups;
+  std::vector<fec::NodeGroup> node_groups;
+  bool groups_ready = false;
   std::vector<DevBuf> d_affine;        // per block: the tensor-core operand table of a congruent hex8 block
                                        // or of a tet10/hex27 block of translation classes
   bool single_launch = false;          // FP64 mechanics: every element block in one launch
@@ -274,8 +279,47 @@ struct LaunchTimer {
   }
 };
 
+// FEC_GATHER_RUNS=generic gathers a mesh of mixed element sizes in one launch on
+// the one-element-at-a-time routine (bitwise the same results as the groups).
+bool gather_runs_generic() {
+  const char* e = getenv("FEC_GATHER_RUNS");
+  return e && e[0] == 'g';
+}
+
+// The node groups of launch_gather_groups: a node whose adjacent elements all come
+// from one block joins the group of that block's element size (4, 8, 10, 27), every
+// other node (elements of several blocks, or none) the group A = 0.
+int build_node_groups(fec_ctx* c) {
+  std::vector<int> owner(size_t(c->nn), -1);
+  for (size_t b = 0; b < c->blocks.size(); ++b) {
+    const Block& B = c->blocks[b];
+    for (int64_t i = 0; i < B.ne * B.nnpe; ++i) {
+      int& o = owner[size_t(c->conn[B.conn_off + i])];
+      o = (o == -1 || o == int(b)) ? int(b) : -2;
+    }
+  }
+  static const int kSizes[5] = {4, 8, 10, 27, 0};
+  std::vector<int32_t> list;
+  list.reserve(size_t(c->nn));
+  c->node_groups.clear();
+  for (int gi = 0; gi < 5; ++gi) {
+    const int64_t off = int64_t(list.size());
+    for (int64_t n = 0; n < c->nn; ++n) {
+      const int A = owner[size_t(n)] >= 0 ? c->blocks[size_t(owner[size_t(n)])].nnpe : 0;
+      const int Ag = (A == 4 || A == 8 || A == 10 || A == 27) ? A : 0;
+      if (Ag == kSizes[gi]) list.push_back(int32_t(n));
+    }
+    if (int64_t(list.size()) > off) c->node_groups.push_back({kSizes[gi], off, int64_t(list.size()) - off});
+  }
+  if (int rc = upload(c, c->d_node_groups, list.data(), sizeof(int32_t) * list.size())) return rc;
+  c->groups_ready = true;
+  return FEC_OK;
+}
+
 void invalidate_pattern(fec_ctx* c) {
   c->pattern_ready = false;
+  c->groups_ready = false;
+  c->d_node_groups.release();
   c->nnz = 0;
   c->d_colptr0.release();
   c->d_rowval32.release();
@@ -324,7 +368,7 @@ int fec_ctx_destroy(fec_ctx* c) {
   for (DevBuf* b : {&c->d_coords, &c->d_conn, &c->d_ref, &c->d_nadj_ptr, &c->d_nadj, &c->d_epos, &c->d_umask,
                     &c->d_col_base, &c->d_col_len, &c->d_dtu, &c->d_unknown_dofs, &c->d_Ke, &c->d_Re, &c->d_cl_w,
                     &c->d_cl_norm, &c->d_cl_cnt, &c->d_cl_args, &c->d_cl_img, &c->d_cl_table, &c->d_V, &c->d_colptr0, &c->d_rowval32,
-                    &c->d_cg, &c->d_flag, &c->d_nbr_ptr, &c->d_nbr, &c->d_tile_counter})
+                    &c->d_cg, &c->d_flag, &c->d_nbr_ptr, &c->d_nbr, &c->d_tile_counter, &c->d_node_groups})
     b->release();
   for (DevBuf& b : c->d_affine) b.release();
   delete c;
@@ -1125,9 +1169,18 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
   ga.R_u = want_r ? R_u : nullptr;
   ga.acc_stride = c->acc_stride;
   cudaError_t e;
+  // meshes of mixed element sizes: one gather launch per group of nodes of one size
+  bool mixed_sizes = false;
+  for (const Block& B : c->blocks) mixed_sizes = mixed_sizes || B.nnpe != c->blocks[0].nnpe;
+  if (mixed_sizes && !gather_runs_generic() && !c->groups_ready)
+    if (int rc = build_node_groups(c)) return rc;
   {
     LaunchTimer timer(c, s, "node_gather");
-    e = fec::launch_gather(precision, c->nf, ga, s, &c->last_launches);
+    if (mixed_sizes && !gather_runs_generic())
+      e = fec::launch_gather_groups(precision, c->nf, ga, static_cast<const int32_t*>(c->d_node_groups.p),
+                                    c->node_groups.data(), int(c->node_groups.size()), s, &c->last_launches);
+    else
+      e = fec::launch_gather(precision, c->nf, ga, s, &c->last_launches);
   }
   if (e != cudaSuccess) return fail(c, FEC_ERR_CUDA, "gather launch: %s", cudaGetErrorString(e));
   return ok(c);

@@ -37,7 +37,8 @@ cudaError_t go1(const GatherArgs& g, cudaStream_t s, int* launches) {
   auto kern = node_gather_kernel<Real, NF, A, WPB, MINB, BUDGET>;
   cudaError_t err = ensure_smem<node_gather_kernel<Real, NF, A, WPB, MINB, BUDGET>>(smem);
   if (err != cudaSuccess) return err;
-  const unsigned grid = unsigned((g.nn + WPB - 1) / WPB);
+  const int64_t count = g.nodes ? g.nnodes : g.nn;
+  const unsigned grid = unsigned((count + WPB - 1) / WPB);
   kern<<<grid, WPB * 32, smem, s>>>(g);
   ++*launches;
   return cudaGetLastError();
@@ -45,7 +46,7 @@ cudaError_t go1(const GatherArgs& g, cudaStream_t s, int* launches) {
 
 template <typename Real, int NF, int A>
 cudaError_t go(const GatherArgs& g, cudaStream_t s, int* launches) {
-  if (g.nn <= 0) return cudaSuccess;
+  if ((g.nodes ? g.nnodes : g.nn) <= 0) return cudaSuccess;
   if (gather_variant() == 1) return go1<Real, NF, A, 2, sizeof(Real) == 8 ? 12 : 18>(g, s, launches);
   return go1<Real, NF, A, 3, sizeof(Real) == 8 ? 6 : 12>(g, s, launches);
 }
@@ -89,7 +90,38 @@ cudaError_t by_size(const GatherArgs& g, cudaStream_t s, int* launches) {
     default: return go<Real, NF, 0>(g, s, launches);
   }
 }
+template <typename Real, int NF>
+cudaError_t groups(const GatherArgs& g0, const int32_t* nodes, const NodeGroup* grp, int ngroups, cudaStream_t s,
+                   int* launches) {
+  for (int i = 0; i < ngroups; ++i) {
+    GatherArgs g = g0;
+    g.nodes = nodes + grp[i].off;
+    g.nnodes = grp[i].count;
+    cudaError_t e;
+    switch (grp[i].A) {
+      case 4: e = go<Real, NF, 4>(g, s, launches); break;
+      case 8: e = go<Real, NF, 8>(g, s, launches); break;
+      case 10: e = go<Real, NF, 10>(g, s, launches); break;
+      case 27: e = go<Real, NF, 27>(g, s, launches); break;
+      default: e = go<Real, NF, 0>(g, s, launches); break;
+    }
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
 }  // namespace
+
+cudaError_t launch_gather_groups(int precision, int nf, const GatherArgs& g, const int32_t* nodes,
+                                 const NodeGroup* grp, int ngroups, cudaStream_t s, int* launches) {
+  if (precision == 0) {
+    if (nf == 1) return groups<float2, 1>(g, nodes, grp, ngroups, s, launches);
+    if (nf == 3) return groups<float2, 3>(g, nodes, grp, ngroups, s, launches);
+  } else if (precision == 1) {
+    if (nf == 1) return groups<float, 1>(g, nodes, grp, ngroups, s, launches);
+    if (nf == 3) return groups<float, 3>(g, nodes, grp, ngroups, s, launches);
+  }
+  return cudaErrorNotSupported;
+}
 
 cudaError_t launch_gather(int precision, int nf, const GatherArgs& g, cudaStream_t s, int* launches) {
   if (precision == 0) {  // FP64 kernels leave double-float workspace entries

@@ -878,6 +878,8 @@ struct GatherArgs {
   double* nzval;               // may be null
   double* R_u;                 // may be null
   int acc_stride;              // doubles of accumulator per warp
+  const int32_t* nodes;        // node_gather_kernel: gather nodes[0 .. nnodes) instead of 0 .. nn (may be null)
+  int64_t nnodes;
 };
 
 // Bit 7 of umask[n]: node n and every node it couples to have all NF components
@@ -1155,8 +1157,13 @@ template <typename Real, int NF, int A, int WPB, int MINB, int BUDGET>
 __global__ void __launch_bounds__(WPB * 32, MINB) node_gather_kernel(GatherArgs g) {
   extern __shared__ __align__(16) float s_acc[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t n = int64_t(blockIdx.x) * WPB + warp;
-  if (n >= g.nn) return;
+  int64_t n = int64_t(blockIdx.x) * WPB + warp;
+  if (g.nodes) {
+    if (n >= g.nnodes) return;
+    n = g.nodes[n];
+  } else if (n >= g.nn) {
+    return;
+  }
   const unsigned um_raw = g.umask[n];
   const bool fast = (um_raw & UMASK_FULL_NBR) != 0;
   const unsigned um = um_raw & ~UMASK_FULL_NBR;

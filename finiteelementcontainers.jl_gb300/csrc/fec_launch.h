@@ -30,6 +30,17 @@ cudaError_t launch_poisson(int elem_type, int precision, bool want_r, bool want_
 cudaError_t launch_mech(int physics, int elem_type, int precision, bool want_r, bool want_k, const ElemArgs& args,
                         cudaStream_t stream, int* launches);
 cudaError_t launch_gather(int precision, int nf, const GatherArgs& args, cudaStream_t stream, int* launches);
+// The node gather of a mesh of mixed element sizes, one launch per group of nodes:
+// nodes[off .. off + count) are the nodes whose adjacent elements all have A nodes
+// (A = 4, 8, 10 or 27: the gather with that element size at compile time, several
+// elements' loads in flight), A = 0 the rest (shared between element sizes).  The
+// groups partition the nodes; the results are bitwise those of launch_gather.
+struct NodeGroup {
+  int A;
+  int64_t off, count;
+};
+cudaError_t launch_gather_groups(int precision, int nf, const GatherArgs& args, const int32_t* nodes,
+                                 const NodeGroup* groups, int ngroups, cudaStream_t stream, int* launches);
 // Matrix-free tangent action: element contributions K_e v_e (summed over points
 // in point order) into the residual workspace args.Re; V is the full direction
 // field (zero on Dirichlet dofs).  The state is read only.

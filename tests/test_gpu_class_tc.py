@@ -11,7 +11,7 @@ import os
 import numpy as np
 import pytest
 
-from helpers import FLOOR32, blocks_of, rel_err, stretch_field
+from helpers import FLOOR32, FLOOR64, blocks_of, rel_err, stretch_field
 
 pytestmark = pytest.mark.gpu
 TOL32 = 1e-5
@@ -129,3 +129,50 @@ def test_mixed_mesh_fp32_against_oracle(fec, orc):
     Ro, _, _, nzo = orc.assembled_system(blocks_of(mesh), mesh.nodal_coords, "neohookean", phys.create_properties(),
                                          U, asm.dof.dof_to_unknown, asm.dof.unknown_dofs)
     assert max(rel_err(R, Ro, FLOOR32)) <= TOL32 and max(rel_err(nz, nzo, FLOOR32)) <= TOL32
+
+
+def _hex_tet_mesh(fec, n=4):
+    """A hex8 box whose last layer of cubes is split into Kuhn tets: a hex8 block
+    and a tet4 block sharing the interface nodes."""
+    from fec_gb300.meshes import _KUHN, _orient_tets
+    box = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n + 1, n + 1, n + 1))
+    X = box.nodal_coords
+    hexes = box.element_conns["block_1"]
+    last = X[hexes - 1][:, :, 0].max(axis=1) > 1.0 - 1e-12   # cubes touching x = 1
+    tets = _orient_tets(X, hexes[last][:, _KUHN].reshape(-1, 4))
+    return fec.UnstructuredMesh(X, {"hexes": ("HEX8", hexes[~last]), "tets": ("TETRA4", tets)})
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_element"])
+@pytest.mark.parametrize("kind", ["mixed", "hex_tet"])
+def test_mixed_mesh_gather_groups(fec, orc, precision, kind):
+    """Meshes of mixed element sizes gather their nodes in groups of one element size
+    (several elements' loads in flight), nodes shared between sizes on the generic
+    routine; FEC_GATHER_RUNS=generic gathers every node on the generic routine in one
+    launch: bitwise the same residual and nzval, and the FP64 oracle agrees."""
+    torch = _torch()
+    from fec_gb300 import batching
+    mesh = batching.mixed_mesh(2, 2, 3) if kind == "mixed" else _hex_tet_mesh(fec)
+    phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+    V = fec.FunctionSpace(mesh)
+    asm = fec.SparseMatrixAssembler(fec.VectorFunction(V, "u"), device=0, precision=precision)
+    p = fec.create_parameters(mesh, asm, phys)
+    U = stretch_field(mesh.nodal_coords, seed=8).ravel()
+    Uu = torch.from_numpy(U[asm.dof.unknown_dofs - 1].copy()).cuda()
+    out = []
+    for runs in (None, "generic"):
+        if runs:
+            os.environ["FEC_GATHER_RUNS"] = runs
+        try:
+            R, K = fec.assemble_residual_and_stiffness(asm, Uu, p)
+            torch.cuda.synchronize()
+            out.append((R.cpu().numpy().copy(), K.nzval.cpu().numpy().copy()))
+        finally:
+            os.environ.pop("FEC_GATHER_RUNS", None)
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    Ro, _, _, nzo = orc.assembled_system(blocks_of(mesh), mesh.nodal_coords, "neohookean", phys.create_properties(),
+                                         U, asm.dof.dof_to_unknown, asm.dof.unknown_dofs)
+    tol, floor = (1e-12, FLOOR64) if precision == "fp64" else (TOL32, FLOOR32)
+    e_r, e_k = rel_err(out[0][0], Ro, floor), rel_err(out[0][1], nzo, floor)
+    print(kind, precision, "vs oracle: residual", e_r, "nzval", e_k)
+    assert max(e_r[:2]) <= tol and max(e_k) <= tol   # residual normwise (it cancels), nzval entry by entry
