@@ -189,12 +189,15 @@ int build_affine(fec_ctx* c, size_t b) {
 // The table a launch of block b may use: FP64 assemblies of congruent hex8
 // blocks on their own launch (the single launch across blocks keeps the
 // per-element kernels), unless FEC_HEX8_AFFINE=0.
-// FP32-element assemblies of tet10/hex27 blocks of translation classes get theirs.
+// Assemblies of tet10/hex27 blocks of translation classes get theirs: FP32-element
+// (tet10 and hex27) and FP64 (tet10).
 const void* affine_table(const fec_ctx* c, size_t b, int precision, bool mixed) {
   if (mixed || b >= c->d_affine.size()) return nullptr;
   if (c->blocks[b].elem_type == FEC_HEX8)
     return precision == FEC_FP64 && fec::hex8_affine_enabled() ? c->d_affine[b].p : nullptr;
-  return precision == FEC_FP32_ELEMENT ? c->d_affine[b].p : nullptr;
+  if (precision == FEC_FP32_ELEMENT || (precision == FEC_FP64 && c->blocks[b].elem_type == FEC_TET10))
+    return c->d_affine[b].p;
+  return nullptr;
 }
 
 int ensure(fec_ctx* c, DevBuf& b, size_t bytes) {
@@ -212,7 +215,8 @@ inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3); }
 // writes the symmetric half (KE_PAIRS), every other kernel the whole K_e.
 int64_t ke_entries(const fec_ctx* c, size_t b, int precision, bool want_k, bool mixed) {
   const Block& B = c->blocks[b];
-  if (fec::class_tc_runs(B.physics, B.elem_type, precision, want_k, affine_table(c, b, precision, mixed) != nullptr))
+  if (want_k && fec::class_tc_runs(B.physics, B.elem_type, precision, true, want_k,
+                                   affine_table(c, b, precision, mixed) != nullptr))
     return pad4(B.ne * (int64_t(B.nnpe) * (B.nnpe + 1) / 2 * 9));
   const int ndof = c->nf * B.nnpe;
   return pad4(B.ne * ndof * ndof);
@@ -1133,7 +1137,7 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     bi.ndof = ndof;
     // the hex8 mechanics kernels write the node-rows layout, the class tensor-core
     // kernel the symmetric half
-    const bool pairs = fec::class_tc_runs(B.physics, B.elem_type, precision, want_k, ea.affine != nullptr);
+    const bool pairs = want_k && fec::class_tc_runs(B.physics, B.elem_type, precision, want_r, want_k, ea.affine != nullptr);
     bi.layout = (B.elem_type == FEC_HEX8 && (B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2 ||
                                              tc_closure(B, precision)))
                     ? fec::KE_NODE_ROWS
@@ -1669,7 +1673,7 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
     bi.ndof = ndof;
     // the hex8 mechanics kernels write the node-rows layout, the class tensor-core
     // kernel the symmetric half
-    const bool pairs = fec::class_tc_runs(B.physics, B.elem_type, precision, want_k, ea.affine != nullptr);
+    const bool pairs = want_k && fec::class_tc_runs(B.physics, B.elem_type, precision, want_r, want_k, ea.affine != nullptr);
     bi.layout = (B.elem_type == FEC_HEX8 && (B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2))
                     ? fec::KE_NODE_ROWS
                     : (pairs ? fec::KE_PAIRS : fec::KE_ROW_MAJOR);

@@ -119,7 +119,7 @@ __device__ __forceinline__ int64_t tile_elem(int c, int64_t u, int el, int P) {
   return int64_t(c) + int64_t(P) * (u * EPT + el);
 }
 
-template <int ET, class Model, bool WANT_R>
+template <int ET, class Model, bool WANT_R, bool WANT_K>
 __global__ void __launch_bounds__(NTHR, Shape<ET>::MINB) class_tc_kernel(ElemArgs g, int* err) {
   using namespace tc;
   using G = L<ET>;
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(NTHR, Shape<ET>::MINB) class_tc_kernel(ElemArg
   constexpr int A = G::A, NQ = G::NQ, NDOF = G::NDOF, SCR = Model::SCR, NS = Model::NS;
   extern __shared__ __align__(1024) unsigned char sm[];
   const unsigned char* tab = static_cast<const unsigned char*>(g.affine);
-  const int P = *reinterpret_cast<const int*>(tab);
+  const int P = reinterpret_cast<const int*>(tab)[0], off32 = reinterpret_cast<const int*>(tab)[1];
   float* s_ent = reinterpret_cast<float*>(sm + Sm::ENT);
   float* s_P = reinterpret_cast<float*>(sm + Sm::P);
   float* s_g = reinterpret_cast<float*>(sm + Sm::GR);  // dNX [q][a][3], then JxW [q]
@@ -176,9 +176,9 @@ __global__ void __launch_bounds__(NTHR, Shape<ET>::MINB) class_tc_kernel(ElemArg
       u -= nt;
       ++c;
     }
-    const unsigned char* ctab = tab + HEADER + size_t(c) * G::CLASS_BYTES;
+    const unsigned char* ctab = tab + off32 + size_t(c) * G::CLASS_BYTES;
     // W steps 0 .. NWB-1 of this tile (every W buffer is free: the previous tile's MMAs completed)
-    if (tid == 0) {
+    if (WANT_K && tid == 0) {
       for (int j = 0; j < NWB && j < G::KSTEPS; ++j) {
         mbar_expect_tx(&wbar[j], uint32_t(G::W_STEP));
         bulk_g2s(sm + Sm::W + j * G::W_STEP, ctab + size_t(j) * G::W_STEP, uint32_t(G::W_STEP), &wbar[j]);
@@ -255,6 +255,10 @@ __global__ void __launch_bounds__(NTHR, Shape<ET>::MINB) class_tc_kernel(ElemArg
         }
         static_cast<float*>(g.Re)[e * NDOF + r] = R;
       }
+    }
+    if (!WANT_K) {  // residual only: the next tile may reuse the point data
+      __syncthreads();
+      continue;
     }
     // ---- K loop: A slices double buffered against the MMAs, W streamed ----
     const int row = tid >> 1, half = tid & 1;
@@ -372,25 +376,451 @@ __global__ void __launch_bounds__(NTHR, Shape<ET>::MINB) class_tc_kernel(ElemArg
   }
 }
 
-template <int ET, class Model, bool R>
+template <int ET, class Model, bool R, bool K>
 cudaError_t go(const ElemArgs& a, int* err, cudaStream_t s) {
   constexpr int smem = Smem<ET, Model>::BYTES;
-  cudaError_t e = ensure_smem<class_tc_kernel<ET, Model, R>>(size_t(smem));
+  cudaError_t e = ensure_smem<class_tc_kernel<ET, Model, R, K>>(size_t(smem));
   if (e != cudaSuccess) return e;
   // the class count P <= 8 is read on the device; its tiles number at most ceil(ne / EPT) + P
   const int64_t tiles = (a.ne + EPT - 1) / EPT + 8;
   const int64_t cap = int64_t(Shape<ET>::MINB) * num_sms();
   const unsigned grid = unsigned(tiles < cap ? tiles : cap);
-  class_tc_kernel<ET, Model, R><<<grid, NTHR, smem, s>>>(a, err);
+  class_tc_kernel<ET, Model, R, K><<<grid, NTHR, smem, s>>>(a, err);
   return cudaGetLastError();
 }
 
 template <int ET, class Model>
-cudaError_t launch(bool want_r, const ElemArgs& a, int* err, cudaStream_t s, int* launches) {
-  if (a.ne <= 0) return cudaSuccess;
+cudaError_t launch(bool want_r, bool want_k, const ElemArgs& a, int* err, cudaStream_t s, int* launches) {
+  if (a.ne <= 0 || (!want_r && !want_k)) return cudaSuccess;
   ++*launches;
-  return want_r ? go<ET, Model, true>(a, err, s) : go<ET, Model, false>(a, err, s);
+  if (!want_k) return go<ET, Model, true, false>(a, err, s);
+  return want_r ? go<ET, Model, true, true>(a, err, s) : go<ET, Model, false, true>(a, err, s);
 }
+
+// ---------------------------------------------------------------------------
+// FP64 tet10 blocks of translation classes: the same GEMM with FP64 accuracy from
+// BF16 tensor cores, by exact digit slicing of both operands (the scheme of the
+// FP64 hex8 kernel, fec_hex8_affine_tc.cu: the Ozaki scheme, Ozaki, Ogita, Oishi
+// and Rump, Numer. Algorithms 59 (2012) 95-118, restated for BF16 digits).  Each
+// A row (element e, scaled by 2^(7 - tau_e) above its largest tangent entry) and
+// each W row (pair n, 2^(7 - sigma_n)) is seven signed 8-bit digits, exact in
+// BF16; the digit products of level L = s + t (s + t <= 6) accumulate exactly in
+// their own FP32 accumulator (36 reduction terms: below 2^23), seven levels x 64
+// pairs = 448 TMEM columns; the epilogue sums the levels in double-float and
+// scales by 2^(tau_e + sigma_n - 14).  Per tile of 12 elements: the FP64 point
+// phase (displacement gradient from absolute displacements and the class's FP64
+// gradients, constitutive update, the double-float scratch, the 45 unique tangent
+// entries in double-float, the element scale), the residual in double-float, the
+// A digit slices of the three K steps (K = 36 padded to 48), 30 MMAs (10 groups of
+// digit pairs per K step, consecutive W slices as one N = 64..256 operand), the
+// epilogue into the KE_PAIRS workspace (double-float pairs).
+// ---------------------------------------------------------------------------
+namespace x64 {
+constexpr int A = 10, NQ = 4, NDOF = 30, NP = 55, NPAD = 64, KR = 36, KS = 3, EPT = 12, NPT = EPT * NQ;
+constexpr int ND = 7, NLEV = 7;
+constexpr int A_SLICE = 128 * 16 * 2, A_STEP = ND * A_SLICE;  // one digit of one K step; the seven digits
+constexpr int W_SLICE = NPAD * 16 * 2, W_STEP = ND * W_SLICE, W_BYTES = KS * W_STEP;
+// class section: W digit images [KS][ND][NPAD x 16], sigma int[NPAD], dNX double [NQ][A][3], JxW double [NQ]
+constexpr int C_W = 0, C_SIG = W_BYTES, C_G = C_SIG + NPAD * 4, C_JXW = C_G + NQ * A * 3 * 8;
+constexpr int C_BYTES = (C_JXW + NQ * 8 + 15) / 16 * 16;
+static_assert(W_BYTES % 16 == 0 && C_G % 8 == 0, "class section layout");
+// shared memory
+constexpr int S_A = 0, S_W = S_A + KS * A_STEP, S_ENT = S_W + W_BYTES;  // float2 [NPT][45]
+constexpr int S_P2 = S_ENT + NPT * 45 * 8;                             // float2 [NPT][9]
+constexpr int S_G = S_P2 + NPT * 9 * 8;                                // double [NQ][A][3]
+constexpr int S_G2 = S_G + NQ * A * 3 * 8;                             // float2 [NQ][A][3]
+constexpr int S_JXW = S_G2 + NQ * A * 3 * 8;                           // double [NQ]
+constexpr int S_SIG = S_JXW + NQ * 8;                                  // int [NPAD]
+constexpr int S_U = S_SIG + NPAD * 4;                                  // double [EPT][A][3]
+constexpr int S_CONN = S_U + EPT * A * 3 * 8;                          // int [EPT][A]
+constexpr int S_SCR = S_CONN + EPT * A * 4;                            // float2 [NPT][SCR2_MAX]: split scratch
+constexpr int SCR2_MAX = 24;
+constexpr int S_BND = S_SCR + NPT * SCR2_MAX * 8;                      // float [NPT]
+constexpr int S_TAU = S_BND + NPT * 4;                                 // int [16]
+constexpr int S_BAR = (S_TAU + 16 * 4 + 15) / 16 * 16;                 // W, MMA barriers
+constexpr int S_TSLOT = S_BAR + 16;
+constexpr int SMEM = S_TSLOT + 16;
+static_assert(SMEM <= 232448, "shared memory");
+constexpr int NGROUP = 10;
+// (A slice t, first W slice s0, W slices ns): every digit pair s + t <= 6 once; the
+// t = 0 groups write each level first
+__device__ __constant__ int8_t kGroups[NGROUP][3] = {{0, 0, 4}, {0, 4, 3}, {1, 0, 4}, {1, 4, 2}, {2, 0, 4},
+                                                      {2, 4, 1}, {3, 0, 4}, {4, 0, 3}, {5, 0, 2}, {6, 0, 1}};
+
+// byte offset of (row, col) in a K-major BF16 operand tile with K = 16
+__host__ __device__ __forceinline__ uint32_t op16(int row, int col) {
+  return uint32_t(row >> 3) * 256u + uint32_t(col >> 3) * 128u + uint32_t(row & 7) * 16u + uint32_t(col & 7) * 2u;
+}
+// 2^k as a float for k in [-126, 127]
+__device__ __forceinline__ float pow2f(int k) { return __uint_as_float(uint32_t(k + 127) << 23); }
+// Seven 4-column loads (the seven levels of four pairs, levels 64 columns apart) under one wait
+__device__ __forceinline__ void tmem_ld4x7(uint32_t taddr, float (*v)[4]) {
+  uint32_t r[28];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%28];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%4, %5, %6, %7}, [%29];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%8, %9, %10, %11}, [%30];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%12, %13, %14, %15}, [%31];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%16, %17, %18, %19}, [%32];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%20, %21, %22, %23}, [%33];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%24, %25, %26, %27}, [%34];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27])
+      : "r"(taddr), "r"(taddr + 64u), "r"(taddr + 128u), "r"(taddr + 192u), "r"(taddr + 256u), "r"(taddr + 320u),
+        "r"(taddr + 384u)
+      : "memory");
+#pragma unroll
+  for (int L = 0; L < NLEV; ++L)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[L][j] = __uint_as_float(r[L * 4 + j]);
+}
+
+template <class Model, bool WANT_R, bool WANT_K>
+__global__ void __launch_bounds__(NTHR, 1) class_tc64_kernel(ElemArgs g, int* err) {
+  using namespace tc;
+  constexpr int NS = Model::NS;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const unsigned char* tab = static_cast<const unsigned char*>(g.affine);
+  const int P = reinterpret_cast<const int*>(tab)[0], off64 = reinterpret_cast<const int*>(tab)[2];
+  float2* s_ent = reinterpret_cast<float2*>(sm + S_ENT);
+  float2* s_P2 = reinterpret_cast<float2*>(sm + S_P2);
+  double* s_g = reinterpret_cast<double*>(sm + S_G);
+  float2* s_g2 = reinterpret_cast<float2*>(sm + S_G2);
+  double* s_jxw = reinterpret_cast<double*>(sm + S_JXW);
+  int* s_sig = reinterpret_cast<int*>(sm + S_SIG);
+  double* s_u = reinterpret_cast<double*>(sm + S_U);
+  int* s_conn = reinterpret_cast<int*>(sm + S_CONN);
+  float* s_bnd = reinterpret_cast<float*>(sm + S_BND);
+  int* s_tau = reinterpret_cast<int*>(sm + S_TAU);
+  float2* s_scr2 = reinterpret_cast<float2*>(sm + S_SCR);
+  static_assert(Model::SCR2 <= SCR2_MAX, "scratch");
+  uint64_t* wbar = reinterpret_cast<uint64_t*>(sm + S_BAR);
+  uint64_t* mbar = wbar + 1;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t s0 = smem_u32(sm);
+
+  // ---- setup: A slices zero (padding rows are never written) ----
+  for (int i = tid; i < KS * A_STEP / 16; i += NTHR)
+    reinterpret_cast<uint4*>(sm + S_A)[i] = make_uint4(0u, 0u, 0u, 0u);
+  if (tid == 0) {
+    mbar_init(wbar, 1);
+    mbar_init(mbar, 1);
+    mbar_fence_init();
+  }
+  if (warp == 0) tmem_alloc(reinterpret_cast<uint32_t*>(sm + S_TSLOT), 512);
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + S_TSLOT);
+  const long long budget = g.wait_budget > 0 ? g.wait_budget : WAIT_BUDGET;
+  uint32_t wph = 0u, mph = 0u;
+  bool wpend = false, failed = false;
+
+  int64_t ntiles = 0;
+  for (int c = 0; c < P; ++c) ntiles += ((g.ne - c + P - 1) / P + EPT - 1) / EPT;
+  int cur = -1;
+  for (int64_t t = blockIdx.x; t < ntiles && !failed; t += gridDim.x) {
+    int c = 0;
+    int64_t u = t;
+    for (;;) {
+      const int64_t nt = ((g.ne - c + P - 1) / P + EPT - 1) / EPT;
+      if (u < nt) break;
+      u -= nt;
+      ++c;
+    }
+    const unsigned char* ctab = tab + off64 + size_t(c) * C_BYTES;
+    if (c != cur) {
+      // the class's W digits (the previous tile's MMAs completed) and gradients
+      if (WANT_K && tid == 0) {
+        mbar_expect_tx(wbar, uint32_t(W_BYTES));
+        bulk_g2s(sm + S_W, ctab + C_W, uint32_t(W_BYTES), wbar);
+        wpend = true;
+      }
+      for (int i = tid; i < NQ * A * 3; i += NTHR) {
+        const double v = __ldg(reinterpret_cast<const double*>(ctab + C_G) + i);
+        s_g[i] = v;
+        s_g2[i] = df64_split(v);
+      }
+      if (tid < NQ) s_jxw[tid] = __ldg(reinterpret_cast<const double*>(ctab + C_JXW) + tid);
+      if (tid < NPAD) s_sig[tid] = __ldg(reinterpret_cast<const int*>(ctab + C_SIG) + tid);
+      cur = c;
+    }
+    for (int i = tid; i < EPT * A; i += NTHR) {
+      const int el = i / A, a = i - el * A;
+      const int64_t e = tile_elem(c, u, el, P);
+      s_conn[i] = e < g.ne ? g.conn[e * A + a] : -1;
+    }
+    __syncthreads();
+    for (int i = tid; i < EPT * A * 3; i += NTHR) {
+      const int el = i / (A * 3), r = i - el * A * 3, a = r / 3, d = r - a * 3;
+      const int n = s_conn[el * A + a];
+      s_u[i] = n >= 0 ? __ldg(&g.U[int64_t(n) * 3 + d]) : 0.0;
+    }
+    __syncthreads();
+    // ---- per point (FP64): displacement gradient, constitutive update ----
+    if (tid < NPT) {
+      const int el = tid / NQ, q = tid - el * NQ;
+      const int64_t e = tile_elem(c, u, el, P);
+      float2* P2 = s_P2 + tid * 9;
+      float2* scr2 = s_scr2 + tid * SCR2_MAX;
+      float bnd = 0.f;
+      if (e < g.ne) {
+        const double* gq = s_g + q * A * 3;
+        const double* ue = s_u + el * A * 3;
+        double gu[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int a = 0; a < A; ++a)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            const double gj = gq[a * 3 + j];
+            gu[0][j] = fma(ue[a * 3], gj, gu[0][j]);
+            gu[1][j] = fma(ue[a * 3 + 1], gj, gu[1][j]);
+            gu[2][j] = fma(ue[a * 3 + 2], gj, gu[2][j]);
+          }
+        const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
+        double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
+        double P9[9], scr[Model::SCR];
+        Model::point(g.props, gu, s_jxw[q], so, sn, P9, scr);
+#pragma unroll
+        for (int m = 0; m < 9; ++m) P2[m] = df64_split(P9[m]);
+        if (WANT_K) {
+          Model::split_scratch(scr, scr2);
+          bnd = Model::abound(scr2) * 1.0001f;
+        }
+      } else {
+        for (int m = 0; m < 9; ++m) P2[m] = make_float2(0.f, 0.f);
+        if (WANT_K)
+          for (int m = 0; m < Model::SCR2; ++m) scr2[m] = make_float2(0.f, 0.f);
+      }
+      s_bnd[tid] = bnd;
+    }
+    __syncthreads();
+    // the 45 unique JxW A entries of every point in double-float, on all threads:
+    // entry w = (r1, r2), r1 = 3i + J <= r2 = 3k + L, in row order
+    if (WANT_K) {
+      for (int idx = tid; idx < NPT * 45; idx += NTHR) {
+        const int pt = idx / 45, w = idx - pt * 45;
+        int r1 = 0, m = w;
+        while (m >= 9 - r1) {
+          m -= 9 - r1;
+          ++r1;
+        }
+        const int r2 = r1 + m;
+        s_ent[idx] = Model::aentry_df64(s_scr2 + pt * SCR2_MAX, r1 / 3, r1 % 3, r2 / 3, r2 % 3);
+      }
+    }
+    if (WANT_K && tid < EPT) {  // the element's scale 2^tau > |every tangent entry|
+      float b = 0.f;
+      for (int q = 0; q < NQ; ++q) b = fmaxf(b, s_bnd[tid * NQ + q]);
+      int tau = 0;
+      if (b > 0.f) frexpf(b, &tau);
+      s_tau[tid] = tau < -119 ? -119 : (tau > 126 ? 126 : tau);
+    }
+    if (WANT_R) {  // R_(a,i) = sum_q sum_J dNX_qaJ P_q,iJ in double-float, q in order
+      for (int i = tid; i < EPT * NDOF; i += NTHR) {
+        const int el = i / NDOF, r = i - el * NDOF, a = r / 3, ii = r - a * 3;
+        const int64_t e = tile_elem(c, u, el, P);
+        if (e >= g.ne) continue;
+        float2 R = make_float2(0.f, 0.f);
+        for (int q = 0; q < NQ; ++q) {
+          const float2* gq = s_g2 + (q * A + a) * 3;
+          const float2* Pq = s_P2 + (el * NQ + q) * 9 + ii * 3;
+          R = df64_dot3_acc(R, gq[0], Pq[0], gq[1], Pq[1], gq[2], Pq[2]);
+        }
+        static_cast<double*>(g.Re)[e * NDOF + r] = widen(R.x) + widen(R.y);
+      }
+    }
+    __syncthreads();
+    if (!WANT_K) continue;
+    // ---- A digit slices of the three K steps: thread (row m, half h), 8 columns each ----
+    {
+      const int m = tid >> 1, h = tid & 1, rq = m & 31;
+      if (rq < 27) {
+        const int el = 3 * (m >> 5) + rq / 9, ik = rq % 9, i = ik / 3, k = ik % 3;
+        const float fs = pow2f(7 - s_tau[el]);
+        const float2* ent = s_ent + el * NQ * 45;
+        for (int ks = 0; ks < KS; ++ks) {
+          uint32_t dig[ND][4];
+#pragma unroll
+          for (int cp = 0; cp < 4; ++cp) {
+            uint32_t lo16[ND], hi16[ND];
+#pragma unroll
+            for (int half2 = 0; half2 < 2; ++half2) {
+              const int r = 16 * ks + 8 * h + 2 * cp + half2;
+              float xh = 0.f, xl = 0.f;
+              if (r < KR) {
+                const int q = r / 9, JL = r - q * 9;
+                const int ra = 3 * i + JL / 3, rb = 3 * k + JL % 3;  // A_iJkL = A_kLiJ
+                const int r1 = ra < rb ? ra : rb, r2 = ra < rb ? rb : ra;
+                const float2 x = ent[q * 45 + r1 * 9 - (r1 * (r1 - 1)) / 2 + (r2 - r1)];
+                xh = x.x * fs;
+                xl = x.y * fs;
+              }
+#pragma unroll
+              for (int d = 0; d < ND; ++d) {
+                const float dh = rintf(xh), dl = rintf(xl);
+                xh = (xh - dh) * 256.f;
+                xl = (xl - dl) * 256.f;
+                const uint32_t bits = __float_as_uint(dh + dl) >> 16;
+                if (half2 == 0) lo16[d] = bits;
+                else hi16[d] = bits;
+              }
+            }
+#pragma unroll
+            for (int d = 0; d < ND; ++d) dig[d][cp] = lo16[d] | (hi16[d] << 16);
+          }
+#pragma unroll
+          for (int d = 0; d < ND; ++d)
+            *reinterpret_cast<uint4*>(sm + S_A + ks * A_STEP + d * A_SLICE + op16(m, 8 * h)) =
+                make_uint4(dig[d][0], dig[d][1], dig[d][2], dig[d][3]);
+        }
+      }
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      if (wpend) {
+        if (!mbar_wait(wbar, wph, budget)) {  // report, then wait the copy out
+          atomicExch(err, 1);
+          mbar_wait(wbar, wph, WAIT_BUDGET);
+        }
+        wph ^= 1u;
+        wpend = false;
+      }
+      tc_fence_after();
+#pragma unroll 1
+      for (int ks = 0; ks < KS; ++ks)
+#pragma unroll 1
+        for (int gi = 0; gi < NGROUP; ++gi) {
+          const int tt = kGroups[gi][0], sg = kGroups[gi][1], ns = kGroups[gi][2];
+          const uint64_t ad = smem_desc(s0 + uint32_t(S_A + ks * A_STEP + tt * A_SLICE), 128, 256);
+          const uint64_t bd = smem_desc(s0 + uint32_t(S_W + ks * W_STEP + sg * W_SLICE), 128, 256);
+          mma_bf16(tmem + uint32_t((sg + tt) * NPAD), ad, bd, idesc_bf16(128, NPAD * ns),
+                   (tt == 0 && ks == 0) ? 0u : 1u);
+        }
+      mma_commit(mbar);
+    }
+    {
+      const bool ok = mbar_wait(mbar, mph, budget);
+      if (__syncthreads_or(!ok)) {
+        failed = true;
+        break;
+      }
+      mph ^= 1u;
+    }
+    tc_fence_after();
+    // ---- epilogue: levels -> double-float pairs, the symmetric half of K_e ----
+    {
+      const int qd = warp & 3, ch = warp >> 2;
+      const int j = lane / 9, ik = lane - 9 * j;
+      const int el = 3 * qd + (lane < 27 ? j : 0);
+      const int64_t e = tile_elem(c, u, el, P);
+      const bool mine = lane < 27 && e < g.ne;
+      const float f1 = pow2f(s_tau[el] - 7);
+      float2* dst = static_cast<float2*>(g.Ke) + e * (NP * 9) + ik;
+#pragma unroll 1
+      for (int n0 = ch * (NPAD / 2); n0 < (ch + 1) * (NPAD / 2); n0 += 4) {
+        float v[NLEV][4];
+        tmem_ld4x7(tmem + (uint32_t(32 * qd) << 16) + uint32_t(n0), v);
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          const int n = n0 + jj;
+          // sum_L v_L 2^(-8L): levels 6..4 in FP32 (their rounding is below 2^-55 of
+          // level 0), then 3..0 in double-float
+          float hi = fmaf(fmaf(v[6][jj], 0.00390625f, v[5][jj]), 0.00390625f, v[4][jj]), lo = 0.f;
+#pragma unroll
+          for (int Lv = 3; Lv >= 0; --Lv) {
+            const float a = v[Lv][jj], b = hi * 0.00390625f;
+            lo *= 0.00390625f;
+            const float s1 = a + b, bb = s1 - a;
+            lo += (a - (s1 - bb)) + (b - bb);
+            hi = s1 + lo;
+            lo = lo - (hi - s1);
+          }
+          if (mine && n < NP) {
+            const float f = f1 * pow2f(s_sig[n] - 7);
+            dst[n * 9] = make_float2(hi * f, lo * f);
+          }
+        }
+      }
+    }
+    tc_fence_before();
+    __syncthreads();
+  }
+  if (failed) {
+    // one more bounded wait on the pending phases (a phase that already completed
+    // returns at once), so that no MMA or copy is left in flight
+    if (tid == 0) {
+      atomicExch(err, 1);
+      if (wpend) mbar_wait(wbar, wph, WAIT_BUDGET);
+    }
+    mbar_wait(mbar, mph, WAIT_BUDGET);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
+template <class Model, bool R, bool K>
+cudaError_t go(const ElemArgs& a, int* err, cudaStream_t s) {
+  cudaError_t e = ensure_smem<class_tc64_kernel<Model, R, K>>(size_t(SMEM));
+  if (e != cudaSuccess) return e;
+  const int64_t tiles = (a.ne + EPT - 1) / EPT + 8;
+  const int64_t cap = num_sms();
+  const unsigned grid = unsigned(tiles < cap ? tiles : cap);
+  class_tc64_kernel<Model, R, K><<<grid, NTHR, SMEM, s>>>(a, err);
+  return cudaGetLastError();
+}
+
+template <class Model>
+cudaError_t launch(bool want_r, bool want_k, const ElemArgs& a, int* err, cudaStream_t s, int* launches) {
+  if (a.ne <= 0 || (!want_r && !want_k)) return cudaSuccess;
+  ++*launches;
+  if (!want_k) return go<Model, true, false>(a, err, s);
+  return want_r ? go<Model, true, true>(a, err, s) : go<Model, false, true>(a, err, s);
+}
+
+// Host: the FP64 section of one class, from its spatial gradients and weights.
+bool section(const std::vector<double>& dnx, const std::vector<double>& jxw, unsigned char* out) {
+  int32_t sig[NPAD] = {0};
+  for (int a = 0, n = 0; a < A; ++a)
+    for (int b = a; b < A; ++b, ++n) {
+      double w[KR], mx = 0.0;
+      for (int r = 0; r < KR; ++r) {
+        const int q = r / 9, J = (r % 9) / 3, Lc = r % 3;
+        w[r] = dnx[(q * A + a) * 3 + J] * dnx[(q * A + b) * 3 + Lc];
+        mx = std::fmax(mx, std::fabs(w[r]));
+      }
+      int ex = 0;
+      if (mx > 0.0) std::frexp(mx, &ex);  // |w| < 2^ex
+      if (ex < -119 || ex > 134) return false;  // the epilogue scales by 2^(ex - 7) in FP32
+      sig[n] = ex;
+      for (int r = 0; r < KR; ++r) {
+        double y = std::ldexp(w[r], 7 - ex);  // |y| < 128, exact
+        for (int d = 0; d < ND; ++d) {
+          const double dd = std::nearbyint(y);
+          y = (y - dd) * 256.0;
+          const float fd = float(dd);
+          uint32_t bits;
+          std::memcpy(&bits, &fd, 4);
+          const uint16_t b16 = uint16_t(bits >> 16);
+          std::memcpy(out + C_W + (r / 16) * W_STEP + d * W_SLICE + op16(n, r % 16), &b16, 2);
+        }
+      }
+    }
+  std::memcpy(out + C_SIG, sig, sizeof sig);
+  std::memcpy(out + C_G, dnx.data(), sizeof(double) * dnx.size());
+  std::memcpy(out + C_JXW, jxw.data(), sizeof(double) * jxw.size());
+  return true;
+}
+}  // namespace x64
 
 // ---- host: the class table ---------------------------------------------------------
 // tf32 with round-to-nearest, ties away (the device's cvt.rna.tf32.f32)
@@ -411,8 +841,11 @@ bool table(int P, const double* xc, const double* ref, std::vector<unsigned char
   const double* dN = ref + NQ * A;
   const double* w = dN + NQ * A * 3;
   (void)N;
-  out.assign(size_t(HEADER) + size_t(P) * G::CLASS_BYTES, 0);
-  std::memcpy(out.data(), &P, sizeof P);
+  // header: class count, offset of the FP32-element section, of the FP64 section (tet10; 0: none)
+  const int off32 = HEADER, off64 = ET == 7 ? HEADER + P * G::CLASS_BYTES : 0;
+  out.assign(size_t(HEADER) + size_t(P) * G::CLASS_BYTES + (ET == 7 ? size_t(P) * x64::C_BYTES : 0), 0);
+  const int hdr[3] = {P, off32, off64};
+  std::memcpy(out.data(), hdr, sizeof hdr);
   std::vector<double> dnx(size_t(NQ) * A * 3), jxw(NQ);
   for (int c = 0; c < P; ++c) {
     const double* X = xc + size_t(c) * A * 3;
@@ -470,6 +903,7 @@ bool table(int P, const double* xc, const double* ref, std::vector<unsigned char
     float* gb = reinterpret_cast<float*>(cb + size_t(G::KSTEPS) * G::W_STEP);
     for (int i = 0; i < NQ * A * 3; ++i) gb[i] = float(dnx[i]);
     for (int q = 0; q < NQ; ++q) gb[NQ * A * 3 + q] = float(jxw[q]);
+    if (ET == 7 && !x64::section(dnx, jxw, out.data() + off64 + size_t(c) * x64::C_BYTES)) return false;
   }
   return true;
 }
@@ -488,24 +922,31 @@ bool class_tc_enabled() {
   return !(v && v[0] == '0');
 }
 
-bool class_tc_runs(int physics, int elem_type, int precision, bool want_k, bool has_table) {
-  if (!has_table || !want_k || precision != 1 || (physics != 2 && physics != 3) || !class_tc_enabled()) return false;
-  return elem_type == 7 || (elem_type == 8 && !hex27_on_cuda_cores());
+bool class_tc_runs(int physics, int elem_type, int precision, bool want_r, bool want_k, bool has_table) {
+  if (!has_table || !(want_r || want_k) || (physics != 2 && physics != 3) || !class_tc_enabled()) return false;
+  if (precision == 1) return elem_type == 7 || (elem_type == 8 && !hex27_on_cuda_cores());
+  return precision == 0 && elem_type == 7;  // FP64: tet10 (the exact digit levels hold 36 reduction terms)
 }
 
-cudaError_t launch_class_tc(int physics, int elem_type, bool want_r, const ElemArgs& a, cudaStream_t s,
-                            int* launches) {
+cudaError_t launch_class_tc(int physics, int elem_type, int precision, bool want_r, bool want_k, const ElemArgs& a,
+                            cudaStream_t s, int* launches) {
   int* err = a.wait_err;
   if (!err) {
     const cudaError_t e = wait_error_flag(&err);
     if (e != cudaSuccess) return e;
   }
+  if (precision == 0) {
+    if (elem_type != 7) return cudaErrorNotSupported;
+    if (physics == 2) return ctc::x64::launch<NeoHookean>(want_r, want_k, a, err, s, launches);
+    if (physics == 3) return ctc::x64::launch<J2>(want_r, want_k, a, err, s, launches);
+    return cudaErrorNotSupported;
+  }
   if (elem_type == 7) {
-    if (physics == 2) return ctc::launch<7, NeoHookean>(want_r, a, err, s, launches);
-    if (physics == 3) return ctc::launch<7, J2>(want_r, a, err, s, launches);
+    if (physics == 2) return ctc::launch<7, NeoHookean>(want_r, want_k, a, err, s, launches);
+    if (physics == 3) return ctc::launch<7, J2>(want_r, want_k, a, err, s, launches);
   } else if (elem_type == 8) {
-    if (physics == 2) return ctc::launch<8, NeoHookean>(want_r, a, err, s, launches);
-    if (physics == 3) return ctc::launch<8, J2>(want_r, a, err, s, launches);
+    if (physics == 2) return ctc::launch<8, NeoHookean>(want_r, want_k, a, err, s, launches);
+    if (physics == 3) return ctc::launch<8, J2>(want_r, want_k, a, err, s, launches);
   }
   return cudaErrorNotSupported;
 }

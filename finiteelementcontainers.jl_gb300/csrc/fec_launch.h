@@ -78,22 +78,25 @@ cudaError_t launch_hex8_affine_tc(int physics, bool want_r, bool want_k, const E
 bool hex8_affine_table(const double* x0, const double* ref, std::vector<unsigned char>& out);
 // FEC_HEX8_AFFINE=0 keeps such blocks on the per-element kernels.
 bool hex8_affine_enabled();
-// FP32-element tet10 (7) / hex27 (8) Neo-Hookean (2) or J2 (3) with the tangent,
-// for a block whose element e is a translate of element e mod P (args.affine:
-// the table class_tc_table built): the stiffness contraction on the tensor cores
-// against each class's constant gradient products (kind::tf32, two-term splits).
-cudaError_t launch_class_tc(int physics, int elem_type, bool want_r, const ElemArgs& args, cudaStream_t stream,
-                            int* launches);
+// Tet10 (7) / hex27 (8) Neo-Hookean (2) or J2 (3) for a block whose element e is
+// a translate of element e mod P (args.affine: the table class_tc_table built):
+// the stiffness contraction on the tensor cores against each class's constant
+// gradient products -- FP32-element (precision 1, tet10 and hex27) with
+// kind::tf32 two-term splits, FP64 (precision 0, tet10) with exact BF16 digit
+// slices; residual-only calls run the same point phase and residual arithmetic.
+cudaError_t launch_class_tc(int physics, int elem_type, int precision, bool want_r, bool want_k, const ElemArgs& args,
+                            cudaStream_t stream, int* launches);
 // Host: that table for nclass (<= 8) classes from the classes' first elements'
 // node coordinates xc[nclass][A][3] and the block's reference tables
 // (RefLayout order); false for an inverted or degenerate element.
 bool class_tc_table(int elem_type, int nclass, const double* xc, const double* ref, std::vector<unsigned char>& out);
 // FEC_CLASS_TC=0 keeps such blocks on the per-element kernels.
 bool class_tc_enabled();
-// Whether an assembly of such a block (physics, element type, precision, the
-// stiffness wanted, a class table present) runs that kernel, which writes the
-// KE_PAIRS workspace layout (A(A+1)/2 * 9 entries per element).
-bool class_tc_runs(int physics, int elem_type, int precision, bool want_k, bool has_table);
+// Whether an assembly of such a block (physics, element type, precision, residual
+// and stiffness wanted, a class table present) runs that kernel; with the
+// stiffness it writes the KE_PAIRS workspace layout (A(A+1)/2 * 9 entries per
+// element).
+bool class_tc_runs(int physics, int elem_type, int precision, bool want_r, bool want_k, bool has_table);
 // FEC_HEX8_DF64=tile selects the one-tile-per-CTA FP64 hex8 kernel instead of
 // the warp-specialised persistent one.
 bool hex8_df64_tile_kernel();

@@ -202,12 +202,12 @@ cudaError_t launch_mech_neohookean(int elem_type, int precision, bool want_r, bo
       return cudaErrorNotSupported;
     case 6: return tuned<6>(precision, want_r, want_k, a, s, launches);
     case 7:
-      if (class_tc_runs(2, 7, precision, want_k, a.affine != nullptr))
-        return launch_class_tc(2, 7, want_r, a, s, launches);
+      if (class_tc_runs(2, 7, precision, want_r, want_k, a.affine != nullptr))
+        return launch_class_tc(2, 7, precision, want_r, want_k, a, s, launches);
       return tuned<7>(precision, want_r, want_k, a, s, launches);
     case 8:
-      if (class_tc_runs(2, 8, precision, want_k, a.affine != nullptr))
-        return launch_class_tc(2, 8, want_r, a, s, launches);
+      if (class_tc_runs(2, 8, precision, want_r, want_k, a.affine != nullptr))
+        return launch_class_tc(2, 8, precision, want_r, want_k, a, s, launches);
       if (precision == 1 && want_k && !hex27_on_cuda_cores())
         return launch_hex27_tc(2, want_r, want_k, a, s, launches);
       if (precision == 0 && !fp64_native()) return hex27_df64(want_r, want_k, a, s, launches);

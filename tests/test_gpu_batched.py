@@ -88,8 +88,10 @@ def test_newton_loop_graph_replays_eager_bits(fec, precision):
 def test_autotuned_generic_kernels_are_bitwise_identical(fec):
     """Every launch configuration the autotuner may pick for the tet4/tet10
     kernels (elements per CTA) gives bitwise the same residual and nzval, in FP64
-    and FP32-element arithmetic; the tuned run reports its choices.  (Hex27 has
-    its own kernels in both arithmetics: double-float in FP64, tensor cores in
+    and FP32-element arithmetic; the tuned run reports its choices.  The tet10
+    box is a block of translation classes, whose tensor-core kernel FEC_CLASS_TC=0
+    switches off here so that the generic kernels run.  (Hex27 has its own
+    kernels in both arithmetics: double-float in FP64, tensor cores in
     FP32-element; its generic configurations stay tunable behind
     FEC_HEX27_ON_CUDA_CORES=1 and FEC_FP64_CONTRACTION=native.)"""
     import os
@@ -98,6 +100,18 @@ def test_autotuned_generic_kernels_are_bitwise_identical(fec):
     from helpers import stretch_field
     mesh = batching.mixed_mesh(3, 3, 2)
     results = {}
+    os.environ["FEC_CLASS_TC"] = "0"
+    try:
+        _autotune_candidates(fec, torch, mesh, stretch_field, results)
+    finally:
+        os.environ.pop("FEC_CLASS_TC", None)
+    report = fec.autotune_report()
+    print("\n".join(report))
+    assert any("tet4" in line for line in report) and any("tet10" in line for line in report)
+
+
+def _autotune_candidates(fec, torch, mesh, stretch_field, results):
+    import os
     for precision in ("fp64", "fp32_element"):
         for cand in ("0", "1", "2", None):
             if cand is None:
@@ -119,17 +133,15 @@ def test_autotuned_generic_kernels_are_bitwise_identical(fec):
         for cand in ("1", "2", None):
             assert np.array_equal(results[(precision, cand)][0], ref[0])
             assert np.array_equal(results[(precision, cand)][1], ref[1])
-    report = fec.autotune_report()
-    print("\n".join(report))
-    assert any("tet4" in line for line in report) and any("tet10" in line for line in report)
 
 
 @pytest.mark.parametrize("physics", ["neohookean", "j2"])
 def test_single_launch_matches_per_block_launches(fec, physics):
     """hex8 + tet4 + tet10 + hex27 blocks in ONE persistent element launch give
     bitwise the residual, nzval and state of one launch per block.  The single
-    launch runs the per-element hex8 kernel, so the per-block launches do too
-    (FEC_HEX8_AFFINE=0: the structured hex8 block would take the affine path)."""
+    launch runs the per-element kernels, so the per-block launches do too
+    (FEC_HEX8_AFFINE=0 and FEC_CLASS_TC=0: the structured hex8 block and the tet10
+    box of translation classes would take their tensor-core kernels)."""
     import os
     torch = _torch()
     from fec_gb300 import batching
@@ -140,10 +152,12 @@ def test_single_launch_matches_per_block_launches(fec, physics):
         names=["hex8", "tet4", "tet10", "hex27"])
     out = []
     os.environ["FEC_HEX8_AFFINE"] = "0"
+    os.environ["FEC_CLASS_TC"] = "0"
     try:
         _single_vs_per_block(fec, torch, mesh, physics, stretch_field, out)
     finally:
         os.environ.pop("FEC_HEX8_AFFINE", None)
+        os.environ.pop("FEC_CLASS_TC", None)
     assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
     if physics == "j2":
         assert torch.equal(out[0][3], out[1][3])
@@ -172,8 +186,18 @@ def _single_vs_per_block(fec, torch, mesh, physics, stretch_field, out):
 def test_newton_loop_graph_with_single_launch(fec):
     """The CUDA-graph Newton loop over the tet4/tet10/hex27 system with all its
     element blocks in one persistent launch replays the eager loop bitwise, and
-    both equal the loop with one launch per block."""
+    both equal the loop with one launch per block (its per-element kernels:
+    FEC_CLASS_TC=0 keeps the tet10 box off its tensor-core kernel)."""
+    import os
     torch = _torch()
+    os.environ["FEC_CLASS_TC"] = "0"
+    try:
+        _newton_single_vs_per_block(fec, torch)
+    finally:
+        os.environ.pop("FEC_CLASS_TC", None)
+
+
+def _newton_single_vs_per_block(fec, torch):
     from fec_gb300 import batching
     runs = []
     for single in (False, True):

@@ -176,3 +176,61 @@ def test_mixed_mesh_gather_groups(fec, orc, precision, kind):
     e_r, e_k = rel_err(out[0][0], Ro, floor), rel_err(out[0][1], nzo, floor)
     print(kind, precision, "vs oracle: residual", e_r, "nzval", e_k)
     assert max(e_r[:2]) <= tol and max(e_k) <= tol   # residual normwise (it cancels), nzval entry by entry
+
+
+@pytest.mark.parametrize("phys_name", ["neohookean", "j2"])
+def test_class_tensor_cores_fp64_tet10(fec, orc, phys_name):
+    """FP64 tet10 blocks of translation classes: the tangent on the tensor cores in
+    exact BF16 digit slices, within the FP64 bar (1e-12) of the oracle entry by entry
+    (nzval) and normwise (the residual, formed in double-float), and of the
+    per-element double-float kernel (FEC_CLASS_TC=0)."""
+    torch = _torch()
+    mesh = _mesh(fec, "tet10")
+    if phys_name == "neohookean":
+        phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+        U = stretch_field(mesh.nodal_coords, seed=3).ravel()
+    else:
+        phys = fec.J2Plasticity(200.0, 0.3, 0.25, 2.0)
+        U = 3.0 * stretch_field(mesh.nodal_coords, seed=2, noise=1e-4, diag=(1.004, 0.999, 0.999)).ravel()
+    V = fec.FunctionSpace(mesh)
+    asm = fec.SparseMatrixAssembler(fec.VectorFunction(V, "u"), device=0, precision="fp64")
+    p = fec.create_parameters(mesh, asm, phys)
+    R, nz, sn, _ = _run(fec, asm, p, U)
+    R0, nz0, sn0, _ = _run(fec, asm, p, U, class_tc=False)
+    ne = mesh.num_elements()
+    st = np.zeros(7 * 4 * ne) if phys_name == "j2" else None
+    st_new = None if st is None else np.zeros_like(st)
+    Ro, _, _, nzo = orc.assembled_system(blocks_of(mesh), mesh.nodal_coords, phys_name, phys.create_properties(), U,
+                                         asm.dof.dof_to_unknown, asm.dof.unknown_dofs, st, st_new)
+    e_r, e_k = rel_err(R, Ro), rel_err(nz, nzo)
+    e_r0, e_k0 = rel_err(R, R0), rel_err(nz, nz0)
+    print("fp64 tet10", phys_name, "class vs oracle: residual", e_r, "nzval", e_k, "| vs per-element: residual", e_r0,
+          "nzval", e_k0)
+    assert max(e_r[:2]) <= 1e-12 and max(e_k) <= 1e-12
+    assert max(e_r0[:2]) <= 1e-12 and max(e_k0) <= 1e-12
+    assert not np.array_equal(nz, nz0)   # (the class kernel ran)
+    if phys_name == "j2":
+        assert max(rel_err(sn, st_new)[:2]) <= 1e-12 and int((sn[6::7] > 0).sum()) > 0
+    assert fec.load_library().fec_tensor_core_status(1) == 0
+
+
+@pytest.mark.parametrize("case", ["tet10-fp64", "tet10-fp32_element", "hex27-fp32_element"])
+def test_class_separate_calls_equal_fused(fec, case):
+    """Residual-only and stiffness-only calls on class blocks run the class kernel's
+    point phase and arithmetic too: bitwise the fused call's residual and tangent."""
+    torch = _torch()
+    kind, precision = case.split("-")
+    mesh = _mesh(fec, kind)
+    V = fec.FunctionSpace(mesh)
+    asm = fec.SparseMatrixAssembler(fec.VectorFunction(V, "u"), device=0, precision=precision)
+    p = fec.create_parameters(mesh, asm, fec.NeoHookean.from_youngs(1.0, 0.3))
+    U = stretch_field(mesh.nodal_coords, seed=9).ravel()
+    Uu = torch.from_numpy(U[asm.dof.unknown_dofs - 1].copy()).cuda()
+    R, K = fec.assemble_residual_and_stiffness(asm, Uu, p)
+    torch.cuda.synchronize()
+    R_f, nz_f = R.cpu().numpy().copy(), K.nzval.cpu().numpy().copy()
+    fec.assemble_vector(asm, fec.residual, Uu, p)
+    R_s = fec.residual(asm).cpu().numpy().copy()
+    fec.assemble_stiffness(asm, fec.stiffness, Uu, p)
+    nz_s = fec.stiffness(asm).nzval.cpu().numpy().copy()
+    assert np.array_equal(R_s, R_f) and np.array_equal(nz_s, nz_f)
