@@ -44,9 +44,23 @@ cudaError_t go1(const GatherArgs& g, cudaStream_t s, int* launches) {
   return cudaGetLastError();
 }
 
+// Hex27 nodes gather 243 values per element: with the default budget a warp has
+// one element's loads in flight.  For the double-float (FP64) workspace, two CTAs
+// per SM (128 registers) and a budget of two elements' loads instead (batched
+// mixed mesh: the FP64 gathers 10.8 -> 10.2 ms; the same for the FP32 workspace
+// was slower, 9.4 -> 9.7 ms); FEC_GATHER_HEX27=narrow keeps the default (bitwise
+// the same results).
+bool gather_hex27_wide() {
+  const char* e = getenv("FEC_GATHER_HEX27");
+  return !(e && e[0] == 'n');
+}
+
 template <typename Real, int NF, int A>
 cudaError_t go(const GatherArgs& g, cudaStream_t s, int* launches) {
   if ((g.nodes ? g.nnodes : g.nn) <= 0) return cudaSuccess;
+  if constexpr (A == 27 && sizeof(Real) == 8) {
+    if (gather_hex27_wide()) return go1<Real, NF, 27, 2, 16>(g, s, launches);
+  }
   if (gather_variant() == 1) return go1<Real, NF, A, 2, sizeof(Real) == 8 ? 12 : 18>(g, s, launches);
   return go1<Real, NF, A, 3, sizeof(Real) == 8 ? 6 : 12>(g, s, launches);
 }
