@@ -190,14 +190,12 @@ int build_affine(fec_ctx* c, size_t b) {
 // blocks on their own launch (the single launch across blocks keeps the
 // per-element kernels), unless FEC_HEX8_AFFINE=0.
 // Assemblies of tet10/hex27 blocks of translation classes get theirs: FP32-element
-// (tet10 and hex27) and FP64 (tet10).
+// and FP64 (tet10: the tensor-core kernels; hex27 FP64: the class gradients).
 const void* affine_table(const fec_ctx* c, size_t b, int precision, bool mixed) {
   if (mixed || b >= c->d_affine.size()) return nullptr;
   if (c->blocks[b].elem_type == FEC_HEX8)
     return precision == FEC_FP64 && fec::hex8_affine_enabled() ? c->d_affine[b].p : nullptr;
-  if (precision == FEC_FP32_ELEMENT || (precision == FEC_FP64 && c->blocks[b].elem_type == FEC_TET10))
-    return c->d_affine[b].p;
-  return nullptr;
+  return (precision == FEC_FP32_ELEMENT || precision == FEC_FP64) ? c->d_affine[b].p : nullptr;
 }
 
 int ensure(fec_ctx* c, DevBuf& b, size_t bytes) {

@@ -37,6 +37,7 @@
 
 #include "fec_kernels.cuh"
 #include "fec_launch.h"
+#include "fec_mech_hex27.cuh"
 #include "fec_tc.cuh"
 
 namespace fec {
@@ -841,9 +842,11 @@ bool table(int P, const double* xc, const double* ref, std::vector<unsigned char
   const double* dN = ref + NQ * A;
   const double* w = dN + NQ * A * 3;
   (void)N;
-  // header: class count, offset of the FP32-element section, of the FP64 section (tet10; 0: none)
-  const int off32 = HEADER, off64 = ET == 7 ? HEADER + P * G::CLASS_BYTES : 0;
-  out.assign(size_t(HEADER) + size_t(P) * G::CLASS_BYTES + (ET == 7 ? size_t(P) * x64::C_BYTES : 0), 0);
+  // header: class count, offset of the FP32-element section, of the FP64 section (tet10: the
+  // exact-digit operands and gradients; hex27: the gradients the double-float kernel reads)
+  constexpr size_t C64 = ET == 7 ? size_t(x64::C_BYTES) : size_t(HEX27_CLASS_BYTES);
+  const int off32 = HEADER, off64 = HEADER + P * G::CLASS_BYTES;
+  out.assign(size_t(off64) + size_t(P) * C64, 0);
   const int hdr[3] = {P, off32, off64};
   std::memcpy(out.data(), hdr, sizeof hdr);
   std::vector<double> dnx(size_t(NQ) * A * 3), jxw(NQ);
@@ -903,7 +906,12 @@ bool table(int P, const double* xc, const double* ref, std::vector<unsigned char
     float* gb = reinterpret_cast<float*>(cb + size_t(G::KSTEPS) * G::W_STEP);
     for (int i = 0; i < NQ * A * 3; ++i) gb[i] = float(dnx[i]);
     for (int q = 0; q < NQ; ++q) gb[NQ * A * 3 + q] = float(jxw[q]);
-    if (ET == 7 && !x64::section(dnx, jxw, out.data() + off64 + size_t(c) * x64::C_BYTES)) return false;
+    if (ET == 7 && !x64::section(dnx, jxw, out.data() + off64 + size_t(c) * C64)) return false;
+    if (ET == 8) {
+      std::memcpy(out.data() + off64 + size_t(c) * C64, dnx.data(), sizeof(double) * dnx.size());
+      std::memcpy(out.data() + off64 + size_t(c) * C64 + sizeof(double) * dnx.size(), jxw.data(),
+                  sizeof(double) * jxw.size());
+    }
   }
   return true;
 }

@@ -11,6 +11,10 @@
 // as it is formed (the 81 gradients of a point are never live together), as a
 // double-float for the contraction and in FP64 for the residual, which is
 // formed in native FP64.
+//
+// Blocks of translation classes (element e a translate of element e mod P) can
+// skip the isoparametric map (CLASS): the class table's FP64 section holds each
+// class's spatial gradients and JxW, the same for every element of the class.
 #pragma once
 #include "fec_kernels.cuh"
 #include "fec_mech_hex8.cuh"
@@ -31,10 +35,13 @@ struct Hex27Df64Smem {
 };
 
 constexpr int HEX27_THREADS = 192;  // 162 contracting threads, padded to whole warps
+// FP64 section of a hex27 class table (header: int P, FP32 offset, FP64 offset):
+// per class, dNX double [27 points][27 nodes][3], then JxW double [27]
+constexpr int HEX27_CLASS_BYTES = (27 * 27 * 3 + 27) * 8;
 
 // One element by NTHR threads (thread tid), shared by the kernel below and the
 // single-launch kernel of mixed element blocks.
-template <class Model, bool WANT_R, bool WANT_K, int NTHR>
+template <class Model, bool WANT_R, bool WANT_K, int NTHR, bool CLASS = false>
 __device__ __forceinline__ void hex27_df64_tile(const ElemArgs& g, unsigned elem, int tid, unsigned char* smem_raw) {
   constexpr int NQ = 27, A = 27, NDOF = 81, NS = Model::NS, SCR = Model::SCR, SCR2 = Model::SCR2;
   static_assert(NTHR >= 2 * NDOF, "162 contracting threads");
@@ -54,17 +61,53 @@ __device__ __forceinline__ void hex27_df64_tile(const ElemArgs& g, unsigned elem
   int* s_conn = reinterpret_cast<int*>(fb + S::N_F2);
 
   const int64_t e = elem;
-  for (int k = tid; k < NQ * A * 3; k += NTHR) s_dN[k] = g.ref[L::DN_OFF + k];
-  for (int k = tid; k < NQ; k += NTHR) s_w[k] = g.ref[L::W_OFF + k];
+  const double* cg = nullptr;  // CLASS: this element's class gradients [q][a][3], then JxW [q]
+  if constexpr (CLASS) {
+    const unsigned char* tab = static_cast<const unsigned char*>(g.affine);
+    const int P = reinterpret_cast<const int*>(tab)[0], off64 = reinterpret_cast<const int*>(tab)[2];
+    cg = reinterpret_cast<const double*>(tab + off64 + size_t(e % P) * HEX27_CLASS_BYTES);
+  } else {
+    for (int k = tid; k < NQ * A * 3; k += NTHR) s_dN[k] = g.ref[L::DN_OFF + k];
+    for (int k = tid; k < NQ; k += NTHR) s_w[k] = g.ref[L::W_OFF + k];
+  }
   if (tid < A) s_conn[tid] = g.conn[e * A + tid];
   __syncthreads();
   if (tid < A * 3) {
     const int64_t dof = int64_t(s_conn[tid / 3]) * 3 + tid % 3;
-    s_x[tid] = __ldg(&g.coords[dof]);
+    if (!CLASS) s_x[tid] = __ldg(&g.coords[dof]);
     s_u[tid] = __ldg(&g.U[dof]);
   }
   __syncthreads();
-  if (tid < NQ) {  // per-point map and constitutive update, native FP64
+  if (CLASS && tid < NQ) {  // the class's gradients: displacement gradient and constitutive update, FP64
+    const int q = tid;
+    const double* gq = cg + q * A * 3;
+    double gu[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    float2* pdNX = s_dNX + q * A * 3;
+#pragma unroll 3
+    for (int a = 0; a < A; ++a) {
+      double gx[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        gx[d] = __ldg(gq + a * 3 + d);
+        pdNX[a * 3 + d] = df64_split(gx[d]);
+        if (WANT_R) s_dNX64[(q * A + a) * 3 + d] = gx[d];
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) gu[i][j] = fma(s_u[a * 3 + i], gx[j], gu[i][j]);
+    }
+    const double jxw = __ldg(cg + NQ * A * 3 + q);
+    const double* so = NS ? g.state_old + (e * NQ + q) * NS : nullptr;
+    double* sn = (NS && g.state_new) ? g.state_new + (e * NQ + q) * NS : nullptr;
+    double P9[9], scr[SCR];
+    Model::point(g.props, gu, jxw, so, sn, P9, scr);
+    if (WANT_R)
+#pragma unroll
+      for (int m = 0; m < 9; ++m) s_P64[q * 9 + m] = P9[m];
+    Model::split_scratch(scr, s_scr + q * SCR2);
+  }
+  if (!CLASS && tid < NQ) {  // per-point map and constitutive update, native FP64
     const int q = tid;
     const double* dN = s_dN + q * A * 3;
     double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
@@ -179,10 +222,10 @@ __device__ __forceinline__ void hex27_df64_tile(const ElemArgs& g, unsigned elem
   }
 }
 
-template <class Model, bool WANT_R, bool WANT_K>
+template <class Model, bool WANT_R, bool WANT_K, bool CLASS = false>
 __global__ void __launch_bounds__(HEX27_THREADS, 3) mech_hex27_df64_kernel(ElemArgs g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  hex27_df64_tile<Model, WANT_R, WANT_K, HEX27_THREADS>(g, blockIdx.x, threadIdx.x, smem_raw);
+  hex27_df64_tile<Model, WANT_R, WANT_K, HEX27_THREADS, CLASS>(g, blockIdx.x, threadIdx.x, smem_raw);
 }
 
 }  // namespace fec

@@ -132,6 +132,11 @@ template <bool R, bool K>
 cudaError_t hex27_df64_1(const ElemArgs& a, cudaStream_t s) {
   constexpr size_t smem = Hex27Df64Smem<J2>::BYTES;
   cudaError_t err;
+  if (a.affine && class_tc_enabled()) {  // a block of translation classes: the class's gradients
+    if ((err = ensure_smem<mech_hex27_df64_kernel<J2, R, K, true>>(smem)) != cudaSuccess) return err;
+    mech_hex27_df64_kernel<J2, R, K, true><<<unsigned(a.ne), HEX27_THREADS, smem, s>>>(a);
+    return cudaGetLastError();
+  }
   if ((err = ensure_smem<mech_hex27_df64_kernel<J2, R, K>>(smem)) != cudaSuccess) return err;
   mech_hex27_df64_kernel<J2, R, K><<<unsigned(a.ne), HEX27_THREADS, smem, s>>>(a);
   return cudaGetLastError();

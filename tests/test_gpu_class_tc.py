@@ -178,14 +178,16 @@ def test_mixed_mesh_gather_groups(fec, orc, precision, kind):
     assert max(e_r[:2]) <= tol and max(e_k) <= tol   # residual normwise (it cancels), nzval entry by entry
 
 
+@pytest.mark.parametrize("kind", ["tet10", "hex27"])
 @pytest.mark.parametrize("phys_name", ["neohookean", "j2"])
-def test_class_tensor_cores_fp64_tet10(fec, orc, phys_name):
-    """FP64 tet10 blocks of translation classes: the tangent on the tensor cores in
-    exact BF16 digit slices, within the FP64 bar (1e-12) of the oracle entry by entry
-    (nzval) and normwise (the residual, formed in double-float), and of the
-    per-element double-float kernel (FEC_CLASS_TC=0)."""
+def test_class_fp64(fec, orc, phys_name, kind):
+    """FP64 blocks of translation classes: tet10 with the tangent on the tensor cores
+    in exact BF16 digit slices, hex27 with the double-float kernel reading each class's
+    gradients instead of mapping every element. Within the FP64 bar (1e-12) of the
+    oracle entry by entry (nzval) and normwise (the residual), and of the per-element
+    double-float kernel (FEC_CLASS_TC=0)."""
     torch = _torch()
-    mesh = _mesh(fec, "tet10")
+    mesh = _mesh(fec, kind)
     if phys_name == "neohookean":
         phys = fec.NeoHookean.from_youngs(1.0, 0.3)
         U = stretch_field(mesh.nodal_coords, seed=3).ravel()
@@ -198,13 +200,14 @@ def test_class_tensor_cores_fp64_tet10(fec, orc, phys_name):
     R, nz, sn, _ = _run(fec, asm, p, U)
     R0, nz0, sn0, _ = _run(fec, asm, p, U, class_tc=False)
     ne = mesh.num_elements()
-    st = np.zeros(7 * 4 * ne) if phys_name == "j2" else None
+    nq = 4 if kind == "tet10" else 27
+    st = np.zeros(7 * nq * ne) if phys_name == "j2" else None
     st_new = None if st is None else np.zeros_like(st)
     Ro, _, _, nzo = orc.assembled_system(blocks_of(mesh), mesh.nodal_coords, phys_name, phys.create_properties(), U,
                                          asm.dof.dof_to_unknown, asm.dof.unknown_dofs, st, st_new)
     e_r, e_k = rel_err(R, Ro), rel_err(nz, nzo)
     e_r0, e_k0 = rel_err(R, R0), rel_err(nz, nz0)
-    print("fp64 tet10", phys_name, "class vs oracle: residual", e_r, "nzval", e_k, "| vs per-element: residual", e_r0,
+    print("fp64", kind, phys_name, "class vs oracle: residual", e_r, "nzval", e_k, "| vs per-element: residual", e_r0,
           "nzval", e_k0)
     assert max(e_r[:2]) <= 1e-12 and max(e_k) <= 1e-12
     assert max(e_r0[:2]) <= 1e-12 and max(e_k0) <= 1e-12
