@@ -209,12 +209,23 @@ int ensure(fec_ctx* c, DevBuf& b, size_t bytes) {
 // element-matrix blocks start on 16-byte boundaries (vectorised copy-out)
 inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3); }
 
-// Workspace entries of block b's element matrices: the class tensor-core kernel
-// writes the symmetric half (KE_PAIRS), every other kernel the whole K_e.
+// Whether an assembly of block b with the stiffness runs the FP64 hex8 tensor-core
+// kernel writing the symmetric half of K_e (KE_PAIRS) rather than node rows.
+bool hex8_pairs(const fec_ctx* c, size_t b, int precision, bool want_k, bool mixed) {
+  const Block& B = c->blocks[b];
+  return want_k && B.elem_type == FEC_HEX8 && (B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2) &&
+         precision == FEC_FP64 && !fp64_native_env() && fec::hex8_pairs_enabled() &&
+         affine_table(c, b, precision, mixed) != nullptr;
+}
+
+// Workspace entries of block b's element matrices: the class tensor-core kernels
+// and the FP64 hex8 tensor-core kernel write the symmetric half (KE_PAIRS), every
+// other kernel the whole K_e.  `mixed`: the single launch across blocks.
 int64_t ke_entries(const fec_ctx* c, size_t b, int precision, bool want_k, bool mixed) {
   const Block& B = c->blocks[b];
-  if (want_k && fec::class_tc_runs(B.physics, B.elem_type, precision, true, want_k,
-                                   affine_table(c, b, precision, mixed) != nullptr))
+  if (hex8_pairs(c, b, precision, want_k, mixed) ||
+      (want_k && fec::class_tc_runs(B.physics, B.elem_type, precision, true, want_k,
+                                    affine_table(c, b, precision, mixed) != nullptr)))
     return pad4(B.ne * (int64_t(B.nnpe) * (B.nnpe + 1) / 2 * 9));
   const int ndof = c->nf * B.nnpe;
   return pad4(B.ne * ndof * ndof);
@@ -1040,18 +1051,7 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
   FEC_CUDA(c, fec::wait_error_flag(&wait_err));
   if (c->n_timed > 1) c->n_timed = 0;  // keep a preceding fec_update_field timing
   const size_t rsz = precision == FEC_FP64 ? sizeof(double) : sizeof(float);
-  int64_t ke_total = 0, re_total = 0;
-  for (size_t b = 0; b < c->blocks.size(); ++b) {
-    ke_total += ke_entries(c, b, precision, want_k, false);
-    re_total += c->blocks[b].ne * c->nf * c->blocks[b].nnpe;
-  }
-  int rc;
-  if (want_k && (rc = ensure(c, c->d_Ke, rsz * size_t(ke_total)))) return rc;
-  if (want_r && (rc = ensure(c, c->d_Re, rsz * size_t(re_total)))) return rc;
   // element kernels: one launch per block, or one for all blocks (fec_set_single_launch)
-  GatherArgs ga;
-  memset(&ga, 0, sizeof ga);
-  int64_t ke_off = 0, re_off = 0, st_off = 0;
   // (a single-block system is one launch already, on its own kernel)
   bool mixed = c->single_launch && precision == FEC_FP64 && c->blocks.size() >= 2 &&
                c->blocks.size() <= size_t(fec::MIXED_MAX_BLOCKS) && !fp64_native_env();
@@ -1062,6 +1062,18 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     mixed_types.push_back(B.elem_type);
   }
   mixed = mixed && fec::mixed_launch_supported(c->blocks[0].physics, int(c->blocks.size()), mixed_types.data());
+  // the workspace as the kernels that run write it (the single launch writes every K_e whole)
+  int64_t ke_total = 0, re_total = 0;
+  for (size_t b = 0; b < c->blocks.size(); ++b) {
+    ke_total += ke_entries(c, b, precision, want_k, mixed);
+    re_total += c->blocks[b].ne * c->nf * c->blocks[b].nnpe;
+  }
+  int rc;
+  if (want_k && (rc = ensure(c, c->d_Ke, rsz * size_t(ke_total)))) return rc;
+  if (want_r && (rc = ensure(c, c->d_Re, rsz * size_t(re_total)))) return rc;
+  GatherArgs ga;
+  memset(&ga, 0, sizeof ga);
+  int64_t ke_off = 0, re_off = 0, st_off = 0;
   for (size_t b = 0; b < c->blocks.size(); ++b) {
     const Block& B = c->blocks[b];
     const int ndof = c->nf * B.nnpe;
@@ -1082,6 +1094,7 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     ea.Re = want_r ? static_cast<char*>(c->d_Re.p) + rsz * size_t(re_off) : nullptr;
     ea.closure = c->d_cl_args.p;
     ea.affine = affine_table(c, b, precision, mixed);
+    ea.ke_pairs = hex8_pairs(c, b, precision, want_k, mixed) ? 1 : 0;
     if (B.physics == FEC_PHYS_J2_MLP && !ea.closure)
       return fail(c, FEC_ERR_STATE, "block %d uses the learned closure but fec_closure_set was not called", int(b) + 1);
     cudaError_t e = cudaSuccess;
@@ -1133,14 +1146,16 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     bi.epos_off = B.epos_off;
     bi.nnpe = B.nnpe;
     bi.ndof = ndof;
-    // the hex8 mechanics kernels write the node-rows layout, the class tensor-core
-    // kernel the symmetric half
-    const bool pairs = want_k && fec::class_tc_runs(B.physics, B.elem_type, precision, want_r, want_k, ea.affine != nullptr);
-    bi.layout = (B.elem_type == FEC_HEX8 && (B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2 ||
-                                             tc_closure(B, precision)))
-                    ? fec::KE_NODE_ROWS
-                    : (pairs ? fec::KE_PAIRS : fec::KE_ROW_MAJOR);
-    ke_off += ke_entries(c, b, precision, want_k, false);
+    // the hex8 mechanics kernels write the node-rows layout (the FP64 tensor-core
+    // kernel the symmetric half), the class tensor-core kernels the symmetric half
+    const bool pairs = ea.ke_pairs ||
+                       (want_k && fec::class_tc_runs(B.physics, B.elem_type, precision, want_r, want_k, ea.affine != nullptr));
+    bi.layout = pairs ? fec::KE_PAIRS
+                      : (B.elem_type == FEC_HEX8 && (B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2 ||
+                                                     tc_closure(B, precision)))
+                            ? fec::KE_NODE_ROWS
+                            : fec::KE_ROW_MAJOR;
+    ke_off += ke_entries(c, b, precision, want_k, mixed);
     re_off += B.ne * ndof;
     st_off += int64_t(ns) * B.nq * B.ne;
   }
@@ -1650,6 +1665,7 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
     ea.Re = want_r ? static_cast<char*>(Re) + rsz * size_t(re_off) : nullptr;
     ea.closure = c->d_cl_args.p;
     ea.affine = affine_table(c, b, precision, false);
+    ea.ke_pairs = hex8_pairs(c, b, precision, want_k, false) ? 1 : 0;
     if (B.physics == FEC_PHYS_J2_MLP && !ea.closure)
       return fail(c, FEC_ERR_STATE, "block %d uses the learned closure but fec_closure_set was not called", int(b) + 1);
     cudaError_t e;
@@ -1669,12 +1685,14 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
     bi.epos_off = B.epos_off;
     bi.nnpe = B.nnpe;
     bi.ndof = ndof;
-    // the hex8 mechanics kernels write the node-rows layout, the class tensor-core
-    // kernel the symmetric half
-    const bool pairs = want_k && fec::class_tc_runs(B.physics, B.elem_type, precision, want_r, want_k, ea.affine != nullptr);
-    bi.layout = (B.elem_type == FEC_HEX8 && (B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2))
-                    ? fec::KE_NODE_ROWS
-                    : (pairs ? fec::KE_PAIRS : fec::KE_ROW_MAJOR);
+    // the hex8 mechanics kernels write the node-rows layout (the FP64 tensor-core
+    // kernel the symmetric half), the class tensor-core kernels the symmetric half
+    const bool pairs = ea.ke_pairs ||
+                       (want_k && fec::class_tc_runs(B.physics, B.elem_type, precision, want_r, want_k, ea.affine != nullptr));
+    bi.layout = pairs ? fec::KE_PAIRS
+                      : (B.elem_type == FEC_HEX8 && (B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2))
+                            ? fec::KE_NODE_ROWS
+                            : fec::KE_ROW_MAJOR;
     ke_off += ke_entries(c, b, precision, want_k, false);
     re_off += B.ne * ndof;
     st_off += int64_t(ns) * B.nq * B.ne;

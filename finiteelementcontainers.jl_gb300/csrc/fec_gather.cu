@@ -66,33 +66,35 @@ cudaError_t go(const GatherArgs& g, cudaStream_t s, int* launches) {
 }
 
 // The software-pipelined hex8 gather: one block of hex8 mechanics elements in
-// the node-rows layout, stiffness wanted.  FEC_GATHER_PIPE=0 keeps the
+// the node-rows layout (or the FP64 pair layout), stiffness wanted.  FEC_GATHER_PIPE=0 keeps the
 // one-warp-per-node kernel (bitwise the same results).
 bool gather_pipe_enabled() {
   const char* e = getenv("FEC_GATHER_PIPE");
   return !(e && e[0] == '0');
 }
 
-template <typename Real>
+template <typename Real, bool PAIRS = false>
 cudaError_t go_pipe(const GatherArgs& g, cudaStream_t s, int* launches) {
   constexpr int MINB = sizeof(Real) == 8 ? 2 : 3;
   const size_t acc_bytes = (size_t(g.acc_stride) * GatherAcc::WORDS * sizeof(float) + 15) / 16 * 16;
-  const size_t smem = size_t(gp::WPB) * (acc_bytes + 2 * gp::Stage<Real>::BYTES);
-  cudaError_t err = ensure_smem<node_gather_hex8_pipe_kernel<Real, MINB>>(smem);
+  const size_t smem = size_t(gp::WPB) * (acc_bytes + 2 * gp::Stage<Real, PAIRS>::BYTES);
+  cudaError_t err = ensure_smem<node_gather_hex8_pipe_kernel<Real, MINB, PAIRS>>(smem);
   if (err != cudaSuccess) return err;
   const int64_t need = (g.nn + gp::WPB - 1) / gp::WPB;
   const int64_t cap = int64_t(num_sms()) * MINB;
   const unsigned grid = unsigned(need < cap ? need : cap);
-  node_gather_hex8_pipe_kernel<Real, MINB><<<grid, gp::WPB * 32, smem, s>>>(g);
+  node_gather_hex8_pipe_kernel<Real, MINB, PAIRS><<<grid, gp::WPB * 32, smem, s>>>(g);
   ++*launches;
   return cudaGetLastError();
 }
 
 template <typename Real, int NF>
 cudaError_t by_size(const GatherArgs& g, cudaStream_t s, int* launches) {
-  if (NF == 3 && g.nn > 0 && g.nblocks == 1 && g.blk[0].nnpe == 8 && g.blk[0].layout == KE_NODE_ROWS &&
-      g.nzval != nullptr && gather_pipe_enabled())
-    return go_pipe<Real>(g, s, launches);
+  if (NF == 3 && g.nn > 0 && g.nblocks == 1 && g.blk[0].nnpe == 8 && g.nzval != nullptr && gather_pipe_enabled()) {
+    if (g.blk[0].layout == KE_NODE_ROWS) return go_pipe<Real>(g, s, launches);
+    if constexpr (sizeof(Real) == 8)
+      if (g.blk[0].layout == KE_PAIRS) return go_pipe<Real, true>(g, s, launches);
+  }
   int A = g.blk[0].nnpe;
   for (int b = 1; b < g.nblocks; ++b)
     if (g.blk[b].nnpe != A) A = 0;

@@ -238,6 +238,22 @@ __device__ __forceinline__ void point_phase(const ElemArgs& g, const double* s_g
   }
 }
 
+// sum_L v_L[j] 2^(-8L) of the seven level accumulators of one pair: levels 6..4
+// in FP32 (their rounding is below 2^-55 of level 0), then 3..0 in double-float
+__device__ __forceinline__ float2 combine_levels(const float (&v)[NLEV][4], int j) {
+  float hi = fmaf(fmaf(v[6][j], 0.00390625f, v[5][j]), 0.00390625f, v[4][j]), lo = 0.f;
+#pragma unroll
+  for (int L = 3; L >= 0; --L) {
+    const float a = v[L][j], b = hi * 0.00390625f;
+    lo *= 0.00390625f;
+    const float s = a + b, bb = s - a;
+    lo += (a - (s - bb)) + (b - bb);
+    hi = s + lo;
+    lo = lo - (hi - s);
+  }
+  return make_float2(hi, lo);
+}
+
 // R_(a,i) of one element from its points' split JxW P [8][9] (double-float, q in order)
 __device__ __forceinline__ double residual_entry(const float2* s_g2, const float2* P8, int a, int i) {
   float2 R = make_float2(0.f, 0.f);
@@ -446,6 +462,25 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
       const bool live = lane < 27 && e0 + el < g.ne;
       const int tau = s_tau[(k & 1) * 16 + el];
       const float f1 = pow2f(tau - 7);
+      if (g.ke_pairs) {
+        // the symmetric half straight from the levels: pair n = (a, b) of row
+        // (el, i, k) is K_(a,i),(b,k), entry 9n + 3i + k of the element's KE_PAIRS block
+        float2* dst = static_cast<float2*>(g.Ke) + (e0 + el) * (NPAIR * 9) + ik;
+#pragma unroll 1
+        for (int c = 0; c < NPAIR / 4; ++c) {
+          float v[NLEV][4];
+          tmem_ld4x7(lane_addr + uint32_t(c * 4), v);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const float2 hl = combine_levels(v, j);
+            const float f = f1 * pow2f(s_sig[c * 4 + j] - 7);
+            if (live) dst[(c * 4 + j) * 9] = make_float2(hl.x * f, hl.y * f);
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(bar_tfree);  // the accumulators may be overwritten
+        continue;
+      }
       // levels -> double-float values of the 36 pairs, staged in this lane's TMEM
       // columns TM_OWN + 2n (hi), + 2n + 1 (lo)
 #pragma unroll 1
@@ -455,21 +490,10 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
         float out[8];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          // sum_L v_L 2^(-8L): levels 6..4 in FP32 (their rounding is below 2^-55
-          // of level 0), then 3..0 in double-float
-          float hi = fmaf(fmaf(v[6][j], 0.00390625f, v[5][j]), 0.00390625f, v[4][j]), lo = 0.f;
-#pragma unroll
-          for (int L = 3; L >= 0; --L) {
-            const float a = v[L][j], b = hi * 0.00390625f;
-            lo *= 0.00390625f;
-            const float s = a + b, bb = s - a;
-            lo += (a - (s - bb)) + (b - bb);
-            hi = s + lo;
-            lo = lo - (hi - s);
-          }
+          const float2 hl = combine_levels(v, j);
           const float f = f1 * pow2f(s_sig[c * 4 + j] - 7);
-          out[2 * j] = hi * f;
-          out[2 * j + 1] = lo * f;
+          out[2 * j] = hl.x * f;
+          out[2 * j + 1] = hl.y * f;
         }
         tmem_st8(lane_addr + uint32_t(TM_OWN + c * 8), out);
       }
@@ -592,6 +616,11 @@ cudaError_t launch_r(const ElemArgs& a, cudaStream_t s, int* launches) {
 
 bool hex8_affine_enabled() {
   const char* v = std::getenv("FEC_HEX8_AFFINE");
+  return !(v && v[0] == '0');
+}
+
+bool hex8_pairs_enabled() {
+  const char* v = std::getenv("FEC_HEX8_PAIRS");
   return !(v && v[0] == '0');
 }
 

@@ -68,6 +68,7 @@ struct ElemArgs {
   const void* affine;       // hex8 blocks of translated elements: the constant operand table (or null)
   int* wait_err;            // set to 1 by a bounded wait that gave up (device flag; may be null)
   long long wait_budget;    // SM clocks a bounded wait allows before giving up (0: the default, ~1 s)
+  int ke_pairs;             // the FP64 hex8 tensor-core kernel writes KE_PAIRS (else KE_NODE_ROWS)
 };
 
 // ---------------------------------------------------------------------------
@@ -1212,7 +1213,7 @@ __global__ void __launch_bounds__(WPB * 32, MINB) node_gather_kernel(GatherArgs 
 
 // ---------------------------------------------------------------------------
 // Software-pipelined node gather for meshes of one hex8 mechanics block (the
-// KE_NODE_ROWS layout).  Each warp walks the nodes gw, gw + GW, ... (GW =
+// KE_NODE_ROWS layout, or KE_PAIRS: the FP64 tensor-core kernel's symmetric half).  Each warp walks the nodes gw, gw + GW, ... (GW =
 // warps in the grid).  While it accumulates node i from shared memory, the
 // rows its elements hold for node i+1 (8 x 72 entries), their element-map
 // entries and residual values are already on their way into the warp's other
@@ -1227,13 +1228,17 @@ __global__ void __launch_bounds__(WPB * 32, MINB) node_gather_kernel(GatherArgs 
 namespace gp {
 constexpr int WPB = 8;
 constexpr int MAXE = 8;  // elements staged per node
-template <typename Real>
+// PAIRS (the KE_PAIRS layout, 8-byte entries): node a's eight 9-entry pair blocks of
+// an element, each copied as the 80 bytes from the 16-byte boundary at or below its
+// start (a block of pair p starts 8 bytes past that boundary when p is odd)
+template <typename Real, bool PAIRS = false>
 struct Stage {
-  static constexpr int K_BYTES = MAXE * 72 * int(sizeof(Real));  // node a's 72 entries of each element
+  static constexpr int BLK = 80;                                 // staged bytes per pair block
+  static constexpr int K_BYTES = PAIRS ? MAXE * 8 * BLK : MAXE * 72 * int(sizeof(Real));  // node a's 72 entries
   static constexpr int EP_OFF = K_BYTES;                         // uint16 [MAXE][8] element-map entries
   static constexpr int R_OFF = EP_OFF + MAXE * 16;               // RE<Real> [MAXE][3] residual values
   static constexpr int BYTES = (R_OFF + MAXE * 3 * int(sizeof(typename RE<Real>::T)) + 15) / 16 * 16;
-  static constexpr int CHUNKS = 72 * int(sizeof(Real)) / 16;     // 16-byte copies per element row block
+  static constexpr int CHUNKS = PAIRS ? 8 * BLK / 16 : 72 * int(sizeof(Real)) / 16;  // 16-byte copies per element
 };
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
 __device__ __forceinline__ void cp16(void* dst, const void* src) {
@@ -1275,10 +1280,13 @@ __device__ __forceinline__ NodeMeta load_meta(const GatherArgs& g, int64_t n, in
   return m;
 }
 
+// pair index of the node pair (x, y), x <= y, of a hex8 element
+__device__ __forceinline__ int hex8_pair(int x, int y) { return (x * (15 - x)) / 2 + y; }
+
 // cp.async of node m's staged data into `st` (all 32 lanes; a commit group always follows)
-template <typename Real>
+template <typename Real, bool PAIRS>
 __device__ __forceinline__ void issue(const GatherArgs& g, const NodeMeta& m, unsigned char* st, int lane) {
-  using S = Stage<Real>;
+  using S = Stage<Real, PAIRS>;
   using RT = typename RE<Real>::T;
   if (!m.pipe) return;
   const BlockInfo& B = g.blk[0];
@@ -1295,7 +1303,17 @@ __device__ __forceinline__ void issue(const GatherArgs& g, const NodeMeta& m, un
     const int c = t / S::CHUNKS < MAXE ? t / S::CHUNKS : MAXE - 1, w = t - c * S::CHUNKS;
     const uint32_t packed = __shfl_sync(0xffffffffu, m.adj, c);
     const uint64_t le = (packed >> 5) - uint32_t(B.elem_start), a = packed & 31u;
-    if (t < total) cp16(st + (c * 72) * sizeof(Real) + w * 16, Ke + ((le * 576u + a * 72u) * sizeof(Real)) + w * 16);
+    if constexpr (PAIRS) {
+      // chunk w: part w % 5 of the block of column node w / 5; the element's 36 x 9
+      // entries are 2,592 bytes, so the 80-byte window stays inside them
+      const int bb = w / 5, part = w - bb * 5;
+      const int p = hex8_pair(int(a) < bb ? int(a) : bb, int(a) < bb ? bb : int(a));
+      if (t < total)
+        cp16(st + c * (8 * S::BLK) + bb * S::BLK + part * 16,
+             Ke + (le * 324u) * sizeof(Real) + ((p * 72) & ~15) + part * 16);
+    } else {
+      if (t < total) cp16(st + (c * 72) * sizeof(Real) + w * 16, Ke + ((le * 576u + a * 72u) * sizeof(Real)) + w * 16);
+    }
   }
   if (lane < m.cnt) {  // element-map row of node a: 8 uint16, 16-byte aligned
     const uint64_t le = (m.adj >> 5) - uint32_t(B.elem_start), a = m.adj & 31u;
@@ -1311,10 +1329,10 @@ __device__ __forceinline__ void issue(const GatherArgs& g, const NodeMeta& m, un
 }
 }  // namespace gp
 
-template <typename Real, int MINB>
+template <typename Real, int MINB, bool PAIRS = false>
 __global__ void __launch_bounds__(gp::WPB * 32, MINB) node_gather_hex8_pipe_kernel(GatherArgs g) {
   using namespace gp;
-  using S = Stage<Real>;
+  using S = Stage<Real, PAIRS>;
   using RT = typename RE<Real>::T;
   extern __shared__ __align__(16) unsigned char smem_g[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1330,12 +1348,12 @@ __global__ void __launch_bounds__(gp::WPB * 32, MINB) node_gather_hex8_pipe_kern
   const int lk = lane >> 3, lb = lane & 7;
 
   NodeMeta cur = load_meta(g, int64_t(blockIdx.x) * WPB + warp, lane);
-  issue<Real>(g, cur, stage[0], lane);
+  issue<Real, PAIRS>(g, cur, stage[0], lane);
   commit();
   NodeMeta nxt = load_meta(g, cur.n < 0 ? g.nn : cur.n + GW, lane);
   for (int it = 0; cur.n >= 0; ++it) {
     const int s = it & 1;
-    issue<Real>(g, nxt, stage[s ^ 1], lane);  // node i+1 into the other stage
+    issue<Real, PAIRS>(g, nxt, stage[s ^ 1], lane);  // node i+1 into the other stage
     commit();
     const NodeMeta nn2 = load_meta(g, nxt.n < 0 ? g.nn : nxt.n + GW, lane);  // node i+2's adjacency
     wait_prev();                              // node i's copies (this lane's) have landed
@@ -1355,11 +1373,25 @@ __global__ void __launch_bounds__(gp::WPB * 32, MINB) node_gather_hex8_pipe_kern
         for (int c = 0; c < cur.cnt; ++c) {
           if (wantR) racc += to_double(reinterpret_cast<const RT*>(st + S::R_OFF)[c * 3 + lane]);
           if (wantK) {
+            int a = 0;
+            if constexpr (PAIRS) a = int(__shfl_sync(0xffffffffu, cur.adj, c) & 31u);
             if (kl) {
               // entries ((k*3 + i)*8 + b) of the element's rows for this node, i = 0..2, go to
               // the three adjacent positions k*Ln + epos[b] + i
-              const Real* row = reinterpret_cast<const Real*>(st) + c * 72 + lk * 24 + lb;
-              const Real v0 = row[0], v1 = row[8], v2 = row[16];
+              Real v0, v1, v2;
+              if constexpr (PAIRS) {  // K_(a,k),(b,i): pair (a, b) entry 3k + i, or pair (b, a) entry 3i + k
+                const int p = hex8_pair(a < lb ? a : lb, a < lb ? lb : a);
+                const Real* blk = reinterpret_cast<const Real*>(st + c * (8 * S::BLK) + lb * S::BLK + (p & 1) * 8);
+                const int o = a <= lb ? lk * 3 : lk, d = a <= lb ? 1 : 3;
+                v0 = blk[o];
+                v1 = blk[o + d];
+                v2 = blk[o + 2 * d];
+              } else {
+                const Real* row = reinterpret_cast<const Real*>(st) + c * 72 + lk * 24 + lb;
+                v0 = row[0];
+                v1 = row[8];
+                v2 = row[16];
+              }
               const int p = base + int(reinterpret_cast<const uint16_t*>(st + S::EP_OFF + c * 16)[lb]);
               float2* A2 = reinterpret_cast<float2*>(acc) + p;
               float2 s0 = A2[0], s1 = A2[1], s2 = A2[2];
@@ -1376,7 +1408,7 @@ __global__ void __launch_bounds__(gp::WPB * 32, MINB) node_gather_hex8_pipe_kern
       } else {
         const bool fast = (cur.um & UMASK_FULL_NBR) != 0;
         const int64_t p1 = cur.p0 + cur.cnt;
-        if (fast)
+        if (fast && !PAIRS)
           gather_run_hex8v<Real>(g, B, cur.p0, p1, Ln, acc, racc, lane, wantK, wantR);
         else
           gather_run_generic<Real, 3>(g, B, cur.p0, p1, um, fast, Ln, acc, racc, lane, wantK, wantR);

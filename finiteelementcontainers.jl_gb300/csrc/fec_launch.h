@@ -78,6 +78,10 @@ cudaError_t launch_hex8_affine_tc(int physics, bool want_r, bool want_k, const E
 bool hex8_affine_table(const double* x0, const double* ref, std::vector<unsigned char>& out);
 // FEC_HEX8_AFFINE=0 keeps such blocks on the per-element kernels.
 bool hex8_affine_enabled();
+// With the stiffness that kernel writes the symmetric half of K_e (args.ke_pairs:
+// the KE_PAIRS layout, 36 * 9 entries per element) unless FEC_HEX8_PAIRS=0
+// (the node rows of the whole K_e, KE_NODE_ROWS).
+bool hex8_pairs_enabled();
 // Tet10 (7) / hex27 (8) Neo-Hookean (2) or J2 (3) for a block whose element e is
 // a translate of element e mod P (args.affine: the table class_tc_table built):
 // the stiffness contraction on the tensor cores against each class's constant

@@ -134,3 +134,61 @@ def test_noncongruent_block_keeps_per_element_kernels(fec, orc):
     with per_element_kernels():
         _, _, _, R_pe, nz_pe, _ = _assemble(fec, mesh, phys, U)
     assert np.array_equal(R, R_pe) and np.array_equal(nz, nz_pe)
+
+
+class node_row_workspace:
+    """with node_row_workspace(): FEC_HEX8_PAIRS=0, the tensor-core kernel writes
+    node rows of the whole K_e instead of the symmetric half."""
+
+    def __enter__(self):
+        os.environ["FEC_HEX8_PAIRS"] = "0"
+
+    def __exit__(self, *exc):
+        os.environ.pop("FEC_HEX8_PAIRS", None)
+
+
+@pytest.mark.parametrize("phys_name", ["neohookean", "j2"])
+def test_pair_workspace_matches_node_rows_bitwise(fec, orc, phys_name):
+    """The symmetric-half workspace (36 node pairs x 9 entries per element) and
+    the node rows of the whole K_e hold the same values, so the pipelined gather
+    over either gives bitwise the same R, nzval and state -- with Dirichlet dofs,
+    whose neighbourhoods the gather assembles in place -- and the pair path is
+    held to the oracle at the FP64 bar."""
+    torch = _torch()
+    n = 9
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (n + 1,) * 3)
+    if phys_name == "neohookean":
+        phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+        U = stretch_field(mesh.nodal_coords, seed=5).ravel()
+    else:
+        phys = fec.J2Plasticity(200.0, 0.3, 0.25, 2.0)
+        U = 3.0 * stretch_field(mesh.nodal_coords, seed=2, noise=1e-4, diag=(1.004, 0.999, 0.999)).ravel()
+    bcs = [fec.DirichletBC("u_x", lambda X, t: 0.0, nodeset_name="left"),
+           fec.DirichletBC("u_y", lambda X, t: 0.0, nodeset_name="bottom")]
+
+    def run():
+        asm = fec.SparseMatrixAssembler(fec.VectorFunction(fec.FunctionSpace(mesh), "u"), device=0)
+        p = fec.create_parameters(mesh, asm, phys, dirichlet_bcs=bcs)
+        Uu = torch.from_numpy(U[asm.dof.unknown_dofs - 1].copy()).cuda()
+        R, K = fec.assemble_residual_and_stiffness(asm, Uu, p)
+        torch.cuda.synchronize()
+        st = p.state_new.cpu().numpy().copy() if phys_name == "j2" else None
+        return asm, R.cpu().numpy().copy(), K.nzval.cpu().numpy().copy(), st
+
+    asm, R, nz, st = run()
+    with node_row_workspace():
+        _, R_nr, nz_nr, st_nr = run()
+    assert np.array_equal(R, R_nr) and np.array_equal(nz, nz_nr)
+    if st is not None:
+        assert np.array_equal(st, st_nr)
+    ne = mesh.num_elements()
+    st_old = np.zeros(7 * 8 * ne) if phys_name == "j2" else None
+    st_new = None if st_old is None else np.zeros_like(st_old)
+    Uo = np.zeros_like(U)   # the field the assembly saw: the Dirichlet dofs at their value 0
+    Uo[asm.dof.unknown_dofs - 1] = U[asm.dof.unknown_dofs - 1]
+    Ro, nzo, ab = _oracle(orc, mesh, asm, phys_name, phys.create_properties(), Uo, st_old, st_new)
+    er = residual_err(R, Ro, ab) if st_old is None else rel_err(R, Ro)[:2]
+    print("pair workspace", phys_name, "residual", er, "nzval", rel_err(nz, nzo))
+    assert max(rel_err(nz, nzo)) <= TOL64 and max(er) <= TOL64
+    if st is not None:
+        assert max(rel_err(st, st_new)) <= TOL64
