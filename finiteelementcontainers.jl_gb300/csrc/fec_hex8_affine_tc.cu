@@ -32,10 +32,9 @@
 //               digits into the seven A slices;
 //   warp 9      the residual R = sum_q dNX P in double-float;
 //   warps 10-13 the epilogue: TMEM -> double-float values (row (e, i, k) holds
-//               K_(a,i),(b,k) for a <= b); each row thread takes the other
-//               half of its node rows from the transposed row (e, k, i) of the
-//               same warp by shuffles and stores whole 64-byte node rows of
-//               K_e to global memory in the layout the node gather reads;
+//               K_(a,i),(b,k) for a <= b), stored as they leave tensor memory:
+//               the symmetric half (KE_PAIRS, entry 9n + 3i + k of pair n), or
+//               each value at its two places in the node rows of the whole K_e;
 //   warp 14     issues the tile's 50 MMAs (10 groups of digit pairs x 5 K steps).
 // The A slices are rewritten as soon as the MMAs that read them completed; the
 // next MMAs wait only for the epilogue's reads of the accumulators.
@@ -71,8 +70,7 @@ constexpr int T_JXW = T_G + NQ * 24 * 8;
 constexpr int T_BYTES = T_JXW + NQ * 8;
 static_assert(T_BYTES % 16 == 0 && T_G % 8 == 0, "table layout");
 constexpr int TMEM_COLS = 512;
-constexpr int TM_OWN = NLEV * NPAD;  // 72 columns after the accumulators: the epilogue's (hi, lo) per pair
-constexpr int TM_ENT = TM_OWN + 2 * NPAIR;  // 2 x 48 columns: the slicers' scaled tangent entries (hi, lo)
+constexpr int TM_ENT = NLEV * NPAD;  // 2 x 48 columns after the accumulators: the slicers' scaled tangent entries (hi, lo)
 static_assert(TM_ENT + 2 * 48 <= TMEM_COLS, "tensor memory columns");
 constexpr long long WAIT_BUDGET = 2000000000LL;
 
@@ -155,14 +153,6 @@ __device__ __forceinline__ void tmem_ld4x7(uint32_t taddr, float (*v)[4]) {
     for (int j = 0; j < 4; ++j) v[L][j] = __uint_as_float(r[L * 4 + j]);
 }
 
-// 8 consecutive 32-bit columns of this thread's lane from registers.
-__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float* v) {
-  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
-               "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
-               "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
-               "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
-               : "memory");
-}
 __device__ __forceinline__ void tmem_st2(uint32_t taddr, float a, float b) {
   asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1, %2};" ::"r"(taddr), "r"(__float_as_uint(a)),
                "r"(__float_as_uint(b))
@@ -180,26 +170,6 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
   for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
 }
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
-// Eight 2-column loads (addresses a[0..7]) under one wait.
-__device__ __forceinline__ void tmem_ld2x8(const uint32_t* a, float2* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%16];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%2, %3}, [%17];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%4, %5}, [%18];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%6, %7}, [%19];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%8, %9}, [%20];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%10, %11}, [%21];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%12, %13}, [%22];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%14, %15}, [%23];\n\t"
-      "tcgen05.wait::ld.sync.aligned;"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7])
-      : "memory");
-#pragma unroll
-  for (int j = 0; j < 8; ++j) v[j] = make_float2(__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1]));
-}
 
 
 // Point phase of quadrature point q of element e (FP64): the eight lanes of an
@@ -237,6 +207,9 @@ __device__ __forceinline__ void point_phase(const ElemArgs& g, const double* s_g
     Model::point(g.props, gu, s_jxw[q], so, sn, P9, scr);
   }
 }
+
+// node pair n = (a, b), a <= b, as a << 4 | b
+__constant__ unsigned char kPairNodes[NPAIR] = {0x00, 0x01, 0x02, 0x03, 0x04, 0x05, 0x06, 0x07, 0x11, 0x12, 0x13, 0x14, 0x15, 0x16, 0x17, 0x22, 0x23, 0x24, 0x25, 0x26, 0x27, 0x33, 0x34, 0x35, 0x36, 0x37, 0x44, 0x45, 0x46, 0x47, 0x55, 0x56, 0x57, 0x66, 0x67, 0x77};
 
 // sum_L v_L[j] 2^(-8L) of the seven level accumulators of one pair: levels 6..4
 // in FP32 (their rounding is below 2^-55 of level 0), then 3..0 in double-float
@@ -449,7 +422,6 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
     // ---------------- epilogue: thread = TMEM lane = row (el, i, k) ----------------
     const int qw = warp & 3;
     const int el = qw * 3 + (lane < 27 ? lane / 9 : 0), ik = lane % 9, i = ik / 3, kc = ik % 3;
-    const int partner = (lane < 27 ? lane - ik : lane) + (lane < 27 ? kc * 3 + i : 0);  // row (el, k, i)
     const uint32_t lane_addr = tmem + (uint32_t(qw * 32) << 16);
     for (int k = 0;; ++k) {
       const int64_t tile = blockIdx.x + int64_t(k) * gridDim.x;
@@ -481,49 +453,27 @@ __global__ void __launch_bounds__(NTHR, 1) hex8_affine_tc_kernel(ElemArgs g, con
         mbar_arrive(bar_tfree);  // the accumulators may be overwritten
         continue;
       }
-      // levels -> double-float values of the 36 pairs, staged in this lane's TMEM
-      // columns TM_OWN + 2n (hi), + 2n + 1 (lo)
+      // node rows of the whole K_e: pair n = (a, b) of row (el, i, k), K_(a,i),(b,k), is
+      // entry b of node row (a, i, k) and, by symmetry, entry a of node row (b, k, i)
+      float2* dst = static_cast<float2*>(g.Ke) + (e0 + el) * 576;
 #pragma unroll 1
       for (int c = 0; c < NPAIR / 4; ++c) {
         float v[NLEV][4];
         tmem_ld4x7(lane_addr + uint32_t(c * 4), v);
-        float out[8];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const float2 hl = combine_levels(v, j);
           const float f = f1 * pow2f(s_sig[c * 4 + j] - 7);
-          out[2 * j] = hl.x * f;
-          out[2 * j + 1] = hl.y * f;
+          const int ab = kPairNodes[c * 4 + j], a = ab >> 4, b = ab & 15;
+          const float2 val = make_float2(hl.x * f, hl.y * f);
+          if (live) {
+            dst[((a * 3 + i) * 3 + kc) * 8 + b] = val;
+            if (a != b) dst[((b * 3 + kc) * 3 + i) * 8 + a] = val;
+          }
         }
-        tmem_st8(lane_addr + uint32_t(TM_OWN + c * 8), out);
       }
-      tmem_wait_st();
       tc_fence_before();
       mbar_arrive(bar_tfree);  // the accumulators may be overwritten
-      // node row (c, i, k) of K_e: K_(c,i),(b,k) = this row's pair (c, b) for b >= c,
-      // the partner row's pair (b, c) for b < c
-      float4* dst = reinterpret_cast<float4*>(static_cast<float2*>(g.Ke) + (e0 + el) * 576);
-#pragma unroll 1
-      for (int c = 0; c < 8; ++c) {
-        uint32_t addr[8];
-#pragma unroll
-        for (int b = 0; b < 8; ++b) {
-          const int n = b >= c ? (c * (15 - c)) / 2 + b : (b * (15 - b)) / 2 + c;
-          addr[b] = lane_addr + uint32_t(TM_OWN + 2 * n);
-        }
-        float2 row[8];
-        tmem_ld2x8(addr, row);
-#pragma unroll
-        for (int b = 0; b < 8; ++b) {
-          const float x = __shfl_sync(0xffffffffu, row[b].x, partner), y = __shfl_sync(0xffffffffu, row[b].y, partner);
-          if (b < c) row[b] = make_float2(x, y);
-        }
-        if (live) {
-          float4* d = dst + ((c * 3 + i) * 3 + kc) * 4;
-#pragma unroll
-          for (int b = 0; b < 8; b += 2) d[b / 2] = make_float4(row[b].x, row[b].y, row[b + 1].x, row[b + 1].y);
-        }
-      }
     }
   } else {
     // ---------------- MMA warp: lane 0 issues, the warp waits together ----------------

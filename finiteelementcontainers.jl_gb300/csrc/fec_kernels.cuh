@@ -1283,9 +1283,37 @@ __device__ __forceinline__ NodeMeta load_meta(const GatherArgs& g, int64_t n, in
 // pair index of the node pair (x, y), x <= y, of a hex8 element
 __device__ __forceinline__ int hex8_pair(int x, int y) { return (x * (15 - x)) / 2 + y; }
 
-// cp.async of node m's staged data into `st` (all 32 lanes; a commit group always follows)
+// Offsets of the KE_PAIRS staging (shared memory, built once per CTA):
+//   chunk[a][w]: byte offset in an element's 2,592 pair bytes of 16-byte chunk w
+//     (part w % 5 of the block of column node w / 5) of node a's rows; the 80-byte
+//     window stays inside the element's entries
+//   blk[a][b]:   byte offset in the staged 640 bytes of node a's block for column
+//     node b, bit 15 set when the block is pair (a, b) itself (a <= b: entry 3k + i
+//     holds K_(a,k),(b,i)), clear for pair (b, a) (entry 3i + k)
+struct PairTables {
+  uint16_t chunk[8][40];
+  uint16_t blk[8][8];
+};
+__device__ __forceinline__ void build_pair_tables(PairTables& t) {
+  for (int i = threadIdx.x; i < 8 * 40 + 64; i += blockDim.x) {
+    if (i < 320) {
+      const int a = i / 40, w = i % 40, bb = w / 5, part = w % 5;
+      const int p = hex8_pair(a < bb ? a : bb, a < bb ? bb : a);
+      t.chunk[a][w] = uint16_t(((p * 72) & ~15) + part * 16);
+    } else {
+      const int a = (i - 320) / 8, b = (i - 320) % 8;
+      const int p = hex8_pair(a < b ? a : b, a < b ? b : a);
+      t.blk[a][b] = uint16_t(b * 80 + (p & 1) * 8) | (a <= b ? 0x8000u : 0u);
+    }
+  }
+}
+
+// cp.async of node m's staged data into `st` (all 32 lanes; a commit group always
+// follows).  Lane (c, sub) = (lane / 4, lane % 4) copies element c's chunks sub,
+// sub + 4, ... (one shuffle per node for the element's entry).
 template <typename Real, bool PAIRS>
-__device__ __forceinline__ void issue(const GatherArgs& g, const NodeMeta& m, unsigned char* st, int lane) {
+__device__ __forceinline__ void issue(const GatherArgs& g, const NodeMeta& m, unsigned char* st, int lane,
+                                      const PairTables* pt) {
   using S = Stage<Real, PAIRS>;
   using RT = typename RE<Real>::T;
   if (!m.pipe) return;
@@ -1293,26 +1321,25 @@ __device__ __forceinline__ void issue(const GatherArgs& g, const NodeMeta& m, un
   const unsigned char* Ke = reinterpret_cast<const unsigned char*>(static_cast<const Real*>(g.Ke) + B.ke_off);
   const uint16_t* ep = g.epos + B.epos_off;
   const RT* Re = static_cast<const RT*>(g.Re) + B.re_off;
-  // element rows: chunk t = lane + 32 j; every lane takes part in every shuffle (the
-  // trip count is fixed), copies only for t < cnt * CHUNKS
-  const int total = m.cnt * S::CHUNKS;
-  constexpr int TRIPS = (MAXE * S::CHUNKS + 31) / 32;
-#pragma unroll
-  for (int j = 0; j < TRIPS; ++j) {
-    const int t = lane + 32 * j;
-    const int c = t / S::CHUNKS < MAXE ? t / S::CHUNKS : MAXE - 1, w = t - c * S::CHUNKS;
+  {
+    const int c = lane >> 2, sub = lane & 3;
     const uint32_t packed = __shfl_sync(0xffffffffu, m.adj, c);
-    const uint64_t le = (packed >> 5) - uint32_t(B.elem_start), a = packed & 31u;
-    if constexpr (PAIRS) {
-      // chunk w: part w % 5 of the block of column node w / 5; the element's 36 x 9
-      // entries are 2,592 bytes, so the 80-byte window stays inside them
-      const int bb = w / 5, part = w - bb * 5;
-      const int p = hex8_pair(int(a) < bb ? int(a) : bb, int(a) < bb ? bb : int(a));
-      if (t < total)
-        cp16(st + c * (8 * S::BLK) + bb * S::BLK + part * 16,
-             Ke + (le * 324u) * sizeof(Real) + ((p * 72) & ~15) + part * 16);
-    } else {
-      if (t < total) cp16(st + (c * 72) * sizeof(Real) + w * 16, Ke + ((le * 576u + a * 72u) * sizeof(Real)) + w * 16);
+    if (c < m.cnt) {
+      const uint64_t le = (packed >> 5) - uint32_t(B.elem_start);
+      const int a = int(packed & 31u);
+      if constexpr (PAIRS) {
+        const unsigned char* src = Ke + le * (324u * sizeof(Real));
+        unsigned char* dst = st + c * (8 * S::BLK);
+        const uint16_t* ch = pt->chunk[a];
+#pragma unroll
+        for (int j = 0; j < S::CHUNKS / 4; ++j) cp16(dst + (sub + 4 * j) * 16, src + ch[sub + 4 * j]);
+      } else {
+        const unsigned char* src = Ke + (le * 576u + uint64_t(a) * 72u) * sizeof(Real);
+        unsigned char* dst = st + c * (72 * sizeof(Real));
+#pragma unroll
+        for (int j = 0; j < (S::CHUNKS + 3) / 4; ++j)
+          if (sub + 4 * j < S::CHUNKS) cp16(dst + (sub + 4 * j) * 16, src + (sub + 4 * j) * 16);
+      }
     }
   }
   if (lane < m.cnt) {  // element-map row of node a: 8 uint16, 16-byte aligned
@@ -1335,7 +1362,12 @@ __global__ void __launch_bounds__(gp::WPB * 32, MINB) node_gather_hex8_pipe_kern
   using S = Stage<Real, PAIRS>;
   using RT = typename RE<Real>::T;
   extern __shared__ __align__(16) unsigned char smem_g[];
+  __shared__ PairTables s_pt;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if constexpr (PAIRS) {
+    build_pair_tables(s_pt);
+    __syncthreads();
+  }
   const size_t acc_bytes = (size_t(g.acc_stride) * GatherAcc::WORDS * sizeof(float) + 15) / 16 * 16;
   unsigned char* wbase = smem_g + warp * (acc_bytes + 2 * S::BYTES);
   float* acc = reinterpret_cast<float*>(wbase);
@@ -1348,12 +1380,12 @@ __global__ void __launch_bounds__(gp::WPB * 32, MINB) node_gather_hex8_pipe_kern
   const int lk = lane >> 3, lb = lane & 7;
 
   NodeMeta cur = load_meta(g, int64_t(blockIdx.x) * WPB + warp, lane);
-  issue<Real, PAIRS>(g, cur, stage[0], lane);
+  issue<Real, PAIRS>(g, cur, stage[0], lane, &s_pt);
   commit();
   NodeMeta nxt = load_meta(g, cur.n < 0 ? g.nn : cur.n + GW, lane);
   for (int it = 0; cur.n >= 0; ++it) {
     const int s = it & 1;
-    issue<Real, PAIRS>(g, nxt, stage[s ^ 1], lane);  // node i+1 into the other stage
+    issue<Real, PAIRS>(g, nxt, stage[s ^ 1], lane, &s_pt);  // node i+1 into the other stage
     commit();
     const NodeMeta nn2 = load_meta(g, nxt.n < 0 ? g.nn : nxt.n + GW, lane);  // node i+2's adjacency
     wait_prev();                              // node i's copies (this lane's) have landed
@@ -1380,9 +1412,10 @@ __global__ void __launch_bounds__(gp::WPB * 32, MINB) node_gather_hex8_pipe_kern
               // the three adjacent positions k*Ln + epos[b] + i
               Real v0, v1, v2;
               if constexpr (PAIRS) {  // K_(a,k),(b,i): pair (a, b) entry 3k + i, or pair (b, a) entry 3i + k
-                const int p = hex8_pair(a < lb ? a : lb, a < lb ? lb : a);
-                const Real* blk = reinterpret_cast<const Real*>(st + c * (8 * S::BLK) + lb * S::BLK + (p & 1) * 8);
-                const int o = a <= lb ? lk * 3 : lk, d = a <= lb ? 1 : 3;
+                const unsigned bo = s_pt.blk[a][lb];
+                const Real* blk = reinterpret_cast<const Real*>(st + c * (8 * S::BLK) + (bo & 0x7fffu));
+                const bool own = (bo & 0x8000u) != 0;
+                const int o = own ? lk * 3 : lk, d = own ? 1 : 3;
                 v0 = blk[o];
                 v1 = blk[o + d];
                 v2 = blk[o + 2 * d];
