@@ -165,6 +165,41 @@ def test_single_launch_matches_per_block_launches(fec, physics):
     assert out[0][2] == 4 + 4 and out[1][2] == 1 + 4
 
 
+@pytest.mark.parametrize("physics", ["neohookean", "j2"])
+def test_single_launch_with_class_tables_present(fec, physics):
+    """With the tables of the structured hex8 block and the tet10 / hex27 boxes of
+    translation classes present (the defaults), the single launch still runs the
+    per-element kernels and its workspace is sized and laid out for whole element
+    matrices: its results are bitwise those with the tables switched off, and within
+    1e-12 of the per-block launches, which take the tensor-core and class kernels
+    (symmetric-half workspaces)."""
+    import os
+    torch = _torch()
+    mesh = fec.meshes.merge_meshes(
+        [fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (5, 5, 5)), fec.meshes.box_tet4((3, 3, 3)),
+         fec.meshes.box_tet10((3, 3, 3)), fec.meshes.box_hex27((3, 3, 3))],
+        names=["hex8", "tet4", "tet10", "hex27"])
+    tables = []
+    _single_vs_per_block(fec, torch, mesh, physics, stretch_field, tables)
+    off = []
+    os.environ["FEC_HEX8_AFFINE"] = "0"
+    os.environ["FEC_CLASS_TC"] = "0"
+    try:
+        _single_vs_per_block(fec, torch, mesh, physics, stretch_field, off)
+    finally:
+        os.environ.pop("FEC_HEX8_AFFINE", None)
+        os.environ.pop("FEC_CLASS_TC", None)
+    (R_pb, nz_pb, _, st_pb), (R_1, nz_1, _, st_1) = tables
+    assert torch.equal(R_1, off[1][0]) and torch.equal(nz_1, off[1][1])
+    assert not torch.equal(nz_pb, off[0][1])   # (the per-block launches took the tensor-core kernels)
+    e_r, e_k = rel_err(R_pb.cpu().numpy(), R_1.cpu().numpy()), rel_err(nz_pb.cpu().numpy(), nz_1.cpu().numpy())
+    print(physics, "per-block (tables) vs single launch: residual", e_r, "nzval", e_k)
+    assert max(e_r[:2]) <= TOL64 and max(e_k) <= TOL64
+    if physics == "j2":
+        assert torch.equal(st_1, off[1][3])
+        assert max(rel_err(st_pb.cpu().numpy(), st_1.cpu().numpy())[:2]) <= TOL64
+
+
 def _single_vs_per_block(fec, torch, mesh, physics, stretch_field, out):
     for single in (False, True):
         asm = fec.SparseMatrixAssembler(fec.VectorFunction(fec.FunctionSpace(mesh), "u"), device=0)
