@@ -1265,6 +1265,10 @@ int fec_assemble_action(fec_ctx* c, int precision, double t, double dt, const do
     const int ns = num_states_of(B.physics);
     ea.state_old = ns ? state_old + st_off : nullptr;
     ea.Re = static_cast<char*>(c->d_Re.p) + rsz * size_t(re_off);
+    // FP64 blocks of translated hex8 elements: the block's constant gradients and JxW
+    if (B.elem_type == FEC_HEX8 && precision == FEC_FP64 && B.congruent)
+      if (const void* tab = affine_table(c, b, precision, false))
+        ea.affine = static_cast<const unsigned char*>(tab) + fec::hex8_affine_grad_offset();
     cudaError_t e;
     {
       LaunchTimer timer(c, s, "element_action");

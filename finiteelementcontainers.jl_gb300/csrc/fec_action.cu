@@ -9,6 +9,8 @@
 // Kv_el = Kv_el + Kv_q) into the element residual workspace, which the node
 // gather then reduces in element order into the unknowns -- the same
 // deterministic path as the residual.  The state is read, never written.
+// FP64 blocks of translated hex8 elements (args.affine: the block's constant
+// spatial gradients and JxW) skip the map and the coordinate loads (AFF).
 #include <type_traits>
 #include "fec_launch.h"
 
@@ -32,7 +34,7 @@ struct ActionSmem {
   static constexpr size_t BYTES = CONN + 4 * size_t(EPB * A);
 };
 
-template <int ET, class Model, typename Real, int EPB, bool SCALAR>
+template <int ET, class Model, typename Real, int EPB, bool SCALAR, bool AFF = false>
 __global__ void __launch_bounds__(EPB * Elem<ET>::NQ) action_kernel(ElemArgs g, const double* V) {
   using E = Elem<ET>;
   using L = RefLayout<ET>;
@@ -52,16 +54,23 @@ __global__ void __launch_bounds__(EPB * Elem<ET>::NQ) action_kernel(ElemArgs g, 
 
   const int tid = threadIdx.x, nthr = EPB * NQ;
   const int64_t e0 = int64_t(blockIdx.x) * EPB;
-  for (int i = tid; i < L::SIZE; i += nthr) {
-    s_ref[i] = g.ref[i];
-    if constexpr (MIXED) s_reff[i] = float(g.ref[i]);
+  static_assert(!AFF || (!MIXED && NQ * A * D + NQ <= L::SIZE), "gradients and JxW in the reference area");
+  if constexpr (AFF) {  // dNX [q][a][d], then JxW [q]
+    const double* tg = static_cast<const double*>(g.affine);
+    for (int i = tid; i < NQ * A * D + NQ; i += nthr) s_ref[i] = tg[i];
+  } else {
+    for (int i = tid; i < L::SIZE; i += nthr) {
+      s_ref[i] = g.ref[i];
+      if constexpr (MIXED) s_reff[i] = float(g.ref[i]);
+    }
   }
   for (int i = tid; i < EPB * A; i += nthr) {
     const int64_t e = e0 + i / A;
     s_conn[i] = e < g.ne ? g.conn[e * A + i % A] : 0;
   }
   __syncthreads();
-  for (int i = tid; i < EPB * A * D; i += nthr) s_x[i] = g.coords[int64_t(s_conn[i / D]) * D + i % D];
+  if constexpr (!AFF)
+    for (int i = tid; i < EPB * A * D; i += nthr) s_x[i] = g.coords[int64_t(s_conn[i / D]) * D + i % D];
   for (int i = tid; i < EPB * A * NF; i += nthr) {
     const int64_t dof = int64_t(s_conn[i / NF]) * NF + i % NF;
     s_u[i] = g.U[dof];
@@ -79,13 +88,18 @@ __global__ void __launch_bounds__(EPB * Elem<ET>::NQ) action_kernel(ElemArgs g, 
   const int64_t e = e0 + el;
   Real* kq = s_kq + (el * NQ + q) * NDOF;
   if (e < g.ne) {
-    Real dNX[A * D];
+    Real dNXr[A * D];
+    const Real* dNX = dNXr;  // AFF: the block's gradients of point q, read from shared memory where used
     const double* x = s_x + el * A * D;
     double jxw;
-    if constexpr (MIXED)
-      jxw = map_point_mixed<ET>(s_ref, s_reff, q, x, s_xd + el * A * D, dNX);
-    else
-      jxw = map_point<ET, Real>(s_ref, q, x, dNX, nullptr);
+    if constexpr (AFF) {
+      dNX = s_ref + q * A * D;
+      jxw = s_ref[NQ * A * D + q];
+    } else if constexpr (MIXED) {
+      jxw = map_point_mixed<ET>(s_ref, s_reff, q, x, s_xd + el * A * D, dNXr);
+    } else {
+      jxw = map_point<ET, Real>(s_ref, q, x, dNXr, nullptr);
+    }
     const double* u = s_u + el * A * NF;
     const double* v = s_v + el * A * NF;
     if constexpr (SCALAR) {  // Poisson: K_q = JxW dN dN^T
@@ -151,6 +165,13 @@ cudaError_t go(int precision, const ElemArgs& a, const double* V, cudaStream_t s
   ++*launches;
   if (precision == 0) {
     constexpr size_t smem = ActionSmem<ET, double, EPB, NF>::BYTES;
+    if constexpr (ET == 1) {
+      if (a.affine) {
+        if ((e = ensure_smem<action_kernel<ET, Model, double, EPB, SCALAR, true>>(smem)) != cudaSuccess) return e;
+        action_kernel<ET, Model, double, EPB, SCALAR, true><<<grid, block, smem, s>>>(a, V);
+        return cudaGetLastError();
+      }
+    }
     if ((e = ensure_smem<action_kernel<ET, Model, double, EPB, SCALAR>>(smem)) != cudaSuccess) return e;
     action_kernel<ET, Model, double, EPB, SCALAR><<<grid, block, smem, s>>>(a, V);
   } else {

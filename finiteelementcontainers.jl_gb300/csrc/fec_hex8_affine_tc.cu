@@ -569,6 +569,11 @@ bool hex8_affine_enabled() {
   return !(v && v[0] == '0');
 }
 
+size_t hex8_affine_grad_offset() {
+  static_assert(aff::T_JXW == aff::T_G + aff::NQ * 24 * 8, "gradients, then JxW");
+  return size_t(aff::T_G);
+}
+
 bool hex8_pairs_enabled() {
   const char* v = std::getenv("FEC_HEX8_PAIRS");
   return !(v && v[0] == '0');

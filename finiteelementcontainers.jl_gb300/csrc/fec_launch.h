@@ -78,6 +78,9 @@ cudaError_t launch_hex8_affine_tc(int physics, bool want_r, bool want_k, const E
 bool hex8_affine_table(const double* x0, const double* ref, std::vector<unsigned char>& out);
 // FEC_HEX8_AFFINE=0 keeps such blocks on the per-element kernels.
 bool hex8_affine_enabled();
+// Byte offset, in that table, of the block's spatial gradients dNX [8 points][8
+// nodes][3] (double), followed by JxW [8] (double): the same for every element.
+size_t hex8_affine_grad_offset();
 // With the stiffness that kernel writes the symmetric half of K_e (args.ke_pairs:
 // the KE_PAIRS layout, 36 * 9 entries per element) unless FEC_HEX8_PAIRS=0
 // (the node rows of the whole K_e, KE_NODE_ROWS).

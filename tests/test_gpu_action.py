@@ -103,3 +103,32 @@ def test_j2_action_with_plastic_state(fec, orc):
     e = rel_err(Kv, K @ Vu)
     print("J2 K v vs assembled:", e)
     assert max(e) <= TOL64
+
+
+@pytest.mark.parametrize("phys_name", ["neohookean", "j2"])
+def test_affine_action_matches_per_element_map(fec, phys_name):
+    """FP64 blocks of translated hex8 elements read the block's constant spatial
+    gradients and JxW instead of mapping every element: within 1e-12 of the
+    per-element map (FEC_HEX8_AFFINE=0), and a different rounding of it (the
+    path ran)."""
+    import os
+    mesh = fec.StructuredMesh("hex", (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (9, 9, 9))
+    asm = fec.SparseMatrixAssembler(fec.VectorFunction(fec.FunctionSpace(mesh), "u"), device=0)
+    if phys_name == "neohookean":
+        phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+        U = stretch_field(mesh.nodal_coords, seed=4).ravel()
+    else:
+        phys = fec.J2Plasticity(200.0, 0.3, 0.25, 2.0)
+        U = 3.0 * stretch_field(mesh.nodal_coords, seed=2, noise=1e-4, diag=(1.004, 0.999, 0.999)).ravel()
+    p = fec.create_parameters(mesh, asm, phys)
+    Vu = np.random.default_rng(5).standard_normal(asm.dof.unknown_dofs.size)
+    Kv = _action(fec, asm, p, U, Vu)
+    os.environ["FEC_HEX8_AFFINE"] = "0"
+    try:
+        Kv_pe = _action(fec, asm, p, U, Vu)
+    finally:
+        os.environ.pop("FEC_HEX8_AFFINE", None)
+    e = rel_err(Kv, Kv_pe)
+    print(phys_name, "affine action vs per-element map:", e)
+    assert max(e) <= TOL64
+    assert not np.array_equal(Kv, Kv_pe)
