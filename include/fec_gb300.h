@@ -230,9 +230,10 @@ int fec_check_finite(fec_ctx* ctx, const double* R_u_dev, const double* nzval_de
  *
  * Its workspace is one static device array of FEC_NOALLOC_SCRATCH_BYTES that
  * every GPU which loads the library holds until the process exits.  Meshes
- * whose element workspace (NE * NDOF^2 element-matrix entries plus NE * NDOF
- * element-residual entries, 8 bytes each in FP64, 4 in FP32) exceeds it are
- * rejected with FEC_ERR_ARG.  Every call made outside stream capture looks up
+ * whose element workspace (NE * NDOF^2 element-matrix entries -- the symmetric
+ * half, NE * A(A+1)/2 * 9, for blocks of translated elements whose tensor-core
+ * kernels write only that -- plus NE * NDOF element-residual entries, 8 bytes
+ * each in FP64, 4 in FP32) exceeds it are rejected with FEC_ERR_ARG.  Every call made outside stream capture looks up
  * the array's device address (cudaGetSymbolAddress), so a reset of the
  * device's primary context in between is harmless; a call under capture uses
  * the address of the last call on that device, so make the first call on a
