@@ -240,9 +240,11 @@ __device__ __forceinline__ void stage_element(const ElemArgs& g, int64_t e, int 
 // ---------------------------------------------------------------------------
 // Poisson (test/poisson/TestPoissonCommon.jl:75-107):
 //   R_q = JxW (grad u . dN_X_a - N_a f(X_q)),  K_q = JxW dN_X_a . dN_X_b
-// one thread per element row a
+// one thread per element row a.  AFF (FP64 blocks of translated hex8 elements,
+// g.affine: the block's spatial gradients [q][a][d] then JxW [q], double): the
+// map is the same for every element and is read, only X_q is formed.
 // ---------------------------------------------------------------------------
-template <int ET, typename Real, int EPB, bool WANT_R, bool WANT_K>
+template <int ET, typename Real, int EPB, bool WANT_R, bool WANT_K, bool AFF = false>
 __global__ void __launch_bounds__(EPB * Elem<ET>::NNPE) poisson_element_kernel(ElemArgs g) {
   using E = Elem<ET>;
   using L = RefLayout<ET>;
@@ -260,11 +262,31 @@ __global__ void __launch_bounds__(EPB * Elem<ET>::NNPE) poisson_element_kernel(E
   const int64_t e = int64_t(blockIdx.x) * EPB + ty;
   stage_element<ET, 1, EPB, TPE>(g, e, tx, ty, s_ref, s_conn_all[ty], s_x_all[ty], s_u_all[ty]);
   const bool live = e < g.ne;
+  static_assert(!AFF || (ET == 1 && sizeof(Real) == 8), "block gradients: FP64 hex8");
   if (live) {
     for (int q = tx; q < NQ; q += TPE) {
       double Xq[3];
       Real* dNX = s_dNX_all[ty][q];
-      const double jxw = map_point<ET, Real>(s_ref, q, s_x_all[ty], dNX, Xq);
+      double jxw;
+      if constexpr (AFF) {
+        const double* tg = static_cast<const double*>(g.affine);
+#pragma unroll
+        for (int k = 0; k < A * D; ++k) dNX[k] = Real(__ldg(tg + q * A * D + k));
+        jxw = __ldg(tg + NQ * A * D + q);
+        if (WANT_R) {
+          const double* N = s_ref + L::N_OFF + q * A;
+          const double* x = s_x_all[ty];
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            double s = 0;
+#pragma unroll
+            for (int a = 0; a < A; ++a) s = fma(N[a], x[a * D + d], s);
+            Xq[d] = s;
+          }
+        }
+      } else {
+        jxw = map_point<ET, Real>(s_ref, q, s_x_all[ty], dNX, Xq);
+      }
       s_jxw_all[ty][q] = Real(jxw);
       if (WANT_R) {
         double f = g.props[0];

@@ -1,4 +1,5 @@
 // fec_poisson.cu -- instantiations of the Poisson element kernel.
+#include <type_traits>
 #include "fec_launch.h"
 
 namespace fec {
@@ -10,6 +11,22 @@ cudaError_t go(bool want_r, bool want_k, const ElemArgs& a, cudaStream_t s, int*
   if (a.ne <= 0) return cudaSuccess;
   const dim3 block(TPE, EPB);
   const dim3 grid(unsigned((a.ne + EPB - 1) / EPB));
+  if constexpr (ET == 1 && std::is_same<Real, double>::value) {
+    if (a.affine) {  // a block of translated elements: its gradients and JxW from the affine table
+      ElemArgs b = a;
+      b.affine = static_cast<const unsigned char*>(a.affine) + hex8_affine_grad_offset();
+      if (want_r && want_k)
+        poisson_element_kernel<ET, Real, EPB, true, true, true><<<grid, block, 0, s>>>(b);
+      else if (want_r)
+        poisson_element_kernel<ET, Real, EPB, true, false, true><<<grid, block, 0, s>>>(b);
+      else if (want_k)
+        poisson_element_kernel<ET, Real, EPB, false, true, true><<<grid, block, 0, s>>>(b);
+      else
+        return cudaSuccess;
+      ++*launches;
+      return cudaGetLastError();
+    }
+  }
   if (want_r && want_k)
     poisson_element_kernel<ET, Real, EPB, true, true><<<grid, block, 0, s>>>(a);
   else if (want_r)
