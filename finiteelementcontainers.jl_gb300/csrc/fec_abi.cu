@@ -209,13 +209,24 @@ int ensure(fec_ctx* c, DevBuf& b, size_t bytes) {
 // element-matrix blocks start on 16-byte boundaries (vectorised copy-out)
 inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3); }
 
-// Whether an assembly of block b with the stiffness runs the FP64 hex8 tensor-core
-// kernel writing the symmetric half of K_e (KE_PAIRS) rather than node rows.
-bool hex8_pairs(const fec_ctx* c, size_t b, int precision, bool want_k, bool mixed) {
+// FEC_HEX27_PAIRS=0: the FP64 hex27 double-float kernel writes its element
+// matrices whole (row-major) instead of the symmetric half; the same values.
+bool hex27_pairs_enabled() {
+  const char* v = std::getenv("FEC_HEX27_PAIRS");
+  return !(v && v[0] == '0');
+}
+
+// Whether an assembly of block b with the stiffness runs an FP64 element kernel
+// that writes the symmetric half of K_e (KE_PAIRS): the hex8 tensor-core kernel
+// (instead of node rows, unless FEC_HEX8_PAIRS=0) and the hex27 double-float
+// kernel (on its own launch, unless FEC_HEX27_PAIRS=0).
+bool fp64_pairs(const fec_ctx* c, size_t b, int precision, bool want_k, bool mixed) {
   const Block& B = c->blocks[b];
-  return want_k && B.elem_type == FEC_HEX8 && (B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2) &&
-         precision == FEC_FP64 && !fp64_native_env() && fec::hex8_pairs_enabled() &&
-         affine_table(c, b, precision, mixed) != nullptr;
+  if (!want_k || precision != FEC_FP64 || fp64_native_env() ||
+      !(B.physics == FEC_PHYS_NEOHOOKEAN || B.physics == FEC_PHYS_J2))
+    return false;
+  if (B.elem_type == FEC_HEX27) return !mixed && hex27_pairs_enabled();
+  return B.elem_type == FEC_HEX8 && fec::hex8_pairs_enabled() && affine_table(c, b, precision, mixed) != nullptr;
 }
 
 // Workspace entries of block b's element matrices: the class tensor-core kernels
@@ -223,7 +234,7 @@ bool hex8_pairs(const fec_ctx* c, size_t b, int precision, bool want_k, bool mix
 // other kernel the whole K_e.  `mixed`: the single launch across blocks.
 int64_t ke_entries(const fec_ctx* c, size_t b, int precision, bool want_k, bool mixed) {
   const Block& B = c->blocks[b];
-  if (hex8_pairs(c, b, precision, want_k, mixed) ||
+  if (fp64_pairs(c, b, precision, want_k, mixed) ||
       (want_k && fec::class_tc_runs(B.physics, B.elem_type, precision, true, want_k,
                                     affine_table(c, b, precision, mixed) != nullptr)))
     return pad4(B.ne * (int64_t(B.nnpe) * (B.nnpe + 1) / 2 * 9));
@@ -1094,7 +1105,7 @@ int fec_assemble(fec_ctx* c, int want, int precision, double t, double dt, const
     ea.Re = want_r ? static_cast<char*>(c->d_Re.p) + rsz * size_t(re_off) : nullptr;
     ea.closure = c->d_cl_args.p;
     ea.affine = affine_table(c, b, precision, mixed);
-    ea.ke_pairs = hex8_pairs(c, b, precision, want_k, mixed) ? 1 : 0;
+    ea.ke_pairs = fp64_pairs(c, b, precision, want_k, mixed) ? 1 : 0;
     if (B.physics == FEC_PHYS_J2_MLP && !ea.closure)
       return fail(c, FEC_ERR_STATE, "block %d uses the learned closure but fec_closure_set was not called", int(b) + 1);
     cudaError_t e = cudaSuccess;
@@ -1669,7 +1680,7 @@ int fec_assemble_noalloc(fec_ctx* c, int want, int precision, double t, double d
     ea.Re = want_r ? static_cast<char*>(Re) + rsz * size_t(re_off) : nullptr;
     ea.closure = c->d_cl_args.p;
     ea.affine = affine_table(c, b, precision, false);
-    ea.ke_pairs = hex8_pairs(c, b, precision, want_k, false) ? 1 : 0;
+    ea.ke_pairs = fp64_pairs(c, b, precision, want_k, false) ? 1 : 0;
     if (B.physics == FEC_PHYS_J2_MLP && !ea.closure)
       return fail(c, FEC_ERR_STATE, "block %d uses the learned closure but fec_closure_set was not called", int(b) + 1);
     cudaError_t e;

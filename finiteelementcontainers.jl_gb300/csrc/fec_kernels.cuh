@@ -68,7 +68,7 @@ struct ElemArgs {
   const void* affine;       // hex8 blocks of translated elements: the constant operand table (or null)
   int* wait_err;            // set to 1 by a bounded wait that gave up (device flag; may be null)
   long long wait_budget;    // SM clocks a bounded wait allows before giving up (0: the default, ~1 s)
-  int ke_pairs;             // the FP64 hex8 tensor-core kernel writes KE_PAIRS (else KE_NODE_ROWS)
+  int ke_pairs;             // the element kernel writes KE_PAIRS (FP64 hex8 tensor-core, FP64 hex27 kernels)
 };
 
 // ---------------------------------------------------------------------------

@@ -6,7 +6,10 @@
 // (a, i) and the node blocks b = a + d (mod 27) for d in [7 cs, 7 cs + 7): with
 // 27 nodes (odd), d = 0..13 covers every unordered node pair once (d = 0 the
 // diagonal block), so the 351 off-diagonal node blocks are formed once and
-// written to both triangles.  Each thread keeps 21 double-float accumulators.
+// written to both triangles (or, PAIRS, once into the symmetric half: the
+// KE_PAIRS layout).  Each thread keeps 21 double-float accumulators; the two
+// threads of a row (adjacent lanes) split its nine row contractions
+// sum_J dN_aJ A_iJkL per point and exchange them by shuffles.
 // The per-point map streams each node's spatial gradient into shared memory
 // as it is formed (the 81 gradients of a point are never live together), as a
 // double-float for the contraction and in FP64 for the residual, which is
@@ -41,7 +44,7 @@ constexpr int HEX27_CLASS_BYTES = (27 * 27 * 3 + 27) * 8;
 
 // One element by NTHR threads (thread tid), shared by the kernel below and the
 // single-launch kernel of mixed element blocks.
-template <class Model, bool WANT_R, bool WANT_K, int NTHR, bool CLASS = false>
+template <class Model, bool WANT_R, bool WANT_K, int NTHR, bool CLASS = false, bool PAIRS = false>
 __device__ __forceinline__ void hex27_df64_tile(const ElemArgs& g, unsigned elem, int tid, unsigned char* smem_raw) {
   constexpr int NQ = 27, A = 27, NDOF = 81, NS = Model::NS, SCR = Model::SCR, SCR2 = Model::SCR2;
   static_assert(NTHR >= 2 * NDOF, "162 contracting threads");
@@ -184,17 +187,27 @@ __device__ __forceinline__ void hex27_df64_tile(const ElemArgs& g, unsigned elem
   float2 K[21];
 #pragma unroll
   for (int c = 0; c < 21; ++c) K[c] = z;
+  const unsigned pm = 3u << ((threadIdx.x & 31u) & ~1u);  // this row's two lanes
 #pragma unroll 1
   for (int q = 0; q < NQ; ++q) {
     const float2* dNX = s_dNX + q * A * 3;
     const float2 g0 = dNX[a * 3], g1 = dNX[a * 3 + 1], g2 = dNX[a * 3 + 2];
     if (WANT_K) {
       const float2* Aq = s_A + q * 45;
+      // t_kL = sum_J dN_aJ A_iJkL: this thread forms kl = cs, cs + 2, ..., the
+      // row's other thread the rest
       float2 t[9];
 #pragma unroll
-      for (int kl = 0; kl < 9; ++kl)
-        t[kl] = df64_dot3(g0, Aq[sym_index(3 * i, kl)], g1, Aq[sym_index(3 * i + 1, kl)], g2,
-                          Aq[sym_index(3 * i + 2, kl)]);
+      for (int j = 0; j < 5; ++j) {
+        const int kl = 2 * j + cs;
+        float2 v = z;
+        if (kl < 9)
+          v = df64_dot3(g0, Aq[sym_index(3 * i, kl)], g1, Aq[sym_index(3 * i + 1, kl)], g2,
+                        Aq[sym_index(3 * i + 2, kl)]);
+        const float2 o = make_float2(__shfl_xor_sync(pm, v.x, 1), __shfl_xor_sync(pm, v.y, 1));
+        t[2 * j] = cs ? o : v;
+        if (2 * j + 1 < 9) t[2 * j + 1] = cs ? v : o;
+      }
 #pragma unroll
       for (int dd = 0; dd < 7; ++dd) {
         int b = a + 7 * cs + dd;
@@ -206,7 +219,16 @@ __device__ __forceinline__ void hex27_df64_tile(const ElemArgs& g, unsigned elem
       }
     }
   }
-  if (WANT_K) {
+  if (WANT_K && PAIRS) {  // K_(a,i),(b,k) at its place in the symmetric half
+    float2* Kp = static_cast<float2*>(g.Ke) + e * (A * (A + 1) / 2 * 9);
+#pragma unroll
+    for (int dd = 0; dd < 7; ++dd) {
+      int b = a + 7 * cs + dd;
+      b = b >= A ? b - A : b;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) Kp[pair_entry(A, a, i, b, k)] = K[dd * 3 + k];
+    }
+  } else if (WANT_K) {
     float2* Ke = static_cast<float2*>(g.Ke) + e * (NDOF * NDOF);
 #pragma unroll
     for (int dd = 0; dd < 7; ++dd) {
@@ -222,10 +244,10 @@ __device__ __forceinline__ void hex27_df64_tile(const ElemArgs& g, unsigned elem
   }
 }
 
-template <class Model, bool WANT_R, bool WANT_K, bool CLASS = false>
+template <class Model, bool WANT_R, bool WANT_K, bool CLASS = false, bool PAIRS = false>
 __global__ void __launch_bounds__(HEX27_THREADS, 3) mech_hex27_df64_kernel(ElemArgs g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  hex27_df64_tile<Model, WANT_R, WANT_K, HEX27_THREADS, CLASS>(g, blockIdx.x, threadIdx.x, smem_raw);
+  hex27_df64_tile<Model, WANT_R, WANT_K, HEX27_THREADS, CLASS, PAIRS>(g, blockIdx.x, threadIdx.x, smem_raw);
 }
 
 }  // namespace fec

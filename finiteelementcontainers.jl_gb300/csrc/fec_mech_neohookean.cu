@@ -128,18 +128,22 @@ cudaError_t hex8_df64(bool want_r, bool want_k, const ElemArgs& a, cudaStream_t 
   return hex8_df64_1<EPB, false, true>(a, s);
 }
 
-template <bool R, bool K>
-cudaError_t hex27_df64_1(const ElemArgs& a, cudaStream_t s) {
+template <bool R, bool K, bool CLASS, bool PAIRS>
+cudaError_t hex27_df64_2(const ElemArgs& a, cudaStream_t s) {
   constexpr size_t smem = Hex27Df64Smem<NeoHookean>::BYTES;
   cudaError_t err;
-  if (a.affine && class_tc_enabled()) {  // a block of translation classes: the class's gradients
-    if ((err = ensure_smem<mech_hex27_df64_kernel<NeoHookean, R, K, true>>(smem)) != cudaSuccess) return err;
-    mech_hex27_df64_kernel<NeoHookean, R, K, true><<<unsigned(a.ne), HEX27_THREADS, smem, s>>>(a);
-    return cudaGetLastError();
-  }
-  if ((err = ensure_smem<mech_hex27_df64_kernel<NeoHookean, R, K>>(smem)) != cudaSuccess) return err;
-  mech_hex27_df64_kernel<NeoHookean, R, K><<<unsigned(a.ne), HEX27_THREADS, smem, s>>>(a);
+  if ((err = ensure_smem<mech_hex27_df64_kernel<NeoHookean, R, K, CLASS, PAIRS>>(smem)) != cudaSuccess) return err;
+  mech_hex27_df64_kernel<NeoHookean, R, K, CLASS, PAIRS><<<unsigned(a.ne), HEX27_THREADS, smem, s>>>(a);
   return cudaGetLastError();
+}
+
+// CLASS: a block of translation classes (the class's gradients); PAIRS: the
+// stiffness into the symmetric half (args.ke_pairs)
+template <bool R, bool K>
+cudaError_t hex27_df64_1(const ElemArgs& a, cudaStream_t s) {
+  const bool cls = a.affine && class_tc_enabled();
+  if (K && a.ke_pairs) return cls ? hex27_df64_2<R, K, true, true>(a, s) : hex27_df64_2<R, K, false, true>(a, s);
+  return cls ? hex27_df64_2<R, K, true, false>(a, s) : hex27_df64_2<R, K, false, false>(a, s);
 }
 
 cudaError_t hex27_df64(bool want_r, bool want_k, const ElemArgs& a, cudaStream_t s, int* launches) {

@@ -216,6 +216,46 @@ def test_hex27_j2_fp64(fec, orc):
     assert max(rel_err(nz, nzo)) <= TOL64
 
 
+@pytest.mark.parametrize("classes", [True, False], ids=["class_gradients", "per_element_map"])
+@pytest.mark.parametrize("phys_name", ["neohookean", "j2"])
+def test_hex27_fp64_pair_workspace_matches_whole_matrices(fec, phys_name, classes):
+    """The FP64 hex27 double-float kernel writes the symmetric half of each
+    element matrix (378 node pairs x 9 entries); with FEC_HEX27_PAIRS=0 it writes
+    them whole.  Both hold the same values, so R, nzval and the state agree
+    bitwise, with and without the class gradients (FEC_CLASS_TC=0) and with a
+    Dirichlet face."""
+    import os
+    torch = _torch()
+    mesh = fec.meshes.box_hex27((3, 3, 3))
+    if phys_name == "neohookean":
+        phys = fec.NeoHookean.from_youngs(1.0, 0.3)
+        U = stretch_field(mesh.nodal_coords, seed=6).ravel()
+    else:
+        phys = fec.J2Plasticity(200.0, 0.3, 0.25, 2.0)
+        U = 3.0 * stretch_field(mesh.nodal_coords, seed=2, noise=1e-4, diag=(1.004, 0.999, 0.999)).ravel()
+    mesh.nodeset_nodes["fix"] = np.flatnonzero(mesh.nodal_coords[:, 0] < 1e-12).astype(np.int64) + 1
+
+    def run():
+        bcs = [fec.DirichletBC("u_x", lambda X, t: 0.0, nodeset_name="fix")]
+        asm, p = _setup(fec, mesh, "vector", phys, bcs)
+        R, nz, _ = _run(fec, asm, p, U)
+        st = p.state_new.cpu().numpy().copy() if phys_name == "j2" else None
+        return R, nz, st
+
+    if not classes:
+        os.environ["FEC_CLASS_TC"] = "0"
+    try:
+        R, nz, st = run()
+        os.environ["FEC_HEX27_PAIRS"] = "0"
+        R0, nz0, st0 = run()
+    finally:
+        os.environ.pop("FEC_HEX27_PAIRS", None)
+        os.environ.pop("FEC_CLASS_TC", None)
+    assert np.array_equal(R, R0) and np.array_equal(nz, nz0)
+    if st is not None:
+        assert np.array_equal(st, st0)
+
+
 @pytest.mark.parametrize("kind", ["tet4", "tet10", "hex27"])
 @pytest.mark.parametrize("phys_name", ["neohookean", "j2"])
 def test_higher_order_fp32_element(fec, orc, kind, phys_name):
