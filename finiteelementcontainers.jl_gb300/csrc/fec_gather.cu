@@ -75,7 +75,7 @@ bool gather_pipe_enabled() {
 
 template <typename Real, bool PAIRS = false>
 cudaError_t go_pipe(const GatherArgs& g, cudaStream_t s, int* launches) {
-  constexpr int MINB = sizeof(Real) == 8 ? 2 : 3;
+  constexpr int MINB = 2;
   const size_t acc_bytes = (size_t(g.acc_stride) * GatherAcc::WORDS * sizeof(float) + 15) / 16 * 16;
   const size_t smem = size_t(gp::WPB) * (acc_bytes + 2 * gp::Stage<Real, PAIRS>::BYTES);
   cudaError_t err = ensure_smem<node_gather_hex8_pipe_kernel<Real, MINB, PAIRS>>(smem);

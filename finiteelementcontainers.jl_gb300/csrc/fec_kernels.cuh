@@ -1275,31 +1275,46 @@ __device__ __forceinline__ void wait_prev() { asm volatile("cp.async.wait_group 
 
 struct NodeMeta {
   int64_t n;        // node, or -1 past the end
-  int64_t p0;       // first adjacency entry
-  int cnt;          // adjacency entries
+  int64_t p0, p1;   // adjacency entries [p0, p1)
   unsigned um;      // umask with the full-neighbourhood bit
   int Ln;           // rows per column
-  uint32_t adj;     // this lane's adjacency entry (lane < cnt)
-  bool pipe;        // staged through shared memory
+  int cnt;          // adjacency entries                             (stage b)
+  uint32_t adj;     // this lane's adjacency entry (lane < cnt)      (stage b)
+  bool pipe;        // staged through shared memory                  (stage b)
+  int64_t col0;     // first nzval entry of the node's columns       (stage c)
+  int64_t dtu;      // lanes 0-2: unknown of the node's component    (stage c)
 };
 
-__device__ __forceinline__ NodeMeta load_meta(const GatherArgs& g, int64_t n, int lane) {
+// The node's metadata in three stages, each a node apart, so that no global load
+// is used in the iteration that issues it: (a) the node's own entries, (b) its
+// adjacency entries, addressed by (a), (c) where its columns and residual go.
+__device__ __forceinline__ NodeMeta meta_a(const GatherArgs& g, int64_t n) {
   NodeMeta m;
   m.n = n < g.nn ? n : -1;
-  m.p0 = 0;
-  m.cnt = 0;
+  m.p0 = m.p1 = 0;
   m.um = 0;
   m.Ln = 0;
+  m.cnt = 0;
   m.adj = 0;
   m.pipe = false;
+  m.col0 = m.dtu = 0;
   if (m.n < 0) return m;
   m.um = g.umask[n];
   m.Ln = g.col_len[n];
   m.p0 = g.nadj_ptr[n];
-  m.cnt = int(g.nadj_ptr[n + 1] - m.p0);
+  m.p1 = g.nadj_ptr[n + 1];
+  return m;
+}
+__device__ __forceinline__ void meta_b(const GatherArgs& g, NodeMeta& m, int lane) {
+  if (m.n < 0) return;
+  m.cnt = int(m.p1 - m.p0);
   m.pipe = (m.um & UMASK_FULL_NBR) != 0 && m.cnt >= 1 && m.cnt <= MAXE;
   if (m.pipe && lane < m.cnt) m.adj = g.nadj[m.p0 + lane];
-  return m;
+}
+__device__ __forceinline__ void meta_c(const GatherArgs& g, NodeMeta& m, int lane) {
+  if (m.n < 0) return;
+  if (g.nzval) m.col0 = g.col_base[m.n];
+  if (g.R_u && lane < 3) m.dtu = g.dof_to_unknown[m.n * 3 + lane];
 }
 
 // pair index of the node pair (x, y), x <= y, of a hex8 element
@@ -1401,18 +1416,26 @@ __global__ void __launch_bounds__(gp::WPB * 32, MINB) node_gather_hex8_pipe_kern
   const bool kl = lane < 24;
   const int lk = lane >> 3, lb = lane & 7;
 
-  NodeMeta cur = load_meta(g, int64_t(blockIdx.x) * WPB + warp, lane);
+  // node i is gathered while node i+1's copies are in flight, node i+2's
+  // adjacency entries and node i+3's own entries are loaded
+  auto next = [&](const NodeMeta& m) { return m.n < 0 ? g.nn : m.n + GW; };
+  NodeMeta cur = meta_a(g, int64_t(blockIdx.x) * WPB + warp);
+  meta_b(g, cur, lane);
+  meta_c(g, cur, lane);
   issue<Real, PAIRS>(g, cur, stage[0], lane, &s_pt);
   commit();
-  NodeMeta nxt = load_meta(g, cur.n < 0 ? g.nn : cur.n + GW, lane);
+  NodeMeta nxt = meta_a(g, next(cur));
+  meta_b(g, nxt, lane);
+  NodeMeta n2 = meta_a(g, next(nxt));
   for (int it = 0; cur.n >= 0; ++it) {
     const int s = it & 1;
     issue<Real, PAIRS>(g, nxt, stage[s ^ 1], lane, &s_pt);  // node i+1 into the other stage
     commit();
-    const NodeMeta nn2 = load_meta(g, nxt.n < 0 ? g.nn : nxt.n + GW, lane);  // node i+2's adjacency
+    meta_c(g, nxt, lane);
+    meta_b(g, n2, lane);
+    const NodeMeta n3 = meta_a(g, next(n2));
     wait_prev();                              // node i's copies (this lane's) have landed
     __syncwarp();                             // ... and every lane's
-    const int64_t n = cur.n;
     const unsigned um = cur.um & ~UMASK_FULL_NBR;
     if (um != 0) {
       const int Ln = cur.Ln, ncols = __popc(um);
@@ -1470,14 +1493,15 @@ __global__ void __launch_bounds__(gp::WPB * 32, MINB) node_gather_hex8_pipe_kern
       }
       __syncwarp();
       if (wantK) {
-        double* out = g.nzval + g.col_base[n];
+        double* out = g.nzval + cur.col0;
         for (int j = lane; j < ncols * Ln; j += 32) out[j] = GatherAcc::value(acc, j);
       }
-      if (wantR) g.R_u[g.dof_to_unknown[n * 3 + lane]] = racc;
+      if (wantR) g.R_u[cur.dtu] = racc;
       __syncwarp();
     }
     cur = nxt;
-    nxt = nn2;
+    nxt = n2;
+    n2 = n3;
   }
   asm volatile("cp.async.wait_all;" ::: "memory");
 }
