@@ -1187,11 +1187,16 @@ __global__ void __launch_bounds__(WPB * 32, MINB) node_gather_kernel(GatherArgs 
   } else if (n >= g.nn) {
     return;
   }
+  // the node's own entries, all issued before any is used (one memory latency)
   const unsigned um_raw = g.umask[n];
+  const int Ln = g.col_len[n];
+  int64_t p = g.nadj_ptr[n];
+  const int64_t p1 = g.nadj_ptr[n + 1];
+  const int64_t col0 = g.nzval ? g.col_base[n] : 0;
+  const int64_t dtu = (g.R_u && lane < NF) ? g.dof_to_unknown[n * NF + lane] : 0;
   const bool fast = (um_raw & UMASK_FULL_NBR) != 0;
   const unsigned um = um_raw & ~UMASK_FULL_NBR;
   if (um == 0) return;
-  const int Ln = g.col_len[n];
   const int ncols = __popc(um);
   float* acc = s_acc + warp * g.acc_stride * GatherAcc::WORDS;
   const bool wantK = g.nzval != nullptr;
@@ -1200,8 +1205,6 @@ __global__ void __launch_bounds__(WPB * 32, MINB) node_gather_kernel(GatherArgs 
     for (int j = lane; j < ncols * Ln; j += 32) GatherAcc::zero(acc, j);
   double racc = 0.0;  // the residual is summed in FP64, in increasing element order
   __syncwarp();
-  int64_t p = g.nadj_ptr[n];
-  const int64_t p1 = g.nadj_ptr[n + 1];
   while (p < p1) {
     // the run of entries from one element block
     const int64_t ge = int64_t(g.nadj[p] >> 5);
@@ -1227,10 +1230,10 @@ __global__ void __launch_bounds__(WPB * 32, MINB) node_gather_kernel(GatherArgs 
     p = q;
   }
   if (wantK) {
-    double* out = g.nzval + g.col_base[n];
+    double* out = g.nzval + col0;
     for (int j = lane; j < ncols * Ln; j += 32) out[j] = GatherAcc::value(acc, j);
   }
-  if (wantR) g.R_u[g.dof_to_unknown[n * NF + lane]] = racc;
+  if (wantR) g.R_u[dtu] = racc;
 }
 
 // ---------------------------------------------------------------------------
