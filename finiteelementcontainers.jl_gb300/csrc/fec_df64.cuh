@@ -122,6 +122,41 @@ __device__ __forceinline__ float2 df64_dot3_acc(float2 c, float2 a0, float2 b0, 
   return df64_fast2sum(s, lo);
 }
 
+// df64_dot3_acc without the final renormalization, for long accumulation chains:
+// c and the result are (s, lo) with s the FP32 running sum and lo the sum of its
+// exact rounding errors (TwoSum) and of the products' low parts, |lo| not held
+// below ulp(s)/2; the chain ends with df64_renorm.  Over n calls lo carries about
+// n ulps of s, so its own rounding stays near n 2^-48 |s|, the bound of the
+// renormalized chain; it saves three of the ~36 operations per call.
+__device__ __forceinline__ float2 df64_dot3_acc_lazy(float2 c, float2 a0, float2 b0, float2 a1, float2 b1, float2 a2,
+                                                     float2 b2) {
+  const float p0 = __fmul_rn(a0.x, b0.x), p1 = __fmul_rn(a1.x, b1.x), p2 = __fmul_rn(a2.x, b2.x);
+  float e = __fmaf_rn(a0.x, b0.x, -p0);
+  e = __fmaf_rn(a0.x, b0.y, e);
+  e = __fmaf_rn(a0.y, b0.x, e);
+  e = __fadd_rn(__fmaf_rn(a1.x, b1.x, -p1), e);
+  e = __fmaf_rn(a1.x, b1.y, e);
+  e = __fmaf_rn(a1.y, b1.x, e);
+  e = __fadd_rn(__fmaf_rn(a2.x, b2.x, -p2), e);
+  e = __fmaf_rn(a2.x, b2.y, e);
+  e = __fmaf_rn(a2.y, b2.x, e);
+  float s = c.x, lo = __fadd_rn(c.y, e);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float p = k == 0 ? p0 : (k == 1 ? p1 : p2);
+    const float t = __fadd_rn(s, p);
+    const float v = __fsub_rn(t, s);
+    lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(s, __fsub_rn(t, v)), __fsub_rn(p, v)));
+    s = t;
+  }
+  return make_float2(s, lo);
+}
+// (s, lo) -> the double-float s + lo, with no ordering precondition (TwoSum)
+__device__ __forceinline__ float2 df64_renorm(float2 v) {
+  const float s = __fadd_rn(v.x, v.y), bb = __fsub_rn(s, v.x);
+  return make_float2(s, __fadd_rn(__fsub_rn(v.x, __fsub_rn(s, bb)), __fsub_rn(v.y, bb)));
+}
+
 // a0 b0 + a1 b1 + a2 b2 (the same without an accumulator: the first high part
 // starts the sum).
 __device__ __forceinline__ float2 df64_dot3(float2 a0, float2 b0, float2 a1, float2 b1, float2 a2, float2 b2) {

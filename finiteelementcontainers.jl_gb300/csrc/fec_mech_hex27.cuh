@@ -215,10 +215,12 @@ __device__ __forceinline__ void hex27_df64_tile(const ElemArgs& g, unsigned elem
         const float2 h0 = dNX[b * 3], h1 = dNX[b * 3 + 1], h2 = dNX[b * 3 + 2];
 #pragma unroll
         for (int k = 0; k < 3; ++k)
-          K[dd * 3 + k] = df64_dot3_acc(K[dd * 3 + k], t[k * 3], h0, t[k * 3 + 1], h1, t[k * 3 + 2], h2);
+          K[dd * 3 + k] = df64_dot3_acc_lazy(K[dd * 3 + k], t[k * 3], h0, t[k * 3 + 1], h1, t[k * 3 + 2], h2);
       }
     }
   }
+#pragma unroll
+  for (int c = 0; c < 21; ++c) K[c] = df64_renorm(K[c]);
   if (WANT_K && PAIRS) {  // K_(a,i),(b,k) at its place in the symmetric half
     float2* Kp = static_cast<float2*>(g.Ke) + e * (A * (A + 1) / 2 * 9);
 #pragma unroll
