@@ -632,6 +632,7 @@ int fec_physics_set(fec_ctx* c, int block, int physics, const double* props, int
   B.physics = physics;
   B.nprops = nprops;
   for (int i = 0; i < 8; ++i) B.props[i] = i < nprops ? props[i] : 0.0;
+  if (physics == FEC_PHYS_J2 || physics == FEC_PHYS_J2_MLP) fec::J2::fill_derived(B.props);  // slots 4-7
   return ok(c);
 }
 

@@ -39,7 +39,7 @@ cudaError_t launch_mech_j2mlp(int elem_type, int precision, bool want_r, bool wa
 namespace {
 
 struct J2Params {
-  double p[4];
+  double p[8];  // E, nu, sigma_y, H and the derived constants (J2::fill_derived)
 };
 
 // exact J2 update of a batch of points (FP64): data generation and the error reference
@@ -210,6 +210,7 @@ int fec_j2_points(const double* props, int64_t n, const double* strain, const do
   if (n == 0) return FEC_OK;
   fec::J2Params P;
   for (int i = 0; i < 4; ++i) P.p[i] = props[i];
+  fec::J2::fill_derived(P.p);
   fec::j2_points_kernel<<<unsigned((n + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
       P, n, strain, state_old, stress, state_new, tangent);
   return cudaGetLastError() == cudaSuccess ? FEC_OK : FEC_ERR_CUDA;

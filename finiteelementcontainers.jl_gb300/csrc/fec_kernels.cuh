@@ -390,17 +390,18 @@ struct NeoHookean {
     const Real c1 = Real(0.5) * Kb * (J * J - J - Real(1));
     const Real r3 = rcbrt(J);  // J^{-1/3}
     const Real c2 = Gs * r3 * r3;
+    const Real I13 = I1 * Real(1.0 / 3.0);  // (a multiply: FP64 divisions are long on the FP64 pipe)
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int j = 0; j < 3; ++j) P9[i * 3 + j] = jxw * (c1 * H[i][j] + c2 * (F[i][j] - I1 / Real(3) * H[i][j]));
+      for (int j = 0; j < 3; ++j) P9[i * 3 + j] = jxw * (c1 * H[i][j] + c2 * (F[i][j] - I13 * H[i][j]));
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
       scr[i] = F[i / 3][i % 3];
       scr[9 + i] = H[i / 3][i % 3];
     }
     scr[18] = jxw * (Real(0.5) * Kb * (Real(2) * J - Real(1)) * J + Real(2.0 / 9.0) * c2 * I1);
-    scr[19] = jxw * (I1 / Real(3) * c2 - c1);
+    scr[19] = jxw * (I13 * c2 - c1);
     scr[20] = jxw * c2;
   }
   // JxW A_iJkL
@@ -500,14 +501,27 @@ struct J2 {
   static constexpr bool USES_TABLE = false;
   static constexpr int NS = 7;
   static constexpr int SCR = 13;  // n(9) kap' 2mu th' 2mu thb' (unused)
+  // props: E, nu, sigma_y, H, then the constants derived from them, filled by the
+  // library (fec_physics_set, fec_j2_points) so that no point divides for them:
+  // mu, kappa, 1 / (2 mu + 2/3 H), 1 / (1 + H / (3 mu)).
+  __host__ __device__ static void fill_derived(double* p) {
+    const double E = p[0], nu = p[1], H = p[3];
+    const double mu = E / (2 * (1 + nu)), lam = E * nu / ((1 + nu) * (1 - 2 * nu));
+    p[4] = mu;
+    p[5] = lam + 2.0 / 3.0 * mu;
+    p[6] = 1.0 / (2 * mu + 2.0 / 3.0 * H);
+    p[7] = 1.0 / (1.0 + H / (3 * mu));
+  }
   // Arithmetic in Real: double for the FP64 variant, float for the FP32-element
-  // variant; the state is accumulated in double either way.
+  // variant; the state is accumulated in double either way.  One reciprocal of
+  // |s| for the flow direction and the factors (FP64 divisions are long
+  // sequences on the FP64 pipe).
   template <typename Real>
   __device__ static void point(const double* props, Real gu[3][3], Real jxw, const double* st_old, double* st_new,
                                Real* P9, Real* scr) {
     using C = Real;
-    const C E = C(props[0]), nu = C(props[1]), sy = C(props[2]), Hh = C(props[3]);
-    const C mu = E / (2 * (1 + nu)), lam = E * nu / ((1 + nu) * (1 - 2 * nu)), kap = lam + C(2.0 / 3.0) * mu;
+    const C sy = C(props[2]), Hh = C(props[3]);
+    const C mu = C(props[4]), kap = C(props[5]), rdg = C(props[6]), thb0 = C(props[7]);
     C eps[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -522,14 +536,14 @@ struct J2 {
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) ee[i][j] = eps[i][j] - ep[i][j];
-    const C tr = ee[0][0] + ee[1][1] + ee[2][2];
+    const C tr = ee[0][0] + ee[1][1] + ee[2][2], tr3 = tr * C(1.0 / 3.0);
     C s[3][3];
     C sn2 = 0;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        s[i][j] = 2 * mu * (ee[i][j] - (i == j ? tr / C(3.0) : C(0.0)));
+        s[i][j] = 2 * mu * (ee[i][j] - (i == j ? tr3 : C(0.0)));
         sn2 += s[i][j] * s[i][j];
       }
     const C snorm = sqrt(sn2);
@@ -538,13 +552,14 @@ struct J2 {
     C dgam = 0, th = 1, thb = 0;
     C n[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     if (f > 0) {
-      dgam = f / (2 * mu + C(2.0 / 3.0) * Hh);
+      dgam = f * rdg;
+      const C rsn = C(1.0) / snorm;
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) n[i][j] = s[i][j] / snorm;
-      th = C(1.0) - 2 * mu * dgam / snorm;
-      thb = C(1.0) / (C(1.0) + Hh / (3 * mu)) - (C(1.0) - th);
+        for (int j = 0; j < 3; ++j) n[i][j] = s[i][j] * rsn;
+      th = C(1.0) - 2 * mu * dgam * rsn;
+      thb = thb0 - (C(1.0) - th);
     }
 #pragma unroll
     for (int i = 0; i < 3; ++i)

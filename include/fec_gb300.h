@@ -114,7 +114,10 @@ int fec_block_reference_set(fec_ctx* ctx, int block, int num_q, const double* N,
 int fec_block_reference_get(const fec_ctx* ctx, int block, int* num_q, double* N, double* dN, double* w);
 
 /* Per-block physics and properties (the (physics, props) pair that
- * foreach_block hands to _assemble_block!, src/Utils.jl:171-189). */
+ * foreach_block hands to _assemble_block!, src/Utils.jl:171-189).  Poisson: the
+ * source amplitude; Neo-Hookean: bulk and shear modulus; J2 and J2-MLP: E, nu,
+ * sigma_y, H -- the library keeps constants derived from these in property
+ * slots 4-7 (values passed there are replaced). */
 int fec_physics_set(fec_ctx* ctx, int block, int physics, const double* props, int num_props);
 
 /* DofManager ---------------------------------------------------------------- */
