@@ -350,6 +350,12 @@ __global__ void __launch_bounds__(EPB * Elem<ET>::NNPE) poisson_element_kernel(E
 // what aentries() needs to produce JxW-scaled A_iJkL for one i.
 // ---------------------------------------------------------------------------
 
+// A product rounded on its own: never fused into an FMA, so every kernel that
+// inlines a constitutive update rounds it alike (the single launch across blocks
+// and the per-block kernels give bitwise the same results).
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+
 // Compressible Neo-Hookean (test/mechanics/TestMechanicsLargeDeformation.jl:17-27)
 //   psi = K/2 (1/2 (J-1)^2 - ln J) + G/2 (J^{-2/3} F:F - 3)
 //   P = c1 H + c2 (F - I1/3 H),  H = F^{-T}, c1 = K/2 (J^2-J-1), c2 = G J^{-2/3}
@@ -390,7 +396,7 @@ struct NeoHookean {
     const Real c1 = Real(0.5) * Kb * (J * J - J - Real(1));
     const Real r3 = rcbrt(J);  // J^{-1/3}
     const Real c2 = Gs * r3 * r3;
-    const Real I13 = I1 * Real(1.0 / 3.0);  // (a multiply: FP64 divisions are long on the FP64 pipe)
+    const Real I13 = mul_rn(I1, Real(1.0 / 3.0));  // (a multiply: FP64 divisions are long on the FP64 pipe)
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -536,7 +542,7 @@ struct J2 {
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) ee[i][j] = eps[i][j] - ep[i][j];
-    const C tr = ee[0][0] + ee[1][1] + ee[2][2], tr3 = tr * C(1.0 / 3.0);
+    const C tr = ee[0][0] + ee[1][1] + ee[2][2], tr3 = mul_rn(tr, C(1.0 / 3.0));
     C s[3][3];
     C sn2 = 0;
 #pragma unroll
@@ -552,13 +558,13 @@ struct J2 {
     C dgam = 0, th = 1, thb = 0;
     C n[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     if (f > 0) {
-      dgam = f * rdg;
+      dgam = mul_rn(f, rdg);
       const C rsn = C(1.0) / snorm;
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) n[i][j] = s[i][j] * rsn;
-      th = C(1.0) - 2 * mu * dgam * rsn;
+        for (int j = 0; j < 3; ++j) n[i][j] = mul_rn(s[i][j], rsn);
+      th = C(1.0) - mul_rn(2 * mu * dgam, rsn);
       thb = thb0 - (C(1.0) - th);
     }
 #pragma unroll
@@ -577,9 +583,11 @@ struct J2 {
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) scr[i] = Real(n[i / 3][i % 3]);
-    scr[9] = Real(C(jxw) * kap);
-    scr[10] = Real(C(jxw) * 2 * mu * th);
-    scr[11] = Real(C(jxw) * 2 * mu * thb);
+    // (rounded on their own: the tangent's consumers subtract them, and a product
+    // fused there in one kernel but not in another would differ in the last bit)
+    scr[9] = Real(mul_rn(C(jxw), kap));
+    scr[10] = Real(mul_rn(mul_rn(C(jxw) * 2, mu), th));
+    scr[11] = Real(mul_rn(mul_rn(C(jxw) * 2, mu), thb));
     scr[12] = 0;
   }
   template <typename Real>
